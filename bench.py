@@ -1,0 +1,336 @@
+"""Benchmark: FP64 sensitivity assembly (G entries/s) on one GB300.
+
+Workload (the reference's nine-component FP64 forward at scale): uniform
+64 x 64 x 32 = 131,072 prism cells over x, y in [0, 20 km], z in [0, 8 km];
+101 x 101 = 10,201 observation points on [0, 20 km]^2 at 50 m height;
+components gz, gx, gy, Txx, Txy, Txz, Tyy, Tyz, Tzz (field flag 0x3FE), so G
+is 91,809 x 131,072 = 1.2034e10 entries (96.3 GB in FP64).  One step is one
+full assembly of G (Fwd::compute_G).  The inputs are the geometry only
+(synthetic, built the way the reference's Mesh/Observation classes build
+them); the output (96 GB) is far larger than L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference algorithm on the host cores instead
+(the CPU oracle restating the reference's face-integral kernels, OpenMP over
+all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+WORKLOAD = {
+    "workload": "fp64 sensitivity assembly, 9 components",
+    "cells": [64, 64, 32],
+    "domain_m": [20000.0, 20000.0, 8000.0],
+    "obs": [101, 101],
+    "obs_height_m": 50.0,
+    "field_flag": "0x3FE",
+    "rows": 91809,
+    "cols": 131072,
+    "storage": "fp64",
+}
+MASK = 0x3FE
+METRIC = "G entries/s"
+UNIT = "entries/s"
+
+# FP64 floating-point operations per (observation, cell) pair of the assembly
+# kernel for the nine-component flag, counted from its SASS instruction mix by
+# ncu (DFMA = 2, DADD/DMUL = 1) on a 1,024-point x 4,096-cell case; see
+# profiles/assemble_fp64_9comp.md.  None until measured.
+FP64_FLOPS_PER_PAIR = None
+
+
+def build_problem():
+    from graada3d_gb300 import mesh
+
+    prisms = mesh.regular_mesh((0.0, 20000.0), 64, (0.0, 20000.0), 64, (0.0, 8000.0), 32)
+    obs = mesh.observation_grid(101, 0.0, 20000.0, 101, 0.0, 20000.0, -50.0)
+    rng = np.random.default_rng(3)
+    boxes = []
+    for _ in range(20):
+        x0, y0 = rng.uniform(0, 20000, 2)
+        z0 = rng.uniform(0, 8000)
+        sx, sy, sz = rng.uniform(500, 4000, 3)
+        boxes.append([x0, x0 + sx, y0, y0 + sy, z0, z0 + sz, rng.uniform(-500, 500)])
+    rho = mesh.set_boxes(prisms, boxes)
+    return prisms, obs, rho
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        rows = [r for r in csv.reader(io.StringIO(out)) if len(r) >= 9]
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        load = [s for s in sm if smax and s > 0.3 * smax] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(prisms, obs, target_s: float = 12.0):
+    """Reference algorithm (CPU oracle) on a bounded observation subset."""
+    from oracle import prism as oracle_prism
+
+    oracle_prism.build()
+    threads = oracle_prism.num_threads()
+    n = 2
+    t0 = time.perf_counter()
+    oracle_prism.compute_G(prisms, obs[:n], MASK)
+    dt = time.perf_counter() - t0
+    n_obs = int(min(obs.shape[0], max(n, round(n * target_s / max(dt, 1e-3)))))
+    t0 = time.perf_counter()
+    oracle_prism.compute_G(prisms, obs[:n_obs], MASK)
+    dt = time.perf_counter() - t0
+    entries = 9 * n_obs * prisms.shape[0]
+    return {
+        "value": entries / dt,
+        "unit": UNIT,
+        "cores": threads,
+        "kind": "port",
+        "sample": f"Fwd::compute_G restated in C (oracle/prism_oracle.c), {n_obs} observation points x "
+                  f"{prisms.shape[0]} cells x 9 components = {entries:.3e} entries in {dt:.2f} s",
+        "seconds": dt,
+    }
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group(backend="gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(world, v: float) -> float:
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    world, rank, _ = dist_init()
+    if rank != 0:
+        return
+    prisms, obs, _ = build_problem()
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_sample(prisms, obs, target_s=2.0)
+    times = []
+    samples = []
+    for _ in range(args.steps):
+        s = cpu_sample(prisms, obs, target_s=args.ref_seconds)
+        samples.append(s)
+        times.append(s["seconds"])
+    value = float(np.median([s["value"] for s in samples]))
+    entries_full = 9 * obs.shape[0] * prisms.shape[0]
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * entries_full / value,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": dict(WORKLOAD, sample="bounded observation subset per step, extrapolated by entries/s"),
+        "cpu_baseline": {k: samples[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    line["cpu_baseline"]["value"] = value
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    world, rank, local = dist_init()
+    import torch
+
+    from graada3d_gb300 import Context, Fwd
+
+    torch.cuda.set_device(local)
+    prisms, obs, rho = build_problem()
+    ctx = Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    fp64_peak = ctx.fp64_peak()
+    f = Fwd(prisms, obs, MASK, ctx=ctx)
+    entries = f.Nd * f.Nm
+    pairs = f.N_obs * f.Nm
+
+    # ---- device-resident assembly (value) ---------------------------------
+    for _ in range(args.warmup):
+        f.compute_G("fp64")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        f.compute_G("fp64")
+        ev[k][1].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    per_launch_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = max_over_ranks(world, total_ms)
+    ms_per_step = total_ms / args.steps
+    value = world * entries * args.steps / (total_ms * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers (e2e) --------------
+    h2d = prisms.nbytes + obs.nbytes + rho.nbytes
+    d2h = f.Nd * 8
+    e2e_steps = max(1, min(args.steps, 3))
+    f.set_geometry(prisms, obs, MASK)
+    f.compute_G("fp64")
+    f.G_vec_mul(rho)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        f.set_geometry(prisms, obs, MASK)  # H2D of the geometry
+        f.compute_G("fp64")
+        d = f.G_vec_mul(rho)  # predicted field back to the host
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(world, (time.perf_counter() - t0) / e2e_steps)
+    assert np.isfinite(d).all()
+    e2e_value = world * entries / e2e_s
+
+    roofline = None
+    per_launch = statistics.median(per_launch_ms) * 1e-3
+    if FP64_FLOPS_PER_PAIR:
+        achieved = FP64_FLOPS_PER_PAIR * pairs / per_launch
+        roofline = {"bound": "fp64", "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
+                    "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                    "peak_source": "DFMA loop measured in this run (grada_measure_fp64_peak)"}
+    else:
+        roofline = {"bound": "fp64", "achieved": None, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                    "frac": None, "traffic": None,
+                    "peak_source": "DFMA loop measured in this run (grada_measure_fp64_peak)"}
+    g_bytes = entries * 8
+    hbm = {"write_GBps": g_bytes / per_launch / 1e9}
+    try:
+        peaks = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
+        hbm["peak_GBps"] = peaks.get("hbm_gbs")
+        hbm["frac"] = hbm["write_GBps"] / peaks["hbm_gbs"]
+    except Exception:
+        pass
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_per_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic",
+            "config": dict(WORKLOAD, l2="output per step (96 GB) is larger than L2; inputs are 6.5 MB of geometry",
+                           parallelism="replicas" if world > 1 else "single GPU"),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+                    "includes": "grada_set_geometry (H2D) + grada_compute_G + grada_G_vec_mul (host rho -> host field)"},
+            "gpu_launches": args.steps,
+            "kernel_ms": {"median": statistics.median(per_launch_ms), "min": min(per_launch_ms),
+                          "max": max(per_launch_ms)},
+            "roofline": roofline,
+            "hbm_write": hbm,
+            "clocks": clk,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            cb = cpu_sample(prisms, obs, target_s=args.ref_seconds)
+            cb.pop("seconds", None)
+            line["cpu_baseline"] = cb
+        print(json.dumps(line))
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,361 @@
+// C ABI of the library (include/grada_gpu.h) and the host-side context that
+// mirrors the reference's Fwd object: the geometry it is bound to, the field
+// flag, and the dense sensitivity matrix it owns (src/Forward_modelling/Fwd.h:14-94).
+// Every entry point converts internal errors into a status code and keeps
+// the message for grada_last_error().
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/grada_gpu.h"
+#include "common.cuh"
+#include "context.h"
+#include "kernels.h"
+
+using grada::Error;
+
+namespace grada {
+
+DevBuf::~DevBuf() { release(); }
+
+void DevBuf::release() {
+  if (ptr) {
+    cudaFree(ptr);
+    if (owner) owner->bytes_held -= (int64_t)bytes;
+  }
+  ptr = nullptr;
+  bytes = 0;
+}
+
+void DevBuf::alloc(Context *ctx, size_t nbytes) {
+  if (ptr && bytes >= nbytes) return;
+  release();
+  owner = ctx;
+  if (nbytes == 0) return;
+  cudaError_t e = cudaMalloc(&ptr, nbytes);
+  if (e != cudaSuccess) {
+    ptr = nullptr;
+    cudaGetLastError();
+    throw Error(e == cudaErrorMemoryAllocation ? GRADA_ERR_OUT_OF_MEMORY : GRADA_ERR_CUDA,
+                "cudaMalloc of " + std::to_string(nbytes) + " bytes: " + cudaGetErrorString(e));
+  }
+  bytes = nbytes;
+  ctx->bytes_held += (int64_t)nbytes;
+}
+
+void Context::upload(void *dst, const void *src, size_t nbytes) {
+  if (nbytes == 0) return;
+  GRADA_CUDA_CHECK(cudaMemcpyAsync(dst, src, nbytes, cudaMemcpyHostToDevice, stream));
+}
+
+void Context::download(void *dst, const void *src, size_t nbytes) {
+  if (nbytes == 0) return;
+  GRADA_CUDA_CHECK(cudaMemcpyAsync(dst, src, nbytes, cudaMemcpyDeviceToHost, stream));
+}
+
+void Context::sync() { GRADA_CUDA_CHECK(cudaStreamSynchronize(stream)); }
+
+DevGeometry Context::geometry() const {
+  DevGeometry g;
+  g.prisms = prisms.as<double>();
+  g.obs = obs.as<double>();
+  g.n_cells = n_cells;
+  g.n_obs = n_obs;
+  g.mask = mask;
+  g.n_fields = n_fields;
+  return g;
+}
+
+DevG Context::devG() const {
+  DevG d;
+  d.kind = (GKind)g_storage;
+  d.data = G.ptr;
+  d.row_scale = row_scale.as<float>();
+  d.nd = nd;
+  d.nm = n_cells;
+  d.ld = ld;
+  return d;
+}
+
+double *Context::scratch_doubles(int64_t n) {
+  scratch.alloc(this, sizeof(double) * (size_t)n);
+  return scratch.as<double>();
+}
+
+void Context::require_G() const {
+  if (g_storage < 0) throw Error(GRADA_ERR_STATE, "G has not been assembled (call grada_compute_G)");
+}
+
+void Context::require_geometry() const {
+  if (n_cells <= 0 || n_obs <= 0) throw Error(GRADA_ERR_STATE, "geometry has not been set");
+}
+
+void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_obs, int64_t no,
+                           uint32_t fmask) {
+  if (!h_prisms || !h_obs) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null geometry pointer");
+  if (nc <= 0 || no <= 0) throw Error(GRADA_ERR_INVALID_ARGUMENT, "empty mesh or observation set");
+  if (fmask == 0 || (fmask & ~0x3FFu)) throw Error(GRADA_ERR_INVALID_ARGUMENT, "bad field flag");
+  for (int64_t c = 0; c < nc; c++) {
+    const double *p = h_prisms + 6 * c;
+    for (int k = 0; k < 6; k++)
+      if (!std::isfinite(p[k])) throw Error(GRADA_ERR_NONFINITE, "non-finite prism coordinate");
+    if (!(p[0] < p[1] && p[2] < p[3] && p[4] < p[5]))
+      throw Error(GRADA_ERR_INVALID_ARGUMENT,
+                  "prism " + std::to_string(c) + " is not (x0<x1, y0<y1, z0<z1)");
+  }
+  for (int64_t i = 0; i < 3 * no; i++)
+    if (!std::isfinite(h_obs[i])) throw Error(GRADA_ERR_NONFINITE, "non-finite observation point");
+  // The old G is invalid from here on; its allocation is kept for reuse by the
+  // next compute_G when large enough.
+  g_storage = -1;
+  n_cells = nc;
+  n_obs = no;
+  mask = fmask;
+  n_fields = __builtin_popcount(fmask);
+  nd = (int64_t)n_fields * no;
+  ld = round_up(nd, 8);
+  prisms.alloc(this, sizeof(double) * 6 * nc);
+  obs.alloc(this, sizeof(double) * 3 * no);
+  upload(prisms.ptr, h_prisms, sizeof(double) * 6 * nc);
+  upload(obs.ptr, h_obs, sizeof(double) * 3 * no);
+  sync();
+}
+
+void Context::compute_G(int storage) {
+  require_geometry();
+  if (storage < GRADA_G_FP64 || storage > GRADA_G_BF16_ROWSCALE)
+    throw Error(GRADA_ERR_INVALID_ARGUMENT, "unknown G storage");
+  const DevGeometry g = geometry();
+  const size_t n_entries = (size_t)ld * (size_t)n_cells;
+  g_storage = -1;
+  if (storage == GRADA_G_FP64) {
+    G.alloc(this, n_entries * sizeof(double));
+    if (ld > nd)
+      GRADA_CUDA_CHECK(cudaMemsetAsync(G.ptr, 0, n_entries * sizeof(double), stream));
+    launch_assemble_fp64(g, g.prisms, n_cells, nullptr, 0, G.as<double>(), ld, stream);
+  } else if (storage == GRADA_G_FP32) {
+    G.alloc(this, n_entries * sizeof(float));
+    if (ld > nd) GRADA_CUDA_CHECK(cudaMemsetAsync(G.ptr, 0, n_entries * sizeof(float), stream));
+    launch_assemble_fp32(g, g.prisms, n_cells, nullptr, 0, G.as<float>(), ld, stream);
+  } else {
+    DevBuf tmp;
+    tmp.alloc(this, n_entries * sizeof(float));
+    if (ld > nd) GRADA_CUDA_CHECK(cudaMemsetAsync(tmp.ptr, 0, n_entries * sizeof(float), stream));
+    launch_assemble_fp32(g, g.prisms, n_cells, nullptr, 0, tmp.as<float>(), ld, stream);
+    G.alloc(this, n_entries * sizeof(uint16_t));
+    row_scale.alloc(this, sizeof(float) * (size_t)nd);
+    launch_rowscale_bf16(tmp.as<float>(), nd, n_cells, ld, row_scale.as<float>(),
+                         G.as<uint16_t>(), stream);
+    sync();
+  }
+  g_storage = storage;
+}
+
+void Context::G_vec_mul_dev(const double *d_x, double *d_y) {
+  require_G();
+  const DevG d = devG();
+  double *sc = scratch_doubles(gemv_scratch_doubles(d, sm_count));
+  launch_G_vec_mul(d, d_x, d_y, sc, sm_count, stream);
+}
+
+void Context::GT_vec_mul_dev(const double *d_y, double *d_x) {
+  require_G();
+  const DevG d = devG();
+  double *sc = scratch_doubles(gemv_scratch_doubles(d, sm_count));
+  launch_GT_vec_mul(d, d_y, d_x, sc, sm_count, stream);
+}
+
+void Context::forward_field_dev(const double *d_rho, double *d_fields) {
+  require_geometry();
+  const DevGeometry g = geometry();
+  const int splits = forward_field_splits(g, sm_count);
+  double *partial = scratch_doubles((int64_t)splits * n_obs * n_fields);
+  launch_forward_field(g, d_rho, splits, partial, d_fields, stream);
+}
+
+}  // namespace grada
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+struct grada_ctx : public grada::Context {};
+
+namespace {
+
+template <class F>
+int guarded(grada_ctx *ctx, F &&f) {
+  if (!ctx) return GRADA_ERR_INVALID_ARGUMENT;
+  try {
+    GRADA_CUDA_CHECK(cudaSetDevice(ctx->device));
+    f();
+    ctx->last_error.clear();
+    return GRADA_OK;
+  } catch (const Error &e) {
+    ctx->last_error = e.what();
+    return e.status;
+  } catch (const std::exception &e) {
+    ctx->last_error = e.what();
+    return GRADA_ERR_CUDA;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int grada_version(void) { return 100; }
+
+int grada_ctx_create(int device, grada_ctx **out) {
+  if (!out) return GRADA_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    cudaGetLastError();
+    return GRADA_ERR_CUDA;
+  }
+  grada_ctx *c = new grada_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return GRADA_ERR_CUDA;
+  }
+  *out = c;
+  return GRADA_OK;
+}
+
+int grada_ctx_destroy(grada_ctx *ctx) {
+  if (!ctx) return GRADA_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->release_all();
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GRADA_OK;
+}
+
+const char *grada_last_error(const grada_ctx *ctx) {
+  return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+void *grada_ctx_stream(grada_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int grada_sync(grada_ctx *ctx) {
+  return guarded(ctx, [&] { ctx->sync(); });
+}
+
+int64_t grada_ctx_device_bytes(const grada_ctx *ctx) { return ctx ? ctx->bytes_held : 0; }
+
+int grada_set_geometry(grada_ctx *ctx, const double *prisms, int64_t n_cells, const double *obs,
+                       int64_t n_obs, uint32_t field_flag) {
+  return guarded(ctx, [&] { ctx->set_geometry(prisms, n_cells, obs, n_obs, field_flag); });
+}
+
+int grada_get_dims(const grada_ctx *ctx, int64_t *n_cells, int64_t *n_obs, int *n_fields,
+                   int64_t *nd, int64_t *ld) {
+  if (!ctx) return GRADA_ERR_INVALID_ARGUMENT;
+  if (n_cells) *n_cells = ctx->n_cells;
+  if (n_obs) *n_obs = ctx->n_obs;
+  if (n_fields) *n_fields = ctx->n_fields;
+  if (nd) *nd = ctx->nd;
+  if (ld) *ld = ctx->ld;
+  return GRADA_OK;
+}
+
+int grada_compute_G(grada_ctx *ctx, int storage) {
+  return guarded(ctx, [&] {
+    ctx->compute_G(storage);
+    ctx->sync();
+  });
+}
+
+int grada_G_storage(const grada_ctx *ctx) { return ctx ? ctx->g_storage : -1; }
+
+int grada_get_G(grada_ctx *ctx, double *host, int64_t ld_host) {
+  return guarded(ctx, [&] {
+    ctx->require_G();
+    if (!host || ld_host < ctx->nd) throw Error(GRADA_ERR_INVALID_ARGUMENT, "bad host buffer");
+    // Widen column blocks to FP64 on the device, then copy them out.
+    const int64_t cols_per_block = 256;
+    grada::DevBuf stage;
+    stage.alloc(ctx, sizeof(double) * (size_t)ctx->ld * cols_per_block);
+    std::vector<double> tmp;
+    for (int64_t c0 = 0; c0 < ctx->n_cells; c0 += cols_per_block) {
+      const int64_t nc = std::min(cols_per_block, ctx->n_cells - c0);
+      grada::launch_widen_columns(ctx->devG(), c0, nc, stage.as<double>(), ctx->stream);
+      if (ld_host == ctx->ld) {
+        ctx->download(host + c0 * ld_host, stage.ptr, sizeof(double) * (size_t)(ctx->ld * nc));
+      } else {
+        GRADA_CUDA_CHECK(cudaMemcpy2DAsync(host + c0 * ld_host, sizeof(double) * ld_host,
+                                           stage.ptr, sizeof(double) * ctx->ld,
+                                           sizeof(double) * ctx->nd, nc, cudaMemcpyDeviceToHost,
+                                           ctx->stream));
+      }
+      ctx->sync();
+    }
+  });
+}
+
+int grada_G_vec_mul(grada_ctx *ctx, const double *x, double *y) {
+  return guarded(ctx, [&] {
+    ctx->require_G();
+    if (!x || !y) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null vector");
+    ctx->vx.alloc(ctx, sizeof(double) * ctx->n_cells);
+    ctx->vy.alloc(ctx, sizeof(double) * ctx->ld);
+    ctx->upload(ctx->vx.ptr, x, sizeof(double) * ctx->n_cells);
+    ctx->G_vec_mul_dev(ctx->vx.as<double>(), ctx->vy.as<double>());
+    ctx->download(y, ctx->vy.ptr, sizeof(double) * ctx->nd);
+    ctx->sync();
+  });
+}
+
+int grada_GT_vec_mul(grada_ctx *ctx, const double *y, double *x) {
+  return guarded(ctx, [&] {
+    ctx->require_G();
+    if (!x || !y) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null vector");
+    ctx->vx.alloc(ctx, sizeof(double) * ctx->n_cells);
+    ctx->vy.alloc(ctx, sizeof(double) * ctx->ld);
+    ctx->upload(ctx->vy.ptr, y, sizeof(double) * ctx->nd);
+    ctx->GT_vec_mul_dev(ctx->vy.as<double>(), ctx->vx.as<double>());
+    ctx->download(x, ctx->vx.ptr, sizeof(double) * ctx->n_cells);
+    ctx->sync();
+  });
+}
+
+int grada_G_vec_mul_dev(grada_ctx *ctx, const double *d_x, double *d_y) {
+  return guarded(ctx, [&] { ctx->G_vec_mul_dev(d_x, d_y); });
+}
+
+int grada_GT_vec_mul_dev(grada_ctx *ctx, const double *d_y, double *d_x) {
+  return guarded(ctx, [&] { ctx->GT_vec_mul_dev(d_y, d_x); });
+}
+
+int grada_forward_field(grada_ctx *ctx, const double *rho, double *fields) {
+  return guarded(ctx, [&] {
+    ctx->require_geometry();
+    if (!rho || !fields) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null vector");
+    ctx->vx.alloc(ctx, sizeof(double) * ctx->n_cells);
+    ctx->vy.alloc(ctx, sizeof(double) * ctx->ld);
+    ctx->upload(ctx->vx.ptr, rho, sizeof(double) * ctx->n_cells);
+    ctx->forward_field_dev(ctx->vx.as<double>(), ctx->vy.as<double>());
+    ctx->download(fields, ctx->vy.ptr, sizeof(double) * ctx->nd);
+    ctx->sync();
+  });
+}
+
+int grada_forward_field_dev(grada_ctx *ctx, const double *d_rho, double *d_fields) {
+  return guarded(ctx, [&] { ctx->forward_field_dev(d_rho, d_fields); });
+}
+
+int grada_measure_fp64_peak(grada_ctx *ctx, double *flops_per_s) {
+  return guarded(ctx, [&] {
+    if (!flops_per_s) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null output");
+    *flops_per_s = grada::measure_fp64_fma_rate(ctx->sm_count, ctx->stream);
+  });
+}
+
+}  // extern "C"

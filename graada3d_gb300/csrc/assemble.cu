@@ -1,0 +1,221 @@
+// K1: sensitivity assembly and the matrix-free field sum.
+//
+// Reference: Fwd::compute_G (src/Forward_modelling/Fwd.cpp:47-78), which
+// loops observations serially and cells in an OpenMP loop, calling
+// GravFormula::field_caused_by_single_prism per (observation, cell) pair;
+// and the field sum of src/compute.cpp:246-260.
+//
+// Mapping: a block owns 128 consecutive observation points (one per thread)
+// and a chunk of ASM_CHUNK consecutive cells whose geometry is staged in
+// shared memory once and read by all 128 threads.  Each thread evaluates the
+// closed-form terms of prism.cuh for its point against every cell of the chunk
+// and writes the requested components; for a fixed cell and component, a warp
+// writes 32 consecutive rows of G's column (256 B for FP64), so every store is
+// coalesced.  The kernel is bound by the FP64 pipe (log/atan2/sqrt/division),
+// not by memory: the G write is ~1% of the FP64 time.
+#include "common.cuh"
+#include "kernels.h"
+#include "prism.cuh"
+
+namespace grada {
+
+namespace {
+
+constexpr int ASM_THREADS = 128;
+constexpr int ASM_CHUNK = 16;
+
+template <typename OutT>
+__global__ void __launch_bounds__(ASM_THREADS)
+    assemble_kernel(const double *__restrict__ obs, int64_t n_obs,
+                    const double *__restrict__ prisms, int64_t n_cells,
+                    const int64_t *__restrict__ col_index, int64_t col_offset, uint32_t mask,
+                    OutT *__restrict__ G, int64_t ld) {
+  __shared__ double sp[ASM_CHUNK * 6];
+  const int64_t c0 = (int64_t)blockIdx.x * ASM_CHUNK;
+  const int64_t left = n_cells - c0;
+  const int nc = left < ASM_CHUNK ? (int)left : ASM_CHUNK;
+  for (int t = threadIdx.x; t < nc * 6; t += ASM_THREADS) sp[t] = prisms[c0 * 6 + t];
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.y * ASM_THREADS + threadIdx.x;
+  if (i >= n_obs) return;
+  const double px = obs[3 * i], py = obs[3 * i + 1], pz = obs[3 * i + 2];
+  const uint32_t fam = families_for_mask(mask);
+  for (int c = 0; c < nc; c++) {
+    const double *p = sp + 6 * c;
+    PrismTerms t;
+    prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, t);
+    const int64_t col = col_index ? col_index[c0 + c] : c0 + c + col_offset;
+    OutT *gcol = G + col * ld + i;
+    int slot = 0;
+#pragma unroll
+    for (int b = 0; b < 10; b++) {
+      if (mask & (1u << b)) {
+        store_entry(gcol + (int64_t)slot * n_obs, prism_component(t, b));
+        slot++;
+      }
+    }
+  }
+}
+
+template <typename OutT>
+void launch_assemble(const DevGeometry &g, const double *prisms, int64_t n_cells,
+                     const int64_t *col_index, int64_t col_offset, OutT *G, int64_t ld,
+                     cudaStream_t s) {
+  if (n_cells <= 0 || g.n_obs <= 0) return;
+  dim3 grid((unsigned)ceil_div(n_cells, ASM_CHUNK), (unsigned)ceil_div(g.n_obs, ASM_THREADS));
+  if (grid.y > 65535u) throw Error(-1, "too many observation points for one launch");
+  assemble_kernel<OutT><<<grid, ASM_THREADS, 0, s>>>(g.obs, g.n_obs, prisms, n_cells, col_index,
+                                                     col_offset, g.mask, G, ld);
+  GRADA_LAUNCH_CHECK();
+}
+
+// ---- bf16 with a per-row scale ---------------------------------------------
+
+__global__ void row_absmax_kernel(const float *__restrict__ G, int64_t nd, int64_t nm, int64_t ld,
+                                  int cols_per_block, unsigned int *__restrict__ row_max_bits) {
+  const int64_t row = (int64_t)blockIdx.y * blockDim.x + threadIdx.x;
+  if (row >= nd) return;
+  const int64_t c0 = (int64_t)blockIdx.x * cols_per_block;
+  const int64_t c1 = min(nm, c0 + cols_per_block);
+  float m = 0.f;
+  for (int64_t c = c0; c < c1; c++) m = fmaxf(m, fabsf(G[row + c * ld]));
+  // |x| of a finite float orders like its bit pattern.
+  atomicMax(row_max_bits + row, __float_as_uint(m));
+}
+
+__global__ void row_scale_kernel(const unsigned int *__restrict__ row_max_bits, int64_t nd,
+                                 float *__restrict__ scale) {
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= nd) return;
+  const float m = __uint_as_float(row_max_bits[row]);
+  scale[row] = (m > 0.f) ? m : 1.f;
+}
+
+__global__ void quantize_bf16_kernel(const float *__restrict__ G, int64_t nd, int64_t nm,
+                                     int64_t ld, const float *__restrict__ scale,
+                                     __nv_bfloat16 *__restrict__ out) {
+  const int64_t row = (int64_t)blockIdx.y * blockDim.x + threadIdx.x;
+  const int64_t col = blockIdx.x;
+  if (row >= ld) return;
+  const int64_t idx = row + col * ld;
+  const float v = (row < nd) ? G[idx] / scale[row] : 0.f;
+  out[idx] = __float2bfloat16_rn(v);
+}
+
+// ---- matrix-free field sum ------------------------------------------------
+
+constexpr int FF_THREADS = 128;
+constexpr int FF_CHUNK = 32;
+
+__global__ void __launch_bounds__(FF_THREADS)
+    forward_field_kernel(const double *__restrict__ obs, int64_t n_obs,
+                         const double *__restrict__ prisms, const double *__restrict__ rho,
+                         int64_t n_cells, int64_t cells_per_split, uint32_t mask, int nf,
+                         double *__restrict__ partial) {
+  __shared__ double sp[FF_CHUNK * 7];
+  const int64_t split = blockIdx.x;
+  const int64_t c_begin = split * cells_per_split;
+  const int64_t c_end = min(n_cells, c_begin + cells_per_split);
+  const int64_t i = (int64_t)blockIdx.y * FF_THREADS + threadIdx.x;
+  const bool active = i < n_obs;
+  double px = 0, py = 0, pz = 0;
+  if (active) {
+    px = obs[3 * i];
+    py = obs[3 * i + 1];
+    pz = obs[3 * i + 2];
+  }
+  const uint32_t fam = families_for_mask(mask);
+  double acc[10];
+#pragma unroll
+  for (int b = 0; b < 10; b++) acc[b] = 0.0;
+  for (int64_t c0 = c_begin; c0 < c_end; c0 += FF_CHUNK) {
+    const int nc = (int)min((int64_t)FF_CHUNK, c_end - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc * 6; t += FF_THREADS) sp[t] = prisms[c0 * 6 + t];
+    for (int t = threadIdx.x; t < nc; t += FF_THREADS) sp[FF_CHUNK * 6 + t] = rho[c0 + t];
+    __syncthreads();
+    if (!active) continue;
+    for (int c = 0; c < nc; c++) {
+      const double *p = sp + 6 * c;
+      const double w = sp[FF_CHUNK * 6 + c];
+      PrismTerms t;
+      prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, t);
+#pragma unroll
+      for (int b = 0; b < 10; b++)
+        if (mask & (1u << b)) acc[b] = fma(w, prism_component(t, b), acc[b]);
+    }
+  }
+  if (!active) return;
+  double *out = partial + split * n_obs * nf + i * nf;
+  int slot = 0;
+#pragma unroll
+  for (int b = 0; b < 10; b++)
+    if (mask & (1u << b)) out[slot++] = acc[b];
+}
+
+__global__ void sum_splits_kernel(const double *__restrict__ partial, int n_split, int64_t n,
+                                  double *__restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double s = 0.0;
+  for (int k = 0; k < n_split; k++) s += partial[(int64_t)k * n + e];
+  out[e] = s;
+}
+
+}  // namespace
+
+void launch_assemble_fp64(const DevGeometry &g, const double *prisms, int64_t n_cells,
+                          const int64_t *col_index, int64_t col_offset, double *G, int64_t ld,
+                          cudaStream_t s) {
+  launch_assemble<double>(g, prisms, n_cells, col_index, col_offset, G, ld, s);
+}
+
+void launch_assemble_fp32(const DevGeometry &g, const double *prisms, int64_t n_cells,
+                          const int64_t *col_index, int64_t col_offset, float *G, int64_t ld,
+                          cudaStream_t s) {
+  launch_assemble<float>(g, prisms, n_cells, col_index, col_offset, G, ld, s);
+}
+
+void launch_rowscale_bf16(const float *G32, int64_t nd, int64_t nm, int64_t ld, float *row_scale,
+                          uint16_t *Gbf, cudaStream_t s) {
+  // row_scale doubles as the atomicMax target (bit patterns) before scaling.
+  unsigned int *bits = reinterpret_cast<unsigned int *>(row_scale);
+  GRADA_CUDA_CHECK(cudaMemsetAsync(bits, 0, sizeof(unsigned int) * nd, s));
+  const int cols_per_block = 256;
+  dim3 g1((unsigned)ceil_div(nm, cols_per_block), (unsigned)ceil_div(nd, 256));
+  row_absmax_kernel<<<g1, 256, 0, s>>>(G32, nd, nm, ld, cols_per_block, bits);
+  GRADA_LAUNCH_CHECK();
+  row_scale_kernel<<<(unsigned)ceil_div(nd, 256), 256, 0, s>>>(bits, nd, row_scale);
+  GRADA_LAUNCH_CHECK();
+  dim3 g3((unsigned)nm, (unsigned)ceil_div(ld, 256));
+  quantize_bf16_kernel<<<g3, 256, 0, s>>>(G32, nd, nm, ld, row_scale,
+                                          reinterpret_cast<__nv_bfloat16 *>(Gbf));
+  GRADA_LAUNCH_CHECK();
+}
+
+int forward_field_splits(const DevGeometry &g, int sm_count) {
+  const int64_t obs_tiles = ceil_div(g.n_obs, FF_THREADS);
+  const int64_t want_blocks = (int64_t)sm_count * 8;
+  int64_t splits = ceil_div(want_blocks, obs_tiles);
+  const int64_t max_splits = ceil_div(g.n_cells, FF_CHUNK);
+  if (splits > max_splits) splits = max_splits;
+  if (splits < 1) splits = 1;
+  if (splits > 65535) splits = 65535;
+  return (int)splits;
+}
+
+void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, double *partial,
+                          double *fields, cudaStream_t s) {
+  if (g.n_obs <= 0) return;
+  const int64_t per = round_up(ceil_div(g.n_cells, n_split), FF_CHUNK);
+  dim3 grid((unsigned)n_split, (unsigned)ceil_div(g.n_obs, FF_THREADS));
+  if (grid.y > 65535u) throw Error(-1, "too many observation points for one launch");
+  forward_field_kernel<<<grid, FF_THREADS, 0, s>>>(g.obs, g.n_obs, g.prisms, rho, g.n_cells, per,
+                                                   g.mask, g.n_fields, partial);
+  GRADA_LAUNCH_CHECK();
+  const int64_t n = g.n_obs * g.n_fields;
+  sum_splits_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(partial, n_split, n, fields);
+  GRADA_LAUNCH_CHECK();
+}
+
+}  // namespace grada

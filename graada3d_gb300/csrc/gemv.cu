@@ -1,0 +1,295 @@
+// K2/K3: dense products with the stored sensitivity matrix.
+//
+// Reference: Fwd::G_vec_mul / Fwd::GT_vec_mul, dense branches
+// (src/Forward_modelling/Fwd.cpp:145 `product = G * vec`, :111
+// `product = G.transpose() * vec`), i.e. Eigen GEMV on a column-major
+// MatrixXd.
+//
+// Both products stream G once from HBM with 16-byte vector loads and are
+// bound by HBM bandwidth.  G is column-major with leading dimension ld (a
+// multiple of 8, padding rows zero), so:
+//  * G^T y: a block owns COLS consecutive columns; each thread walks the rows
+//    with 16-byte loads, multiplies by y (loaded once per row chunk and reused
+//    for the block's COLS columns) and the block reduces COLS sums with warp
+//    shuffles.  Deterministic: fixed per-thread row order and reduction tree.
+//  * G x: a block owns a tile of 256*VEC rows and a range of columns; threads
+//    accumulate VEC rows each over that range; the column ranges' partial rows
+//    go to scratch and a second pass sums them in split order (deterministic,
+//    no atomics).
+// FP64 G accumulates in FP64.  FP32 / bf16 G multiply and accumulate in FP32
+// (the vector is rounded to FP32 once); partial sums across blocks are added
+// in FP64.  bf16 rows carry an FP32 scale applied after the row sum (G x) or
+// folded into y (G^T y).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace grada {
+
+namespace {
+
+constexpr int GV_THREADS = 256;
+
+// ---- element loaders: VEC consecutive entries from a 16-byte load ----------
+
+struct LoadF64 {
+  static constexpr int VEC = 2;
+  using Acc = double;
+  __device__ static void load(const void *base, int64_t idx, double (&v)[2]) {
+    const double2 d = __ldcs(reinterpret_cast<const double2 *>(static_cast<const double *>(base) + idx));
+    v[0] = d.x;
+    v[1] = d.y;
+  }
+};
+struct LoadF32 {
+  static constexpr int VEC = 4;
+  using Acc = float;
+  __device__ static void load(const void *base, int64_t idx, float (&v)[4]) {
+    const float4 d = __ldcs(reinterpret_cast<const float4 *>(static_cast<const float *>(base) + idx));
+    v[0] = d.x;
+    v[1] = d.y;
+    v[2] = d.z;
+    v[3] = d.w;
+  }
+};
+struct LoadBF16 {
+  static constexpr int VEC = 8;
+  using Acc = float;
+  __device__ static void load(const void *base, int64_t idx, float (&v)[8]) {
+    const uint4 d = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(base) + idx));
+    const uint32_t w[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      v[2 * k] = __uint_as_float(w[k] << 16);
+      v[2 * k + 1] = __uint_as_float(w[k] & 0xffff0000u);
+    }
+  }
+};
+
+// ---- G x ----------------------------------------------------------------------
+
+template <class L>
+__global__ void __launch_bounds__(GV_THREADS)
+    gx_partial_kernel(const void *__restrict__ G, int64_t ld, int64_t nm, int64_t cols_per_split,
+                      const double *__restrict__ x, double *__restrict__ partial) {
+  using Acc = typename L::Acc;
+  constexpr int VEC = L::VEC;
+  constexpr int XCH = 256;
+  __shared__ Acc xs[XCH];
+  const int64_t row = ((int64_t)blockIdx.x * GV_THREADS + threadIdx.x) * VEC;
+  const int64_t c_begin = (int64_t)blockIdx.y * cols_per_split;
+  const int64_t c_end = min(nm, c_begin + cols_per_split);
+  Acc acc[VEC];
+#pragma unroll
+  for (int v = 0; v < VEC; v++) acc[v] = Acc(0);
+  for (int64_t c0 = c_begin; c0 < c_end; c0 += XCH) {
+    const int nc = (int)min((int64_t)XCH, c_end - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc; t += GV_THREADS) xs[t] = (Acc)x[c0 + t];
+    __syncthreads();
+    if (row < ld) {
+      const int64_t base = row + c0 * ld;
+      int c = 0;
+      for (; c + 4 <= nc; c += 4) {
+        Acc g0[VEC], g1[VEC], g2[VEC], g3[VEC];
+        L::load(G, base + (int64_t)c * ld, g0);
+        L::load(G, base + (int64_t)(c + 1) * ld, g1);
+        L::load(G, base + (int64_t)(c + 2) * ld, g2);
+        L::load(G, base + (int64_t)(c + 3) * ld, g3);
+        const Acc x0 = xs[c], x1 = xs[c + 1], x2 = xs[c + 2], x3 = xs[c + 3];
+#pragma unroll
+        for (int v = 0; v < VEC; v++) {
+          acc[v] = fma(g0[v], x0, acc[v]);
+          acc[v] = fma(g1[v], x1, acc[v]);
+          acc[v] = fma(g2[v], x2, acc[v]);
+          acc[v] = fma(g3[v], x3, acc[v]);
+        }
+      }
+      for (; c < nc; c++) {
+        Acc g0[VEC];
+        L::load(G, base + (int64_t)c * ld, g0);
+#pragma unroll
+        for (int v = 0; v < VEC; v++) acc[v] = fma(g0[v], xs[c], acc[v]);
+      }
+    }
+  }
+  if (row < ld) {
+    double *out = partial + (int64_t)blockIdx.y * ld + row;
+#pragma unroll
+    for (int v = 0; v < VEC; v++) out[v] = (double)acc[v];
+  }
+}
+
+__global__ void gx_finish_kernel(const double *__restrict__ partial, int n_split, int64_t ld,
+                                 int64_t nd, const float *__restrict__ row_scale,
+                                 double *__restrict__ y) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nd) return;
+  double s = 0.0;
+  for (int k = 0; k < n_split; k++) s += partial[(int64_t)k * ld + r];
+  if (row_scale) s *= (double)row_scale[r];
+  y[r] = s;
+}
+
+// ---- G^T y --------------------------------------------------------------------
+
+template <class L, int COLS>
+__global__ void __launch_bounds__(GV_THREADS)
+    gty_kernel(const void *__restrict__ G, int64_t ld, int64_t nm,
+               const typename L::Acc *__restrict__ y, double *__restrict__ x) {
+  using Acc = typename L::Acc;
+  constexpr int VEC = L::VEC;
+  const int64_t c0 = (int64_t)blockIdx.x * COLS;
+  const int ncol = (int)min((int64_t)COLS, nm - c0);
+  Acc acc[COLS];
+#pragma unroll
+  for (int c = 0; c < COLS; c++) acc[c] = Acc(0);
+  for (int64_t row = (int64_t)threadIdx.x * VEC; row < ld; row += (int64_t)GV_THREADS * VEC) {
+    Acc yv[VEC];
+#pragma unroll
+    for (int v = 0; v < VEC; v++) yv[v] = y[row + v];
+#pragma unroll
+    for (int c = 0; c < COLS; c++) {
+      if (c < ncol) {
+        Acc g[VEC];
+        L::load(G, row + (c0 + c) * ld, g);
+#pragma unroll
+        for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
+      }
+    }
+  }
+  __shared__ double red[GV_THREADS / 32][COLS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < COLS; c++) {
+    double v = (double)acc[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][c] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < ncol) {
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < GV_THREADS / 32; w++) s += red[w][threadIdx.x];
+    x[c0 + threadIdx.x] = s;
+  }
+}
+
+// y (FP64, nd entries) -> padded vector of the accumulation type, times the
+// row scale for bf16, zero in the padding rows.
+template <typename Acc>
+__global__ void prep_y_kernel(const double *__restrict__ y, int64_t nd, int64_t ld,
+                              const float *__restrict__ row_scale, Acc *__restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= ld) return;
+  double v = (r < nd) ? y[r] : 0.0;
+  if (row_scale && r < nd) v *= (double)row_scale[r];
+  out[r] = (Acc)v;
+}
+
+int gx_splits(const DevG &G, int sm_count, int vec) {
+  const int64_t tiles = ceil_div(G.ld, (int64_t)GV_THREADS * vec);
+  int64_t splits = ceil_div((int64_t)sm_count * 8, tiles);
+  const int64_t max_splits = ceil_div(G.nm, 64);
+  if (splits > max_splits) splits = max_splits;
+  if (splits < 1) splits = 1;
+  if (splits > 65535) splits = 65535;
+  return (int)splits;
+}
+
+int vec_of(GKind k) { return k == GKind::FP64 ? 2 : (k == GKind::FP32 ? 4 : 8); }
+
+__global__ void widen_kernel(const void *__restrict__ G, int kind, const float *__restrict__ scale,
+                             int64_t nd, int64_t ld, int64_t c0, double *__restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.y * blockDim.x + threadIdx.x;
+  const int64_t c = blockIdx.x;
+  if (r >= ld) return;
+  const int64_t src = r + (c0 + c) * ld;
+  double v;
+  if (kind == 0) {
+    v = static_cast<const double *>(G)[src];
+  } else if (kind == 1) {
+    v = (double)static_cast<const float *>(G)[src];
+  } else {
+    const uint32_t bits = (uint32_t) static_cast<const uint16_t *>(G)[src] << 16;
+    v = (double)__uint_as_float(bits) * (r < nd ? (double)scale[r] : 0.0);
+  }
+  out[r + c * ld] = v;
+}
+
+template <class L>
+void run_gx(const DevG &G, const double *x, double *y, double *scratch, int sm_count,
+            cudaStream_t s) {
+  const int splits = gx_splits(G, sm_count, L::VEC);
+  const int64_t per = ceil_div(G.nm, splits);
+  dim3 grid((unsigned)ceil_div(G.ld, (int64_t)GV_THREADS * L::VEC), (unsigned)splits);
+  gx_partial_kernel<L><<<grid, GV_THREADS, 0, s>>>(G.data, G.ld, G.nm, per, x, scratch);
+  GRADA_LAUNCH_CHECK();
+  gx_finish_kernel<<<(unsigned)ceil_div(G.nd, 256), 256, 0, s>>>(scratch, splits, G.ld, G.nd,
+                                                                 G.row_scale, y);
+  GRADA_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+int64_t gemv_scratch_doubles(const DevG &G, int sm_count) {
+  const int splits = gx_splits(G, sm_count, vec_of(G.kind));
+  const int64_t gx = (int64_t)splits * G.ld;
+  const int64_t gty = G.ld;  // converted y (FP32 uses half of it)
+  return gx > gty ? gx : gty;
+}
+
+void launch_G_vec_mul(const DevG &G, const double *x, double *y, double *scratch, int sm_count,
+                      cudaStream_t s) {
+  if (G.nd <= 0 || G.nm <= 0) return;
+  switch (G.kind) {
+    case GKind::FP64: run_gx<LoadF64>(G, x, y, scratch, sm_count, s); break;
+    case GKind::FP32: run_gx<LoadF32>(G, x, y, scratch, sm_count, s); break;
+    case GKind::BF16: run_gx<LoadBF16>(G, x, y, scratch, sm_count, s); break;
+  }
+}
+
+void launch_widen_columns(const DevG &G, int64_t c0, int64_t nc, double *out, cudaStream_t s) {
+  if (nc <= 0) return;
+  dim3 grid((unsigned)nc, (unsigned)ceil_div(G.ld, 256));
+  widen_kernel<<<grid, 256, 0, s>>>(G.data, (int)G.kind, G.row_scale, G.nd, G.ld, c0, out);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratch, int sm_count,
+                       cudaStream_t s) {
+  (void)sm_count;
+  if (G.nd <= 0 || G.nm <= 0) return;
+  const unsigned prep_blocks = (unsigned)ceil_div(G.ld, 256);
+  switch (G.kind) {
+    case GKind::FP64: {
+      prep_y_kernel<double><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, nullptr, scratch);
+      GRADA_LAUNCH_CHECK();
+      constexpr int COLS = 4;
+      gty_kernel<LoadF64, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
+          G.data, G.ld, G.nm, scratch, x);
+      break;
+    }
+    case GKind::FP32: {
+      float *y32 = reinterpret_cast<float *>(scratch);
+      prep_y_kernel<float><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, nullptr, y32);
+      GRADA_LAUNCH_CHECK();
+      constexpr int COLS = 4;
+      gty_kernel<LoadF32, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
+          G.data, G.ld, G.nm, y32, x);
+      break;
+    }
+    case GKind::BF16: {
+      float *y32 = reinterpret_cast<float *>(scratch);
+      prep_y_kernel<float><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, G.row_scale, y32);
+      GRADA_LAUNCH_CHECK();
+      constexpr int COLS = 4;
+      gty_kernel<LoadBF16, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
+          G.data, G.ld, G.nm, y32, x);
+      break;
+    }
+  }
+  GRADA_LAUNCH_CHECK();
+}
+
+}  // namespace grada

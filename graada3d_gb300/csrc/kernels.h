@@ -1,0 +1,63 @@
+// Internal launcher interface between the host context (abi.cu) and the CUDA
+// kernels.  Nothing here is part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace grada {
+
+// Device-resident problem geometry (mesh leaf cells and observation points).
+struct DevGeometry {
+  const double *prisms = nullptr;  // n_cells x 6: x0 x1 y0 y1 z0 z1
+  const double *obs = nullptr;     // n_obs x 3
+  int64_t n_cells = 0;
+  int64_t n_obs = 0;
+  uint32_t mask = 0;
+  int n_fields = 0;
+};
+
+// ---- sensitivity assembly (assemble.cu) ---------------------------------
+// Writes the columns of G for cells [0, n_cells) of `prisms`; column of cell c
+// is col_index[c] when col_index is non-null, else c + col_offset.
+void launch_assemble_fp64(const DevGeometry &g, const double *prisms, int64_t n_cells,
+                          const int64_t *col_index, int64_t col_offset, double *G, int64_t ld,
+                          cudaStream_t s);
+void launch_assemble_fp32(const DevGeometry &g, const double *prisms, int64_t n_cells,
+                          const int64_t *col_index, int64_t col_offset, float *G, int64_t ld,
+                          cudaStream_t s);
+// Per-row maximum of |G| over the columns, then bf16 entries G/scale with the
+// FP32 scale per row (entries of an all-zero row get scale 1).
+void launch_rowscale_bf16(const float *G32, int64_t nd, int64_t nm, int64_t ld, float *row_scale,
+                          uint16_t *Gbf, cudaStream_t s);
+
+// Matrix-free field sum: fields[i*nf + k] = sum_j rho_j field_k(obs_i, cell_j).
+// `partial` must hold n_split * n_obs * nf doubles.
+int forward_field_splits(const DevGeometry &g, int sm_count);
+void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, double *partial,
+                          double *fields, cudaStream_t s);
+
+// ---- dense products (gemv.cu) -------------------------------------------
+enum class GKind : int { FP64 = 0, FP32 = 1, BF16 = 2 };
+
+struct DevG {
+  GKind kind = GKind::FP64;
+  const void *data = nullptr;
+  const float *row_scale = nullptr;  // bf16 only
+  int64_t nd = 0, nm = 0, ld = 0;
+};
+
+// Scratch (in doubles) the products need for a given G, and the launches.
+int64_t gemv_scratch_doubles(const DevG &G, int sm_count);
+void launch_G_vec_mul(const DevG &G, const double *x, double *y, double *scratch, int sm_count,
+                      cudaStream_t s);
+void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratch, int sm_count,
+                       cudaStream_t s);
+// Columns [c0, c0+nc) of G widened to FP64 (scale applied for bf16) into
+// out (ld x nc, column-major).
+void launch_widen_columns(const DevG &G, int64_t c0, int64_t nc, double *out, cudaStream_t s);
+
+// ---- diagnostics (diag.cu) ----------------------------------------------
+double measure_fp64_fma_rate(int sm_count, cudaStream_t s);
+
+}  // namespace grada

@@ -1,0 +1,162 @@
+"""Python view of the reference's ``Fwd`` interface over the C ABI.
+
+Mirrors ``Fwd`` (src/Forward_modelling/Fwd.h:14-94): bind a mesh (prisms in
+leaf order) and observation points with a field flag, ``compute_G``,
+``G_vec_mul``, ``GT_vec_mul``, ``get_G``.  All arithmetic happens in
+``libgrada_gpu.so`` on the GPU; this module only moves NumPy arrays across
+the ABI.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import GradaError
+
+# Field bits of GS::ComputationOptions (gs.h:46-57).
+FIELD_BITS = {
+    "V": 0x001, "gz": 0x002, "gx": 0x004, "gy": 0x008, "Tzz": 0x010,
+    "Txz": 0x020, "Tyz": 0x040, "Txx": 0x080, "Txy": 0x100, "Tyy": 0x200,
+}
+FIELD_ORDER = ["V", "gz", "gx", "gy", "Tzz", "Txz", "Tyz", "Txx", "Txy", "Tyy"]
+
+G_FP64, G_FP32, G_BF16_ROWSCALE = 0, 1, 2
+STORAGE = {"fp64": G_FP64, "fp32": G_FP32, "bf16": G_BF16_ROWSCALE}
+
+
+def field_mask(names) -> int:
+    m = 0
+    for n in names:
+        m |= FIELD_BITS[n]
+    return m
+
+
+def mask_fields(mask: int) -> list[str]:
+    return [n for b, n in enumerate(FIELD_ORDER) if mask & (1 << b)]
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Context:
+    """One library context (one CUDA stream, owned device buffers)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        st = self.lib.grada_ctx_create(int(device), ctypes.byref(h))
+        if st != 0:
+            raise GradaError(st, f"grada_ctx_create(device={device}) failed")
+        self.handle = h
+
+    def check(self, status: int) -> None:
+        if status != 0:
+            msg = self.lib.grada_last_error(self.handle)
+            raise GradaError(status, msg.decode() if msg else "")
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.grada_ctx_stream(self.handle) or 0)
+
+    def sync(self) -> None:
+        self.check(self.lib.grada_sync(self.handle))
+
+    def device_bytes(self) -> int:
+        return int(self.lib.grada_ctx_device_bytes(self.handle))
+
+    def fp64_peak(self) -> float:
+        out = ctypes.c_double()
+        self.check(self.lib.grada_measure_fp64_peak(self.handle, ctypes.byref(out)))
+        return out.value
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.grada_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Fwd:
+    """GPU-backed counterpart of the reference ``Fwd`` class."""
+
+    def __init__(self, prisms, obs, field_flag, ctx: Context | None = None):
+        self.ctx = ctx or Context()
+        self.set_geometry(prisms, obs, field_flag)
+
+    # Fwd::set_mesh / set_observation / set_field_flag
+    def set_geometry(self, prisms, obs, field_flag) -> None:
+        if not isinstance(field_flag, (int, np.integer)):
+            field_flag = field_mask(field_flag)
+        self.prisms = np.ascontiguousarray(prisms, dtype=np.float64).reshape(-1, 6)
+        self.obs = np.ascontiguousarray(obs, dtype=np.float64).reshape(-1, 3)
+        self.field_flag = int(field_flag)
+        self.ctx.check(
+            self.ctx.lib.grada_set_geometry(
+                self.ctx.handle, _ptr(self.prisms), self.prisms.shape[0], _ptr(self.obs),
+                self.obs.shape[0], self.field_flag,
+            )
+        )
+        self._dims()
+
+    def _dims(self) -> None:
+        nc, no, nd, ld = (ctypes.c_int64() for _ in range(4))
+        nf = ctypes.c_int()
+        self.ctx.check(
+            self.ctx.lib.grada_get_dims(
+                self.ctx.handle, ctypes.byref(nc), ctypes.byref(no), ctypes.byref(nf),
+                ctypes.byref(nd), ctypes.byref(ld),
+            )
+        )
+        self.Nm, self.N_obs, self.n_fields, self.Nd, self.ld = nc.value, no.value, nf.value, nd.value, ld.value
+
+    def get_n_fields(self) -> int:
+        return self.n_fields
+
+    def compute_G(self, storage: str | int = "fp64") -> None:
+        s = STORAGE[storage] if isinstance(storage, str) else int(storage)
+        self.ctx.check(self.ctx.lib.grada_compute_G(self.ctx.handle, s))
+
+    def get_G(self) -> np.ndarray:
+        """G as an (Nd, Nm) float64 array in column-major (Fortran) order."""
+        out = np.empty((self.ld, self.Nm), dtype=np.float64, order="F")
+        self.ctx.check(self.ctx.lib.grada_get_G(self.ctx.handle, _ptr(out), self.ld))
+        return out[: self.Nd, :]
+
+    def G_vec_mul(self, vec) -> np.ndarray:
+        x = np.ascontiguousarray(vec, dtype=np.float64)
+        if x.shape != (self.Nm,):
+            raise ValueError(f"expected a vector of {self.Nm} cells")
+        y = np.empty(self.Nd, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.grada_G_vec_mul(self.ctx.handle, _ptr(x), _ptr(y)))
+        return y
+
+    def GT_vec_mul(self, vec) -> np.ndarray:
+        y = np.ascontiguousarray(vec, dtype=np.float64)
+        if y.shape != (self.Nd,):
+            raise ValueError(f"expected a vector of {self.Nd} data")
+        x = np.empty(self.Nm, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.grada_GT_vec_mul(self.ctx.handle, _ptr(y), _ptr(x)))
+        return x
+
+    def forward_field(self, rho) -> np.ndarray:
+        """compute.cpp field sum: (N_obs, n_fields) array, components in bit order."""
+        r = np.ascontiguousarray(rho, dtype=np.float64)
+        if r.shape != (self.Nm,):
+            raise ValueError(f"expected a density per cell ({self.Nm})")
+        out = np.empty((self.N_obs, self.n_fields), dtype=np.float64)
+        self.ctx.check(self.ctx.lib.grada_forward_field(self.ctx.handle, _ptr(r), _ptr(out)))
+        return out

@@ -1,0 +1,260 @@
+"""Generate the golden fixtures under tests/golden/ from the reference.
+
+Run in a checkout that has the reference tree (default /root/reference) after
+``make -C oracle all ref``:
+
+    python tests/golden/make_golden.py [--ref /root/reference] [--only NAME]
+
+Fixtures written (all .npz):
+  forward_models.npz  the reference's committed noise-free forward fields
+                      (Examples/Forward_modelling/{model1,model2,model3}/result/
+                      data_no_noise and tests/test_compute/result_no_noise) with
+                      the observation points read from the same files and the
+                      density model rebuilt from the anomaly lists the
+                      examples' makeModel calls use.
+  ref_fields.npz      G blocks (all ten components) from the reference's own
+                      GravFormula, compiled from its sources into
+                      oracle/_ref/ref_fields, on seeded geometries including
+                      degenerate ones (points on cell-face planes and above
+                      vertical edges, far-away cells).
+  ref_inversion_*.npz regular-mesh inversion problems with the reference's
+                      G, host-built operators, one solve_cg call and a full
+                      invert_with_own_CG run (oracle/_ref/ref_inversion).
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import re
+import struct
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+REF_BIN = REPO / "oracle" / "_ref"
+
+# ---------------------------------------------------------------------------
+# forward models from Examples/Forward_modelling
+# ---------------------------------------------------------------------------
+
+FIELD_BIT = {"V": 0, "gz": 1, "gx": 2, "gy": 3, "Tzz": 4, "Txz": 5, "Tyz": 6, "Txx": 7, "Txy": 8,
+             "Tyy": 9}
+HEADER_FIELD = {"g_z": "gz", "g_x": "gx", "g_y": "gy", "T_zz": "Tzz", "T_xz": "Txz",
+                "T_yz": "Tyz", "T_xx": "Txx", "T_xy": "Txy", "T_yy": "Tyy", "V": "V"}
+
+
+def parse_make_model(script: str):
+    """-R x0/x1/y0/y1/z0/z1 --nx --ny --nz and -a boxes of the first makeModel line."""
+    for line in script.splitlines():
+        line = line.split("#", 1)[0]
+        if "makeModel" not in line:
+            continue
+        R = re.search(r"-R\s+(\S+)", line).group(1).split("/")
+        nx = int(re.search(r"--nx\s+(\d+)", line).group(1))
+        ny = int(re.search(r"--ny\s+(\d+)", line).group(1))
+        nz = int(re.search(r"--nz\s+(\d+)", line).group(1))
+        boxes = [list(map(float, a.split("/"))) for a in re.findall(r"-a\s+(\S+)", line)]
+        afile = re.search(r"-A\s+(\S+)", line)
+        return [float(v) for v in R], (nx, ny, nz), boxes, (afile.group(1) if afile else None)
+    raise ValueError("no makeModel line")
+
+
+def read_anomaly_file(path: Path):
+    boxes = []
+    for line in path.read_text().splitlines():
+        line = line.split("#", 1)[0].strip()
+        if line:
+            boxes.append([float(v) for v in line.split()[:7]])
+    return boxes
+
+
+def read_data_file(path: Path):
+    lines = path.read_text().splitlines()
+    header = lines[0]
+    names = [HEADER_FIELD[m] for m in re.findall(r"([gT]_[xyz]{1,2}|V) \(", header)]
+    arr = np.array([[float(v) for v in l.split()] for l in lines[1:] if l.strip()])
+    return names, arr[:, :3], arr[:, 3:]
+
+
+def forward_models(ref: Path) -> None:
+    ex = ref / "Examples" / "Forward_modelling"
+    cases = {
+        "model1": (ex / "model1" / "build_density_model2.sh", ex / "model1" / "result" / "data_no_noise"),
+        "model2": (ex / "model2" / "build_density_model.sh", ex / "model2" / "result" / "data_no_noise"),
+        "model3": (ex / "model3" / "build_density_model.sh", ex / "model3" / "result" / "data_no_noise"),
+        "test_compute": (ex / "tests" / "test_make_model" / "build.sh",
+                         ex / "tests" / "test_compute" / "result_no_noise"),
+    }
+    out = {}
+    for name, (script, data) in cases.items():
+        R, n, boxes, afile = parse_make_model(script.read_text())
+        if afile:
+            boxes = read_anomaly_file(script.parent / afile)
+        names, obs, fields = read_data_file(data)
+        mask = 0
+        for f in names:
+            mask |= 1 << FIELD_BIT[f]
+        # the file lists components in the order compute.cpp writes them, which is
+        # ascending field-bit order
+        assert [FIELD_BIT[f] for f in names] == sorted(FIELD_BIT[f] for f in names)
+        out[f"{name}_region"] = np.array(R)
+        out[f"{name}_n"] = np.array(n, dtype=np.int64)
+        out[f"{name}_boxes"] = np.array(boxes)
+        out[f"{name}_obs"] = obs
+        out[f"{name}_fields"] = fields
+        out[f"{name}_mask"] = np.array(mask, dtype=np.int64)
+        print(f"{name}: {len(boxes)} boxes, {obs.shape[0]} points, fields {names}")
+    out["cases"] = np.array(list(cases))
+    np.savez_compressed(HERE / "forward_models.npz", **out)
+
+
+# ---------------------------------------------------------------------------
+# G blocks from the compiled reference kernels
+# ---------------------------------------------------------------------------
+
+
+def run_ref_fields(prisms: np.ndarray, obs: np.ndarray, mask: int) -> np.ndarray:
+    exe = REF_BIN / "ref_fields"
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
+        with open(fin, "wb") as f:
+            f.write(struct.pack("<qqI", prisms.shape[0], obs.shape[0], mask))
+            f.write(np.ascontiguousarray(prisms, dtype="<f8").tobytes())
+            f.write(np.ascontiguousarray(obs, dtype="<f8").tobytes())
+        subprocess.run([str(exe), str(fin), str(fout)], check=True)
+        nf = bin(mask).count("1")
+        G = np.fromfile(fout, dtype="<f8").reshape(prisms.shape[0], nf * obs.shape[0]).T
+    return np.asfortranarray(G)
+
+
+def regular_prisms(xl, yl, zl, nx, ny, nz):
+    """Cells of Mesh::generate_regular_mesh in leaf order (x outer, z inner)."""
+    def pts(a, b, n):
+        step = (b - a) / n
+        v = a + step * np.arange(n + 1)
+        v[-1] = b
+        return v
+    xs, ys, zs = pts(*xl, nx), pts(*yl, ny), pts(*zl, nz)
+    out = np.empty((nx * ny * nz, 6))
+    idx = 0
+    for i in range(nx):
+        for j in range(ny):
+            for k in range(nz):
+                out[idx] = [xs[i], xs[i + 1], ys[j], ys[j + 1], zs[k], zs[k + 1]]
+                idx += 1
+    return out
+
+
+def exact_field(ob, pr):
+    """Closed-form corner sums of 1/r's antiderivatives (see prism.cuh) in
+    40-digit arithmetic: an independent, cancellation-free value of all ten
+    components for one (point, prism) pair."""
+    import mpmath as mp
+
+    mp.mp.dps = 40
+    g0 = mp.mpf("6.673e-11")
+    px, py, pz = (mp.mpf(float(v)) for v in ob)
+    X = [mp.mpf(float(pr[0])) - px, mp.mpf(float(pr[1])) - px]
+    Y = [mp.mpf(float(pr[2])) - py, mp.mpf(float(pr[3])) - py]
+    Z = [mp.mpf(float(pr[4])) - pz, mp.mpf(float(pr[5])) - pz]
+    acc = [mp.mpf(0)] * 10
+
+    def at(b, a):  # atan(b/a); a == 0 terms cancel between the faces they touch
+        return mp.mpf(0) if a == 0 else mp.atan(b / a)
+
+    def ln(v):  # only reached with v > 0 for points outside the prism
+        return mp.log(v) if v > 0 else mp.mpf(0)
+
+    for i in range(2):
+        for j in range(2):
+            for k in range(2):
+                x, y, z = X[i], Y[j], Z[k]
+                s = (-1) ** (i + j + k + 1)
+                r = mp.sqrt(x * x + y * y + z * z)
+                lx, ly, lz = ln(x + r), ln(y + r), ln(z + r)
+                ax, ay, az = at(y * z, x * r), at(x * z, y * r), at(x * y, z * r)
+                v = [x * y * lz + y * z * lx + z * x * ly - x * x * ax / 2 - y * y * ay / 2 - z * z * az / 2,
+                     -(x * ly + y * lx - z * az), -(y * lz + z * ly - x * ax), -(z * lx + x * lz - y * ay),
+                     -az, ly, lx, -ax, lz, -ay]
+                for c in range(10):
+                    acc[c] += s * v[c]
+    sc = [g0] + [g0 * 100000] * 3 + [g0 * 1000000000] * 6
+    return np.array([float(acc[c] * sc[c]) for c in range(10)])
+
+
+def exact_G(prisms, obs):
+    n = obs.shape[0]
+    E = np.zeros((10 * n, prisms.shape[0]), order="F")
+    for i in range(n):
+        for j in range(prisms.shape[0]):
+            e = exact_field(obs[i], prisms[j])
+            for k in range(10):
+                E[i + k * n, j] = e[k]
+    return E
+
+
+def ref_fields() -> None:
+    rng = np.random.default_rng(20240601)
+    cases = {}
+    # (a) random prisms, random points above them
+    n = 64
+    x0 = rng.uniform(-2000, 2000, n); dx = rng.uniform(20, 600, n)
+    y0 = rng.uniform(-2000, 2000, n); dy = rng.uniform(20, 600, n)
+    z0 = rng.uniform(0, 1500, n); dz = rng.uniform(20, 600, n)
+    pr = np.stack([x0, x0 + dx, y0, y0 + dy, z0, z0 + dz], 1)
+    ob = np.stack([rng.uniform(-2500, 2500, 48), rng.uniform(-2500, 2500, 48),
+                   -rng.uniform(0.05, 300, 48)], 1)
+    cases["random"] = (pr, ob)
+    # (b) regular mesh with points on the cell-face planes (x, y multiples of the cell size)
+    pr = regular_prisms((0.0, 400.0), (0.0, 300.0), (0.0, 200.0), 4, 3, 2)
+    gx, gy = np.meshgrid(np.arange(-100.0, 501.0, 100.0), np.arange(-100.0, 401.0, 50.0), indexing="xy")
+    ob = np.stack([gx.ravel(), gy.ravel(), np.full(gx.size, -0.1)], 1)
+    cases["coincident"] = (pr, ob)
+    # (c) far field: 50 m cells seen from 20-60 km away
+    pr = regular_prisms((0.0, 100.0), (0.0, 100.0), (0.0, 100.0), 2, 2, 2)
+    ang = rng.uniform(0, 2 * np.pi, 24); dist = rng.uniform(2e4, 6e4, 24)
+    ob = np.stack([dist * np.cos(ang), dist * np.sin(ang), -rng.uniform(1, 500, 24)], 1)
+    cases["far"] = (pr, ob)
+    # (d) points above vertical edges and above the centre of a cell
+    pr = np.array([[0.0, 100.0, 0.0, 80.0, 10.0, 60.0], [100.0, 250.0, 0.0, 80.0, 10.0, 60.0]])
+    ob = np.array([[0.0, 0.0, -5.0], [100.0, 80.0, -0.1], [50.0, 40.0, -1.0], [250.0, 0.0, -20.0],
+                   [100.0, 40.0, -0.5], [175.0, 0.0, -3.0]])
+    cases["edges"] = (pr, ob)
+    out = {}
+    for name, (pr, ob) in cases.items():
+        G = run_ref_fields(pr, ob, 0x3FF)
+        out[f"{name}_prisms"] = pr
+        out[f"{name}_obs"] = ob
+        out[f"{name}_G"] = G
+        out[f"{name}_exact"] = exact_G(pr, ob)
+        print(f"ref_fields {name}: G {G.shape}")
+    out["cases"] = np.array(list(cases))
+    np.savez_compressed(HERE / "ref_fields.npz", **out)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args()
+    ref = Path(a.ref)
+    jobs = {"forward_models": lambda: forward_models(ref), "ref_fields": ref_fields}
+    try:
+        from inversion_cases import inversion_fixtures  # noqa: E402
+        jobs["ref_inversion"] = inversion_fixtures
+    except ImportError:
+        pass
+    for name, fn in jobs.items():
+        if a.only and a.only != name:
+            continue
+        fn()
+
+
+if __name__ == "__main__":
+    sys.path.insert(0, str(HERE))
+    main()
