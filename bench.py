@@ -317,8 +317,31 @@ def run_gpu(args):
     ctx.close()
 
 
+def run_profile_case(args):
+    """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
+    50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
+    benchmark domain), nine components, one FP64 assembly, then the dense
+    products on it."""
+    from graada3d_gb300 import Fwd, mesh
+
+    prisms = mesh.regular_mesh((0.0, 20000.0), 16, (0.0, 20000.0), 16, (0.0, 8000.0), 16)
+    obs = mesh.observation_grid(32, 0.0, 20000.0, 32, 0.0, 20000.0, -50.0)
+    f = Fwd(prisms, obs, MASK)
+    t0 = time.perf_counter()
+    f.compute_G("fp64")
+    dt = time.perf_counter() - t0
+    x = np.ones(f.Nm)
+    y = f.G_vec_mul(x)
+    z = f.GT_vec_mul(y)
+    assert np.isfinite(z).all()
+    print(json.dumps({"case": "profile", "pairs": f.N_obs * f.Nm, "entries": f.Nd * f.Nm,
+                      "assemble_s": dt}))
+    f.ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default="bench", choices=["bench", "profile"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -326,7 +349,9 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.case == "profile":
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -71,7 +71,8 @@ DevG Context::devG() const {
   DevG d;
   d.kind = (GKind)g_storage;
   d.data = G.ptr;
-  d.row_scale = row_scale.as<float>();
+  // The scale buffer may be left over from an earlier bf16 G; only bf16 uses it.
+  d.row_scale = (g_storage == GRADA_G_BF16_ROWSCALE) ? row_scale.as<float>() : nullptr;
   d.nd = nd;
   d.nm = n_cells;
   d.ld = ld;
