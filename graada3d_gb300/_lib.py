@@ -47,7 +47,36 @@ SIGNATURES = {
     "grada_forward_field": (c_int, [c_void_p, _dp, _dp]),
     "grada_forward_field_dev": (c_int, [c_void_p, c_void_p, c_void_p]),
     "grada_measure_fp64_peak": (c_int, [c_void_p, _dp]),
+    "grada_set_operator": (c_int, [c_void_p, c_int, c_int64, c_int64, _ip32, _ip32, _dp]),
+    "grada_set_cross_gradient": (c_int, [c_void_p, c_int, c_double, _dp]),
+    "grada_set_data": (c_int, [c_void_p, _dp, _dp]),
+    "grada_solve_cg": (c_int, [c_void_p, c_double, c_int, c_double, _dp, _dp, _dp, POINTER(_dp), _dp,
+                               _dp, POINTER(c_int)]),
+    "grada_invert": (c_int, [c_void_p, c_void_p, _dp, _dp, _dp, _dp, _dp, c_void_p]),
+    "grada_get_trials": (c_int, [c_void_p, _dp, c_int64, _ip64]),
+    "grada_get_iterations": (c_int, [c_void_p, _dp, c_int64, _ip64]),
 }
+
+
+class InvertParams(ctypes.Structure):
+    """grada_invert_params (include/grada_gpu.h)."""
+
+    _fields_ = [
+        ("max_lambda", c_double), ("n_lambda", c_int), ("lambda_decreasing_rate", c_double),
+        ("target_misfit", c_double), ("stag_tol", c_double), ("cg_tol", c_double),
+        ("cg_iteration_factor", c_double), ("gn_iterations", c_int), ("lp_s", c_int),
+        ("lp_x", c_int), ("lp_y", c_int), ("lp_z", c_int), ("lp_t", c_int), ("epsilon2", c_double),
+        ("start_from_reference", c_int), ("fp64_refinement", c_int),
+    ]
+
+
+class InvertReport(ctypes.Structure):
+    """grada_invert_report (include/grada_gpu.h)."""
+
+    _fields_ = [
+        ("final_misfit", c_double), ("final_lambda", c_double), ("gn_iterations", c_int),
+        ("n_trials", c_int), ("cg_iterations", c_int64), ("fp64_refinements", c_int64),
+    ]
 
 _lib = None
 

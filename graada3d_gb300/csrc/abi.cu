@@ -172,7 +172,7 @@ void Context::forward_field_dev(const double *d_rho, double *d_fields) {
   const DevGeometry g = geometry();
   const int splits = forward_field_splits(g, sm_count);
   double *partial = scratch_doubles((int64_t)splits * n_obs * n_fields);
-  launch_forward_field(g, d_rho, splits, partial, d_fields, stream);
+  launch_forward_field(g, d_rho, splits, partial, d_fields, false, stream);
 }
 
 }  // namespace grada
@@ -357,6 +357,98 @@ int grada_measure_fp64_peak(grada_ctx *ctx, double *flops_per_s) {
     if (!flops_per_s) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null output");
     *flops_per_s = grada::measure_fp64_fma_rate(ctx->sm_count, ctx->stream);
   });
+}
+
+int grada_set_operator(grada_ctx *ctx, int which, int64_t n, int64_t nnz, const int *rowptr,
+                       const int *col, const double *val) {
+  return guarded(ctx, [&] { ctx->set_operator(which, n, nnz, rowptr, col, val); });
+}
+
+int grada_set_cross_gradient(grada_ctx *ctx, int enabled, double a_crg, const double *S_crg) {
+  return guarded(ctx, [&] { ctx->set_cross_gradient(enabled, a_crg, S_crg); });
+}
+
+int grada_set_data(grada_ctx *ctx, const double *dobs, const double *wd) {
+  return guarded(ctx, [&] { ctx->set_data(dobs, wd); });
+}
+
+int grada_solve_cg(grada_ctx *ctx, double tol, int maxit, double lambda, const double *mk,
+                   const double *mref, const double *P, const double *const WL[7], double *dx,
+                   double *err, int *iterations) {
+  return guarded(ctx, [&] {
+    ctx->require_G();
+    if (!mk || !mref || !P || !dx) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null vector");
+    if (!(lambda >= 0.0) || !std::isfinite(lambda))
+      throw Error(GRADA_ERR_INVALID_ARGUMENT, "lambda must be finite and >= 0");
+    const int64_t Nm = ctx->n_cells;
+    const size_t vb = sizeof(double) * Nm;
+    ctx->iv_m.alloc(ctx, vb);
+    ctx->iv_m0.alloc(ctx, vb);
+    ctx->iv_P.alloc(ctx, vb);
+    ctx->iv_dx.alloc(ctx, vb);
+    ctx->iv_wl.alloc(ctx, vb * 7);
+    ctx->upload(ctx->iv_m.ptr, mk, vb);
+    ctx->upload(ctx->iv_m0.ptr, mref, vb);
+    ctx->upload(ctx->iv_P.ptr, P, vb);
+    const double *wl_dev[7];
+    for (int k = 0; k < 7; k++) {
+      if (WL && WL[k]) {
+        double *d = ctx->iv_wl.as<double>() + k * Nm;
+        ctx->upload(d, WL[k], vb);
+        wl_dev[k] = d;
+      } else {
+        wl_dev[k] = nullptr;
+      }
+    }
+    grada::CgResult r = ctx->solve_cg_dev(lambda, tol, maxit, ctx->iv_m.as<double>(),
+                                          ctx->iv_m0.as<double>(), ctx->iv_P.as<double>(), wl_dev,
+                                          ctx->iv_dx.as<double>(), nullptr, nullptr);
+    ctx->download(dx, ctx->iv_dx.ptr, vb);
+    ctx->sync();
+    if (err) *err = r.err;
+    if (iterations) *iterations = r.iterations;
+  });
+}
+
+int grada_invert(grada_ctx *ctx, const grada_invert_params *params, const double *m_ini,
+                 const double *m_min, const double *m_max, const double *m0, double *m_out,
+                 grada_invert_report *report) {
+  return guarded(ctx, [&] {
+    if (!params) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null parameters");
+    grada_invert_report rep;
+    ctx->invert(*params, m_ini, m_min, m_max, m0, m_out, rep);
+    if (report) *report = rep;
+  });
+}
+
+int grada_get_trials(const grada_ctx *ctx, double *rows, int64_t cap, int64_t *n) {
+  if (!ctx) return GRADA_ERR_INVALID_ARGUMENT;
+  const int64_t total = (int64_t)ctx->trials.size();
+  if (n) *n = total;
+  for (int64_t k = 0; k < total && k < cap && rows; k++) {
+    const grada::TrialRecord &t = ctx->trials[k];
+    double *o = rows + 5 * k;
+    o[0] = t.gn_iteration;
+    o[1] = t.lambda;
+    o[2] = t.misfit;
+    o[3] = t.cg_iterations;
+    o[4] = t.cg_error;
+  }
+  return GRADA_OK;
+}
+
+int grada_get_iterations(const grada_ctx *ctx, double *rows, int64_t cap, int64_t *n) {
+  if (!ctx) return GRADA_ERR_INVALID_ARGUMENT;
+  const int64_t total = (int64_t)ctx->iterations.size();
+  if (n) *n = total;
+  for (int64_t k = 0; k < total && k < cap && rows; k++) {
+    const grada::IterationRecord &t = ctx->iterations[k];
+    double *o = rows + 3 * k;
+    o[0] = t.gn_iteration;
+    o[1] = t.n_trials;
+    o[2] = t.misfit;
+  }
+  return GRADA_OK;
 }
 
 }  // extern "C"

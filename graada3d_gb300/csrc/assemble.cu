@@ -153,13 +153,21 @@ __global__ void __launch_bounds__(FF_THREADS)
     if (mask & (1u << b)) out[slot++] = acc[b];
 }
 
+// Sums the per-split partials in split order.  With g_rows the result is
+// written in G's row order (component k of point i at k*n_obs + i) instead of
+// point-major order.
 __global__ void sum_splits_kernel(const double *__restrict__ partial, int n_split, int64_t n,
-                                  double *__restrict__ out) {
+                                  int nf, int64_t n_obs, int g_rows, double *__restrict__ out) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   double s = 0.0;
   for (int k = 0; k < n_split; k++) s += partial[(int64_t)k * n + e];
-  out[e] = s;
+  if (g_rows) {
+    const int64_t i = e / nf, c = e - i * nf;
+    out[c * n_obs + i] = s;
+  } else {
+    out[e] = s;
+  }
 }
 
 }  // namespace
@@ -205,7 +213,7 @@ int forward_field_splits(const DevGeometry &g, int sm_count) {
 }
 
 void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, double *partial,
-                          double *fields, cudaStream_t s) {
+                          double *fields, bool g_rows, cudaStream_t s) {
   if (g.n_obs <= 0) return;
   const int64_t per = round_up(ceil_div(g.n_cells, n_split), FF_CHUNK);
   dim3 grid((unsigned)n_split, (unsigned)ceil_div(g.n_obs, FF_THREADS));
@@ -214,7 +222,8 @@ void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, 
                                                    g.mask, g.n_fields, partial);
   GRADA_LAUNCH_CHECK();
   const int64_t n = g.n_obs * g.n_fields;
-  sum_splits_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(partial, n_split, n, fields);
+  sum_splits_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(partial, n_split, n, g.n_fields,
+                                                               g.n_obs, g_rows ? 1 : 0, fields);
   GRADA_LAUNCH_CHECK();
 }
 

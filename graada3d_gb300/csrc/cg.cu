@@ -1,0 +1,377 @@
+// K4-K7: the vector and sparse-operator kernels of the Gauss-Newton + CG
+// inversion (src/Inversion/GaussNewtonInversion.cpp:657-1698).
+//
+// All arithmetic is FP64.  Reductions are deterministic: each dot product is
+// a fixed grid of block partial sums followed by one block that adds the
+// partials in order, so repeated runs give bit-identical scalars.  The
+// sparse operators are the host-built regularisation matrices (CSR, <= 9
+// entries per row on the reference's meshes); one thread owns one row.
+#include "cg_kernels.h"
+#include "common.cuh"
+
+namespace grada {
+
+namespace {
+
+constexpr int VT = 256;  // threads per block for vector kernels
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double red[VT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (warp == 0) {
+    s = (lane < VT / 32) ? red[lane] : 0.0;
+    s = warp_sum(s);
+  }
+  __syncthreads();
+  return s;  // valid in thread 0
+}
+
+// y = c * wl .* (A (x - xs))    (wl, xs optional)
+__global__ void csr_apply_kernel(DevCSR A, const double *__restrict__ x,
+                                 const double *__restrict__ xs, double c,
+                                 const double *__restrict__ wl, double *__restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i >= A.n) return;
+  double acc = 0.0;
+  for (int k = A.rowptr[i]; k < A.rowptr[i + 1]; k++) {
+    const int j = A.col[k];
+    const double xv = xs ? (x[j] - xs[j]) : x[j];
+    acc = fma(A.val[k], xv, acc);
+  }
+  double v = c * acc;
+  if (wl) v *= wl[i];
+  y[i] = v;
+}
+
+// Forward regulariser rows for up to 7 terms in one launch (blockIdx.y = term).
+__global__ void multi_forward_kernel(ForwardTerms T, const double *__restrict__ x) {
+  const ForwardTerm &t = T.t[blockIdx.y];
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i >= t.A.n) return;
+  double acc = 0.0;
+  for (int k = t.A.rowptr[i]; k < t.A.rowptr[i + 1]; k++) acc = fma(t.A.val[k], x[t.A.col[k]], acc);
+  double v = t.c * acc;
+  if (t.wl) v *= t.wl[i];
+  t.out[i] = v;
+}
+
+// r = P .* (sign_g * gtw + sum_t c_t A_t^T (wl_t .* s_t)), A_t^T given as CSR.
+__global__ void adjoint_kernel(AdjointTerms T, int64_t n, const double *__restrict__ P,
+                               const double *__restrict__ gtw, double sign_g,
+                               double *__restrict__ r) {
+  const int64_t j = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (j >= n) return;
+  double acc = gtw ? sign_g * gtw[j] : 0.0;
+  for (int q = 0; q < T.count; q++) {
+    const AdjointTerm &t = T.t[q];
+    double s = 0.0;
+    for (int k = t.AT.rowptr[j]; k < t.AT.rowptr[j + 1]; k++) {
+      const int i = t.AT.col[k];
+      const double w = t.wl ? t.wl[i] : 1.0;
+      s = fma(t.AT.val[k], w * t.s[i], s);
+    }
+    acc = fma(t.c, s, acc);
+  }
+  r[j] = P ? P[j] * acc : acc;
+}
+
+__global__ void dot_partial_kernel(const double *__restrict__ a, const double *__restrict__ b,
+                                   int64_t n, double *__restrict__ partial) {
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT)
+    v = fma(a[i], b ? b[i] : a[i], v);
+  v = block_sum(v);
+  if (threadIdx.x == 0) partial[blockIdx.x] = v;
+}
+
+__global__ void sum_partials_kernel(const double *__restrict__ partial, int nblocks,
+                                    double *__restrict__ out) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nblocks; i += VT) v += partial[i];
+  v = block_sum(v);
+  if (threadIdx.x == 0) *out = v;
+}
+
+// b0 = wd .* (dobs - g);  s0 = -b0
+__global__ void data_residual_kernel(const double *__restrict__ dobs, const double *__restrict__ g,
+                                     const double *__restrict__ wd, int64_t n,
+                                     double *__restrict__ b0, double *__restrict__ s0) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i >= n) return;
+  const double v = wd[i] * (dobs[i] - g[i]);
+  b0[i] = v;
+  if (s0) s0[i] = -v;
+}
+
+__global__ void scale_kernel(const double *__restrict__ a, const double *__restrict__ w, int64_t n,
+                             double c, double *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i >= n) return;
+  out[i] = c * (w ? w[i] * a[i] : a[i]);
+}
+
+__global__ void negate_kernel(const double *__restrict__ a, int64_t n, double *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i < n) out[i] = -a[i];
+}
+
+// p = -r + beta p ;  pp = P .* p
+__global__ void p_update_kernel(const double *__restrict__ r, const double *__restrict__ P,
+                                const double *__restrict__ scal, int64_t n, double *__restrict__ p,
+                                double *__restrict__ pp) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i >= n) return;
+  const double beta = scal[CG_BETA];
+  const double v = -r[i] + beta * p[i];
+  p[i] = v;
+  pp[i] = P[i] * v;
+}
+
+// s += alpha t (nrow) ;  dx += alpha p (n)
+__global__ void axpy_kernel(const double *__restrict__ t, const double *__restrict__ p,
+                            const double *__restrict__ scal, int64_t nrow, int64_t n,
+                            double *__restrict__ s, double *__restrict__ dx) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  const double alpha = scal[CG_ALPHA];
+  if (i < nrow) s[i] = fma(alpha, t[i], s[i]);
+  if (i < n) dx[i] = fma(alpha, p[i], dx[i]);
+}
+
+__global__ void alpha_kernel(double *scal) {
+  // alpha = r2 / t2   (GaussNewtonInversion.cpp:1601)
+  scal[CG_ALPHA] = scal[CG_R2] / scal[CG_T2];
+}
+
+__global__ void beta_kernel(double *scal) {
+  // rlast2 = r2 ; r2 = ||r||^2 ; beta = r2/rlast2 ; err = r2/ATb2   (:1674-1684)
+  const double rlast2 = scal[CG_R2];
+  const double r2 = scal[CG_R2NEW];
+  scal[CG_RLAST2] = rlast2;
+  scal[CG_R2] = r2;
+  scal[CG_BETA] = r2 / rlast2;
+  scal[CG_ERR] = r2 / scal[CG_ATB2];
+}
+
+// Bound transform, GaussNewtonInversion.cpp:877-911.  Cells that hit the
+// infinity / zero-denominator guards are flagged; their values depend on a
+// neighbour updated earlier in the same sweep and are fixed sequentially.
+__global__ void bound_update_kernel(const double *__restrict__ m, const double *__restrict__ dx,
+                                    const double *__restrict__ mmin, const double *__restrict__ mmax,
+                                    int64_t n, double *__restrict__ mt, int *__restrict__ guard,
+                                    int *__restrict__ any_guard) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i >= n) return;
+  const double temp = exp(dx[i]);
+  const double temp2 = mmin[i] * (mmax[i] - m[i]) + mmax[i] * (m[i] - mmin[i]) * temp;
+  const double temp3 = (mmax[i] - m[i]) + (m[i] - mmin[i]) * temp;
+  int g = 0;
+  if (isinf(temp) || isinf(temp2)) g = 1;
+  else if (fabs(temp3) < 1e-10) g = 2;
+  guard[i] = g;
+  if (g) {
+    atomicOr(any_guard, 1);
+  } else {
+    mt[i] = temp2 / temp3;
+  }
+}
+
+// Sequential pass over guarded cells in index order (one thread).  mt_old is
+// m_trial before this sweep (the id == 0 branch reads the not-yet-updated
+// neighbour 1).
+__global__ void bound_fixup_kernel(const int *__restrict__ guard, const double *__restrict__ mmin,
+                                   const double *__restrict__ mmax,
+                                   const double *__restrict__ mt_old, int64_t n,
+                                   double *__restrict__ mt) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int64_t id = 0; id < n; id++) {
+    const int g = guard[id];
+    if (!g) continue;
+    double v;
+    if (g == 1) v = (mmax[id] - 1e-6 + mt_old[id]) / 2.0;
+    else v = (mmin[id] + 1e-6 + mt_old[id]) / 2.0;
+    if (id == 0) {
+      v = 0.5 * (v + (n > 1 ? mt_old[1] : v));
+    } else {
+      v = 0.5 * (v + mt[id - 1]);
+    }
+    mt[id] = v;
+  }
+}
+
+// P_ii = (mmax - m)(m - mmin)/(mmax - mmin)   (GaussNewtonInversion.cpp:856-861)
+__global__ void p_diag_kernel(const double *__restrict__ m, const double *__restrict__ mmin,
+                              const double *__restrict__ mmax, int64_t n, double *__restrict__ P) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i >= n) return;
+  const double nn = 1.0;
+  P[i] = nn * (mmax[i] - m[i]) * (m[i] - mmin[i]) / (mmax[i] - mmin[i]);
+}
+
+// WL_ii = (v_i^2 + eps2)^(-(2-p)/4)   (GaussNewtonInversion.cpp:962-1022)
+__global__ void irls_weight_kernel(const double *__restrict__ v, int64_t n, double eps2, double expo,
+                                   double *__restrict__ wl) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i >= n) return;
+  wl[i] = pow(v[i] * v[i] + eps2, expo);
+}
+
+__global__ void sub_kernel(const double *__restrict__ a, const double *__restrict__ b, int64_t n,
+                           double *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i < n) out[i] = a[i] - b[i];
+}
+
+__global__ void add_kernel(const double *__restrict__ a, const double *__restrict__ b, int64_t n,
+                           double *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
+  if (i < n) out[i] = a[i] + b[i];
+}
+
+// misfit partials: sum (wd (g - dobs))^2
+__global__ void misfit_partial_kernel(const double *__restrict__ g, const double *__restrict__ dobs,
+                                      const double *__restrict__ wd, int64_t n,
+                                      double *__restrict__ partial) {
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
+    const double e = wd[i] * (g[i] - dobs[i]);
+    v = fma(e, e, v);
+  }
+  v = block_sum(v);
+  if (threadIdx.x == 0) partial[blockIdx.x] = v;
+}
+
+unsigned blocks_for(int64_t n) { return (unsigned)std::max<int64_t>(1, ceil_div(n, VT)); }
+
+}  // namespace
+
+int dot_blocks(int64_t n, int sm_count) {
+  int64_t b = ceil_div(n, VT);
+  const int64_t cap = (int64_t)sm_count * 4;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+void launch_csr_apply(const DevCSR &A, const double *x, const double *xs, double c, const double *wl,
+                      double *y, cudaStream_t s) {
+  if (A.n <= 0) return;
+  csr_apply_kernel<<<blocks_for(A.n), VT, 0, s>>>(A, x, xs, c, wl, y);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_multi_forward(const ForwardTerms &T, int64_t n, const double *x, cudaStream_t s) {
+  if (T.count <= 0 || n <= 0) return;
+  dim3 grid(blocks_for(n), (unsigned)T.count);
+  multi_forward_kernel<<<grid, VT, 0, s>>>(T, x);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_adjoint(const AdjointTerms &T, int64_t n, const double *P, const double *gtw,
+                    double sign_g, double *r, cudaStream_t s) {
+  if (n <= 0) return;
+  adjoint_kernel<<<blocks_for(n), VT, 0, s>>>(T, n, P, gtw, sign_g, r);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_dot(const double *a, const double *b, int64_t n, double *partial, int nblocks,
+                double *out, cudaStream_t s) {
+  dot_partial_kernel<<<nblocks, VT, 0, s>>>(a, b, n, partial);
+  GRADA_LAUNCH_CHECK();
+  sum_partials_kernel<<<1, VT, 0, s>>>(partial, nblocks, out);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_misfit_sq(const double *g, const double *dobs, const double *wd, int64_t n,
+                      double *partial, int nblocks, double *out, cudaStream_t s) {
+  misfit_partial_kernel<<<nblocks, VT, 0, s>>>(g, dobs, wd, n, partial);
+  GRADA_LAUNCH_CHECK();
+  sum_partials_kernel<<<1, VT, 0, s>>>(partial, nblocks, out);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_data_residual(const double *dobs, const double *g, const double *wd, int64_t n,
+                          double *b0, double *s0, cudaStream_t s) {
+  data_residual_kernel<<<blocks_for(n), VT, 0, s>>>(dobs, g, wd, n, b0, s0);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_scale(const double *a, const double *w, int64_t n, double c, double *out,
+                  cudaStream_t s) {
+  scale_kernel<<<blocks_for(n), VT, 0, s>>>(a, w, n, c, out);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_negate(const double *a, int64_t n, double *out, cudaStream_t s) {
+  negate_kernel<<<blocks_for(n), VT, 0, s>>>(a, n, out);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_p_update(const double *r, const double *P, const double *scal, int64_t n, double *p,
+                     double *pp, cudaStream_t s) {
+  p_update_kernel<<<blocks_for(n), VT, 0, s>>>(r, P, scal, n, p, pp);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_axpy(const double *t, const double *p, const double *scal, int64_t nrow, int64_t n,
+                 double *sv, double *dx, cudaStream_t s) {
+  axpy_kernel<<<blocks_for(std::max(nrow, n)), VT, 0, s>>>(t, p, scal, nrow, n, sv, dx);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_alpha(double *scal, cudaStream_t s) {
+  alpha_kernel<<<1, 1, 0, s>>>(scal);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_beta(double *scal, cudaStream_t s) {
+  beta_kernel<<<1, 1, 0, s>>>(scal);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_bound_update(const double *m, const double *dx, const double *mmin, const double *mmax,
+                         int64_t n, double *mt, const double *mt_old, int *guard, int *any_guard,
+                         int *h_any_guard, cudaStream_t s) {
+  GRADA_CUDA_CHECK(cudaMemsetAsync(any_guard, 0, sizeof(int), s));
+  bound_update_kernel<<<blocks_for(n), VT, 0, s>>>(m, dx, mmin, mmax, n, mt, guard, any_guard);
+  GRADA_LAUNCH_CHECK();
+  GRADA_CUDA_CHECK(cudaMemcpyAsync(h_any_guard, any_guard, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GRADA_CUDA_CHECK(cudaStreamSynchronize(s));
+  if (*h_any_guard) {
+    bound_fixup_kernel<<<1, 1, 0, s>>>(guard, mmin, mmax, mt_old, n, mt);
+    GRADA_LAUNCH_CHECK();
+  }
+}
+
+void launch_p_diag(const double *m, const double *mmin, const double *mmax, int64_t n, double *P,
+                   cudaStream_t s) {
+  p_diag_kernel<<<blocks_for(n), VT, 0, s>>>(m, mmin, mmax, n, P);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_irls_weight(const double *v, int64_t n, double eps2, double expo, double *wl,
+                        cudaStream_t s) {
+  irls_weight_kernel<<<blocks_for(n), VT, 0, s>>>(v, n, eps2, expo, wl);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_sub(const double *a, const double *b, int64_t n, double *out, cudaStream_t s) {
+  sub_kernel<<<blocks_for(n), VT, 0, s>>>(a, b, n, out);
+  GRADA_LAUNCH_CHECK();
+}
+
+void launch_add(const double *a, const double *b, int64_t n, double *out, cudaStream_t s) {
+  add_kernel<<<blocks_for(n), VT, 0, s>>>(a, b, n, out);
+  GRADA_LAUNCH_CHECK();
+}
+
+}  // namespace grada

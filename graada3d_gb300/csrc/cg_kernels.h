@@ -1,0 +1,90 @@
+// Launchers of the inversion kernels (cg.cu).  Internal interface.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+namespace grada {
+
+// CSR matrix on the device, Eigen RowMajor compressed layout (int indices).
+struct DevCSR {
+  int64_t n = 0;
+  int64_t nnz = 0;
+  const int *rowptr = nullptr;
+  const int *col = nullptr;
+  const double *val = nullptr;
+};
+
+// out = c * wl .* (A x)
+struct ForwardTerm {
+  DevCSR A;
+  double c = 1.0;
+  const double *wl = nullptr;
+  double *out = nullptr;
+};
+struct ForwardTerms {
+  ForwardTerm t[7];
+  int count = 0;
+};
+
+// contribution c * A^T (wl .* s), with A^T stored as its own CSR
+struct AdjointTerm {
+  DevCSR AT;
+  double c = 1.0;
+  const double *wl = nullptr;
+  const double *s = nullptr;
+};
+struct AdjointTerms {
+  AdjointTerm t[7];
+  int count = 0;
+};
+
+// Slots of the device scalar array of one CG solve.
+enum : int {
+  CG_R2 = 0,
+  CG_T2 = 1,
+  CG_ALPHA = 2,
+  CG_BETA = 3,
+  CG_RLAST2 = 4,
+  CG_ERR = 5,
+  CG_ATB2 = 6,
+  CG_R2NEW = 7,
+  CG_MISFIT2 = 8,
+  CG_NSCALARS = 16
+};
+
+int dot_blocks(int64_t n, int sm_count);
+
+void launch_csr_apply(const DevCSR &A, const double *x, const double *xs, double c, const double *wl,
+                      double *y, cudaStream_t s);
+void launch_multi_forward(const ForwardTerms &T, int64_t n, const double *x, cudaStream_t s);
+void launch_adjoint(const AdjointTerms &T, int64_t n, const double *P, const double *gtw,
+                    double sign_g, double *r, cudaStream_t s);
+void launch_dot(const double *a, const double *b, int64_t n, double *partial, int nblocks,
+                double *out, cudaStream_t s);
+void launch_misfit_sq(const double *g, const double *dobs, const double *wd, int64_t n,
+                      double *partial, int nblocks, double *out, cudaStream_t s);
+void launch_data_residual(const double *dobs, const double *g, const double *wd, int64_t n,
+                          double *b0, double *s0, cudaStream_t s);
+void launch_scale(const double *a, const double *w, int64_t n, double c, double *out,
+                  cudaStream_t s);
+void launch_negate(const double *a, int64_t n, double *out, cudaStream_t s);
+void launch_p_update(const double *r, const double *P, const double *scal, int64_t n, double *p,
+                     double *pp, cudaStream_t s);
+void launch_axpy(const double *t, const double *p, const double *scal, int64_t nrow, int64_t n,
+                 double *sv, double *dx, cudaStream_t s);
+void launch_alpha(double *scal, cudaStream_t s);
+void launch_beta(double *scal, cudaStream_t s);
+void launch_bound_update(const double *m, const double *dx, const double *mmin, const double *mmax,
+                         int64_t n, double *mt, const double *mt_old, int *guard, int *any_guard,
+                         int *h_any_guard, cudaStream_t s);
+void launch_p_diag(const double *m, const double *mmin, const double *mmax, int64_t n, double *P,
+                   cudaStream_t s);
+void launch_irls_weight(const double *v, int64_t n, double eps2, double expo, double *wl,
+                        cudaStream_t s);
+void launch_sub(const double *a, const double *b, int64_t n, double *out, cudaStream_t s);
+void launch_add(const double *a, const double *b, int64_t n, double *out, cudaStream_t s);
+
+}  // namespace grada

@@ -7,7 +7,10 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
+#include "../../include/grada_gpu.h"
+#include "cg_kernels.h"
 #include "kernels.h"
 
 namespace grada {
@@ -31,6 +34,36 @@ struct DevBuf {
   }
 };
 
+// A host-built sparse operator and its transpose on the device.
+struct DevOperator {
+  DevBuf rowptr, col, val, t_rowptr, t_col, t_val;
+  int64_t n = 0, nnz = 0;
+  bool set = false;
+  DevCSR A() const;
+  DevCSR AT() const;
+};
+
+// One lambda trial of the Gauss-Newton loop (a line of lambda_misfit_GN).
+struct TrialRecord {
+  int gn_iteration;
+  double lambda;
+  double misfit;
+  int cg_iterations;
+  double cg_error;
+};
+
+// One Gauss-Newton iteration (a line of Iteration_misfit_GN).
+struct IterationRecord {
+  int gn_iteration;
+  int n_trials;
+  double misfit;
+};
+
+struct CgResult {
+  double err = 0.0;
+  int iterations = 0;
+};
+
 struct Context {
   int device = 0;
   int sm_count = 0;
@@ -51,15 +84,46 @@ struct Context {
   // Work space.
   DevBuf scratch, vx, vy;
 
-  void release_all() {
-    prisms.release();
-    obs.release();
-    G.release();
-    row_scale.release();
-    scratch.release();
-    vx.release();
-    vy.release();
-  }
+  // Inversion data (InversionBase / GaussNewtonInversion members).
+  // Operator slots follow GRADA_OP_*: Ws, Wx, Wy, Wz, Tx, Ty, Tz (the T slots
+  // hold the unscaled set_Tmatrix() operators; crg[] the a_crg*S_crg*T ones).
+  DevOperator ops[7];
+  DevOperator crg[3];
+  std::vector<int> host_T_rowptr[3], host_T_col[3];
+  std::vector<double> host_T_val[3];
+  bool crg_enabled = false;
+  double a_crg = 1.0;
+  std::vector<double> s_crg;
+  DevBuf dobs, wd;
+  bool data_set = false;
+
+  // CG work vectors.
+  DevBuf cg_b, cg_s, cg_t, cg_p, cg_pp, cg_r, cg_atb, cg_gtw, cg_gx, cg_tmpd, cg_scal, cg_part;
+  DevBuf cg_wl_ones;
+  double *h_scal = nullptr;  // pinned
+  int *h_flag = nullptr;     // pinned
+
+  // Inversion work vectors and records.
+  DevBuf iv_m, iv_mt, iv_mt_old, iv_mopt, iv_dx, iv_P, iv_mmin, iv_mmax, iv_m0, iv_wl, iv_tmp,
+      iv_tmp2, iv_dpre, iv_d64, iv_mstart, iv_guard, iv_flag;
+  std::vector<TrialRecord> trials;
+  std::vector<IterationRecord> iterations;
+
+  void release_all();
+
+  // inversion.cu
+  void set_operator(int which, int64_t n, int64_t nnz, const int *rowptr, const int *col,
+                    const double *val);
+  void set_cross_gradient(int enabled, double a, const double *S);
+  void set_data(const double *h_dobs, const double *h_wd);
+  void ensure_cg_workspace(int nterms);
+  void data_prediction(const double *m, const double *m_start, const double *d64, double *out);
+  CgResult solve_cg_dev(double lambda, double tol, int maxit, const double *mk, const double *mref,
+                        const double *P, const double *const WL[7], double *dx,
+                        const double *d64, const double *m_start);
+  double misfit_of(const double *m, const double *m_start, const double *d64);
+  void invert(const grada_invert_params &prm, const double *h_m_ini, const double *h_mmin,
+              const double *h_mmax, const double *h_m0, double *h_m_out, grada_invert_report &rep);
 
   void upload(void *dst, const void *src, size_t nbytes);
   void download(void *dst, const void *src, size_t nbytes);

@@ -1,0 +1,513 @@
+// Host orchestration of the Gauss-Newton + CG inversion on the device.
+//
+// Reference: GaussNewtonInversion::solve_cg (src/Inversion/
+// GaussNewtonInversion.cpp:1417-1698) and invert_with_own_CG (:657-1103).
+// The control flow (lambda search, stopping tests, IRLS updates) is the
+// reference's, line for line, on host scalars; every vector operation runs on
+// the device (cg.cu, gemv.cu) and only a few scalars per CG iteration cross to
+// the host (the stopping test needs ||r||^2 / ||A^T b||^2 there).
+//
+// Row segments of the stacked CG system, in the reference's order
+// (GaussNewtonInversion.cpp:1461-1471): data (Nd), Ws, Wz, Wx, Wy and, with
+// the cross-gradient constraint, Tz, Tx, Ty (Nm each).
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "common.cuh"
+#include "context.h"
+
+namespace grada {
+
+DevCSR DevOperator::A() const {
+  DevCSR c;
+  c.n = n;
+  c.nnz = nnz;
+  c.rowptr = rowptr.as<int>();
+  c.col = col.as<int>();
+  c.val = val.as<double>();
+  return c;
+}
+
+DevCSR DevOperator::AT() const {
+  DevCSR c;
+  c.n = n;
+  c.nnz = nnz;
+  c.rowptr = t_rowptr.as<int>();
+  c.col = t_col.as<int>();
+  c.val = t_val.as<double>();
+  return c;
+}
+
+void Context::release_all() {
+  prisms.release();
+  obs.release();
+  G.release();
+  row_scale.release();
+  scratch.release();
+  vx.release();
+  vy.release();
+  for (auto &o : ops) {
+    o.rowptr.release(); o.col.release(); o.val.release();
+    o.t_rowptr.release(); o.t_col.release(); o.t_val.release();
+  }
+  for (auto &o : crg) {
+    o.rowptr.release(); o.col.release(); o.val.release();
+    o.t_rowptr.release(); o.t_col.release(); o.t_val.release();
+  }
+  DevBuf *bufs[] = {&dobs, &wd, &cg_b, &cg_s, &cg_t, &cg_p, &cg_pp, &cg_r, &cg_atb, &cg_gtw,
+                    &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &iv_m, &iv_mt, &iv_mt_old,
+                    &iv_mopt, &iv_dx, &iv_P, &iv_mmin, &iv_mmax, &iv_m0, &iv_wl, &iv_tmp, &iv_tmp2,
+                    &iv_dpre, &iv_d64, &iv_mstart, &iv_guard, &iv_flag};
+  for (DevBuf *b : bufs) b->release();
+  if (h_scal) cudaFreeHost(h_scal);
+  if (h_flag) cudaFreeHost(h_flag);
+  h_scal = nullptr;
+  h_flag = nullptr;
+}
+
+namespace {
+
+// CSR (n x n) -> CSR of its transpose, by counting sort over columns (entries
+// of a transposed row come out in increasing original-row order).
+void transpose_csr(int64_t n, const int *rp, const int *ci, const double *v, std::vector<int> &trp,
+                   std::vector<int> &tci, std::vector<double> &tv) {
+  const int64_t nnz = rp[n];
+  trp.assign(n + 1, 0);
+  for (int64_t k = 0; k < nnz; k++) trp[ci[k] + 1]++;
+  for (int64_t i = 0; i < n; i++) trp[i + 1] += trp[i];
+  std::vector<int> pos(trp.begin(), trp.end() - 1);
+  tci.resize(nnz);
+  tv.resize(nnz);
+  for (int64_t r = 0; r < n; r++)
+    for (int k = rp[r]; k < rp[r + 1]; k++) {
+      const int c = ci[k];
+      tci[pos[c]] = (int)r;
+      tv[pos[c]] = v[k];
+      pos[c]++;
+    }
+}
+
+void upload_operator(Context *ctx, DevOperator &op, int64_t n, const int *rp, const int *ci,
+                     const double *v) {
+  const int64_t nnz = rp[n];
+  std::vector<int> trp, tci;
+  std::vector<double> tv;
+  transpose_csr(n, rp, ci, v, trp, tci, tv);
+  op.rowptr.alloc(ctx, sizeof(int) * (n + 1));
+  op.col.alloc(ctx, sizeof(int) * std::max<int64_t>(nnz, 1));
+  op.val.alloc(ctx, sizeof(double) * std::max<int64_t>(nnz, 1));
+  op.t_rowptr.alloc(ctx, sizeof(int) * (n + 1));
+  op.t_col.alloc(ctx, sizeof(int) * std::max<int64_t>(nnz, 1));
+  op.t_val.alloc(ctx, sizeof(double) * std::max<int64_t>(nnz, 1));
+  ctx->upload(op.rowptr.ptr, rp, sizeof(int) * (n + 1));
+  ctx->upload(op.col.ptr, ci, sizeof(int) * nnz);
+  ctx->upload(op.val.ptr, v, sizeof(double) * nnz);
+  ctx->upload(op.t_rowptr.ptr, trp.data(), sizeof(int) * (n + 1));
+  ctx->upload(op.t_col.ptr, tci.data(), sizeof(int) * nnz);
+  ctx->upload(op.t_val.ptr, tv.data(), sizeof(double) * nnz);
+  ctx->sync();  // host vectors go out of scope
+  op.n = n;
+  op.nnz = nnz;
+  op.set = true;
+}
+
+double *dptr(const DevBuf &b) { return b.as<double>(); }
+
+}  // namespace
+
+void Context::set_operator(int which, int64_t n, int64_t nnz, const int *rp, const int *ci,
+                           const double *v) {
+  require_geometry();
+  if (which < GRADA_OP_WS || which > GRADA_OP_TZ)
+    throw Error(GRADA_ERR_INVALID_ARGUMENT, "unknown operator slot");
+  if (n != n_cells) throw Error(GRADA_ERR_INVALID_ARGUMENT, "operator size differs from the cell count");
+  if (!rp || (nnz > 0 && (!ci || !v))) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null operator array");
+  if (rp[0] != 0 || rp[n] != nnz) throw Error(GRADA_ERR_INVALID_ARGUMENT, "rowptr does not match nnz");
+  for (int64_t r = 0; r < n; r++)
+    if (rp[r + 1] < rp[r]) throw Error(GRADA_ERR_INVALID_ARGUMENT, "rowptr not monotone");
+  for (int64_t k = 0; k < nnz; k++) {
+    if (ci[k] < 0 || ci[k] >= n) throw Error(GRADA_ERR_INVALID_ARGUMENT, "column index out of range");
+    if (!std::isfinite(v[k])) throw Error(GRADA_ERR_NONFINITE, "non-finite operator entry");
+  }
+  upload_operator(this, ops[which], n, rp, ci, v);
+  if (which >= GRADA_OP_TX) {
+    const int t = which - GRADA_OP_TX;
+    host_T_rowptr[t].assign(rp, rp + n + 1);
+    host_T_col[t].assign(ci, ci + nnz);
+    host_T_val[t].assign(v, v + nnz);
+    crg[t].set = false;  // rescaled on next use
+  }
+}
+
+void Context::set_cross_gradient(int enabled, double a, const double *S) {
+  require_geometry();
+  crg_enabled = enabled != 0;
+  a_crg = a;
+  if (S) s_crg.assign(S, S + n_cells);
+  else s_crg.clear();
+  for (auto &c : crg) c.set = false;
+}
+
+void Context::set_data(const double *h_dobs, const double *h_wd) {
+  require_geometry();
+  if (!h_dobs || !h_wd) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null data vector");
+  for (int64_t i = 0; i < nd; i++)
+    if (!std::isfinite(h_dobs[i]) || !std::isfinite(h_wd[i]))
+      throw Error(GRADA_ERR_NONFINITE, "non-finite observed datum or weight at row " + std::to_string(i));
+  dobs.alloc(this, sizeof(double) * nd);
+  wd.alloc(this, sizeof(double) * nd);
+  upload(dobs.ptr, h_dobs, sizeof(double) * nd);
+  upload(wd.ptr, h_wd, sizeof(double) * nd);
+  sync();
+  data_set = true;
+}
+
+void Context::ensure_cg_workspace(int nterms) {
+  const int64_t Nm = n_cells;
+  const int64_t nrow = nd + (int64_t)nterms * Nm;
+  cg_b.alloc(this, sizeof(double) * nrow);
+  cg_s.alloc(this, sizeof(double) * nrow);
+  cg_t.alloc(this, sizeof(double) * nrow);
+  cg_p.alloc(this, sizeof(double) * Nm);
+  cg_pp.alloc(this, sizeof(double) * Nm);
+  cg_r.alloc(this, sizeof(double) * Nm);
+  cg_atb.alloc(this, sizeof(double) * Nm);
+  cg_gtw.alloc(this, sizeof(double) * Nm);
+  cg_gx.alloc(this, sizeof(double) * ld);
+  cg_tmpd.alloc(this, sizeof(double) * ld);
+  cg_scal.alloc(this, sizeof(double) * CG_NSCALARS);
+  cg_part.alloc(this, sizeof(double) * (size_t)sm_count * 4);
+  if (!h_scal) GRADA_CUDA_CHECK(cudaMallocHost(&h_scal, sizeof(double) * CG_NSCALARS));
+  if (!h_flag) GRADA_CUDA_CHECK(cudaMallocHost(&h_flag, sizeof(int) * 4));
+  if (crg_enabled) {
+    for (int t = 0; t < 3; t++) {
+      if (crg[t].set) continue;
+      if (!ops[GRADA_OP_TX + t].set)
+        throw Error(GRADA_ERR_STATE, "cross-gradient constraint enabled but T operators not set");
+      // a_crg * S_crg * T0 (GaussNewtonInversion.cpp:1447-1449): row i scaled by a_crg*S_ii
+      std::vector<double> v = host_T_val[t];
+      const std::vector<int> &rp = host_T_rowptr[t];
+      for (int64_t r = 0; r < Nm; r++) {
+        const double sc = a_crg * (s_crg.empty() ? 1.0 : s_crg[r]);
+        for (int k = rp[r]; k < rp[r + 1]; k++) v[k] = sc * host_T_val[t][k];
+      }
+      upload_operator(this, crg[t], Nm, rp.data(), host_T_col[t].data(), v.data());
+    }
+  }
+}
+
+// d = G m in the precision of the stored G; with an FP64 reference prediction
+// d64 = G m_start: d = d64 + G (m - m_start) (the low-precision product only
+// carries the increment).
+void Context::data_prediction(const double *m, const double *m_start, const double *d64,
+                              double *out) {
+  if (d64) {
+    double *dm = dptr(iv_tmp2);
+    launch_sub(m, m_start, n_cells, dm, stream);
+    G_vec_mul_dev(dm, out);
+    launch_add(out, d64, nd, out, stream);
+  } else {
+    G_vec_mul_dev(m, out);
+  }
+}
+
+double Context::misfit_of(const double *m, const double *m_start, const double *d64) {
+  double *g = dptr(iv_dpre);
+  data_prediction(m, m_start, d64, g);
+  double *scal = dptr(cg_scal);
+  launch_misfit_sq(g, dptr(dobs), dptr(wd), nd, dptr(cg_part), dot_blocks(nd, sm_count),
+                   scal + CG_MISFIT2, stream);
+  GRADA_CUDA_CHECK(cudaMemcpyAsync(h_scal + CG_MISFIT2, scal + CG_MISFIT2, sizeof(double),
+                                   cudaMemcpyDeviceToHost, stream));
+  sync();
+  return std::sqrt(h_scal[CG_MISFIT2] / (double)nd);  // GaussNewtonInversion.cpp:784, :916
+}
+
+CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const double *mk,
+                               const double *mref, const double *P, const double *const WL[7],
+                               double *dx, const double *d64, const double *m_start) {
+  require_G();
+  if (!data_set) throw Error(GRADA_ERR_STATE, "observed data not set (grada_set_data)");
+  for (int t = 0; t < 4; t++)
+    if (!ops[t].set) throw Error(GRADA_ERR_STATE, "regularisation operators Ws/Wx/Wy/Wz not set");
+  const int nterms = crg_enabled ? 7 : 4;
+  ensure_cg_workspace(nterms);
+  const int64_t Nm = n_cells, Nd = nd, nrow = Nd + (int64_t)nterms * Nm;
+  const double sl = std::sqrt(lambda);
+  // WL in the reference argument order: s, x, y, z, tx, ty, tz
+  const double *WL_s = WL[0], *WL_x = WL[1], *WL_y = WL[2], *WL_z = WL[3];
+  const double *WL_tx = WL[4], *WL_ty = WL[5], *WL_tz = WL[6];
+  // segment operators in row order s, z, x, y, tz, tx, ty
+  const DevOperator *seg_op[7] = {&ops[GRADA_OP_WS], &ops[GRADA_OP_WZ], &ops[GRADA_OP_WX],
+                                  &ops[GRADA_OP_WY], &crg[2], &crg[0], &crg[1]};
+  double *b = dptr(cg_b), *s = dptr(cg_s), *t = dptr(cg_t);
+  double *p = dptr(cg_p), *pp = dptr(cg_pp), *r = dptr(cg_r), *atb = dptr(cg_atb);
+  double *gtw = dptr(cg_gtw), *gx = dptr(cg_gx), *tmpd = dptr(cg_tmpd);
+  double *scal = dptr(cg_scal), *part = dptr(cg_part);
+  auto seg = [&](double *base, int k) { return base + Nd + (int64_t)k * Nm; };
+  const int nb_m = dot_blocks(Nm, sm_count), nb_row = dot_blocks(nrow, sm_count);
+
+  // b and s = -b   (GaussNewtonInversion.cpp:1458-1472)
+  data_prediction(mk, m_start, d64, gx);
+  launch_data_residual(dptr(dobs), gx, dptr(wd), Nd, b, s, stream);
+  launch_csr_apply(seg_op[0]->A(), mk, mref, -sl, WL_s, seg(b, 0), stream);
+  launch_csr_apply(seg_op[1]->A(), mk, nullptr, -sl, WL_z, seg(b, 1), stream);
+  launch_csr_apply(seg_op[2]->A(), mk, nullptr, -sl, WL_x, seg(b, 2), stream);
+  launch_csr_apply(seg_op[3]->A(), mk, nullptr, -sl, WL_y, seg(b, 3), stream);
+  if (crg_enabled) {
+    launch_csr_apply(seg_op[4]->A(), mk, nullptr, -1.0, WL_tz, seg(b, 4), stream);
+    launch_csr_apply(seg_op[5]->A(), mk, nullptr, -1.0, WL_tx, seg(b, 5), stream);
+    launch_csr_apply(seg_op[6]->A(), mk, nullptr, -1.0, WL_ty, seg(b, 6), stream);
+  }
+  launch_negate(b + Nd, nrow - Nd, s + Nd, stream);
+
+  // A^T b and the initial r = A^T s (:1485-1551).  G^T(Wd s0) = -G^T(Wd b0)
+  // exactly, so one product serves both.
+  launch_scale(b, dptr(wd), Nd, 1.0, tmpd, stream);
+  GT_vec_mul_dev(tmpd, gtw);
+  const double adj_c[7] = {sl, sl, sl, sl, 1.0, 1.0, 1.0};
+  const double *adj_wl[7] = {WL_s, WL_z, WL_x, WL_y, WL_tz, WL_tx, WL_ty};
+  AdjointTerms AT_b, AT_s0, AT_s;
+  for (int k = 0; k < nterms; k++) {
+    AdjointTerm a;
+    a.AT = seg_op[k]->AT();
+    a.c = adj_c[k];
+    a.wl = adj_wl[k];
+    a.s = seg(b, k);
+    AT_b.t[k] = a;
+    a.s = seg(s, k);
+    AT_s.t[k] = a;
+    if (k == 6) a.wl = WL_y;  // the initial adjoint weights the crg-y rows by WL_y (:1508)
+    AT_s0.t[k] = a;
+  }
+  AT_b.count = AT_s.count = AT_s0.count = nterms;
+  launch_adjoint(AT_b, Nm, P, gtw, 1.0, atb, stream);
+  launch_adjoint(AT_s0, Nm, P, gtw, -1.0, r, stream);
+  launch_dot(atb, nullptr, Nm, part, nb_m, scal + CG_ATB2, stream);
+
+  GRADA_CUDA_CHECK(cudaMemsetAsync(p, 0, sizeof(double) * Nm, stream));
+  GRADA_CUDA_CHECK(cudaMemsetAsync(dx, 0, sizeof(double) * Nm, stream));
+  GRADA_CUDA_CHECK(cudaMemsetAsync(t, 0, sizeof(double) * nrow, stream));
+  GRADA_CUDA_CHECK(cudaMemsetAsync(scal + CG_BETA, 0, sizeof(double), stream));
+  launch_dot(r, nullptr, Nm, part, nb_m, scal + CG_R2, stream);
+
+  // forward rows of t = A p (:1569-1586): Ws row without WL_s, crg rows
+  // weighted by WL_z / WL_x / WL_y
+  const double fwd_c[7] = {sl, sl, sl, sl, 1.0, 1.0, 1.0};
+  const double *fwd_wl[7] = {nullptr, WL_z, WL_x, WL_y, WL_z, WL_x, WL_y};
+  ForwardTerms FT;
+  for (int k = 0; k < nterms; k++) {
+    FT.t[k].A = seg_op[k]->A();
+    FT.t[k].c = fwd_c[k];
+    FT.t[k].wl = fwd_wl[k];
+    FT.t[k].out = seg(t, k);
+  }
+  FT.count = nterms;
+
+  CgResult res;
+  int i = 0;
+  for (i = 0; i < maxit; i++) {
+    launch_p_update(r, P, scal, Nm, p, pp, stream);
+    G_vec_mul_dev(pp, gx);
+    launch_scale(gx, dptr(wd), Nd, 1.0, t, stream);
+    launch_multi_forward(FT, Nm, pp, stream);
+    launch_dot(t, nullptr, nrow, part, nb_row, scal + CG_T2, stream);
+    launch_alpha(scal, stream);
+    launch_axpy(t, p, scal, nrow, Nm, s, dx, stream);
+    launch_scale(s, dptr(wd), Nd, 1.0, tmpd, stream);
+    GT_vec_mul_dev(tmpd, gtw);
+    launch_adjoint(AT_s, Nm, P, gtw, 1.0, r, stream);
+    launch_dot(r, nullptr, Nm, part, nb_m, scal + CG_R2NEW, stream);
+    launch_beta(scal, stream);
+    GRADA_CUDA_CHECK(cudaMemcpyAsync(h_scal, scal, sizeof(double) * CG_NSCALARS,
+                                     cudaMemcpyDeviceToHost, stream));
+    sync();
+    res.err = h_scal[CG_ERR];
+    if (h_scal[CG_T2] == 0.0)
+      throw Error(GRADA_ERR_BREAKDOWN, "CG breakdown: ||t||^2 = 0 at iteration " + std::to_string(i));
+    if (!std::isfinite(h_scal[CG_ALPHA]) || !std::isfinite(res.err))
+      throw Error(GRADA_ERR_NONFINITE, "non-finite CG scalar at iteration " + std::to_string(i));
+    if (res.err < tol) {
+      res.iterations = i + 1;
+      return res;
+    }
+  }
+  res.iterations = maxit;
+  if (maxit <= 0) {
+    sync();
+    res.err = 0.0;
+  }
+  return res;
+}
+
+void Context::invert(const grada_invert_params &prm, const double *h_m_ini, const double *h_mmin,
+                     const double *h_mmax, const double *h_m0, double *h_m_out,
+                     grada_invert_report &rep) {
+  require_G();
+  if (!data_set) throw Error(GRADA_ERR_STATE, "observed data not set (grada_set_data)");
+  if (!h_m_ini || !h_mmin || !h_mmax || !h_m_out)
+    throw Error(GRADA_ERR_INVALID_ARGUMENT, "null model vector");
+  if (prm.n_lambda < 1 || prm.gn_iterations < 1)
+    throw Error(GRADA_ERR_INVALID_ARGUMENT, "n_lambda and gn_iterations must be >= 1");
+  const int64_t Nm = n_cells, Nd = nd;
+  std::memset(&rep, 0, sizeof(rep));
+  trials.clear();
+  iterations.clear();
+
+  // starting model (GaussNewtonInversion.cpp:757-786)
+  std::vector<double> m(Nm), mmin(h_mmin, h_mmin + Nm), mmax(h_mmax, h_mmax + Nm);
+  std::vector<double> m0(Nm, 0.0);
+  if (h_m0) m0.assign(h_m0, h_m0 + Nm);
+  for (int64_t i = 0; i < Nm; i++) {
+    if (!(mmin[i] < mmax[i])) throw Error(GRADA_ERR_INVALID_ARGUMENT, "m_min must be < m_max");
+    if (prm.start_from_reference) {
+      m[i] = m0[i];
+      if (m[i] > mmax[i] || std::abs(m[i] - mmax[i]) < 1e-7) m[i] = mmax[i] - 0.01;
+      if (m[i] < mmin[i] || std::abs(m[i] - mmin[i]) < 1e-7) m[i] = mmin[i] + 0.01;
+    } else {
+      m[i] = h_m_ini[i];
+      if (m[i] > mmax[i] || std::abs(m[i] - mmax[i]) < 1e-7) m[i] = 0.5 * (mmax[i] + mmin[i]);
+      if (m[i] < mmin[i] || std::abs(m[i] - mmin[i]) < 1e-7) m[i] = 0.5 * (mmax[i] + mmin[i]);
+    }
+  }
+  const size_t vb = sizeof(double) * Nm;
+  DevBuf *vecs[] = {&iv_m, &iv_mt, &iv_mt_old, &iv_mopt, &iv_dx, &iv_P, &iv_mmin, &iv_mmax,
+                    &iv_m0, &iv_tmp, &iv_tmp2, &iv_mstart};
+  for (DevBuf *b : vecs) b->alloc(this, vb);
+  iv_wl.alloc(this, vb * 7);
+  iv_dpre.alloc(this, sizeof(double) * ld);
+  iv_guard.alloc(this, sizeof(int) * Nm);
+  iv_flag.alloc(this, sizeof(int) * 4);
+  const bool refine = prm.fp64_refinement && g_storage != GRADA_G_FP64;
+  if (refine) iv_d64.alloc(this, sizeof(double) * ld);
+  ensure_cg_workspace(crg_enabled ? 7 : 4);
+  upload(iv_m.ptr, m.data(), vb);
+  upload(iv_mmin.ptr, mmin.data(), vb);
+  upload(iv_mmax.ptr, mmax.data(), vb);
+  upload(iv_m0.ptr, m0.data(), vb);
+  {
+    std::vector<double> ones(7 * Nm, 1.0);
+    upload(iv_wl.ptr, ones.data(), vb * 7);
+    sync();
+  }
+  double *dm = dptr(iv_m), *dmt = dptr(iv_mt), *dmt_old = dptr(iv_mt_old), *dmopt = dptr(iv_mopt);
+  double *ddx = dptr(iv_dx), *dP = dptr(iv_P), *dmin = dptr(iv_mmin), *dmax = dptr(iv_mmax);
+  double *dm0 = dptr(iv_m0), *dtmp = dptr(iv_tmp);
+  double *wlv = dptr(iv_wl);
+  // WL slots in the reference argument order s, x, y, z, tx, ty, tz
+  double *WLs = wlv, *WLx = wlv + Nm, *WLy = wlv + 2 * Nm, *WLz = wlv + 3 * Nm;
+  double *WLtx = wlv + 4 * Nm, *WLty = wlv + 5 * Nm, *WLtz = wlv + 6 * Nm;
+  const double *WL[7] = {WLs, WLx, WLy, WLz, WLtx, WLty, WLtz};
+  double *d64 = refine ? dptr(iv_d64) : nullptr;
+  double *mstart = dptr(iv_mstart);
+
+  auto refresh_fp64 = [&](const double *mref_point) {
+    // FP64 matrix-free prediction at the current model: the residual
+    // refinement step of the mixed-precision path
+    const DevGeometry g = geometry();
+    const int splits = forward_field_splits(g, sm_count);
+    double *partial = scratch_doubles((int64_t)splits * n_obs * n_fields);
+    launch_forward_field(g, mref_point, splits, partial, d64, true, stream);
+    GRADA_CUDA_CHECK(cudaMemcpyAsync(mstart, mref_point, vb, cudaMemcpyDeviceToDevice, stream));
+    rep.fp64_refinements++;
+  };
+  if (refine) refresh_fp64(dm);
+
+  double misfit = misfit_of(dm, mstart, d64);
+  double misfit_last_iteration = 5 * misfit;
+  (void)misfit_last_iteration;
+  double lambda = prm.max_lambda;
+  double lambda_opt = lambda;
+  double misfit_opt = misfit;
+  GRADA_CUDA_CHECK(cudaMemcpyAsync(dmopt, dm, vb, cudaMemcpyDeviceToDevice, stream));
+  const double rate = prm.lambda_decreasing_rate;
+  int i = 0, j = 0;
+  const double p_expo[5] = {-(2 - prm.lp_s) / 4.0, -(2 - prm.lp_x) / 4.0, -(2 - prm.lp_y) / 4.0,
+                            -(2 - prm.lp_z) / 4.0, -(2 - prm.lp_t) / 4.0};
+  for (i = 0; i < prm.gn_iterations; i++) {
+    GRADA_CUDA_CHECK(cudaMemcpyAsync(dmt, dm, vb, cudaMemcpyDeviceToDevice, stream));
+    double misfit_last1 = 10 * misfit;
+    double misfit_last2 = 100 * misfit;
+    misfit_last_iteration = misfit;
+    if (i == 0 || prm.n_lambda == 1 || std::abs(rate - 1) < 1e-6) {
+      lambda = prm.max_lambda;
+    } else {
+      lambda = lambda_opt * std::pow(1 / rate, std::min(3, prm.n_lambda - 2));
+      const double min_lambda = std::min(prm.max_lambda * std::pow(rate, 20), 1.0e-5);
+      if (lambda < min_lambda) lambda = 1.0;
+    }
+    int cg_maxit = 0;
+    if (prm.cg_iteration_factor < 1) cg_maxit = (int)(prm.cg_iteration_factor * Nm);
+    else cg_maxit = (int)prm.cg_iteration_factor;
+    if (refine && i > 0) refresh_fp64(dm);
+    launch_p_diag(dm, dmin, dmax, Nm, dP, stream);
+    for (j = 0; j < prm.n_lambda; j++) {
+      CgResult cg = solve_cg_dev(lambda, prm.cg_tol, cg_maxit, dm, dm0, dP, WL, ddx, d64, mstart);
+      rep.cg_iterations += cg.iterations;
+      GRADA_CUDA_CHECK(cudaMemcpyAsync(dmt_old, dmt, vb, cudaMemcpyDeviceToDevice, stream));
+      launch_bound_update(dm, ddx, dmin, dmax, Nm, dmt, dmt_old, iv_guard.as<int>(),
+                          iv_flag.as<int>(), h_flag, stream);
+      misfit_last2 = misfit_last1;
+      misfit_last1 = misfit;
+      misfit = misfit_of(dmt, mstart, d64);
+      trials.push_back({i + 1, lambda, misfit, cg.iterations, cg.err});
+      if (j == 0 || misfit < misfit_opt) {
+        misfit_opt = misfit;
+        GRADA_CUDA_CHECK(cudaMemcpyAsync(dmopt, dmt, vb, cudaMemcpyDeviceToDevice, stream));
+        if (i > 0) GRADA_CUDA_CHECK(cudaMemcpyAsync(dm, dmopt, vb, cudaMemcpyDeviceToDevice, stream));
+        lambda_opt = lambda;
+      }
+      if ((std::abs(misfit - misfit_last1) / std::min(misfit, misfit_last1) < prm.stag_tol) &&
+          (std::abs(misfit_last1 - misfit_last2) / std::min(misfit_last1, misfit_last2) < prm.stag_tol) &&
+          j > 1)
+        break;
+      if (misfit > misfit_last1 && misfit_last1 > misfit_last2 && j > 1) {
+        break;
+      } else {
+        lambda = lambda * rate;
+        // IRLS (:962-1022)
+        if (prm.lp_s != 2) {
+          launch_csr_apply(ops[GRADA_OP_WS].A(), dmopt, dm0, 1.0, nullptr, dtmp, stream);
+          launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[0], WLs, stream);
+        }
+        if (prm.lp_x != 2) {
+          launch_csr_apply(ops[GRADA_OP_WX].A(), dmopt, nullptr, 1.0, nullptr, dtmp, stream);
+          launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[1], WLx, stream);
+        }
+        if (prm.lp_y != 2) {
+          launch_csr_apply(ops[GRADA_OP_WY].A(), dmopt, nullptr, 1.0, nullptr, dtmp, stream);
+          launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[2], WLy, stream);
+        }
+        if (prm.lp_z != 2) {
+          launch_csr_apply(ops[GRADA_OP_WZ].A(), dmopt, nullptr, 1.0, nullptr, dtmp, stream);
+          launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[3], WLz, stream);
+        }
+        if (prm.lp_t != 2 && crg_enabled) {
+          double *wt[3] = {WLtx, WLty, WLtz};
+          for (int q = 0; q < 3; q++) {
+            launch_csr_apply(ops[GRADA_OP_TX + q].A(), dmopt, nullptr, 1.0, nullptr, dtmp, stream);
+            launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[4], wt[q], stream);
+          }
+        }
+      }
+      if (misfit < prm.target_misfit) break;
+    }
+    GRADA_CUDA_CHECK(cudaMemcpyAsync(dm, dmopt, vb, cudaMemcpyDeviceToDevice, stream));
+    misfit = misfit_opt;
+    iterations.push_back({i + 1, (j == prm.n_lambda) ? prm.n_lambda : (j + 1), misfit});
+    if (misfit < prm.target_misfit || i == prm.gn_iterations - 1) break;
+    const bool flag1 = std::abs(misfit - misfit_last_iteration) /
+                           std::min(misfit, misfit_last_iteration) < prm.stag_tol;
+    // no refinement on a fixed mesh: c_refinement (0) >= max_refinement_number (0)
+    if (flag1) break;
+  }
+  download(h_m_out, dm, vb);
+  sync();
+  rep.final_misfit = misfit;
+  rep.final_lambda = lambda;
+  rep.gn_iterations = (int)iterations.size();
+  rep.n_trials = (int)trials.size();
+}
+
+}  // namespace grada

@@ -35,7 +35,7 @@ void launch_rowscale_bf16(const float *G32, int64_t nd, int64_t nm, int64_t ld, 
 // `partial` must hold n_split * n_obs * nf doubles.
 int forward_field_splits(const DevGeometry &g, int sm_count);
 void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, double *partial,
-                          double *fields, cudaStream_t s);
+                          double *fields, bool g_rows, cudaStream_t s);
 
 // ---- dense products (gemv.cu) -------------------------------------------
 enum class GKind : int { FP64 = 0, FP32 = 1, BF16 = 2 };

@@ -1,0 +1,125 @@
+"""Python view of the reference's ``GaussNewtonInversion`` over the C ABI.
+
+Mirrors the members the hot path uses (src/Inversion/GaussNewtonInversion.h,
+InversionBase.h): ``set_dobs`` (data and Wd), the host-built regularisation
+operators, ``solve_cg`` and ``invert`` (invert_with_own_CG on a fixed mesh),
+plus the records the reference writes to lambda_misfit_GN and
+Iteration_misfit_GN.  The forward part (``compute_G``, products) is inherited
+from :class:`graada3d_gb300.fwd.Fwd`, as GaussNewtonInversion inherits Fwd.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from ._lib import InvertParams, InvertReport
+from .fwd import Fwd, _ptr
+
+OP_SLOTS = {"Ws": 0, "Wx": 1, "Wy": 2, "Wz": 3, "Tx": 4, "Ty": 5, "Tz": 6}
+WL_ORDER = ["s", "x", "y", "z", "tx", "ty", "tz"]
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+class GaussNewtonInversion(Fwd):
+    """GPU-backed counterpart of the reference GaussNewtonInversion."""
+
+    def set_dobs(self, dobs, wd) -> None:
+        """Observed data (Nd) and the diagonal of Wd (InversionBase::set_dobs)."""
+        self.dobs = np.ascontiguousarray(dobs, dtype=np.float64)
+        self.wd = np.ascontiguousarray(wd, dtype=np.float64)
+        if self.dobs.shape != (self.Nd,) or self.wd.shape != (self.Nd,):
+            raise ValueError(f"expected {self.Nd} data and weights")
+        self.ctx.check(self.ctx.lib.grada_set_data(self.ctx.handle, _ptr(self.dobs), _ptr(self.wd)))
+
+    def set_operator(self, name: str, A) -> None:
+        A = sp.csr_matrix(A)
+        A.sort_indices()
+        rp = np.ascontiguousarray(A.indptr, dtype=np.int32)
+        ci = np.ascontiguousarray(A.indices, dtype=np.int32)
+        v = np.ascontiguousarray(A.data, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.grada_set_operator(self.ctx.handle, OP_SLOTS[name], A.shape[0],
+                                                       v.size, _iptr(rp), _iptr(ci), _ptr(v)))
+
+    def set_operators(self, ops: dict) -> None:
+        for name in ["Ws", "Wx", "Wy", "Wz", "Tx", "Ty", "Tz"]:
+            if name in ops and ops[name] is not None:
+                self.set_operator(name, ops[name])
+
+    def set_cross_gradient(self, enabled: bool, a_crg: float = 1.0, S_crg=None) -> None:
+        S = None
+        if S_crg is not None:
+            self._s_crg = np.ascontiguousarray(S_crg, dtype=np.float64)
+            S = _ptr(self._s_crg)
+        self.ctx.check(self.ctx.lib.grada_set_cross_gradient(self.ctx.handle, int(bool(enabled)),
+                                                             float(a_crg), S))
+
+    def solve_cg(self, tol, maxit, lam, mk, mref, P, WL=None):
+        """GaussNewtonInversion::solve_cg; WL dict keyed s,x,y,z,tx,ty,tz (None = I).
+        Returns (dx, err, iterations)."""
+        vec = [np.ascontiguousarray(v, dtype=np.float64) for v in (mk, mref, P)]
+        wl_arrays = []
+        arr = (ctypes.POINTER(ctypes.c_double) * 7)()
+        for k, key in enumerate(WL_ORDER):
+            w = None if WL is None else WL.get(key)
+            if w is None:
+                arr[k] = ctypes.POINTER(ctypes.c_double)()
+            else:
+                w = np.ascontiguousarray(w, dtype=np.float64)
+                wl_arrays.append(w)
+                arr[k] = _ptr(w)
+        dx = np.empty(self.Nm)
+        err = ctypes.c_double()
+        it = ctypes.c_int()
+        self.ctx.check(self.ctx.lib.grada_solve_cg(
+            self.ctx.handle, float(tol), int(maxit), float(lam), _ptr(vec[0]), _ptr(vec[1]),
+            _ptr(vec[2]), arr, _ptr(dx), ctypes.byref(err), ctypes.byref(it)))
+        return dx, err.value, it.value
+
+    def invert(self, prm: dict, m_ini, m_min, m_max, m0=None, fp64_refinement: bool = False):
+        """invert_with_own_CG on the current G.  prm keys as oracle.inversion.invert
+        (max_lambda, n_lambda, rate, target, stag, cg_tol, cg_factor, gn_iter,
+        lp[5], eps2, start_from_reference).  Returns (m, report)."""
+        p = InvertParams()
+        p.max_lambda = prm["max_lambda"]
+        p.n_lambda = prm["n_lambda"]
+        p.lambda_decreasing_rate = prm["rate"]
+        p.target_misfit = prm["target"]
+        p.stag_tol = prm["stag"]
+        p.cg_tol = prm["cg_tol"]
+        p.cg_iteration_factor = prm["cg_factor"]
+        p.gn_iterations = prm["gn_iter"]
+        p.lp_s, p.lp_x, p.lp_y, p.lp_z, p.lp_t = (int(v) for v in prm["lp"])
+        p.epsilon2 = prm["eps2"]
+        p.start_from_reference = int(bool(prm.get("start_from_reference", False)))
+        p.fp64_refinement = int(bool(fp64_refinement))
+        vecs = [np.ascontiguousarray(v, dtype=np.float64) for v in (m_ini, m_min, m_max)]
+        m0a = None if m0 is None else np.ascontiguousarray(m0, dtype=np.float64)
+        out = np.empty(self.Nm)
+        rep = InvertReport()
+        self.ctx.check(self.ctx.lib.grada_invert(
+            self.ctx.handle, ctypes.byref(p), _ptr(vecs[0]), _ptr(vecs[1]), _ptr(vecs[2]),
+            None if m0a is None else _ptr(m0a), _ptr(out), ctypes.byref(rep)))
+        return out, {f: getattr(rep, f) for f, _ in InvertReport._fields_}
+
+    def trials(self) -> np.ndarray:
+        """(n, 5): gn_iteration, lambda, misfit, cg_iterations, cg_error."""
+        n = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.grada_get_trials(self.ctx.handle, None, 0, ctypes.byref(n)))
+        out = np.empty((n.value, 5))
+        self.ctx.check(self.ctx.lib.grada_get_trials(self.ctx.handle, _ptr(out), n.value,
+                                                     ctypes.byref(n)))
+        return out
+
+    def iterations(self) -> np.ndarray:
+        """(n, 3): gn_iteration, n_trials, misfit."""
+        n = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.grada_get_iterations(self.ctx.handle, None, 0, ctypes.byref(n)))
+        out = np.empty((n.value, 3))
+        self.ctx.check(self.ctx.lib.grada_get_iterations(self.ctx.handle, _ptr(out), n.value,
+                                                         ctypes.byref(n)))
+        return out

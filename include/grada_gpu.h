@@ -129,6 +129,100 @@ int grada_forward_field_dev(grada_ctx *ctx, const double *d_rho, double *d_field
  */
 int grada_measure_fp64_peak(grada_ctx *ctx, double *flops_per_s);
 
+/* ------------------------------------------------------------------------
+ * Inversion (GaussNewtonInversion on top of InversionBase / AdaptiveInversion)
+ * ------------------------------------------------------------------------ */
+
+/* Operator slots of grada_set_operator. */
+#define GRADA_OP_WS 0 /* a_s*S_s*V*D_s*Z   (GaussNewtonInversion.cpp:711) */
+#define GRADA_OP_WX 1 /* a_x*S_x*V*D_x1*Z  (:712) */
+#define GRADA_OP_WY 2 /* a_y*S_y*V*D_y1*Z  (:713) */
+#define GRADA_OP_WZ 3 /* a_z*S_z*V*D_z1*Z  (:714) */
+#define GRADA_OP_TX 4 /* T_x of InversionBase::set_Tmatrix (InversionBase.cpp:468-495) */
+#define GRADA_OP_TY 5 /* T_y */
+#define GRADA_OP_TZ 6 /* T_z */
+
+/*
+ * Uploads one host-built regularisation operator (Nm x Nm), in the compressed
+ * row storage of Eigen::SparseMatrix<double, RowMajor> (gs.h:29): rowptr[n+1]
+ * = outerIndexPtr(), col[nnz] = innerIndexPtr(), val[nnz] = valuePtr().  The
+ * construction of these operators stays on the host, as in the reference.
+ */
+int grada_set_operator(grada_ctx *ctx, int which, int64_t n, int64_t nnz, const int *rowptr,
+                       const int *col, const double *val);
+
+/*
+ * Cross-gradient coupling (use_cross_gradient_constraint, InversionBase.h:125):
+ * when enabled the CG system gains the rows a_crg*S_crg*T_{z,x,y}
+ * (GaussNewtonInversion.cpp:1445-1450).  S_crg: Nm diagonal, NULL = identity.
+ */
+int grada_set_cross_gradient(grada_ctx *ctx, int enabled, double a_crg, const double *S_crg);
+
+/* Replaces InversionBase::set_dobs (InversionBase.cpp:530-579): observed data
+ * (Nd) and the diagonal of Wd (Nd). */
+int grada_set_data(grada_ctx *ctx, const double *dobs, const double *wd);
+
+/*
+ * Replaces GaussNewtonInversion::solve_cg (GaussNewtonInversion.cpp:1417-1698),
+ * with the reference's semantics: CGLS from dx = 0 on the stacked system
+ * [Wd G P; sqrt(lambda) WL_s Ws P; sqrt(lambda) WL_z Wz P; ...], including the
+ * operator choices of the reference (forward Ws row without WL_s; forward crg
+ * rows weighted by WL_z/WL_x/WL_y; WL_y in the initial crg-y adjoint), and the
+ * stopping test ||r||^2 / ||A^T b||^2 < tol.  WL[7] in the reference argument
+ * order (WL_s, WL_x, WL_y, WL_z, WL_tx, WL_ty, WL_tz), Nm diagonals, NULL =
+ * identity.  Host pointers; dx[Nm] out.  Returns GRADA_ERR_BREAKDOWN when
+ * ||t||^2 becomes 0 (the reference would divide by zero).
+ */
+int grada_solve_cg(grada_ctx *ctx, double tol, int maxit, double lambda, const double *mk,
+                   const double *mref, const double *P, const double *const WL[7], double *dx,
+                   double *err, int *iterations);
+
+typedef struct grada_invert_params {
+  double max_lambda;             /* InversionBase::set_max_lambda */
+  int n_lambda;                  /* set_n_lambda */
+  double lambda_decreasing_rate; /* set_lambda_decreasing_rate */
+  double target_misfit;          /* set_target_misfit */
+  double stag_tol;               /* GaussNewtonInversion::set_stagnation_tolerance */
+  double cg_tol;                 /* set_CG_parameter */
+  double cg_iteration_factor;    /* set_CG_parameter: >= 1 iterations, < 1 fraction of Nm */
+  int gn_iterations;             /* set_max_GN_iterations */
+  int lp_s, lp_x, lp_y, lp_z, lp_t; /* set_Lp_inversion_parameter (p in {0,1,2}) */
+  double epsilon2;
+  int start_from_reference;      /* use_petrophysical_constraint: start from m0 */
+  int fp64_refinement;           /* with FP32/bf16 G: FP64 matrix-free residual once per GN iteration */
+} grada_invert_params;
+
+typedef struct grada_invert_report {
+  double final_misfit;      /* InversionBase::get_final_misfit */
+  double final_lambda;      /* get_final_lambda */
+  int gn_iterations;        /* Gauss-Newton iterations run */
+  int n_trials;             /* lambda trials (lines of lambda_misfit_GN) */
+  int64_t cg_iterations;    /* CG iterations over all trials */
+  int64_t fp64_refinements; /* FP64 matrix-free residual evaluations */
+} grada_invert_report;
+
+/*
+ * Replaces GaussNewtonInversion::invert_with_own_CG on a fixed mesh
+ * (GaussNewtonInversion.cpp:657-1103; the mesh-refinement branch stays with
+ * the host's AdaptiveInversion): lambda search with cooling, IRLS reweighting
+ * of the Ws/Wx/Wy/Wz (and crg) terms for p != 2, exponential bound transform,
+ * stopping on the target misfit, stagnation, or increasing misfit.  Uses the
+ * G assembled by grada_compute_G in whatever storage it has (FP64: the
+ * reference arithmetic; FP32/bf16: the CG products in reduced precision).
+ * m_ini, m_min, m_max, m0: Nm host vectors (m0 NULL = 0); m_out: Nm.
+ */
+int grada_invert(grada_ctx *ctx, const grada_invert_params *params, const double *m_ini,
+                 const double *m_min, const double *m_max, const double *m0, double *m_out,
+                 grada_invert_report *report);
+
+/* The records of the last grada_invert: trials as rows of 5 doubles
+ * (gn_iteration, lambda, misfit, cg_iterations, cg_error) -- lambda_misfit_GN,
+ * GaussNewtonInversion.cpp:921-923 -- and iterations as rows of 3 doubles
+ * (gn_iteration, n_trials, misfit) -- Iteration_misfit_GN, :1046-1048.  At
+ * most cap rows are written; *n gets the total. */
+int grada_get_trials(const grada_ctx *ctx, double *rows, int64_t cap, int64_t *n);
+int grada_get_iterations(const grada_ctx *ctx, double *rows, int64_t cap, int64_t *n);
+
 #ifdef __cplusplus
 }
 #endif

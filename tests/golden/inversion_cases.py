@@ -1,0 +1,193 @@
+"""Inversion fixtures from the reference compiled into oracle/_ref/ref_inversion.
+
+Each case sets up GaussNewtonInversion on a small regular mesh the way
+GraAdaInv::start_inversion does and records: the reference's G, the
+host-built operators (Ws, Wx, Wy, Wz and, with the cross-gradient constraint,
+T_x, T_y, T_z), Wd, one solve_cg call with non-trivial WL weights, and a full
+invert_with_own_CG run (final model, misfit, lambda, and the
+lambda_misfit_GN / Iteration_misfit_GN records).  Imported by make_golden.py.
+"""
+from __future__ import annotations
+
+import os
+import struct
+import subprocess
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+EXE = REPO / "oracle" / "_ref" / "ref_inversion"
+
+
+def _read_csr(buf, off):
+    n, nnz = struct.unpack_from("<qq", buf, off)
+    off += 16
+    rp = np.frombuffer(buf, "<i8", n + 1, off).astype(np.int32)
+    off += 8 * (n + 1)
+    ci = np.frombuffer(buf, "<i8", nnz, off).astype(np.int32)
+    off += 8 * nnz
+    v = np.frombuffer(buf, "<f8", nnz, off).copy()
+    off += 8 * nnz
+    return (rp, ci, v), off
+
+
+def _parse_table(path: Path):
+    rows = []
+    for line in path.read_text().splitlines()[1:]:
+        if line.strip():
+            rows.append([float(t) for t in line.split()])
+    return np.array(rows)
+
+
+def run_case(c: dict, solve: dict | None, full: bool):
+    nx, ny, nz = c["n"]
+    nm = nx * ny * nz
+    obs = c["obs"]
+    mask = c["mask"]
+    nf = bin(mask).count("1")
+    nd = nf * obs.shape[0]
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        for mode in ([1] if solve else []) + ([2] if full else []):
+            b = bytearray()
+            b += struct.pack("<qqq", nx, ny, nz)
+            b += struct.pack("<6d", *c["xl"], *c["yl"], *c["zl"])
+            b += struct.pack("<q", obs.shape[0]) + obs.astype("<f8").tobytes()
+            b += struct.pack("<I", mask)
+            b += c["dobs"].astype("<f8").tobytes()
+            b += np.asarray(c["rel"], "<f8").tobytes() + np.asarray(c["abs"], "<f8").tobytes()
+            b += struct.pack("<d", c["beta"])
+            b += struct.pack("<5d", *c["alphas"])
+            b += struct.pack("<dqd", c["max_lambda"], c["n_lambda"], c["rate"])
+            b += struct.pack("<4d", c["target"], c["stag"], c["cg_tol"], c["cg_factor"])
+            b += struct.pack("<q", c["gn_iter"])
+            b += struct.pack("<5q", *c["lp"])
+            b += struct.pack("<d", c["eps2"])
+            b += struct.pack("<3d", c["m_min"], c["m_max"], c["m_ini"])
+            b += struct.pack("<q", 1 if c.get("m0s") is not None else 0)
+            if c.get("m0s") is not None:
+                b += c["m0s"].astype("<f8").tobytes()
+            b += struct.pack("<q", 1 if c.get("m0") is not None else 0)
+            if c.get("m0") is not None:
+                b += c["m0"].astype("<f8").tobytes()
+            b += struct.pack("<q", mode)
+            if mode == 1:
+                b += struct.pack("<ddq", solve["lambda"], solve["tol"], solve["maxit"])
+                for v in [solve["mk"], solve["mref"], solve["P"]] + list(solve["WL"]):
+                    b += np.asarray(v, "<f8").tobytes()
+            wd = td / f"run{mode}"
+            wd.mkdir()
+            (wd / "in.bin").write_bytes(bytes(b))
+            # one OpenMP thread: the reference's reductions are then reproducible
+            env = dict(os.environ, OMP_NUM_THREADS="1")
+            subprocess.run([str(EXE), "in.bin", "out.bin"], cwd=wd, check=True,
+                           stdout=subprocess.DEVNULL, env=env)
+            buf = (wd / "out.bin").read_bytes()
+            off = 0
+            rows, cols = struct.unpack_from("<qq", buf, off)
+            off += 16
+            G = np.frombuffer(buf, "<f8", rows * cols, off).reshape(cols, rows).T.copy()
+            off += 8 * rows * cols
+            ops = {}
+            for name in ["Ws", "Wx", "Wy", "Wz"]:
+                ops[name], off = _read_csr(buf, off)
+            (use_crg,) = struct.unpack_from("<q", buf, off)
+            off += 8
+            if use_crg:
+                for name in ["Tx", "Ty", "Tz"]:
+                    ops[name], off = _read_csr(buf, off)
+                out["S_crg"] = np.frombuffer(buf, "<f8", nm, off).copy()
+                off += 8 * nm
+            wdiag = np.frombuffer(buf, "<f8", nd, off).copy()
+            off += 8 * nd
+            out["G"] = G
+            out["Wd"] = wdiag
+            for name, (rp, ci, v) in ops.items():
+                out[f"{name}_rowptr"], out[f"{name}_col"], out[f"{name}_val"] = rp, ci, v
+            if mode == 1:
+                out["cg_dx"] = np.frombuffer(buf, "<f8", nm, off).copy()
+                off += 8 * nm
+                out["cg_err"], out["cg_iters"] = struct.unpack_from("<dq", buf, off)
+            else:
+                out["inv_m"] = np.frombuffer(buf, "<f8", nm, off).copy()
+                off += 8 * nm
+                out["inv_misfit"], out["inv_lambda"] = struct.unpack_from("<dd", buf, off)
+                out["inv_trials"] = _parse_table(wd / "lambda_misfit_GN")
+                out["inv_iterations"] = _parse_table(wd / "Iteration_misfit_GN")
+    return out
+
+
+def make_case(name: str, seed: int):
+    from graada3d_gb300 import mesh as gm
+    from oracle import prism as oracle_prism
+
+    rng = np.random.default_rng(seed)
+    if name == "l2":
+        n, lp, mask, crg, ref = (8, 8, 4), (2, 2, 2, 2, 2), 0x012, False, False
+    elif name == "l1_crg":
+        n, lp, mask, crg, ref = (6, 7, 5), (1, 1, 1, 1, 1), 0x072, True, True
+    else:  # l0
+        n, lp, mask, crg, ref = (7, 6, 4), (0, 0, 0, 0, 2), 0x002, False, False
+    nx, ny, nz = n
+    xl, yl, zl = (0.0, 1000.0), (0.0, 900.0), (0.0, 500.0)
+    prisms = gm.regular_mesh(xl, nx, yl, ny, zl, nz)
+    obs = gm.observation_grid(9, 0.0, 1000.0, 8, 0.0, 900.0, -10.0)
+    boxes = [[250, 500, 200, 450, 100, 300, 300.0], [600, 850, 500, 800, 150, 400, -200.0]]
+    rho = gm.set_boxes(prisms, boxes)
+    G = oracle_prism.compute_G(prisms, obs, mask)
+    d = G @ rho
+    dobs = d + 0.02 * np.abs(d) * rng.standard_normal(d.size)
+    nf = bin(mask).count("1")
+    c = dict(n=n, xl=xl, yl=yl, zl=zl, obs=obs, mask=mask, dobs=dobs, rel=[0.02] * nf,
+             abs=[1e-3 if (mask >> 1) & 1 and k == 0 else 1e-2 for k in range(nf)], beta=1.5,
+             alphas=(1.0, 1.0, 1.0, 1.0, 1.0 if crg else 0.0), max_lambda=1e-1, n_lambda=8,
+             rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6, cg_factor=30, gn_iter=3, lp=lp,
+             eps2=1e-9, m_min=-1000.0, m_max=1000.0, m_ini=0.0)
+    if crg:
+        xc = 0.5 * (prisms[:, 0] + prisms[:, 1])
+        zc = 0.5 * (prisms[:, 4] + prisms[:, 5])
+        c["m0s"] = np.sin(xc / 300.0) + 0.5 * np.cos(zc / 200.0)
+    if ref:
+        c["m0"] = 50.0 * np.sin(xc / 400.0) * np.cos(zc / 250.0)
+    nm = nx * ny * nz
+    mk = rng.uniform(-300, 300, nm)
+    P = (c["m_max"] - mk) * (mk - c["m_min"]) / (c["m_max"] - c["m_min"])
+    WL = [rng.uniform(0.5, 2.0, nm) for _ in range(7)]
+    solve = {"lambda": 0.05, "tol": 1e-9, "maxit": 40, "mk": mk,
+             "mref": c.get("m0", np.zeros(nm)), "P": P, "WL": WL}
+    return c, solve
+
+
+def inversion_fixtures() -> None:
+    for name, seed in [("l2", 11), ("l1_crg", 12), ("l0", 13)]:
+        c, solve = make_case(name, seed)
+        res = run_case(c, solve, full=True)
+        out = {
+            "n": np.array(c["n"]), "xl": np.array(c["xl"]), "yl": np.array(c["yl"]),
+            "zl": np.array(c["zl"]), "obs": c["obs"], "mask": np.array(c["mask"]),
+            "dobs": c["dobs"], "rel": np.array(c["rel"]), "abs": np.array(c["abs"]),
+            "beta": np.array(c["beta"]), "alphas": np.array(c["alphas"]),
+            "max_lambda": np.array(c["max_lambda"]), "n_lambda": np.array(c["n_lambda"]),
+            "rate": np.array(c["rate"]), "target": np.array(c["target"]),
+            "stag": np.array(c["stag"]), "cg_tol": np.array(c["cg_tol"]),
+            "cg_factor": np.array(c["cg_factor"]), "gn_iter": np.array(c["gn_iter"]),
+            "lp": np.array(c["lp"]), "eps2": np.array(c["eps2"]),
+            "bounds": np.array([c["m_min"], c["m_max"], c["m_ini"]]),
+            "solve_lambda": np.array(solve["lambda"]), "solve_tol": np.array(solve["tol"]),
+            "solve_maxit": np.array(solve["maxit"]), "solve_mk": solve["mk"],
+            "solve_mref": solve["mref"], "solve_P": solve["P"], "solve_WL": np.array(solve["WL"]),
+        }
+        if c.get("m0s") is not None:
+            out["m0s"] = c["m0s"]
+        if c.get("m0") is not None:
+            out["m0"] = c["m0"]
+        for k, v in res.items():
+            out[k] = np.asarray(v)
+        np.savez_compressed(HERE / f"ref_inversion_{name}.npz", **out)
+        print(f"ref_inversion {name}: Nm={np.prod(c['n'])} Nd={res['G'].shape[0]} "
+              f"cg_iters={res['cg_iters']} final misfit={res['inv_misfit']:.4f} "
+              f"trials={len(res['inv_trials'])}")

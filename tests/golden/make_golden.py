@@ -257,4 +257,5 @@ def main() -> None:
 
 if __name__ == "__main__":
     sys.path.insert(0, str(HERE))
+    sys.path.insert(0, str(REPO))
     main()

@@ -1,0 +1,172 @@
+"""Parity of the GPU inversion path (solve_cg, invert_with_own_CG) with the
+reference compiled from source (fixtures) and with the NumPy oracle, through
+the C ABI."""
+import numpy as np
+import pytest
+
+import inversion_fixtures as fx
+from graada3d_gb300 import GradaError, mesh
+from graada3d_gb300 import regularization as reg
+from graada3d_gb300.inversion import GaussNewtonInversion
+from oracle import inversion as oinv
+from test_inversion_oracle import check_invert_against_reference
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(f, ctx, storage="fp64"):
+    inv = GaussNewtonInversion(fx.prisms(f), f["obs"], int(f["mask"]), ctx=ctx)
+    inv.compute_G(storage)
+    ops = {k: fx.csr(f, k) for k in ["Ws", "Wx", "Wy", "Wz"]}
+    if fx.has_crg(f):
+        ops.update({k: fx.csr(f, k) for k in ["Tx", "Ty", "Tz"]})
+        inv.set_cross_gradient(True, float(f["alphas"][4]))
+    else:
+        inv.set_cross_gradient(False)
+    inv.set_operators(ops)
+    inv.set_dobs(f["dobs"], f["Wd"])
+    return inv
+
+
+@pytest.mark.parametrize("name", fx.CASES)
+def test_gpu_G_matches_reference_G(gpu_ctx, name):
+    f = fx.load(name)
+    inv = _setup(f, gpu_ctx)
+    G = inv.get_G()
+    n = f["obs"].shape[0]
+    for k in range(G.shape[0] // n):
+        blk = slice(k * n, (k + 1) * n)
+        assert np.abs(G[blk] - f["G"][blk]).max() <= 1e-9 * np.abs(f["G"][blk]).max()
+
+
+@pytest.mark.parametrize("name", fx.CASES)
+def test_solve_cg_matches_reference(gpu_ctx, name):
+    f = fx.load(name)
+    inv = _setup(f, gpu_ctx)
+    dx, err, it = inv.solve_cg(float(f["solve_tol"]), int(f["solve_maxit"]), float(f["solve_lambda"]),
+                               f["solve_mk"], f["solve_mref"], f["solve_P"], fx.wl_dict(f))
+    assert it == int(f["cg_iters"])
+    ref = f["cg_dx"]
+    assert np.abs(dx - ref).max() <= 1e-7 * np.abs(ref).max()
+    assert abs(err - float(f["cg_err"])) <= 1e-5 * abs(float(f["cg_err"]))
+
+
+@pytest.mark.parametrize("name", fx.CASES)
+def test_invert_matches_reference(gpu_ctx, name):
+    f = fx.load(name)
+    inv = _setup(f, gpu_ctx)
+    nm = inv.Nm
+    mmin, mmax, mini = f["bounds"]
+    m0 = f["m0"] if "m0" in f.files else None
+    m, rep = inv.invert(fx.prm(f), np.full(nm, mini), np.full(nm, mmin), np.full(nm, mmax), m0)
+    trials = [tuple(r) for r in inv.trials()]
+    iters = [tuple(r) for r in inv.iterations()]
+    assert rep["n_trials"] == len(trials)
+    check_invert_against_reference(f, m, rep["final_misfit"], trials, iters)
+
+
+def _l2_problem(n=(16, 16, 8), nobs=(20, 20), mask=0x012, seed=21):
+    prisms = mesh.regular_mesh((0.0, 4000.0), n[0], (0.0, 4000.0), n[1], (0.0, 2000.0), n[2])
+    obs = mesh.observation_grid(nobs[0], 0.0, 4000.0, nobs[1], 0.0, 4000.0, -20.0)
+    rho = mesh.set_boxes(prisms, [[1000, 2000, 1250, 2500, 500, 1250, 300.0],
+                                  [2500, 3500, 500, 1500, 250, 1000, -200.0]])
+    return prisms, obs, rho, n, mask, np.random.default_rng(seed)
+
+
+def test_solve_cg_stops_on_tolerance_like_oracle(gpu_ctx):
+    prisms, obs, rho, n, mask, rng = _l2_problem()
+    inv = GaussNewtonInversion(prisms, obs, mask, ctx=gpu_ctx)
+    inv.compute_G("fp64")
+    G = inv.get_G()
+    d = G @ rho
+    dobs = d + 0.02 * np.abs(d) * rng.standard_normal(d.size)
+    wd = reg.data_weights(dobs, [0.02, 0.02], [1e-3, 1e-2], obs.shape[0])
+    ops = reg.regular_mesh_operators(n, prisms, obs, 1.5)
+    inv.set_cross_gradient(False)
+    inv.set_operators(ops)
+    inv.set_dobs(dobs, wd)
+    mk = rng.uniform(-100, 100, inv.Nm)
+    P = reg.p_diag(mk, -1000.0, 1000.0)
+    for lam in (10.0, 0.1):
+        dx, err, it = inv.solve_cg(1e-4, 200, lam, mk, np.zeros(inv.Nm), P)
+        dxo, erro, ito = oinv.solve_cg(1e-4, 200, lam, mk, np.zeros(inv.Nm), wd, dobs, P, G,
+                                       ops["Ws"], ops["Wx"], ops["Wy"], ops["Wz"])
+        assert it == ito and it < 200
+        assert np.abs(dx - dxo).max() <= 1e-8 * np.abs(dxo).max()
+
+
+def test_invert_l2_matches_oracle_at_2048_cells(gpu_ctx):
+    prisms, obs, rho, n, mask, rng = _l2_problem()
+    inv = GaussNewtonInversion(prisms, obs, mask, ctx=gpu_ctx)
+    inv.compute_G("fp64")
+    G = inv.get_G()
+    d = G @ rho
+    dobs = d + 0.02 * np.abs(d) * rng.standard_normal(d.size)
+    wd = reg.data_weights(dobs, [0.02, 0.02], [1e-3, 1e-2], obs.shape[0])
+    ops = reg.regular_mesh_operators(n, prisms, obs, 1.5)
+    inv.set_cross_gradient(False)
+    inv.set_operators(ops)
+    inv.set_dobs(dobs, wd)
+    prm = dict(max_lambda=1e-1, n_lambda=12, rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6,
+               cg_factor=50, gn_iter=3, lp=[2, 2, 2, 2, 2], eps2=1e-9)
+    nm = inv.Nm
+    m, rep = inv.invert(prm, np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0))
+    mo, misfit_o, lam_o, trials_o, iters_o = oinv.invert(
+        G, dobs, wd, ops["Ws"], ops["Wx"], ops["Wy"], ops["Wz"], prm, np.zeros(nm),
+        np.full(nm, -1000.0), np.full(nm, 1000.0))
+    tr = inv.trials()
+    assert tr.shape[0] == len(trials_o)
+    np.testing.assert_allclose(tr[:, 1:3], np.array([t[1:3] for t in trials_o]), rtol=1e-6)
+    np.testing.assert_array_equal(tr[:, 3], [t[3] for t in trials_o])
+    assert abs(rep["final_misfit"] - misfit_o) <= 1e-6 * misfit_o
+    assert np.abs(m - mo).max() <= 1e-5 * np.abs(mo).max()
+
+
+@pytest.mark.parametrize("storage", ["fp32", "bf16"])
+def test_mixed_precision_inversion_close_to_fp64(gpu_ctx, storage):
+    prisms, obs, rho, n, mask, rng = _l2_problem(mask=0x072)
+    inv = GaussNewtonInversion(prisms, obs, mask, ctx=gpu_ctx)
+    inv.compute_G("fp64")
+    G = inv.get_G()
+    d = G @ rho
+    dobs = d + 0.02 * np.abs(d) * rng.standard_normal(d.size)
+    wd = reg.data_weights(dobs, [0.02] * 4, [1e-3, 1e-2, 1e-2, 1e-2], obs.shape[0])
+    ops = reg.regular_mesh_operators(n, prisms, obs, 1.5)
+    inv.set_cross_gradient(False)
+    inv.set_operators(ops)
+    inv.set_dobs(dobs, wd)
+    prm = dict(max_lambda=1e-1, n_lambda=12, rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6,
+               cg_factor=50, gn_iter=3, lp=[1, 1, 1, 1, 2], eps2=1e-9)
+    nm = inv.Nm
+    args = (np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0))
+    m64, rep64 = inv.invert(prm, *args)
+    inv.compute_G(storage)
+    mlp, replp = inv.invert(prm, *args, fp64_refinement=True)
+    assert replp["fp64_refinements"] >= 1
+    rel = np.linalg.norm(mlp - m64) / np.linalg.norm(m64)
+    assert rel < (0.01 if storage == "fp32" else 0.05), rel
+    assert abs(replp["final_misfit"] - rep64["final_misfit"]) <= 0.02 * rep64["final_misfit"]
+
+
+def test_inversion_error_paths(gpu_ctx):
+    prisms, obs, rho, n, mask, rng = _l2_problem(n=(4, 4, 2), nobs=(5, 5))
+    inv = GaussNewtonInversion(prisms, obs, mask, ctx=gpu_ctx)
+    nm = inv.Nm
+    with pytest.raises(GradaError):  # G not assembled
+        inv.solve_cg(1e-6, 10, 1.0, np.zeros(nm), np.zeros(nm), np.ones(nm))
+    inv.compute_G("fp64")
+    with pytest.raises(GradaError):  # no data yet
+        inv.solve_cg(1e-6, 10, 1.0, np.zeros(nm), np.zeros(nm), np.ones(nm))
+    bad = np.ones(inv.Nd)
+    bad[3] = np.nan
+    with pytest.raises(GradaError):
+        inv.set_dobs(bad, np.ones(inv.Nd))
+    # a column index outside the matrix is rejected before any upload
+    from graada3d_gb300.fwd import _ptr
+    from graada3d_gb300.inversion import _iptr
+    rp = np.arange(nm + 1, dtype=np.int32)
+    ci = np.arange(nm, dtype=np.int32)
+    ci[0] = nm + 5
+    v = np.ones(nm)
+    st = inv.ctx.lib.grada_set_operator(inv.ctx.handle, 0, nm, nm, _iptr(rp), _iptr(ci), _ptr(v))
+    assert st == -1
