@@ -108,8 +108,14 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
   for (int64_t i = 0; i < 3 * no; i++)
     if (!std::isfinite(h_obs[i])) throw Error(GRADA_ERR_NONFINITE, "non-finite observation point");
   // The old G is invalid from here on; its allocation is kept for reuse by the
-  // next compute_G when large enough.
+  // next compute_G when large enough.  Data and operators belong to the old
+  // mesh/observation set and must be set again (InversionBase::set_mesh and
+  // set_observation reinitialise them the same way).
   g_storage = -1;
+  data_set = false;
+  for (auto &o : ops) o.set = false;
+  for (auto &o : crg) o.set = false;
+  crg_enabled = false;
   n_cells = nc;
   n_obs = no;
   mask = fmask;
