@@ -20,6 +20,7 @@ STATUS_NAMES = {
     -4: "GRADA_ERR_STATE",
     -5: "GRADA_ERR_NONFINITE",
     -6: "GRADA_ERR_BREAKDOWN",
+    -7: "GRADA_ERR_SCRATCH_LIMIT",
 }
 
 _dp = POINTER(c_double)
@@ -55,6 +56,8 @@ SIGNATURES = {
     "grada_invert": (c_int, [c_void_p, c_void_p, _dp, _dp, _dp, _dp, _dp, c_void_p]),
     "grada_get_trials": (c_int, [c_void_p, _dp, c_int64, _ip64]),
     "grada_get_iterations": (c_int, [c_void_p, _dp, c_int64, _ip64]),
+    "grada_G_vec_mul_noalloc": (c_int, [c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p,
+                                        c_void_p]),
 }
 
 

@@ -45,6 +45,7 @@ extern "C" {
 #define GRADA_ERR_STATE (-4)      /* call made before the data it needs was set */
 #define GRADA_ERR_NONFINITE (-5)  /* NaN/Inf met in data or in a CG scalar */
 #define GRADA_ERR_BREAKDOWN (-6)  /* CG scalar ||t||^2 == 0 */
+#define GRADA_ERR_SCRATCH_LIMIT (-7) /* problem larger than a fixed scratch array */
 
 /* Field bits, same layout as GS::ComputationOptions (gs.h:46-57). */
 #define GRADA_FIELD_V 0x001u
@@ -113,6 +114,25 @@ int grada_GT_vec_mul(grada_ctx *ctx, const double *y, double *x);
 /* Device-pointer forms of the two products, enqueued on the context stream. */
 int grada_G_vec_mul_dev(grada_ctx *ctx, const double *d_x, double *d_y);
 int grada_GT_vec_mul_dev(grada_ctx *ctx, const double *d_y, double *d_x);
+
+/*
+ * d_y[nd] = G d_x[nm] for an FP64 G that the caller owns (column-major,
+ * leading dimension ld >= nd, ld even, 16-byte aligned), enqueued on `stream`
+ * (a cudaStream_t; NULL = legacy default stream) of the current device,
+ * without allocating anything: no context, no cudaMalloc/cudaFree.  No
+ * counterpart in the reference; it exists for callers that cannot allocate
+ * device memory at the point of the call (inside another library's stream
+ * capture, under their own fixed device-memory budget, or on a path where
+ * an allocation's device-wide synchronisation is not acceptable).  Its
+ * scratch is an 8 MiB array built into the library (every GPU that loads the
+ * library holds it until exit): ld above 1,048,576 returns
+ * GRADA_ERR_SCRATCH_LIMIT.  The first call on a device looks up the array's
+ * device address (make it before any stream capture that should contain
+ * later calls).  All calls on a device share the array: calls that may
+ * overlap on the GPU race.
+ */
+int grada_G_vec_mul_noalloc(const double *d_G, int64_t nd, int64_t nm, int64_t ld,
+                            const double *d_x, double *d_y, void *stream);
 
 /*
  * Replaces the field sum of compute.cpp:246-260 (and Fwd::compute_gobs,
