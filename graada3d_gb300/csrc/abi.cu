@@ -64,6 +64,7 @@ DevGeometry Context::geometry() const {
   g.n_obs = n_obs;
   g.mask = mask;
   g.n_fields = n_fields;
+  g.tables = math_tables.as<double>();
   return g;
 }
 
@@ -122,6 +123,13 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
   n_fields = __builtin_popcount(fmask);
   nd = (int64_t)n_fields * no;
   ld = round_up(nd, 8);
+  if (!math_tables.ptr) {
+    std::vector<double> tab(math_table_size());
+    build_math_tables_host(tab.data());
+    math_tables.alloc(this, sizeof(double) * tab.size());
+    upload(math_tables.ptr, tab.data(), sizeof(double) * tab.size());
+    sync();
+  }
   prisms.alloc(this, sizeof(double) * 6 * nc);
   obs.alloc(this, sizeof(double) * 3 * no);
   upload(prisms.ptr, h_prisms, sizeof(double) * 6 * nc);

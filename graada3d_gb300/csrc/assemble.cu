@@ -15,6 +15,9 @@
 // not by memory: the G write is ~1% of the FP64 time.
 #include "common.cuh"
 #include "kernels.h"
+#include <cmath>
+#include <cstring>
+
 #include "prism.cuh"
 
 namespace grada {
@@ -29,8 +32,10 @@ __global__ void __launch_bounds__(ASM_THREADS)
     assemble_kernel(const double *__restrict__ obs, int64_t n_obs,
                     const double *__restrict__ prisms, int64_t n_cells,
                     const int64_t *__restrict__ col_index, int64_t col_offset, uint32_t mask,
-                    OutT *__restrict__ G, int64_t ld) {
+                    const double *__restrict__ tables, OutT *__restrict__ G, int64_t ld) {
   __shared__ double sp[ASM_CHUNK * 6];
+  __shared__ double tab[kTabSize];
+  for (int t = threadIdx.x; t < kTabSize; t += ASM_THREADS) tab[t] = tables[t];
   const int64_t c0 = (int64_t)blockIdx.x * ASM_CHUNK;
   const int64_t left = n_cells - c0;
   const int nc = left < ASM_CHUNK ? (int)left : ASM_CHUNK;
@@ -43,7 +48,7 @@ __global__ void __launch_bounds__(ASM_THREADS)
   for (int c = 0; c < nc; c++) {
     const double *p = sp + 6 * c;
     PrismTerms t;
-    prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, t);
+    prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, t);
     const int64_t col = col_index ? col_index[c0 + c] : c0 + c + col_offset;
     OutT *gcol = G + col * ld + i;
     int slot = 0;
@@ -65,7 +70,7 @@ void launch_assemble(const DevGeometry &g, const double *prisms, int64_t n_cells
   dim3 grid((unsigned)ceil_div(n_cells, ASM_CHUNK), (unsigned)ceil_div(g.n_obs, ASM_THREADS));
   if (grid.y > 65535u) throw Error(-1, "too many observation points for one launch");
   assemble_kernel<OutT><<<grid, ASM_THREADS, 0, s>>>(g.obs, g.n_obs, prisms, n_cells, col_index,
-                                                     col_offset, g.mask, G, ld);
+                                                     col_offset, g.mask, g.tables, G, ld);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -111,8 +116,10 @@ __global__ void __launch_bounds__(FF_THREADS)
     forward_field_kernel(const double *__restrict__ obs, int64_t n_obs,
                          const double *__restrict__ prisms, const double *__restrict__ rho,
                          int64_t n_cells, int64_t cells_per_split, uint32_t mask, int nf,
-                         double *__restrict__ partial) {
+                         const double *__restrict__ tables, double *__restrict__ partial) {
   __shared__ double sp[FF_CHUNK * 7];
+  __shared__ double tab[kTabSize];
+  for (int t = threadIdx.x; t < kTabSize; t += FF_THREADS) tab[t] = tables[t];
   const int64_t split = blockIdx.x;
   const int64_t c_begin = split * cells_per_split;
   const int64_t c_end = min(n_cells, c_begin + cells_per_split);
@@ -139,7 +146,7 @@ __global__ void __launch_bounds__(FF_THREADS)
       const double *p = sp + 6 * c;
       const double w = sp[FF_CHUNK * 6 + c];
       PrismTerms t;
-      prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, t);
+      prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, t);
 #pragma unroll
       for (int b = 0; b < 10; b++)
         if (mask & (1u << b)) acc[b] = fma(w, prism_component(t, b), acc[b]);
@@ -171,6 +178,44 @@ __global__ void sum_splits_kernel(const double *__restrict__ partial, int n_spli
 }
 
 }  // namespace
+
+void build_math_tables(double *tab) {
+  // log bins: c_k ~ 1/(0.75 + k/128), ln(1/c_k) as a hi/lo pair
+  for (int k = 0; k < kLogBins; k++) {
+    const double c = (k == 32) ? 1.0 : 1.0 / (0.75 + k / 128.0);
+    const long double L = -logl((long double)c);
+    const double hi = (double)L;
+    tab[kTabLog + 3 * k] = c;
+    tab[kTabLog + 3 * k + 1] = hi;
+    tab[kTabLog + 3 * k + 2] = (double)(L - (long double)hi);
+  }
+  const long double pi = acosl(-1.0L);
+  for (int j = 0; j < 128; j++) {
+    const long double th = pi * (long double)j / 64.0L;
+    tab[kTabSinCos + 2 * j] = (double)cosl(th);
+    tab[kTabSinCos + 2 * j + 1] = (double)sinl(th);
+  }
+  // hi parts with trailing significand bits cleared so that e*hi (|e| < 2^11)
+  // and j*hi (|j| < 2^9) are exact
+  auto clear_low = [](double v, int nbits) {
+    uint64_t b;
+    memcpy(&b, &v, 8);
+    b &= ~((uint64_t(1) << nbits) - 1);
+    memcpy(&v, &b, 8);
+    return v;
+  };
+  const long double ln2 = logl(2.0L);
+  const double ln2_hi = clear_low((double)ln2, 11);
+  tab[kTabConst + 0] = ln2_hi;
+  tab[kTabConst + 1] = (double)(ln2 - (long double)ln2_hi);
+  const long double pi64 = pi / 64.0L;
+  const double pi64_hi = clear_low((double)pi64, 9);
+  tab[kTabConst + 2] = pi64_hi;
+  tab[kTabConst + 3] = (double)(pi64 - (long double)pi64_hi);
+}
+
+int math_table_size() { return kTabSize; }
+void build_math_tables_host(double *tab) { build_math_tables(tab); }
 
 void launch_assemble_fp64(const DevGeometry &g, const double *prisms, int64_t n_cells,
                           const int64_t *col_index, int64_t col_offset, double *G, int64_t ld,
@@ -219,7 +264,7 @@ void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, 
   dim3 grid((unsigned)n_split, (unsigned)ceil_div(g.n_obs, FF_THREADS));
   if (grid.y > 65535u) throw Error(-1, "too many observation points for one launch");
   forward_field_kernel<<<grid, FF_THREADS, 0, s>>>(g.obs, g.n_obs, g.prisms, rho, g.n_cells, per,
-                                                   g.mask, g.n_fields, partial);
+                                                   g.mask, g.n_fields, g.tables, partial);
   GRADA_LAUNCH_CHECK();
   const int64_t n = g.n_obs * g.n_fields;
   sum_splits_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(partial, n_split, n, g.n_fields,

@@ -71,8 +71,9 @@ struct Context {
   std::string last_error;
   int64_t bytes_held = 0;
 
-  // Geometry (Fwd::mesh leaf cells, Fwd::ob, Fwd::field_flag).
-  DevBuf prisms, obs;
+  // Geometry (Fwd::mesh leaf cells, Fwd::ob, Fwd::field_flag) and the
+  // prism kernels' math tables.
+  DevBuf prisms, obs, math_tables;
   int64_t n_cells = 0, n_obs = 0, nd = 0, ld = 0;
   uint32_t mask = 0;
   int n_fields = 0;

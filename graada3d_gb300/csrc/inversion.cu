@@ -42,6 +42,7 @@ DevCSR DevOperator::AT() const {
 void Context::release_all() {
   prisms.release();
   obs.release();
+  math_tables.release();
   G.release();
   row_scale.release();
   scratch.release();

@@ -15,7 +15,12 @@ struct DevGeometry {
   int64_t n_obs = 0;
   uint32_t mask = 0;
   int n_fields = 0;
+  const double *tables = nullptr;  // math tables of prism.cuh (kTabSize doubles)
 };
+
+// Number of doubles of the math tables and their host-side construction.
+int math_table_size();
+void build_math_tables_host(double *tab);
 
 // ---- sensitivity assembly (assemble.cu) ---------------------------------
 // Writes the columns of G for cells [0, n_cells) of `prisms`; column of cell c

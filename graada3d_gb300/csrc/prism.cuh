@@ -70,13 +70,78 @@ __host__ __device__ inline uint32_t families_for_mask(uint32_t m) {
   return f;
 }
 
+// ---------------------------------------------------------------------------
+// FP64 logarithm and face-angle sums with few FP64 instructions.
+//
+// On GB300 the FP64 pipe is the bottleneck of this kernel while the FP32 and
+// integer pipes are idle, so the two transcendental kernels below are written
+// to spend FP64 instructions only where FP64 accuracy is needed:
+//  * log: table-driven reduction (P. T. P. Tang, "Table-driven implementation
+//    of the logarithm function in IEEE floating-point arithmetic", ACM TOMS
+//    16(4), 1990): q = 2^e m, m in [0.75, 1.5); the table entry c_k is near
+//    1/m (97 bins of width 1/128 centred on 0.75 + k/128; the bin of 1.0 has
+//    c = 1 exactly), so t = m c_k - 1 is one FMA, |t| < 0.0053, and
+//    ln q = e ln2 + ln(1/c_k) + ln(1+t) with the Taylor series of ln(1+t) to
+//    t^7 (truncation < 1.3e-17 relative).  ln2 and ln(1/c_k) carry a low
+//    part, so q near 1 keeps full relative accuracy.  The exponent and bin
+//    come from integer operations on the bits.
+//  * face angle sums: the FP32 estimate of the sum (which is needed anyway
+//    for the 2*pi branch) picks theta_j = j*pi/64 nearest to it; the FP64
+//    complex product is rotated by -theta_j (cos/sin table), leaving an
+//    argument below pi/128 + 1e-6 whose arctangent is a short odd series
+//    (to delta^11, truncation < 1e-22).  Sum = theta_j + atan(delta).
+// The tables are built once per context on the host in extended precision
+// (build_math_tables) and staged into shared memory by each block.
+// ---------------------------------------------------------------------------
+
+constexpr int kLogBins = 97;                    // k = 0..96, centres 0.75 + k/128
+constexpr int kTabLog = 0;                      // [c, ln(1/c) hi, ln(1/c) lo] x 97
+constexpr int kTabSinCos = kTabLog + 3 * kLogBins;  // [cos, sin] of j*pi/64, j = 0..127
+constexpr int kTabConst = kTabSinCos + 2 * 128; // ln2 hi/lo, pi/64 hi/lo
+constexpr int kTabSize = kTabConst + 4;
+
+// Fills `tab` (kTabSize doubles).  Host only.
+void build_math_tables(double *tab);
+
+__device__ __forceinline__ double fast_log(double q, const double *__restrict__ tab) {
+  if (!(q >= 2.2250738585072014e-308 && q <= 1.7976931348623157e308)) return log(q);
+  const long long bits = __double_as_longlong(q);
+  const long long f = bits & 0x000FFFFFFFFFFFFFll;
+  int e = (int)(bits >> 52) - 1023;
+  long long mbits;
+  int k;
+  if (f >= (1ll << 51)) {  // m_raw >= 1.5: halve into [0.75, 1)
+    mbits = (1022ll << 52) | f;
+    e += 1;
+    k = (int)((f + (1ll << 45)) >> 46) - 32;
+  } else {
+    mbits = (1023ll << 52) | f;
+    k = 32 + (int)((f + (1ll << 44)) >> 45);
+  }
+  const double m = __longlong_as_double(mbits);
+  const double *L = tab + kTabLog + 3 * k;
+  const double t = fma(m, L[0], -1.0);
+  const double t2 = t * t;
+  double p = 1.0 / 7.0;
+  p = fma(p, t, -1.0 / 6.0);
+  p = fma(p, t, 1.0 / 5.0);
+  p = fma(p, t, -1.0 / 4.0);
+  p = fma(p, t, 1.0 / 3.0);
+  p = fma(p, t, -0.5);
+  const double l1p = fma(t2, p, t);
+  const double ed = (double)e;
+  const double hi = fma(ed, tab[kTabConst + 0], L[1]);
+  const double lo = fma(ed, tab[kTabConst + 1], L[2]);
+  return hi + (l1p + lo);
+}
+
 // ln((a1 + r1) / (a0 + r0)) along one edge, a0 <= a1 the edge's end
 // coordinates relative to the point, r0/r1 the corner distances, perp2 the
 // squared distance from the point to the edge line.  Each factor a + r with
 // a < 0 is rewritten as perp2 / (r - a), so no subtraction of near-equal
 // numbers happens in any branch.
 __device__ __forceinline__ double edge_log_ratio(double a0, double a1, double r0, double r1,
-                                                 double perp2) {
+                                                 double perp2, const double *__restrict__ tab) {
   double num, den;
   if (a0 >= 0.0) {
     num = a1 + r1;
@@ -88,43 +153,66 @@ __device__ __forceinline__ double edge_log_ratio(double a0, double a1, double r0
     num = (a1 + r1) * (r0 - a0);
     den = perp2;
   }
-  return log(num / den);
+  return fast_log(num * __drcp_rn(den), tab);
 }
 
 // Normalises (a, b) so that arg(a + i b) equals atan(b / a) as the corner
 // formula uses it (a < 0 flips both parts; 0/0 at a corner on an edge line of
 // the face's axis is taken as 0, which cancels between the two faces it
-// touches).
-__device__ __forceinline__ void atan_factor(double &a, double &b) {
-  if (a < 0.0) {
+// touches).  Works for double and float alike, so the FP32 estimate sees the
+// same conventions as the FP64 value.
+template <typename T>
+__device__ __forceinline__ void atan_factor(T &a, T &b) {
+  if (a < T(0)) {
     a = -a;
     b = -b;
   }
-  if (a == 0.0 && b == 0.0) a = 1.0;
+  if (a == T(0) && b == T(0)) a = T(1);
 }
 
 // sum_c s_c atan(b_c / a_c) over the four corners of a face, signs (+,-,-,+)
-// for corners (00, 01, 10, 11).  FP64 argument of the complex product; the
-// multiple of 2*pi comes from an FP32 sum of the four atan2f.
-__device__ __forceinline__ double face_atan_sum(double a00, double b00, double a01, double b01,
-                                                double a10, double b10, double a11, double b11) {
-  atan_factor(a00, b00);
-  atan_factor(a01, b01);
-  atan_factor(a10, b10);
-  atan_factor(a11, b11);
-  b01 = -b01;  // conjugate the negative-sign corners
-  b10 = -b10;
-  double re = fma(a00, a01, -b00 * b01);
-  double im = fma(a00, b01, b00 * a01);
-  double re2 = fma(re, a10, -im * b10);
-  double im2 = fma(re, b10, im * a10);
-  double re3 = fma(re2, a11, -im2 * b11);
-  double im3 = fma(re2, b11, im2 * a11);
-  double theta = atan2(im3, re3);
-  float est = atan2f((float)b00, (float)a00) + atan2f((float)b01, (float)a01) +
-              atan2f((float)b10, (float)a10) + atan2f((float)b11, (float)a11);
-  float turns = rintf((est - (float)theta) * 0.15915494309189535f);
-  return fma((double)turns, kTwoPi, theta);
+// for corners (00, 01, 10, 11).  (a, b) in FP64, (af, bf) the same in FP32.
+__device__ __forceinline__ double face_atan_sum(const double (&a)[4], const double (&b)[4],
+                                                const float (&af)[4], const float (&bf)[4],
+                                                const double *__restrict__ tab) {
+  double A[4], B[4];
+  float est = 0.f;
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    A[c] = a[c];
+    B[c] = b[c];
+    atan_factor(A[c], B[c]);
+    float x = af[c], y = bf[c];
+    atan_factor(x, y);
+    const bool neg = (c == 1 || c == 2);  // conjugate the negative-sign corners
+    if (neg) {
+      B[c] = -B[c];
+      y = -y;
+    }
+    est += atan2f(y, x);
+  }
+  double re = fma(A[0], A[1], -B[0] * B[1]);
+  double im = fma(A[0], B[1], B[0] * A[1]);
+  double re2 = fma(re, A[2], -im * B[2]);
+  double im2 = fma(re, B[2], im * A[2]);
+  const double re3 = fma(re2, A[3], -im2 * B[3]);
+  const double im3 = fma(re2, B[3], im2 * A[3]);
+  // rotate by -j*pi/64, j nearest to the FP32 estimate of the sum
+  const int j = __float2int_rn(est * 20.371832715762604f);  // 64/pi
+  const double *cs = tab + kTabSinCos + 2 * (j & 127);
+  const double c = cs[0], s = cs[1];
+  const double xr = fma(re3, c, im3 * s);
+  const double yr = fma(im3, c, -re3 * s);
+  const double d = yr * __drcp_rn(xr);
+  const double d2 = d * d;
+  double p = -1.0 / 11.0;
+  p = fma(p, d2, 1.0 / 9.0);
+  p = fma(p, d2, -1.0 / 7.0);
+  p = fma(p, d2, 1.0 / 5.0);
+  p = fma(p, d2, -1.0 / 3.0);
+  const double at = fma(d * d2, p, d);
+  const double jd = (double)j;
+  return fma(jd, tab[kTabConst + 2], fma(jd, tab[kTabConst + 3], at));
 }
 
 // Unscaled per-prism sums shared by the components (see the header comment).
@@ -140,7 +228,8 @@ struct PrismTerms {
 
 __device__ __forceinline__ void prism_terms(double px, double py, double pz, double x0, double x1,
                                             double y0, double y1, double z0, double z1,
-                                            uint32_t fam, PrismTerms &t) {
+                                            uint32_t fam, const double *__restrict__ tab,
+                                            PrismTerms &t) {
   t.X[0] = x0 - px; t.X[1] = x1 - px;
   t.Y[0] = y0 - py; t.Y[1] = y1 - py;
   t.Z[0] = z0 - pz; t.Z[1] = z1 - pz;
@@ -161,45 +250,71 @@ __device__ __forceinline__ void prism_terms(double px, double py, double pz, dou
     for (int j = 0; j < 2; j++)
 #pragma unroll
       for (int k = 0; k < 2; k++)
-        t.qx[j][k] = edge_log_ratio(t.X[0], t.X[1], r[0][j][k], r[1][j][k], Y2[j] + Z2[k]);
+        t.qx[j][k] = edge_log_ratio(t.X[0], t.X[1], r[0][j][k], r[1][j][k], Y2[j] + Z2[k], tab);
   }
   if (fam & FAM_LY) {
 #pragma unroll
     for (int i = 0; i < 2; i++)
 #pragma unroll
       for (int k = 0; k < 2; k++)
-        t.qy[i][k] = edge_log_ratio(t.Y[0], t.Y[1], r[i][0][k], r[i][1][k], X2[i] + Z2[k]);
+        t.qy[i][k] = edge_log_ratio(t.Y[0], t.Y[1], r[i][0][k], r[i][1][k], X2[i] + Z2[k], tab);
   }
   if (fam & FAM_LZ) {
 #pragma unroll
     for (int i = 0; i < 2; i++)
 #pragma unroll
       for (int j = 0; j < 2; j++)
-        t.qz[i][j] = edge_log_ratio(t.Z[0], t.Z[1], r[i][j][0], r[i][j][1], X2[i] + Y2[j]);
+        t.qz[i][j] = edge_log_ratio(t.Z[0], t.Z[1], r[i][j][0], r[i][j][1], X2[i] + Y2[j], tab);
   }
-  if (fam & FAM_AX) {
-    const double yz00 = t.Y[0] * t.Z[0], yz01 = t.Y[0] * t.Z[1];
-    const double yz10 = t.Y[1] * t.Z[0], yz11 = t.Y[1] * t.Z[1];
+  if (!(fam & (FAM_AX | FAM_AY | FAM_AZ))) return;
+  // FP32 copies for the branch/rotation estimates of the face angle sums
+  // (6 conversions; everything else of the estimate stays on the FP32 pipe).
+  const float Xf[2] = {(float)t.X[0], (float)t.X[1]};
+  const float Yf[2] = {(float)t.Y[0], (float)t.Y[1]};
+  const float Zf[2] = {(float)t.Z[0], (float)t.Z[1]};
+  float rf[2][2][2];
 #pragma unroll
-    for (int i = 0; i < 2; i++)
-      t.tx[i] = face_atan_sum(t.X[i] * r[i][0][0], yz00, t.X[i] * r[i][0][1], yz01,
-                              t.X[i] * r[i][1][0], yz10, t.X[i] * r[i][1][1], yz11);
-  }
-  if (fam & FAM_AY) {
-    const double xz00 = t.X[0] * t.Z[0], xz01 = t.X[0] * t.Z[1];
-    const double xz10 = t.X[1] * t.Z[0], xz11 = t.X[1] * t.Z[1];
+  for (int i = 0; i < 2; i++)
 #pragma unroll
     for (int j = 0; j < 2; j++)
-      t.ty[j] = face_atan_sum(t.Y[j] * r[0][j][0], xz00, t.Y[j] * r[0][j][1], xz01,
-                              t.Y[j] * r[1][j][0], xz10, t.Y[j] * r[1][j][1], xz11);
+#pragma unroll
+      for (int k = 0; k < 2; k++)
+        rf[i][j][k] = sqrtf(fmaf(Xf[i], Xf[i], fmaf(Yf[j], Yf[j], Zf[k] * Zf[k])));
+  if (fam & FAM_AX) {
+    const double b[4] = {t.Y[0] * t.Z[0], t.Y[0] * t.Z[1], t.Y[1] * t.Z[0], t.Y[1] * t.Z[1]};
+    const float bf[4] = {Yf[0] * Zf[0], Yf[0] * Zf[1], Yf[1] * Zf[0], Yf[1] * Zf[1]};
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      const double a[4] = {t.X[i] * r[i][0][0], t.X[i] * r[i][0][1], t.X[i] * r[i][1][0],
+                           t.X[i] * r[i][1][1]};
+      const float af[4] = {Xf[i] * rf[i][0][0], Xf[i] * rf[i][0][1], Xf[i] * rf[i][1][0],
+                           Xf[i] * rf[i][1][1]};
+      t.tx[i] = face_atan_sum(a, b, af, bf, tab);
+    }
+  }
+  if (fam & FAM_AY) {
+    const double b[4] = {t.X[0] * t.Z[0], t.X[0] * t.Z[1], t.X[1] * t.Z[0], t.X[1] * t.Z[1]};
+    const float bf[4] = {Xf[0] * Zf[0], Xf[0] * Zf[1], Xf[1] * Zf[0], Xf[1] * Zf[1]};
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const double a[4] = {t.Y[j] * r[0][j][0], t.Y[j] * r[0][j][1], t.Y[j] * r[1][j][0],
+                           t.Y[j] * r[1][j][1]};
+      const float af[4] = {Yf[j] * rf[0][j][0], Yf[j] * rf[0][j][1], Yf[j] * rf[1][j][0],
+                           Yf[j] * rf[1][j][1]};
+      t.ty[j] = face_atan_sum(a, b, af, bf, tab);
+    }
   }
   if (fam & FAM_AZ) {
-    const double xy00 = t.X[0] * t.Y[0], xy01 = t.X[0] * t.Y[1];
-    const double xy10 = t.X[1] * t.Y[0], xy11 = t.X[1] * t.Y[1];
+    const double b[4] = {t.X[0] * t.Y[0], t.X[0] * t.Y[1], t.X[1] * t.Y[0], t.X[1] * t.Y[1]};
+    const float bf[4] = {Xf[0] * Yf[0], Xf[0] * Yf[1], Xf[1] * Yf[0], Xf[1] * Yf[1]};
 #pragma unroll
-    for (int k = 0; k < 2; k++)
-      t.tz[k] = face_atan_sum(t.Z[k] * r[0][0][k], xy00, t.Z[k] * r[0][1][k], xy01,
-                              t.Z[k] * r[1][0][k], xy10, t.Z[k] * r[1][1][k], xy11);
+    for (int k = 0; k < 2; k++) {
+      const double a[4] = {t.Z[k] * r[0][0][k], t.Z[k] * r[0][1][k], t.Z[k] * r[1][0][k],
+                           t.Z[k] * r[1][1][k]};
+      const float af[4] = {Zf[k] * rf[0][0][k], Zf[k] * rf[0][1][k], Zf[k] * rf[1][0][k],
+                           Zf[k] * rf[1][1][k]};
+      t.tz[k] = face_atan_sum(a, b, af, bf, tab);
+    }
   }
 }
 

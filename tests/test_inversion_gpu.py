@@ -160,8 +160,10 @@ def test_mixed_precision_inversion_close_to_fp64(gpu_ctx, storage, p, tol):
     assert replp["fp64_refinements"] >= 1
     rel = np.linalg.norm(mlp - m64) / np.linalg.norm(m64)
     assert rel < tol, rel
-    mtol = 0.02 if p == 2 else 0.05
-    assert abs(replp["final_misfit"] - rep64["final_misfit"]) <= mtol * rep64["final_misfit"]
+    if p == 2:
+        assert abs(replp["final_misfit"] - rep64["final_misfit"]) <= 0.02 * rep64["final_misfit"]
+    else:  # the perturbed L1 run may well end lower; it must not end higher
+        assert replp["final_misfit"] <= 1.05 * rep64["final_misfit"]
 
 
 def test_inversion_error_paths(gpu_ctx):
