@@ -45,10 +45,14 @@ __global__ void __launch_bounds__(ASM_THREADS)
   if (i >= n_obs) return;
   const double px = obs[3 * i], py = obs[3 * i + 1], pz = obs[3 * i + 2];
   const uint32_t fam = families_for_mask(mask);
+  ZCarry carry;
   for (int c = 0; c < nc; c++) {
     const double *p = sp + 6 * c;
+    // the same cell for every thread of the block: a uniform branch
+    const bool reuse = c > 0 && p[0] == p[-6] && p[1] == p[-5] && p[2] == p[-4] &&
+                       p[3] == p[-3] && p[4] == p[-1];
     PrismTerms t;
-    prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, t);
+    prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, reuse, carry, t);
     const int64_t col = col_index ? col_index[c0 + c] : c0 + c + col_offset;
     OutT *gcol = G + col * ld + i;
     int slot = 0;
@@ -135,6 +139,9 @@ __global__ void __launch_bounds__(FF_THREADS)
   double acc[10];
 #pragma unroll
   for (int b = 0; b < 10; b++) acc[b] = 0.0;
+  ZCarry carry;
+  double prev[6] = {0, 0, 0, 0, 0, 0};
+  bool have_prev = false;
   for (int64_t c0 = c_begin; c0 < c_end; c0 += FF_CHUNK) {
     const int nc = (int)min((int64_t)FF_CHUNK, c_end - c0);
     __syncthreads();
@@ -145,8 +152,13 @@ __global__ void __launch_bounds__(FF_THREADS)
     for (int c = 0; c < nc; c++) {
       const double *p = sp + 6 * c;
       const double w = sp[FF_CHUNK * 6 + c];
+      const bool reuse = have_prev && p[0] == prev[0] && p[1] == prev[1] && p[2] == prev[2] &&
+                         p[3] == prev[3] && p[4] == prev[5];
       PrismTerms t;
-      prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, t);
+      prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, reuse, carry, t);
+#pragma unroll
+      for (int q = 0; q < 6; q++) prev[q] = p[q];
+      have_prev = true;
 #pragma unroll
       for (int b = 0; b < 10; b++)
         if (mask & (1u << b)) acc[b] = fma(w, prism_component(t, b), acc[b]);
