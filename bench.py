@@ -309,12 +309,108 @@ def run_gpu(args):
             "hbm_write": hbm,
             "clocks": clk,
         }
+        if world == 1 and not args.no_inversion:
+            # second half of the metric: inversion time to chi^2 = N, mixed precision vs
+            # all-FP64 (configs[0] sizes; the 196,608-cell configs[2] run is --case inversion-cfg3)
+            line["inversion"] = run_inversion("cfg1")
         if world == 1 and not args.no_cpu_baseline:
             cb = cpu_sample(prisms, obs, target_s=args.ref_seconds)
             cb.pop("seconds", None)
             line["cpu_baseline"] = cb
         print(json.dumps(line))
     ctx.close()
+
+
+INVERSION_CASES = {
+    # BASELINE configs[0]: 32 x 32 x 16 cells over [0,10 km]^2 x [0,5 km], gz + Tzz at
+    # 41 x 41 points 100 m above, L2, lambda0 = 0.1, 30 lambdas, rate 0.6, CG max 50
+    "cfg1": dict(cells=(32, 32, 16), domain=(10000.0, 10000.0, 5000.0), obs=(41, 41), height=100.0,
+                 mask=0x012, lp=[2, 2, 2, 2, 2], eps2=1e-9, boxes="cfg1", gn_iter=10),
+    # BASELINE configs[2] on a uniform stand-in mesh of 196,608 cells (64 x 64 x 48 over the
+    # same domain; the reference refines to ~200k leaves on the host): gz, Tzz, Txz, Tyz at
+    # 101 x 101 points 100 m above, two dykes of +400 kg/m^3, L1 IRLS
+    "cfg3": dict(cells=(64, 64, 48), domain=(10000.0, 10000.0, 5000.0), obs=(101, 101),
+                 height=100.0, mask=0x072, lp=[1, 1, 1, 1, 2], eps2=1e-10, boxes="dykes",
+                 gn_iter=10),
+}
+
+
+def inversion_problem(name: str):
+    from graada3d_gb300 import mesh
+    from graada3d_gb300 import regularization as reg
+
+    c = INVERSION_CASES[name]
+    nx, ny, nz = c["cells"]
+    Lx, Ly, Lz = c["domain"]
+    prisms = mesh.regular_mesh((0.0, Lx), nx, (0.0, Ly), ny, (0.0, Lz), nz)
+    obs = mesh.observation_grid(c["obs"][0], 0.0, Lx, c["obs"][1], 0.0, Ly, -c["height"])
+    rng = np.random.default_rng(1 if c["boxes"] == "cfg1" else 4)
+    if c["boxes"] == "cfg1":
+        boxes = []
+        for v in (300.0, -200.0):
+            sx, sy, sz = rng.uniform(1000, 3000, 3)
+            x0, y0 = rng.uniform(0, Lx - sx), rng.uniform(0, Ly - sy)
+            z0 = rng.uniform(0, Lz - sz)
+            boxes.append([x0, x0 + sx, y0, y0 + sy, z0, z0 + sz, v])
+    else:
+        boxes = [[2500, 3500, 1000, 9000, 500, 3500, 400.0], [6000, 7000, 1000, 9000, 500, 3500, 400.0]]
+    rho = mesh.set_boxes(prisms, boxes)
+    nf = bin(c["mask"]).count("1")
+    rel = [0.02] * nf
+    absf = [1e-3 if (c["mask"] & 2) and k == 0 else 1e-2 for k in range(nf)]
+    ops = reg.regular_mesh_operators((nx, ny, nz), prisms, obs, 1.5)
+    return c, prisms, obs, rho, rel, absf, ops, rng
+
+
+def run_inversion(name: str, storages=("fp64", "fp32", "bf16")):
+    """Inversion to chi^2 = N (misfit < 1) on the GPU: all-FP64 vs reduced-precision
+    G with one FP64 residual refinement per Gauss-Newton iteration."""
+    import torch
+
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.inversion import GaussNewtonInversion
+
+    c, prisms, obs, rho, rel, absf, ops, rng = inversion_problem(name)
+    inv = GaussNewtonInversion(prisms, obs, c["mask"])
+    inv.compute_G("fp64")
+    d = inv.G_vec_mul(rho)
+    dobs = d + 0.02 * np.abs(d) * np.random.default_rng(2 if name == "cfg1" else 5).standard_normal(d.size)
+    wd = reg.data_weights(dobs, rel, absf, obs.shape[0])
+    inv.set_cross_gradient(False)
+    inv.set_operators(ops)
+    inv.set_dobs(dobs, wd)
+    nm = inv.Nm
+    prm = dict(max_lambda=1e-1, n_lambda=30, rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6,
+               cg_factor=50, gn_iter=c["gn_iter"], lp=c["lp"], eps2=c["eps2"])
+    args = (np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0))
+    out = {"case": name, "cells": nm, "data": inv.Nd, "lp": c["lp"][0]}
+    m64 = None
+    for st in storages:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        inv.compute_G(st)
+        torch.cuda.synchronize()
+        t_asm = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        m, rep = inv.invert(prm, *args, fp64_refinement=(st != "fp64"))
+        t_inv = time.perf_counter() - t0
+        r = {"assemble_s": t_asm, "invert_s": t_inv, "total_s": t_asm + t_inv,
+             "misfit": rep["final_misfit"], "chi2_reached": rep["final_misfit"] < 1.0,
+             "gn_iterations": rep["gn_iterations"], "trials": rep["n_trials"],
+             "cg_iterations": int(rep["cg_iterations"]),
+             "ms_per_cg_iteration": 1e3 * t_inv / max(1, rep["cg_iterations"])}
+        if st == "fp64":
+            m64 = m
+        else:
+            r["model_rel_diff_vs_fp64"] = float(np.linalg.norm(m - m64) / np.linalg.norm(m64))
+            r["fp64_refinements"] = int(rep["fp64_refinements"])
+        out[st] = r
+    if "fp64" in out:
+        for st in storages:
+            if st != "fp64":
+                out[st]["invert_speedup_vs_fp64"] = out["fp64"]["invert_s"] / out[st]["invert_s"]
+    inv.ctx.close()
+    return out
 
 
 def run_profile_case(args):
@@ -341,16 +437,20 @@ def run_profile_case(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="bench", choices=["bench", "profile"])
+    ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-cfg1",
+                                                         "inversion-cfg3"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-inversion", action="store_true")
     args = ap.parse_args()
     if args.case == "profile":
         run_profile_case(args)
+    elif args.case.startswith("inversion-"):
+        print(json.dumps(run_inversion(args.case.split("-", 1)[1])))
     elif args.impl == "reference":
         run_reference(args)
     else:

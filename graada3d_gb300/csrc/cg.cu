@@ -54,7 +54,9 @@ __global__ void csr_apply_kernel(DevCSR A, const double *__restrict__ x,
 }
 
 // Forward regulariser rows for up to 7 terms in one launch (blockIdx.y = term).
-__global__ void multi_forward_kernel(ForwardTerms T, const double *__restrict__ x) {
+__global__ void multi_forward_kernel(ForwardTerms T, const double *__restrict__ x,
+                                     const int *__restrict__ skip) {
+  if (skip && *skip) return;
   const ForwardTerm &t = T.t[blockIdx.y];
   const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
   if (i >= t.A.n) return;
@@ -68,7 +70,8 @@ __global__ void multi_forward_kernel(ForwardTerms T, const double *__restrict__ 
 // r = P .* (sign_g * gtw + sum_t c_t A_t^T (wl_t .* s_t)), A_t^T given as CSR.
 __global__ void adjoint_kernel(AdjointTerms T, int64_t n, const double *__restrict__ P,
                                const double *__restrict__ gtw, double sign_g,
-                               double *__restrict__ r) {
+                               double *__restrict__ r, const int *__restrict__ skip) {
+  if (skip && *skip) return;
   const int64_t j = (int64_t)blockIdx.x * VT + threadIdx.x;
   if (j >= n) return;
   double acc = gtw ? sign_g * gtw[j] : 0.0;
@@ -86,7 +89,9 @@ __global__ void adjoint_kernel(AdjointTerms T, int64_t n, const double *__restri
 }
 
 __global__ void dot_partial_kernel(const double *__restrict__ a, const double *__restrict__ b,
-                                   int64_t n, double *__restrict__ partial) {
+                                   int64_t n, double *__restrict__ partial,
+                                   const int *__restrict__ skip) {
+  if (skip && *skip) return;
   double v = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT)
     v = fma(a[i], b ? b[i] : a[i], v);
@@ -95,7 +100,8 @@ __global__ void dot_partial_kernel(const double *__restrict__ a, const double *_
 }
 
 __global__ void sum_partials_kernel(const double *__restrict__ partial, int nblocks,
-                                    double *__restrict__ out) {
+                                    double *__restrict__ out, const int *__restrict__ skip) {
+  if (skip && *skip) return;
   double v = 0.0;
   for (int i = threadIdx.x; i < nblocks; i += VT) v += partial[i];
   v = block_sum(v);
@@ -114,7 +120,8 @@ __global__ void data_residual_kernel(const double *__restrict__ dobs, const doub
 }
 
 __global__ void scale_kernel(const double *__restrict__ a, const double *__restrict__ w, int64_t n,
-                             double c, double *__restrict__ out) {
+                             double c, double *__restrict__ out, const int *__restrict__ skip) {
+  if (skip && *skip) return;
   const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
   if (i >= n) return;
   out[i] = c * (w ? w[i] * a[i] : a[i]);
@@ -128,7 +135,8 @@ __global__ void negate_kernel(const double *__restrict__ a, int64_t n, double *_
 // p = -r + beta p ;  pp = P .* p
 __global__ void p_update_kernel(const double *__restrict__ r, const double *__restrict__ P,
                                 const double *__restrict__ scal, int64_t n, double *__restrict__ p,
-                                double *__restrict__ pp) {
+                                double *__restrict__ pp, const int *__restrict__ skip) {
+  if (skip && *skip) return;
   const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
   if (i >= n) return;
   const double beta = scal[CG_BETA];
@@ -140,26 +148,51 @@ __global__ void p_update_kernel(const double *__restrict__ r, const double *__re
 // s += alpha t (nrow) ;  dx += alpha p (n)
 __global__ void axpy_kernel(const double *__restrict__ t, const double *__restrict__ p,
                             const double *__restrict__ scal, int64_t nrow, int64_t n,
-                            double *__restrict__ s, double *__restrict__ dx) {
+                            double *__restrict__ s, double *__restrict__ dx,
+                            const int *__restrict__ skip) {
+  if (skip && *skip) return;
   const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
   const double alpha = scal[CG_ALPHA];
   if (i < nrow) s[i] = fma(alpha, t[i], s[i]);
   if (i < n) dx[i] = fma(alpha, p[i], dx[i]);
 }
 
-__global__ void alpha_kernel(double *scal) {
+// ctl[CTL_DONE] != 0 turns every later kernel of the iteration (and of later
+// iterations) into a no-op; ctl[CTL_STATUS] says why the solve stopped early.
+__global__ void alpha_kernel(double *scal, int *ctl) {
+  if (ctl && ctl[CTL_DONE]) return;
   // alpha = r2 / t2   (GaussNewtonInversion.cpp:1601)
-  scal[CG_ALPHA] = scal[CG_R2] / scal[CG_T2];
+  const double t2 = scal[CG_T2];
+  const double a = scal[CG_R2] / t2;
+  scal[CG_ALPHA] = a;
+  if (ctl && (t2 == 0.0 || !isfinite(a))) {
+    ctl[CTL_STATUS] = (t2 == 0.0) ? CG_STATUS_BREAKDOWN : CG_STATUS_NONFINITE;
+    ctl[CTL_DONE] = 1;
+  }
 }
 
-__global__ void beta_kernel(double *scal) {
+__global__ void beta_kernel(double *scal, int *ctl) {
+  if (ctl && ctl[CTL_DONE]) return;
   // rlast2 = r2 ; r2 = ||r||^2 ; beta = r2/rlast2 ; err = r2/ATb2   (:1674-1684)
   const double rlast2 = scal[CG_R2];
   const double r2 = scal[CG_R2NEW];
   scal[CG_RLAST2] = rlast2;
   scal[CG_R2] = r2;
   scal[CG_BETA] = r2 / rlast2;
-  scal[CG_ERR] = r2 / scal[CG_ATB2];
+  const double err = r2 / scal[CG_ATB2];
+  scal[CG_ERR] = err;
+  if (ctl) {
+    const int it = ++ctl[CTL_ITER];
+    if (!isfinite(err)) {
+      ctl[CTL_STATUS] = CG_STATUS_NONFINITE;
+      ctl[CTL_DONE] = 1;
+    } else if (err < scal[CG_TOL]) {  // iterations = i + 1 (:1685-1691)
+      ctl[CTL_STATUS] = CG_STATUS_CONVERGED;
+      ctl[CTL_DONE] = 1;
+    } else if (it >= ctl[CTL_MAXIT]) {
+      ctl[CTL_DONE] = 1;
+    }
+  }
 }
 
 // Bound transform, GaussNewtonInversion.cpp:877-911.  Cells that hit the
@@ -269,25 +302,26 @@ void launch_csr_apply(const DevCSR &A, const double *x, const double *xs, double
   GRADA_LAUNCH_CHECK();
 }
 
-void launch_multi_forward(const ForwardTerms &T, int64_t n, const double *x, cudaStream_t s) {
+void launch_multi_forward(const ForwardTerms &T, int64_t n, const double *x, cudaStream_t s,
+                          const int *skip) {
   if (T.count <= 0 || n <= 0) return;
   dim3 grid(blocks_for(n), (unsigned)T.count);
-  multi_forward_kernel<<<grid, VT, 0, s>>>(T, x);
+  multi_forward_kernel<<<grid, VT, 0, s>>>(T, x, skip);
   GRADA_LAUNCH_CHECK();
 }
 
 void launch_adjoint(const AdjointTerms &T, int64_t n, const double *P, const double *gtw,
-                    double sign_g, double *r, cudaStream_t s) {
+                    double sign_g, double *r, cudaStream_t s, const int *skip) {
   if (n <= 0) return;
-  adjoint_kernel<<<blocks_for(n), VT, 0, s>>>(T, n, P, gtw, sign_g, r);
+  adjoint_kernel<<<blocks_for(n), VT, 0, s>>>(T, n, P, gtw, sign_g, r, skip);
   GRADA_LAUNCH_CHECK();
 }
 
 void launch_dot(const double *a, const double *b, int64_t n, double *partial, int nblocks,
-                double *out, cudaStream_t s) {
-  dot_partial_kernel<<<nblocks, VT, 0, s>>>(a, b, n, partial);
+                double *out, cudaStream_t s, const int *skip) {
+  dot_partial_kernel<<<nblocks, VT, 0, s>>>(a, b, n, partial, skip);
   GRADA_LAUNCH_CHECK();
-  sum_partials_kernel<<<1, VT, 0, s>>>(partial, nblocks, out);
+  sum_partials_kernel<<<1, VT, 0, s>>>(partial, nblocks, out, skip);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -295,7 +329,7 @@ void launch_misfit_sq(const double *g, const double *dobs, const double *wd, int
                       double *partial, int nblocks, double *out, cudaStream_t s) {
   misfit_partial_kernel<<<nblocks, VT, 0, s>>>(g, dobs, wd, n, partial);
   GRADA_LAUNCH_CHECK();
-  sum_partials_kernel<<<1, VT, 0, s>>>(partial, nblocks, out);
+  sum_partials_kernel<<<1, VT, 0, s>>>(partial, nblocks, out, nullptr);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -306,8 +340,8 @@ void launch_data_residual(const double *dobs, const double *g, const double *wd,
 }
 
 void launch_scale(const double *a, const double *w, int64_t n, double c, double *out,
-                  cudaStream_t s) {
-  scale_kernel<<<blocks_for(n), VT, 0, s>>>(a, w, n, c, out);
+                  cudaStream_t s, const int *skip) {
+  scale_kernel<<<blocks_for(n), VT, 0, s>>>(a, w, n, c, out, skip);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -317,24 +351,24 @@ void launch_negate(const double *a, int64_t n, double *out, cudaStream_t s) {
 }
 
 void launch_p_update(const double *r, const double *P, const double *scal, int64_t n, double *p,
-                     double *pp, cudaStream_t s) {
-  p_update_kernel<<<blocks_for(n), VT, 0, s>>>(r, P, scal, n, p, pp);
+                     double *pp, cudaStream_t s, const int *skip) {
+  p_update_kernel<<<blocks_for(n), VT, 0, s>>>(r, P, scal, n, p, pp, skip);
   GRADA_LAUNCH_CHECK();
 }
 
 void launch_axpy(const double *t, const double *p, const double *scal, int64_t nrow, int64_t n,
-                 double *sv, double *dx, cudaStream_t s) {
-  axpy_kernel<<<blocks_for(std::max(nrow, n)), VT, 0, s>>>(t, p, scal, nrow, n, sv, dx);
+                 double *sv, double *dx, cudaStream_t s, const int *skip) {
+  axpy_kernel<<<blocks_for(std::max(nrow, n)), VT, 0, s>>>(t, p, scal, nrow, n, sv, dx, skip);
   GRADA_LAUNCH_CHECK();
 }
 
-void launch_alpha(double *scal, cudaStream_t s) {
-  alpha_kernel<<<1, 1, 0, s>>>(scal);
+void launch_alpha(double *scal, int *ctl, cudaStream_t s) {
+  alpha_kernel<<<1, 1, 0, s>>>(scal, ctl);
   GRADA_LAUNCH_CHECK();
 }
 
-void launch_beta(double *scal, cudaStream_t s) {
-  beta_kernel<<<1, 1, 0, s>>>(scal);
+void launch_beta(double *scal, int *ctl, cudaStream_t s) {
+  beta_kernel<<<1, 1, 0, s>>>(scal, ctl);
   GRADA_LAUNCH_CHECK();
 }
 

@@ -52,31 +52,44 @@ enum : int {
   CG_ATB2 = 6,
   CG_R2NEW = 7,
   CG_MISFIT2 = 8,
+  CG_TOL = 9,
   CG_NSCALARS = 16
+};
+
+// Slots of the device control block of one CG solve (ints).
+enum : int { CTL_DONE = 0, CTL_ITER = 1, CTL_MAXIT = 2, CTL_STATUS = 3, CTL_NINTS = 4 };
+enum : int {
+  CG_STATUS_RUNNING = 0,
+  CG_STATUS_CONVERGED = 1,
+  CG_STATUS_BREAKDOWN = 2,
+  CG_STATUS_NONFINITE = 3
 };
 
 int dot_blocks(int64_t n, int sm_count);
 
 void launch_csr_apply(const DevCSR &A, const double *x, const double *xs, double c, const double *wl,
                       double *y, cudaStream_t s);
-void launch_multi_forward(const ForwardTerms &T, int64_t n, const double *x, cudaStream_t s);
+// Kernels taking `skip` return at once while *skip != 0 (see CTL_DONE).
+void launch_multi_forward(const ForwardTerms &T, int64_t n, const double *x, cudaStream_t s,
+                          const int *skip = nullptr);
 void launch_adjoint(const AdjointTerms &T, int64_t n, const double *P, const double *gtw,
-                    double sign_g, double *r, cudaStream_t s);
+                    double sign_g, double *r, cudaStream_t s, const int *skip = nullptr);
 void launch_dot(const double *a, const double *b, int64_t n, double *partial, int nblocks,
-                double *out, cudaStream_t s);
+                double *out, cudaStream_t s, const int *skip = nullptr);
 void launch_misfit_sq(const double *g, const double *dobs, const double *wd, int64_t n,
                       double *partial, int nblocks, double *out, cudaStream_t s);
 void launch_data_residual(const double *dobs, const double *g, const double *wd, int64_t n,
                           double *b0, double *s0, cudaStream_t s);
 void launch_scale(const double *a, const double *w, int64_t n, double c, double *out,
-                  cudaStream_t s);
+                  cudaStream_t s, const int *skip = nullptr);
 void launch_negate(const double *a, int64_t n, double *out, cudaStream_t s);
 void launch_p_update(const double *r, const double *P, const double *scal, int64_t n, double *p,
-                     double *pp, cudaStream_t s);
+                     double *pp, cudaStream_t s, const int *skip = nullptr);
 void launch_axpy(const double *t, const double *p, const double *scal, int64_t nrow, int64_t n,
-                 double *sv, double *dx, cudaStream_t s);
-void launch_alpha(double *scal, cudaStream_t s);
-void launch_beta(double *scal, cudaStream_t s);
+                 double *sv, double *dx, cudaStream_t s, const int *skip = nullptr);
+// alpha = r2/t2 and beta/err with the stopping test; ctl may be null.
+void launch_alpha(double *scal, int *ctl, cudaStream_t s);
+void launch_beta(double *scal, int *ctl, cudaStream_t s);
 void launch_bound_update(const double *m, const double *dx, const double *mmin, const double *mmax,
                          int64_t n, double *mt, const double *mt_old, int *guard, int *any_guard,
                          int *h_any_guard, cudaStream_t s);

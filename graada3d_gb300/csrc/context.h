@@ -59,6 +59,9 @@ struct IterationRecord {
   double misfit;
 };
 
+// CG iterations captured per CUDA graph replay.
+constexpr int kCgGraphIters = 16;
+
 struct CgResult {
   double err = 0.0;
   int iterations = 0;
@@ -100,9 +103,10 @@ struct Context {
 
   // CG work vectors.
   DevBuf cg_b, cg_s, cg_t, cg_p, cg_pp, cg_r, cg_atb, cg_gtw, cg_gx, cg_tmpd, cg_scal, cg_part;
-  DevBuf cg_wl_ones;
+  DevBuf cg_wl_ones, cg_ctl;
   double *h_scal = nullptr;  // pinned
   int *h_flag = nullptr;     // pinned
+  int *h_ctl = nullptr;      // pinned
 
   // Inversion work vectors and records.
   DevBuf iv_m, iv_mt, iv_mt_old, iv_mopt, iv_dx, iv_P, iv_mmin, iv_mmax, iv_m0, iv_wl, iv_tmp,

@@ -70,7 +70,9 @@ struct LoadBF16 {
 template <class L>
 __global__ void __launch_bounds__(GV_THREADS)
     gx_partial_kernel(const void *__restrict__ G, int64_t ld, int64_t nm, int64_t cols_per_split,
-                      const double *__restrict__ x, double *__restrict__ partial) {
+                      const double *__restrict__ x, double *__restrict__ partial,
+                      const int *__restrict__ skip) {
+  if (skip && *skip) return;
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
   constexpr int XCH = 256;
@@ -121,12 +123,15 @@ __global__ void __launch_bounds__(GV_THREADS)
 
 __global__ void gx_finish_kernel(const double *__restrict__ partial, int n_split, int64_t ld,
                                  int64_t nd, const float *__restrict__ row_scale,
-                                 double *__restrict__ y) {
+                                 const double *__restrict__ post_scale, double *__restrict__ y,
+                                 const int *__restrict__ skip) {
+  if (skip && *skip) return;
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nd) return;
   double s = 0.0;
   for (int k = 0; k < n_split; k++) s += partial[(int64_t)k * ld + r];
   if (row_scale) s *= (double)row_scale[r];
+  if (post_scale) s *= post_scale[r];
   y[r] = s;
 }
 
@@ -135,7 +140,9 @@ __global__ void gx_finish_kernel(const double *__restrict__ partial, int n_split
 template <class L, int COLS>
 __global__ void __launch_bounds__(GV_THREADS)
     gty_kernel(const void *__restrict__ G, int64_t ld, int64_t nm,
-               const typename L::Acc *__restrict__ y, double *__restrict__ x) {
+               const typename L::Acc *__restrict__ y, double *__restrict__ x,
+               const int *__restrict__ skip) {
+  if (skip && *skip) return;
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
   const int64_t c0 = (int64_t)blockIdx.x * COLS;
@@ -179,10 +186,14 @@ __global__ void __launch_bounds__(GV_THREADS)
 // row scale for bf16, zero in the padding rows.
 template <typename Acc>
 __global__ void prep_y_kernel(const double *__restrict__ y, int64_t nd, int64_t ld,
-                              const float *__restrict__ row_scale, Acc *__restrict__ out) {
+                              const float *__restrict__ row_scale,
+                              const double *__restrict__ pre_scale, Acc *__restrict__ out,
+                              const int *__restrict__ skip) {
+  if (skip && *skip) return;
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= ld) return;
   double v = (r < nd) ? y[r] : 0.0;
+  if (pre_scale && r < nd) v = pre_scale[r] * v;
   if (row_scale && r < nd) v *= (double)row_scale[r];
   out[r] = (Acc)v;
 }
@@ -219,14 +230,14 @@ __global__ void widen_kernel(const void *__restrict__ G, int kind, const float *
 
 template <class L>
 void run_gx(const DevG &G, const double *x, double *y, double *scratch, int sm_count,
-            cudaStream_t s) {
+            const GemvOpts &o, cudaStream_t s) {
   const int splits = gx_splits(G, sm_count, L::VEC);
   const int64_t per = ceil_div(G.nm, splits);
   dim3 grid((unsigned)ceil_div(G.ld, (int64_t)GV_THREADS * L::VEC), (unsigned)splits);
-  gx_partial_kernel<L><<<grid, GV_THREADS, 0, s>>>(G.data, G.ld, G.nm, per, x, scratch);
+  gx_partial_kernel<L><<<grid, GV_THREADS, 0, s>>>(G.data, G.ld, G.nm, per, x, scratch, o.skip);
   GRADA_LAUNCH_CHECK();
   gx_finish_kernel<<<(unsigned)ceil_div(G.nd, 256), 256, 0, s>>>(scratch, splits, G.ld, G.nd,
-                                                                 G.row_scale, y);
+                                                                 G.row_scale, o.scale, y, o.skip);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -240,12 +251,12 @@ int64_t gemv_scratch_doubles(const DevG &G, int sm_count) {
 }
 
 void launch_G_vec_mul(const DevG &G, const double *x, double *y, double *scratch, int sm_count,
-                      cudaStream_t s) {
+                      cudaStream_t s, const GemvOpts &o) {
   if (G.nd <= 0 || G.nm <= 0) return;
   switch (G.kind) {
-    case GKind::FP64: run_gx<LoadF64>(G, x, y, scratch, sm_count, s); break;
-    case GKind::FP32: run_gx<LoadF32>(G, x, y, scratch, sm_count, s); break;
-    case GKind::BF16: run_gx<LoadBF16>(G, x, y, scratch, sm_count, s); break;
+    case GKind::FP64: run_gx<LoadF64>(G, x, y, scratch, sm_count, o, s); break;
+    case GKind::FP32: run_gx<LoadF32>(G, x, y, scratch, sm_count, o, s); break;
+    case GKind::BF16: run_gx<LoadBF16>(G, x, y, scratch, sm_count, o, s); break;
   }
 }
 
@@ -257,35 +268,38 @@ void launch_widen_columns(const DevG &G, int64_t c0, int64_t nc, double *out, cu
 }
 
 void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratch, int sm_count,
-                       cudaStream_t s) {
+                       cudaStream_t s, const GemvOpts &o) {
   (void)sm_count;
   if (G.nd <= 0 || G.nm <= 0) return;
   const unsigned prep_blocks = (unsigned)ceil_div(G.ld, 256);
   switch (G.kind) {
     case GKind::FP64: {
-      prep_y_kernel<double><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, nullptr, scratch);
+      prep_y_kernel<double><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, nullptr, o.scale, scratch,
+                                                        o.skip);
       GRADA_LAUNCH_CHECK();
       constexpr int COLS = 4;
       gty_kernel<LoadF64, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
-          G.data, G.ld, G.nm, scratch, x);
+          G.data, G.ld, G.nm, scratch, x, o.skip);
       break;
     }
     case GKind::FP32: {
       float *y32 = reinterpret_cast<float *>(scratch);
-      prep_y_kernel<float><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, nullptr, y32);
+      prep_y_kernel<float><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, nullptr, o.scale, y32,
+                                                       o.skip);
       GRADA_LAUNCH_CHECK();
       constexpr int COLS = 4;
       gty_kernel<LoadF32, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
-          G.data, G.ld, G.nm, y32, x);
+          G.data, G.ld, G.nm, y32, x, o.skip);
       break;
     }
     case GKind::BF16: {
       float *y32 = reinterpret_cast<float *>(scratch);
-      prep_y_kernel<float><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, G.row_scale, y32);
+      prep_y_kernel<float><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, G.row_scale, o.scale, y32,
+                                                       o.skip);
       GRADA_LAUNCH_CHECK();
       constexpr int COLS = 4;
       gty_kernel<LoadBF16, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
-          G.data, G.ld, G.nm, y32, x);
+          G.data, G.ld, G.nm, y32, x, o.skip);
       break;
     }
   }

@@ -57,14 +57,16 @@ void Context::release_all() {
     o.t_rowptr.release(); o.t_col.release(); o.t_val.release();
   }
   DevBuf *bufs[] = {&dobs, &wd, &cg_b, &cg_s, &cg_t, &cg_p, &cg_pp, &cg_r, &cg_atb, &cg_gtw,
-                    &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &iv_m, &iv_mt, &iv_mt_old,
+                    &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &cg_ctl, &iv_m, &iv_mt, &iv_mt_old,
                     &iv_mopt, &iv_dx, &iv_P, &iv_mmin, &iv_mmax, &iv_m0, &iv_wl, &iv_tmp, &iv_tmp2,
                     &iv_dpre, &iv_d64, &iv_mstart, &iv_guard, &iv_flag};
   for (DevBuf *b : bufs) b->release();
   if (h_scal) cudaFreeHost(h_scal);
   if (h_flag) cudaFreeHost(h_flag);
+  if (h_ctl) cudaFreeHost(h_ctl);
   h_scal = nullptr;
   h_flag = nullptr;
+  h_ctl = nullptr;
 }
 
 namespace {
@@ -181,6 +183,7 @@ void Context::ensure_cg_workspace(int nterms) {
   cg_part.alloc(this, sizeof(double) * (size_t)sm_count * 4);
   if (!h_scal) GRADA_CUDA_CHECK(cudaMallocHost(&h_scal, sizeof(double) * CG_NSCALARS));
   if (!h_flag) GRADA_CUDA_CHECK(cudaMallocHost(&h_flag, sizeof(int) * 4));
+  if (!h_ctl) GRADA_CUDA_CHECK(cudaMallocHost(&h_ctl, sizeof(int) * CTL_NINTS));
   if (crg_enabled) {
     for (int t = 0; t < 3; t++) {
       if (crg[t].set) continue;
@@ -307,38 +310,83 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
   FT.count = nterms;
 
   CgResult res;
-  int i = 0;
-  for (i = 0; i < maxit; i++) {
-    launch_p_update(r, P, scal, Nm, p, pp, stream);
-    G_vec_mul_dev(pp, gx);
-    launch_scale(gx, dptr(wd), Nd, 1.0, t, stream);
-    launch_multi_forward(FT, Nm, pp, stream);
-    launch_dot(t, nullptr, nrow, part, nb_row, scal + CG_T2, stream);
-    launch_alpha(scal, stream);
-    launch_axpy(t, p, scal, nrow, Nm, s, dx, stream);
-    launch_scale(s, dptr(wd), Nd, 1.0, tmpd, stream);
-    GT_vec_mul_dev(tmpd, gtw);
-    launch_adjoint(AT_s, Nm, P, gtw, 1.0, r, stream);
-    launch_dot(r, nullptr, Nm, part, nb_m, scal + CG_R2NEW, stream);
-    launch_beta(scal, stream);
-    GRADA_CUDA_CHECK(cudaMemcpyAsync(h_scal, scal, sizeof(double) * CG_NSCALARS,
-                                     cudaMemcpyDeviceToHost, stream));
+  if (maxit <= 0) {  // the loop never runs: iterations = maxit (:1693-1696)
     sync();
-    res.err = h_scal[CG_ERR];
-    if (h_scal[CG_T2] == 0.0)
-      throw Error(GRADA_ERR_BREAKDOWN, "CG breakdown: ||t||^2 = 0 at iteration " + std::to_string(i));
-    if (!std::isfinite(h_scal[CG_ALPHA]) || !std::isfinite(res.err))
-      throw Error(GRADA_ERR_NONFINITE, "non-finite CG scalar at iteration " + std::to_string(i));
-    if (res.err < tol) {
-      res.iterations = i + 1;
-      return res;
+    return res;
+  }
+  // Device-side stopping: the beta kernel counts iterations and raises
+  // ctl[CTL_DONE] on err < tol (or maxit, breakdown, non-finite scalar);
+  // every kernel of an iteration returns at once while it is raised, so a
+  // CUDA graph of CG_GRAPH_ITERS iterations can be replayed until done with
+  // one host synchronisation per replay.
+  cg_ctl.alloc(this, sizeof(int) * CTL_NINTS);
+  int *ctl = cg_ctl.as<int>();
+  h_ctl[CTL_DONE] = 0;
+  h_ctl[CTL_ITER] = 0;
+  h_ctl[CTL_MAXIT] = maxit;
+  h_ctl[CTL_STATUS] = CG_STATUS_RUNNING;
+  upload(ctl, h_ctl, sizeof(int) * CTL_NINTS);
+  h_scal[CG_TOL] = tol;
+  upload(scal + CG_TOL, h_scal + CG_TOL, sizeof(double));
+  const DevG dG = devG();
+  double *sc = scratch_doubles(gemv_scratch_doubles(dG, sm_count));  // allocate before capture
+  const double *wdp = dptr(wd);
+  auto iteration = [&]() {
+    launch_p_update(r, P, scal, Nm, p, pp, stream, ctl);
+    GemvOpts o;
+    o.skip = ctl;
+    o.scale = wdp;  // t0 = Wd (G P p)
+    launch_G_vec_mul(dG, pp, t, sc, sm_count, stream, o);
+    launch_multi_forward(FT, Nm, pp, stream, ctl);
+    launch_dot(t, nullptr, nrow, part, nb_row, scal + CG_T2, stream, ctl);
+    launch_alpha(scal, ctl, stream);
+    launch_axpy(t, p, scal, nrow, Nm, s, dx, stream, ctl);
+    launch_GT_vec_mul(dG, s, gtw, sc, sm_count, stream, o);  // G^T (Wd s0)
+    launch_adjoint(AT_s, Nm, P, gtw, 1.0, r, stream, ctl);
+    launch_dot(r, nullptr, Nm, part, nb_m, scal + CG_R2NEW, stream, ctl);
+    launch_beta(scal, ctl, stream);
+  };
+  const int K = std::min(maxit, kCgGraphIters);
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  GRADA_CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    for (int k = 0; k < K; k++) iteration();
+  } catch (...) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(stream, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  GRADA_CUDA_CHECK(cudaStreamEndCapture(stream, &graph));
+  cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  GRADA_CUDA_CHECK(ie);
+  int launched = 0;
+  try {
+    while (true) {
+      GRADA_CUDA_CHECK(cudaGraphLaunch(exec, stream));
+      launched += K;
+      GRADA_CUDA_CHECK(cudaMemcpyAsync(h_ctl, ctl, sizeof(int) * CTL_NINTS,
+                                       cudaMemcpyDeviceToHost, stream));
+      GRADA_CUDA_CHECK(cudaMemcpyAsync(h_scal, scal, sizeof(double) * CG_NSCALARS,
+                                       cudaMemcpyDeviceToHost, stream));
+      sync();
+      if (h_ctl[CTL_DONE] || launched >= maxit) break;
     }
+  } catch (...) {
+    cudaGraphExecDestroy(exec);
+    throw;
   }
-  res.iterations = maxit;
-  if (maxit <= 0) {
-    sync();
-    res.err = 0.0;
-  }
+  cudaGraphExecDestroy(exec);
+  res.iterations = h_ctl[CTL_ITER];
+  res.err = h_scal[CG_ERR];
+  if (h_ctl[CTL_STATUS] == CG_STATUS_BREAKDOWN)
+    throw Error(GRADA_ERR_BREAKDOWN,
+                "CG breakdown: ||t||^2 = 0 at iteration " + std::to_string(res.iterations));
+  if (h_ctl[CTL_STATUS] == CG_STATUS_NONFINITE)
+    throw Error(GRADA_ERR_NONFINITE,
+                "non-finite CG scalar at iteration " + std::to_string(res.iterations));
   return res;
 }
 

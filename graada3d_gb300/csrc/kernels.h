@@ -52,12 +52,21 @@ struct DevG {
   int64_t nd = 0, nm = 0, ld = 0;
 };
 
+// Optional extras of the products: skip (device flag; when non-zero every
+// kernel of the product returns at once, so a captured CG iteration becomes a
+// no-op after convergence) and a diagonal row scale (G x: applied to the
+// result, y_r *= scale_r; G^T y: applied to the input, y_r -> scale_r y_r).
+struct GemvOpts {
+  const int *skip = nullptr;
+  const double *scale = nullptr;
+};
+
 // Scratch (in doubles) the products need for a given G, and the launches.
 int64_t gemv_scratch_doubles(const DevG &G, int sm_count);
 void launch_G_vec_mul(const DevG &G, const double *x, double *y, double *scratch, int sm_count,
-                      cudaStream_t s);
+                      cudaStream_t s, const GemvOpts &o = GemvOpts());
 void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratch, int sm_count,
-                       cudaStream_t s);
+                       cudaStream_t s, const GemvOpts &o = GemvOpts());
 // Columns [c0, c0+nc) of G widened to FP64 (scale applied for bf16) into
 // out (ld x nc, column-major).
 void launch_widen_columns(const DevG &G, int64_t c0, int64_t nc, double *out, cudaStream_t s);
