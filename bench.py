@@ -362,7 +362,7 @@ def inversion_problem(name: str):
     return c, prisms, obs, rho, rel, absf, ops, rng
 
 
-def run_inversion(name: str, storages=("fp64", "fp32", "bf16")):
+def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16")):
     """Inversion to chi^2 = N (misfit < 1) on the GPU: all-FP64 vs reduced-precision
     G with one FP64 residual refinement per Gauss-Newton iteration."""
     import torch

@@ -72,8 +72,9 @@ DevG Context::devG() const {
   DevG d;
   d.kind = (GKind)g_storage;
   d.data = G.ptr;
-  // The scale buffer may be left over from an earlier bf16 G; only bf16 uses it.
-  d.row_scale = (g_storage == GRADA_G_BF16_ROWSCALE) ? row_scale.as<float>() : nullptr;
+  // The scale buffer may be left over from an earlier 16-bit G; only those use it.
+  const bool scaled = g_storage == GRADA_G_BF16_ROWSCALE || g_storage == GRADA_G_FP16_ROWSCALE;
+  d.row_scale = scaled ? row_scale.as<float>() : nullptr;
   d.nd = nd;
   d.nm = n_cells;
   d.ld = ld;
@@ -139,7 +140,7 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
 
 void Context::compute_G(int storage) {
   require_geometry();
-  if (storage < GRADA_G_FP64 || storage > GRADA_G_BF16_ROWSCALE)
+  if (storage < GRADA_G_FP64 || storage > GRADA_G_FP16_ROWSCALE)
     throw Error(GRADA_ERR_INVALID_ARGUMENT, "unknown G storage");
   const DevGeometry g = geometry();
   const size_t n_entries = (size_t)ld * (size_t)n_cells;
@@ -160,8 +161,8 @@ void Context::compute_G(int storage) {
     launch_assemble_fp32(g, g.prisms, n_cells, nullptr, 0, tmp.as<float>(), ld, stream);
     G.alloc(this, n_entries * sizeof(uint16_t));
     row_scale.alloc(this, sizeof(float) * (size_t)nd);
-    launch_rowscale_bf16(tmp.as<float>(), nd, n_cells, ld, row_scale.as<float>(),
-                         G.as<uint16_t>(), stream);
+    launch_rowscale_16(tmp.as<float>(), nd, n_cells, ld, row_scale.as<float>(),
+                       G.as<uint16_t>(), storage == GRADA_G_FP16_ROWSCALE, stream);
     sync();
   }
   g_storage = storage;

@@ -100,15 +100,16 @@ __global__ void row_scale_kernel(const unsigned int *__restrict__ row_max_bits, 
   scale[row] = (m > 0.f) ? m : 1.f;
 }
 
-__global__ void quantize_bf16_kernel(const float *__restrict__ G, int64_t nd, int64_t nm,
-                                     int64_t ld, const float *__restrict__ scale,
-                                     __nv_bfloat16 *__restrict__ out) {
+__global__ void quantize_16_kernel(const float *__restrict__ G, int64_t nd, int64_t nm,
+                                   int64_t ld, const float *__restrict__ scale, int half16,
+                                   uint16_t *__restrict__ out) {
   const int64_t row = (int64_t)blockIdx.y * blockDim.x + threadIdx.x;
   const int64_t col = blockIdx.x;
   if (row >= ld) return;
   const int64_t idx = row + col * ld;
   const float v = (row < nd) ? G[idx] / scale[row] : 0.f;
-  out[idx] = __float2bfloat16_rn(v);
+  out[idx] = half16 ? __half_as_ushort(__float2half_rn(v))
+                    : __bfloat16_as_ushort(__float2bfloat16_rn(v));
 }
 
 // ---- matrix-free field sum ------------------------------------------------
@@ -241,8 +242,8 @@ void launch_assemble_fp32(const DevGeometry &g, const double *prisms, int64_t n_
   launch_assemble<float>(g, prisms, n_cells, col_index, col_offset, G, ld, s);
 }
 
-void launch_rowscale_bf16(const float *G32, int64_t nd, int64_t nm, int64_t ld, float *row_scale,
-                          uint16_t *Gbf, cudaStream_t s) {
+void launch_rowscale_16(const float *G32, int64_t nd, int64_t nm, int64_t ld, float *row_scale,
+                        uint16_t *G16, bool half16, cudaStream_t s) {
   // row_scale doubles as the atomicMax target (bit patterns) before scaling.
   unsigned int *bits = reinterpret_cast<unsigned int *>(row_scale);
   GRADA_CUDA_CHECK(cudaMemsetAsync(bits, 0, sizeof(unsigned int) * nd, s));
@@ -253,8 +254,7 @@ void launch_rowscale_bf16(const float *G32, int64_t nd, int64_t nm, int64_t ld, 
   row_scale_kernel<<<(unsigned)ceil_div(nd, 256), 256, 0, s>>>(bits, nd, row_scale);
   GRADA_LAUNCH_CHECK();
   dim3 g3((unsigned)nm, (unsigned)ceil_div(ld, 256));
-  quantize_bf16_kernel<<<g3, 256, 0, s>>>(G32, nd, nm, ld, row_scale,
-                                          reinterpret_cast<__nv_bfloat16 *>(Gbf));
+  quantize_16_kernel<<<g3, 256, 0, s>>>(G32, nd, nm, ld, row_scale, half16 ? 1 : 0, G16);
   GRADA_LAUNCH_CHECK();
 }
 

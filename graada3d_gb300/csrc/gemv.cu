@@ -65,6 +65,23 @@ struct LoadBF16 {
   }
 };
 
+struct LoadF16 {
+  static constexpr int VEC = 8;
+  using Acc = float;
+  __device__ static void load(const void *base, int64_t idx, float (&v)[8]) {
+    const uint4 d = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(base) + idx));
+    const uint32_t w[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      __half2 h;
+      memcpy(&h, &w[k], 4);
+      const float2 f = __half22float2(h);
+      v[2 * k] = f.x;
+      v[2 * k + 1] = f.y;
+    }
+  }
+};
+
 // ---- G x ----------------------------------------------------------------------
 
 template <class L>
@@ -221,9 +238,12 @@ __global__ void widen_kernel(const void *__restrict__ G, int kind, const float *
     v = static_cast<const double *>(G)[src];
   } else if (kind == 1) {
     v = (double)static_cast<const float *>(G)[src];
-  } else {
+  } else if (kind == 2) {
     const uint32_t bits = (uint32_t) static_cast<const uint16_t *>(G)[src] << 16;
     v = (double)__uint_as_float(bits) * (r < nd ? (double)scale[r] : 0.0);
+  } else {
+    const __half h = __ushort_as_half(static_cast<const uint16_t *>(G)[src]);
+    v = (double)__half2float(h) * (r < nd ? (double)scale[r] : 0.0);
   }
   out[r + c * ld] = v;
 }
@@ -257,6 +277,7 @@ void launch_G_vec_mul(const DevG &G, const double *x, double *y, double *scratch
     case GKind::FP64: run_gx<LoadF64>(G, x, y, scratch, sm_count, o, s); break;
     case GKind::FP32: run_gx<LoadF32>(G, x, y, scratch, sm_count, o, s); break;
     case GKind::BF16: run_gx<LoadBF16>(G, x, y, scratch, sm_count, o, s); break;
+    case GKind::FP16: run_gx<LoadF16>(G, x, y, scratch, sm_count, o, s); break;
   }
 }
 
@@ -299,6 +320,16 @@ void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratc
       GRADA_LAUNCH_CHECK();
       constexpr int COLS = 4;
       gty_kernel<LoadBF16, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
+          G.data, G.ld, G.nm, y32, x, o.skip);
+      break;
+    }
+    case GKind::FP16: {
+      float *y32 = reinterpret_cast<float *>(scratch);
+      prep_y_kernel<float><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, G.row_scale, o.scale, y32,
+                                                       o.skip);
+      GRADA_LAUNCH_CHECK();
+      constexpr int COLS = 4;
+      gty_kernel<LoadF16, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
           G.data, G.ld, G.nm, y32, x, o.skip);
       break;
     }

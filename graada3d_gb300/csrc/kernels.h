@@ -33,8 +33,9 @@ void launch_assemble_fp32(const DevGeometry &g, const double *prisms, int64_t n_
                           cudaStream_t s);
 // Per-row maximum of |G| over the columns, then bf16 entries G/scale with the
 // FP32 scale per row (entries of an all-zero row get scale 1).
-void launch_rowscale_bf16(const float *G32, int64_t nd, int64_t nm, int64_t ld, float *row_scale,
-                          uint16_t *Gbf, cudaStream_t s);
+// half16 = false: bf16; true: IEEE fp16 (entries in [-1, 1] after scaling).
+void launch_rowscale_16(const float *G32, int64_t nd, int64_t nm, int64_t ld, float *row_scale,
+                        uint16_t *G16, bool half16, cudaStream_t s);
 
 // Matrix-free field sum: fields[i*nf + k] = sum_j rho_j field_k(obs_i, cell_j).
 // `partial` must hold n_split * n_obs * nf doubles.
@@ -43,12 +44,12 @@ void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, 
                           double *fields, bool g_rows, cudaStream_t s);
 
 // ---- dense products (gemv.cu) -------------------------------------------
-enum class GKind : int { FP64 = 0, FP32 = 1, BF16 = 2 };
+enum class GKind : int { FP64 = 0, FP32 = 1, BF16 = 2, FP16 = 3 };
 
 struct DevG {
   GKind kind = GKind::FP64;
   const void *data = nullptr;
-  const float *row_scale = nullptr;  // bf16 only
+  const float *row_scale = nullptr;  // bf16 / fp16 only
   int64_t nd = 0, nm = 0, ld = 0;
 };
 

@@ -16,6 +16,7 @@ pytestmark = pytest.mark.gpu
 TOL_FP64 = 1e-10
 TOL_FP32 = 1e-5
 TOL_BF16 = 1e-2
+TOL_FP16 = 2e-3
 
 
 def _blocks(G, n_obs, nf):
@@ -110,7 +111,7 @@ def test_G_fp64_matches_oracle_and_products(gpu_ctx):
     np.testing.assert_allclose(f.GT_vec_mul(y), G.T @ y, rtol=0, atol=1e-12 * np.abs(G).sum(0).max())
 
 
-@pytest.mark.parametrize("storage,tol", [("fp32", TOL_FP32), ("bf16", TOL_BF16)])
+@pytest.mark.parametrize("storage,tol", [("fp32", TOL_FP32), ("fp16", TOL_FP16), ("bf16", TOL_BF16)])
 def test_G_reduced_storage(gpu_ctx, storage, tol):
     prisms, obs = _random_problem(3)
     mask = 0x072
