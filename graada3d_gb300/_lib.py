@@ -46,6 +46,7 @@ SIGNATURES = {
     "grada_G_vec_mul_dev": (c_int, [c_void_p, c_void_p, c_void_p]),
     "grada_GT_vec_mul_dev": (c_int, [c_void_p, c_void_p, c_void_p]),
     "grada_forward_field": (c_int, [c_void_p, _dp, _dp]),
+    "grada_expand_G": (c_int, [c_void_p, c_int64, _ip64, _dp]),
     "grada_forward_field_dev": (c_int, [c_void_p, c_void_p, c_void_p]),
     "grada_measure_fp64_peak": (c_int, [c_void_p, _dp]),
     "grada_set_operator": (c_int, [c_void_p, c_int, c_int64, c_int64, _ip32, _ip32, _dp]),

@@ -134,6 +134,7 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
   prisms.alloc(this, sizeof(double) * 6 * nc);
   obs.alloc(this, sizeof(double) * 3 * no);
   upload(prisms.ptr, h_prisms, sizeof(double) * 6 * nc);
+  host_prisms.assign(h_prisms, h_prisms + 6 * nc);
   upload(obs.ptr, h_obs, sizeof(double) * 3 * no);
   sync();
 }
@@ -348,6 +349,11 @@ int grada_G_vec_mul_dev(grada_ctx *ctx, const double *d_x, double *d_y) {
 
 int grada_GT_vec_mul_dev(grada_ctx *ctx, const double *d_y, double *d_x) {
   return guarded(ctx, [&] { ctx->GT_vec_mul_dev(d_y, d_x); });
+}
+
+int grada_expand_G(grada_ctx *ctx, int64_t n_split, const int64_t *parent_index,
+                   const double *child_prisms) {
+  return guarded(ctx, [&] { ctx->expand_G(n_split, parent_index, child_prisms); });
 }
 
 int grada_forward_field(grada_ctx *ctx, const double *rho, double *fields) {

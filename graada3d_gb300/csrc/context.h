@@ -77,6 +77,7 @@ struct Context {
   // Geometry (Fwd::mesh leaf cells, Fwd::ob, Fwd::field_flag) and the
   // prism kernels' math tables.
   DevBuf prisms, obs, math_tables;
+  std::vector<double> host_prisms;  // the cell list, kept for expand_G
   int64_t n_cells = 0, n_obs = 0, nd = 0, ld = 0;
   uint32_t mask = 0;
   int n_fields = 0;
@@ -145,6 +146,7 @@ struct Context {
   void G_vec_mul_dev(const double *d_x, double *d_y);
   void GT_vec_mul_dev(const double *d_y, double *d_x);
   void forward_field_dev(const double *d_rho, double *d_fields);
+  void expand_G(int64_t n_split, const int64_t *parent, const double *children);  // expand.cu
 };
 
 }  // namespace grada

@@ -37,6 +37,25 @@ def mask_fields(mask: int) -> list[str]:
     return [n for b, n in enumerate(FIELD_ORDER) if mask & (1 << b)]
 
 
+def split_cells(cells) -> np.ndarray:
+    """Children of each cell as Mesh::refinement makes them (Mesh.cpp:1562-1600):
+    split at the centre, x outermost, then y, z innermost.  (n, 8, 6)."""
+    c = np.asarray(cells, dtype=np.float64).reshape(-1, 6)
+    out = np.empty((c.shape[0], 8, 6))
+    mids = [0.5 * (c[:, 1] + c[:, 0]), 0.5 * (c[:, 3] + c[:, 2]), 0.5 * (c[:, 5] + c[:, 4])]
+    lo = [c[:, 0], c[:, 2], c[:, 4]]
+    hi = [c[:, 1], c[:, 3], c[:, 5]]
+    idx = 0
+    for i in range(2):
+        for j in range(2):
+            for k in range(2):
+                for a, s in enumerate((i, j, k)):
+                    out[:, idx, 2 * a] = lo[a] if s == 0 else mids[a]
+                    out[:, idx, 2 * a + 1] = mids[a] if s == 0 else hi[a]
+                idx += 1
+    return out
+
+
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
@@ -151,6 +170,28 @@ class Fwd:
         x = np.empty(self.Nm, dtype=np.float64)
         self.ctx.check(self.ctx.lib.grada_GT_vec_mul(self.ctx.handle, _ptr(y), _ptr(x)))
         return x
+
+    def expand_G(self, parent_index, children=None) -> None:
+        """AdaptiveInversion::expand_G: replace each listed cell (ascending
+        indices) by its 8 children (x outer, y, z inner; split at the centre when
+        children is None) in G and in the cell list."""
+        idx = np.ascontiguousarray(parent_index, dtype=np.int64)
+        kids = None
+        if children is not None:
+            kids = np.ascontiguousarray(children, dtype=np.float64).reshape(idx.size, 8, 6)
+        self.ctx.check(self.ctx.lib.grada_expand_G(
+            self.ctx.handle, idx.size, idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            None if kids is None else _ptr(kids)))
+        if kids is None:
+            kids = split_cells(self.prisms[idx])
+        parts, prev = [], 0
+        for k, j in enumerate(idx):
+            parts.append(self.prisms[prev:j])
+            parts.append(kids[k].reshape(8, 6))
+            prev = j + 1
+        parts.append(self.prisms[prev:])
+        self.prisms = np.ascontiguousarray(np.vstack(parts))
+        self._dims()
 
     def forward_field(self, rho) -> np.ndarray:
         """compute.cpp field sum: (N_obs, n_fields) array, components in bit order."""

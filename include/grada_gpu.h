@@ -136,6 +136,21 @@ int grada_G_vec_mul_noalloc(const double *d_G, int64_t nd, int64_t nm, int64_t l
                             const double *d_x, double *d_y, void *stream);
 
 /*
+ * Replaces AdaptiveInversion::expand_G (AdaptiveInversion.cpp:23-106) after
+ * the host's Mesh::refinement split n_split leaf cells: parent_index[n_split]
+ * (strictly ascending column indices of the current G) are each replaced, in
+ * place, by the columns of their 8 children; child_prisms holds n_split x 8 x 6
+ * doubles in Cell::child_cells order (x outer, y, z inner, Mesh.cpp:1579-1600),
+ * or NULL to split every parent at its centre as Mesh::refinement does.  G
+ * (FP64 or FP32 storage) and the context's cell list grow by 7 per split; the
+ * other columns keep their order.  The regularisation operators must be set
+ * again afterwards (the reference rebuilds them after a refinement,
+ * GaussNewtonInversion.cpp:1160-1290).
+ */
+int grada_expand_G(grada_ctx *ctx, int64_t n_split, const int64_t *parent_index,
+                   const double *child_prisms);
+
+/*
  * Replaces the field sum of compute.cpp:246-260 (and Fwd::compute_gobs,
  * Fwd.h:25-29, without storing G): fields[i*n_fields + k] =
  * sum_j rho[j] * field_k(obs_i, cell_j), FP64 evaluation and accumulation.
