@@ -413,6 +413,47 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16")):
     return out
 
 
+def run_matrix_free_cfg5():
+    """One matrix-free G x and G^T y at BASELINE configs[4] size: 128 x 128 x 64 =
+    1,048,576 cells over [0, 20 km]^2 x [0, 8 km], gz + Tzz at 201 x 201 points
+    50 m above (G would be 80,802 x 1,048,576 = 678 GB in FP64, beyond HBM)."""
+    import torch
+
+    from graada3d_gb300 import mesh
+    from graada3d_gb300.inversion import GaussNewtonInversion
+
+    prisms = mesh.regular_mesh((0.0, 20000.0), 128, (0.0, 20000.0), 128, (0.0, 8000.0), 64)
+    obs = mesh.observation_grid(201, 0.0, 20000.0, 201, 0.0, 20000.0, -50.0)
+    inv = GaussNewtonInversion(prisms, obs, 0x012)
+    inv.compute_G("matrix_free")
+    lib, h = inv.ctx.lib, inv.ctx.handle
+    import ctypes
+
+    dev = torch.device("cuda")
+    x = torch.randn(inv.Nm, dtype=torch.float64, device=dev)
+    y = torch.randn(inv.ld, dtype=torch.float64, device=dev)
+    dout = torch.empty(inv.ld, dtype=torch.float64, device=dev)
+    xout = torch.empty(inv.Nm, dtype=torch.float64, device=dev)
+    stream = torch.cuda.ExternalStream(inv.ctx.stream)
+    out = {"case": "matrix-free-cfg5", "cells": inv.Nm, "points": inv.N_obs, "rows": inv.Nd,
+           "pairs_per_product": inv.N_obs * inv.Nm}
+    for name, fn, a, b in (("G_x", lib.grada_G_vec_mul_dev, x, dout),
+                           ("GT_y", lib.grada_GT_vec_mul_dev, y, xout)):
+        fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()))  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        s = e0.elapsed_time(e1) * 1e-3
+        out[name] = {"s": s, "pairs_per_s": out["pairs_per_product"] / s,
+                     "G_entries_per_s": inv.Nd * inv.Nm / s}
+    out["cg_iteration_s"] = out["G_x"]["s"] + out["GT_y"]["s"]
+    inv.ctx.close()
+    return out
+
+
 def run_profile_case(args):
     """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
     50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
@@ -438,7 +479,7 @@ def run_profile_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-cfg1",
-                                                         "inversion-cfg3"])
+                                                         "inversion-cfg3", "matrix-free-cfg5"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -449,6 +490,8 @@ def main():
     args = ap.parse_args()
     if args.case == "profile":
         run_profile_case(args)
+    elif args.case == "matrix-free-cfg5":
+        print(json.dumps(run_matrix_free_cfg5()))
     elif args.case.startswith("inversion-"):
         print(json.dumps(run_inversion(args.case.split("-", 1)[1])))
     elif args.impl == "reference":

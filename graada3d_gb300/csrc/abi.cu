@@ -141,12 +141,15 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
 
 void Context::compute_G(int storage) {
   require_geometry();
-  if (storage < GRADA_G_FP64 || storage > GRADA_G_FP16_ROWSCALE)
+  if (storage < GRADA_G_FP64 || storage > GRADA_G_MATRIX_FREE)
     throw Error(GRADA_ERR_INVALID_ARGUMENT, "unknown G storage");
   const DevGeometry g = geometry();
   const size_t n_entries = (size_t)ld * (size_t)n_cells;
   g_storage = -1;
-  if (storage == GRADA_G_FP64) {
+  if (storage == GRADA_G_MATRIX_FREE) {
+    // nothing to assemble: products re-evaluate the prisms (cfg-5-sized G
+    // does not fit in HBM)
+  } else if (storage == GRADA_G_FP64) {
     G.alloc(this, n_entries * sizeof(double));
     if (ld > nd)
       GRADA_CUDA_CHECK(cudaMemsetAsync(G.ptr, 0, n_entries * sizeof(double), stream));
@@ -169,18 +172,48 @@ void Context::compute_G(int storage) {
   g_storage = storage;
 }
 
+int64_t Context::product_scratch_doubles() {
+  require_G();
+  if (g_storage == GRADA_G_MATRIX_FREE) {
+    const DevGeometry g = geometry();
+    const int64_t f = (int64_t)forward_field_splits(g, sm_count) * n_obs * n_fields;
+    const int64_t a = (int64_t)adjoint_field_splits(g, sm_count) * n_cells;
+    return f > a ? f : a;
+  }
+  return gemv_scratch_doubles(devG(), sm_count);
+}
+
+void Context::apply_G(const double *x, double *y, const GemvOpts &o) {
+  double *sc = scratch.as<double>();
+  if (g_storage == GRADA_G_MATRIX_FREE) {
+    const DevGeometry g = geometry();
+    launch_forward_field(g, x, forward_field_splits(g, sm_count), sc, y, true, stream, o.scale,
+                         o.skip);
+  } else {
+    launch_G_vec_mul(devG(), x, y, sc, sm_count, stream, o);
+  }
+}
+
+void Context::apply_GT(const double *y, double *x, const GemvOpts &o) {
+  double *sc = scratch.as<double>();
+  if (g_storage == GRADA_G_MATRIX_FREE) {
+    const DevGeometry g = geometry();
+    launch_adjoint_field(g, y, o.scale, adjoint_field_splits(g, sm_count), sc, x, stream, o.skip);
+  } else {
+    launch_GT_vec_mul(devG(), y, x, sc, sm_count, stream, o);
+  }
+}
+
 void Context::G_vec_mul_dev(const double *d_x, double *d_y) {
   require_G();
-  const DevG d = devG();
-  double *sc = scratch_doubles(gemv_scratch_doubles(d, sm_count));
-  launch_G_vec_mul(d, d_x, d_y, sc, sm_count, stream);
+  scratch_doubles(product_scratch_doubles());
+  apply_G(d_x, d_y, GemvOpts());
 }
 
 void Context::GT_vec_mul_dev(const double *d_y, double *d_x) {
   require_G();
-  const DevG d = devG();
-  double *sc = scratch_doubles(gemv_scratch_doubles(d, sm_count));
-  launch_GT_vec_mul(d, d_y, d_x, sc, sm_count, stream);
+  scratch_doubles(product_scratch_doubles());
+  apply_GT(d_y, d_x, GemvOpts());
 }
 
 void Context::forward_field_dev(const double *d_rho, double *d_fields) {
@@ -295,6 +328,8 @@ int grada_G_storage(const grada_ctx *ctx) { return ctx ? ctx->g_storage : -1; }
 int grada_get_G(grada_ctx *ctx, double *host, int64_t ld_host) {
   return guarded(ctx, [&] {
     ctx->require_G();
+    if (ctx->g_storage == GRADA_G_MATRIX_FREE)
+      throw Error(GRADA_ERR_STATE, "matrix-free mode stores no G");
     if (!host || ld_host < ctx->nd) throw Error(GRADA_ERR_INVALID_ARGUMENT, "bad host buffer");
     // Widen column blocks to FP64 on the device, then copy them out.
     const int64_t cols_per_block = 256;

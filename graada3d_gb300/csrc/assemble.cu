@@ -121,7 +121,9 @@ __global__ void __launch_bounds__(FF_THREADS)
     forward_field_kernel(const double *__restrict__ obs, int64_t n_obs,
                          const double *__restrict__ prisms, const double *__restrict__ rho,
                          int64_t n_cells, int64_t cells_per_split, uint32_t mask, int nf,
-                         const double *__restrict__ tables, double *__restrict__ partial) {
+                         const double *__restrict__ tables, double *__restrict__ partial,
+                         const int *__restrict__ skip) {
+  if (skip && *skip) return;
   __shared__ double sp[FF_CHUNK * 7];
   __shared__ double tab[kTabSize];
   for (int t = threadIdx.x; t < kTabSize; t += FF_THREADS) tab[t] = tables[t];
@@ -177,17 +179,100 @@ __global__ void __launch_bounds__(FF_THREADS)
 // written in G's row order (component k of point i at k*n_obs + i) instead of
 // point-major order.
 __global__ void sum_splits_kernel(const double *__restrict__ partial, int n_split, int64_t n,
-                                  int nf, int64_t n_obs, int g_rows, double *__restrict__ out) {
+                                  int nf, int64_t n_obs, int g_rows,
+                                  const double *__restrict__ post_scale, double *__restrict__ out,
+                                  const int *__restrict__ skip) {
+  if (skip && *skip) return;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   double s = 0.0;
   for (int k = 0; k < n_split; k++) s += partial[(int64_t)k * n + e];
   if (g_rows) {
     const int64_t i = e / nf, c = e - i * nf;
-    out[c * n_obs + i] = s;
+    const int64_t r = c * n_obs + i;
+    out[r] = post_scale ? post_scale[r] * s : s;
   } else {
     out[e] = s;
   }
+}
+
+// ---- matrix-free adjoint: x_j = sum_i sum_k G(k*n_obs+i, j) y(k*n_obs+i) ---
+
+constexpr int AD_THREADS = 128;
+constexpr int AD_CHUNK = 16;
+
+// One block: AD_CHUNK consecutive cells x the observation points of one
+// split.  Each thread evaluates its points against the chunk's cells and
+// keeps per-cell sums in shared memory; the block then reduces them over its
+// threads in a fixed order.  Splits are summed by a second pass.
+__global__ void __launch_bounds__(AD_THREADS)
+    adjoint_field_kernel(const double *__restrict__ obs, int64_t n_obs,
+                         const double *__restrict__ prisms, int64_t n_cells, uint32_t mask,
+                         const double *__restrict__ tables, const double *__restrict__ y,
+                         const double *__restrict__ pre_scale, int64_t obs_per_split,
+                         double *__restrict__ partial, const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  __shared__ double sp[AD_CHUNK * 6];
+  __shared__ double tab[kTabSize];
+  __shared__ double acc[AD_CHUNK][AD_THREADS];
+  for (int t = threadIdx.x; t < kTabSize; t += AD_THREADS) tab[t] = tables[t];
+  const int64_t c0 = (int64_t)blockIdx.x * AD_CHUNK;
+  const int nc = (int)min((int64_t)AD_CHUNK, n_cells - c0);
+  for (int t = threadIdx.x; t < nc * 6; t += AD_THREADS) sp[t] = prisms[c0 * 6 + t];
+#pragma unroll
+  for (int c = 0; c < AD_CHUNK; c++) acc[c][threadIdx.x] = 0.0;
+  __syncthreads();
+  const uint32_t fam = families_for_mask(mask);
+  const int64_t i_begin = (int64_t)blockIdx.y * obs_per_split;
+  const int64_t i_end = min(n_obs, i_begin + obs_per_split);
+  for (int64_t i = i_begin + threadIdx.x; i < i_end; i += AD_THREADS) {
+    const double px = obs[3 * i], py = obs[3 * i + 1], pz = obs[3 * i + 2];
+    double w[10];
+    int slot = 0;
+#pragma unroll
+    for (int b = 0; b < 10; b++) {
+      w[b] = 0.0;
+      if (mask & (1u << b)) {
+        const int64_t r = (int64_t)slot * n_obs + i;
+        w[b] = pre_scale ? pre_scale[r] * y[r] : y[r];
+        slot++;
+      }
+    }
+    ZCarry carry;
+    for (int c = 0; c < nc; c++) {
+      const double *p = sp + 6 * c;
+      const bool reuse = c > 0 && p[0] == p[-6] && p[1] == p[-5] && p[2] == p[-4] &&
+                         p[3] == p[-3] && p[4] == p[-1];
+      PrismTerms t;
+      prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, reuse, carry, t);
+      double s = acc[c][threadIdx.x];
+#pragma unroll
+      for (int b = 0; b < 10; b++)
+        if (mask & (1u << b)) s = fma(w[b], prism_component(t, b), s);
+      acc[c][threadIdx.x] = s;
+    }
+  }
+  __syncthreads();
+  // reduce each cell's AD_THREADS sums: warp w takes cells w, w + 4, ...
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c = warp; c < nc; c += AD_THREADS / 32) {
+    double v = 0.0;
+    for (int t = lane; t < AD_THREADS; t += 32) v += acc[c][t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) partial[(int64_t)blockIdx.y * n_cells + c0 + c] = v;
+  }
+}
+
+__global__ void sum_cell_splits_kernel(const double *__restrict__ partial, int n_split,
+                                       int64_t n_cells, double *__restrict__ x,
+                                       const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_cells) return;
+  double s = 0.0;
+  for (int k = 0; k < n_split; k++) s += partial[(int64_t)k * n_cells + j];
+  x[j] = s;
 }
 
 }  // namespace
@@ -225,6 +310,30 @@ void build_math_tables(double *tab) {
   const double pi64_hi = clear_low((double)pi64, 9);
   tab[kTabConst + 2] = pi64_hi;
   tab[kTabConst + 3] = (double)(pi64 - (long double)pi64_hi);
+}
+
+int adjoint_field_splits(const DevGeometry &g, int sm_count) {
+  const int64_t chunks = ceil_div(g.n_cells, AD_CHUNK);
+  int64_t splits = ceil_div((int64_t)sm_count * 8, chunks);
+  const int64_t max_splits = ceil_div(g.n_obs, AD_THREADS);
+  if (splits > max_splits) splits = max_splits;
+  if (splits < 1) splits = 1;
+  if (splits > 65535) splits = 65535;
+  return (int)splits;
+}
+
+void launch_adjoint_field(const DevGeometry &g, const double *y, const double *pre_scale,
+                          int n_split, double *partial, double *x, cudaStream_t s,
+                          const int *skip) {
+  if (g.n_cells <= 0) return;
+  const int64_t per = ceil_div(g.n_obs, n_split);
+  dim3 grid((unsigned)ceil_div(g.n_cells, AD_CHUNK), (unsigned)n_split);
+  adjoint_field_kernel<<<grid, AD_THREADS, 0, s>>>(g.obs, g.n_obs, g.prisms, g.n_cells, g.mask,
+                                                   g.tables, y, pre_scale, per, partial, skip);
+  GRADA_LAUNCH_CHECK();
+  sum_cell_splits_kernel<<<(unsigned)ceil_div(g.n_cells, 256), 256, 0, s>>>(partial, n_split,
+                                                                           g.n_cells, x, skip);
+  GRADA_LAUNCH_CHECK();
 }
 
 int math_table_size() { return kTabSize; }
@@ -270,17 +379,18 @@ int forward_field_splits(const DevGeometry &g, int sm_count) {
 }
 
 void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, double *partial,
-                          double *fields, bool g_rows, cudaStream_t s) {
+                          double *fields, bool g_rows, cudaStream_t s, const double *post_scale,
+                          const int *skip) {
   if (g.n_obs <= 0) return;
   const int64_t per = round_up(ceil_div(g.n_cells, n_split), FF_CHUNK);
   dim3 grid((unsigned)n_split, (unsigned)ceil_div(g.n_obs, FF_THREADS));
   if (grid.y > 65535u) throw Error(-1, "too many observation points for one launch");
   forward_field_kernel<<<grid, FF_THREADS, 0, s>>>(g.obs, g.n_obs, g.prisms, rho, g.n_cells, per,
-                                                   g.mask, g.n_fields, g.tables, partial);
+                                                   g.mask, g.n_fields, g.tables, partial, skip);
   GRADA_LAUNCH_CHECK();
   const int64_t n = g.n_obs * g.n_fields;
-  sum_splits_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(partial, n_split, n, g.n_fields,
-                                                               g.n_obs, g_rows ? 1 : 0, fields);
+  sum_splits_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(
+      partial, n_split, n, g.n_fields, g.n_obs, g_rows ? 1 : 0, post_scale, fields, skip);
   GRADA_LAUNCH_CHECK();
 }
 

@@ -145,6 +145,12 @@ struct Context {
   void compute_G(int storage);
   void G_vec_mul_dev(const double *d_x, double *d_y);
   void GT_vec_mul_dev(const double *d_y, double *d_x);
+  // y = G x and x = G^T y for every storage, matrix-free included (GemvOpts
+  // scale: G x result / G^T y input; skip: CG stop flag).  Scratch must be
+  // sized first with product_scratch_doubles().
+  int64_t product_scratch_doubles();
+  void apply_G(const double *x, double *y, const GemvOpts &o);
+  void apply_GT(const double *y, double *x, const GemvOpts &o);
   void forward_field_dev(const double *d_rho, double *d_fields);
   void expand_G(int64_t n_split, const int64_t *parent, const double *children);  // expand.cu
 };

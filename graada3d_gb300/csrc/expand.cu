@@ -23,7 +23,8 @@ namespace grada {
 
 void Context::expand_G(int64_t n_split, const int64_t *parent, const double *children) {
   require_G();
-  if (g_storage != GRADA_G_FP64 && g_storage != GRADA_G_FP32)
+  const bool matrix_free = g_storage == GRADA_G_MATRIX_FREE;
+  if (!matrix_free && g_storage != GRADA_G_FP64 && g_storage != GRADA_G_FP32)
     throw Error(GRADA_ERR_INVALID_ARGUMENT,
                 "expand_G needs G stored in FP64 or FP32 (re-assemble 16-bit storage instead)");
   if (n_split < 0) throw Error(GRADA_ERR_INVALID_ARGUMENT, "negative split count");
@@ -87,6 +88,16 @@ void Context::expand_G(int64_t n_split, const int64_t *parent, const double *chi
       dst += 8;
       src = parent[k] + 1;
     }
+  }
+  if (matrix_free) {  // no matrix to splice: only the cell list changes
+    n_cells = nm_new;
+    host_prisms.swap(new_prisms);
+    prisms.alloc(this, sizeof(double) * 6 * nm_new);
+    upload(prisms.ptr, host_prisms.data(), sizeof(double) * 6 * nm_new);
+    sync();
+    for (auto &o : ops) o.set = false;
+    for (auto &o : crg) o.set = false;
+    return;
   }
   const size_t esz = (g_storage == GRADA_G_FP64) ? sizeof(double) : sizeof(float);
   DevBuf newG;

@@ -328,20 +328,19 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
   upload(ctl, h_ctl, sizeof(int) * CTL_NINTS);
   h_scal[CG_TOL] = tol;
   upload(scal + CG_TOL, h_scal + CG_TOL, sizeof(double));
-  const DevG dG = devG();
-  double *sc = scratch_doubles(gemv_scratch_doubles(dG, sm_count));  // allocate before capture
+  scratch_doubles(product_scratch_doubles());  // allocate before capture
   const double *wdp = dptr(wd);
   auto iteration = [&]() {
     launch_p_update(r, P, scal, Nm, p, pp, stream, ctl);
     GemvOpts o;
     o.skip = ctl;
     o.scale = wdp;  // t0 = Wd (G P p)
-    launch_G_vec_mul(dG, pp, t, sc, sm_count, stream, o);
+    apply_G(pp, t, o);
     launch_multi_forward(FT, Nm, pp, stream, ctl);
     launch_dot(t, nullptr, nrow, part, nb_row, scal + CG_T2, stream, ctl);
     launch_alpha(scal, ctl, stream);
     launch_axpy(t, p, scal, nrow, Nm, s, dx, stream, ctl);
-    launch_GT_vec_mul(dG, s, gtw, sc, sm_count, stream, o);  // G^T (Wd s0)
+    apply_GT(s, gtw, o);  // G^T (Wd s0)
     launch_adjoint(AT_s, Nm, P, gtw, 1.0, r, stream, ctl);
     launch_dot(r, nullptr, Nm, part, nb_m, scal + CG_R2NEW, stream, ctl);
     launch_beta(scal, ctl, stream);
@@ -428,7 +427,8 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
   iv_dpre.alloc(this, sizeof(double) * ld);
   iv_guard.alloc(this, sizeof(int) * Nm);
   iv_flag.alloc(this, sizeof(int) * 4);
-  const bool refine = prm.fp64_refinement && g_storage != GRADA_G_FP64;
+  const bool refine =
+      prm.fp64_refinement && g_storage != GRADA_G_FP64 && g_storage != GRADA_G_MATRIX_FREE;
   if (refine) iv_d64.alloc(this, sizeof(double) * ld);
   ensure_cg_workspace(crg_enabled ? 7 : 4);
   upload(iv_m.ptr, m.data(), vb);

@@ -40,8 +40,17 @@ void launch_rowscale_16(const float *G32, int64_t nd, int64_t nm, int64_t ld, fl
 // Matrix-free field sum: fields[i*nf + k] = sum_j rho_j field_k(obs_i, cell_j).
 // `partial` must hold n_split * n_obs * nf doubles.
 int forward_field_splits(const DevGeometry &g, int sm_count);
+// With g_rows the result is in G's row order and may be post-scaled; skip as
+// in GemvOpts.
 void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, double *partial,
-                          double *fields, bool g_rows, cudaStream_t s);
+                          double *fields, bool g_rows, cudaStream_t s,
+                          const double *post_scale = nullptr, const int *skip = nullptr);
+// Matrix-free G^T y (y in G's row order, optionally pre-scaled); `partial`
+// holds n_split * n_cells doubles.
+int adjoint_field_splits(const DevGeometry &g, int sm_count);
+void launch_adjoint_field(const DevGeometry &g, const double *y, const double *pre_scale,
+                          int n_split, double *partial, double *x, cudaStream_t s,
+                          const int *skip = nullptr);
 
 // ---- dense products (gemv.cu) -------------------------------------------
 enum class GKind : int { FP64 = 0, FP32 = 1, BF16 = 2, FP16 = 3 };

@@ -22,8 +22,9 @@ FIELD_BITS = {
 }
 FIELD_ORDER = ["V", "gz", "gx", "gy", "Tzz", "Txz", "Tyz", "Txx", "Txy", "Tyy"]
 
-G_FP64, G_FP32, G_BF16_ROWSCALE, G_FP16_ROWSCALE = 0, 1, 2, 3
-STORAGE = {"fp64": G_FP64, "fp32": G_FP32, "bf16": G_BF16_ROWSCALE, "fp16": G_FP16_ROWSCALE}
+G_FP64, G_FP32, G_BF16_ROWSCALE, G_FP16_ROWSCALE, G_MATRIX_FREE = 0, 1, 2, 3, 4
+STORAGE = {"fp64": G_FP64, "fp32": G_FP32, "bf16": G_BF16_ROWSCALE, "fp16": G_FP16_ROWSCALE,
+           "matrix_free": G_MATRIX_FREE}
 
 
 def field_mask(names) -> int:

@@ -64,6 +64,7 @@ extern "C" {
 #define GRADA_G_FP32 1          /* FP64 evaluation rounded to FP32 */
 #define GRADA_G_BF16_ROWSCALE 2 /* bf16 entries times an FP32 scale per row */
 #define GRADA_G_FP16_ROWSCALE 3 /* fp16 entries (|v| <= 1) times an FP32 scale per row */
+#define GRADA_G_MATRIX_FREE 4   /* nothing stored: each product re-evaluates the prisms (FP64) */
 
 typedef struct grada_ctx grada_ctx;
 
