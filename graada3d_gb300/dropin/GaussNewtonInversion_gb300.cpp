@@ -1,0 +1,90 @@
+// Drop-in body for GaussNewtonInversion::solve_cg
+// (src/Inversion/GaussNewtonInversion.cpp:1417-1698) against the unchanged
+// GaussNewtonInversion.h.  A maintainer removes solve_cg from
+// GaussNewtonInversion.cpp and links this file (with Fwd_gb300.cpp,
+// gb300_bridge.cpp and libgrada_gpu.so).  invert_with_own_CG, the lambda
+// search, IRLS and the mesh refinement stay in the reference's host code and
+// call this solve_cg and the GPU-backed G_vec_mul; for a fixed mesh the whole
+// loop can instead go to grada_invert.
+//
+// The host-built operators (Eigen RowMajor SMatrix, gs.h:29) are passed as
+// their compressed arrays; the diagonal matrices (Wd, P, WL_*) as diagonals.
+#include <vector>
+
+#include "GaussNewtonInversion.h"
+#include "gb300_bridge.h"
+
+namespace {
+
+std::vector<double> diagonal(const SMatrix &m) {
+  std::vector<double> d((size_t)m.rows());
+  for (int i = 0; i < m.rows(); i++) d[(size_t)i] = m.coeff(i, i);
+  return d;
+}
+
+void upload(grada_ctx *ctx, int which, const SMatrix &m0) {
+  SMatrix m = m0;
+  m.makeCompressed();
+  gb300::check(ctx,
+               grada_set_operator(ctx, which, m.rows(), m.nonZeros(), m.outerIndexPtr(),
+                                  m.innerIndexPtr(), m.valuePtr()),
+               "grada_set_operator");
+}
+
+}  // namespace
+
+VectorXd GaussNewtonInversion::solve_cg(const double tol,
+                                        const int &maxit,
+                                        double &err,
+                                        int &iterations,
+                                        const double &lambda,
+                                        const VectorXd &mk,
+                                        const VectorXd &mref,
+                                        const SMatrix &Wd,
+                                        const VectorXd &dobs,
+                                        const SMatrix &P,
+                                        const SMatrix &Ws,
+                                        const SMatrix &Wx,
+                                        const SMatrix &Wy,
+                                        const SMatrix &Wz,
+                                        const SMatrix &Tx0,
+                                        const SMatrix &Ty0,
+                                        const SMatrix &Tz0,
+                                        const SMatrix &WL_s,
+                                        const SMatrix &WL_x,
+                                        const SMatrix &WL_y,
+                                        const SMatrix &WL_z,
+                                        const SMatrix &WL_tx,
+                                        const SMatrix &WL_ty,
+                                        const SMatrix &WL_tz)
+{
+  grada_ctx *ctx = gb300::context_for(static_cast<const Fwd *>(this));
+  const std::vector<double> wd = diagonal(Wd);
+  gb300::check(ctx, grada_set_data(ctx, dobs.data(), wd.data()), "grada_set_data");
+  upload(ctx, GRADA_OP_WS, Ws);
+  upload(ctx, GRADA_OP_WX, Wx);
+  upload(ctx, GRADA_OP_WY, Wy);
+  upload(ctx, GRADA_OP_WZ, Wz);
+  if (use_cross_gradient_constraint) {
+    upload(ctx, GRADA_OP_TX, Tx0);
+    upload(ctx, GRADA_OP_TY, Ty0);
+    upload(ctx, GRADA_OP_TZ, Tz0);
+    const std::vector<double> s = diagonal(S_crg);
+    gb300::check(ctx, grada_set_cross_gradient(ctx, 1, a_crg, s.data()),
+                 "grada_set_cross_gradient");
+  } else {
+    gb300::check(ctx, grada_set_cross_gradient(ctx, 0, 0.0, nullptr), "grada_set_cross_gradient");
+  }
+  const std::vector<double> p = diagonal(P);
+  const std::vector<double> wl[7] = {diagonal(WL_s),  diagonal(WL_x),  diagonal(WL_y),
+                                     diagonal(WL_z),  diagonal(WL_tx), diagonal(WL_ty),
+                                     diagonal(WL_tz)};
+  const double *wlp[7];
+  for (int k = 0; k < 7; k++) wlp[k] = wl[k].data();
+  VectorXd dx(Nm);
+  gb300::check(ctx,
+               grada_solve_cg(ctx, tol, maxit, lambda, mk.data(), mref.data(), p.data(), wlp,
+                              dx.data(), &err, &iterations),
+               "grada_solve_cg");
+  return dx;
+}
