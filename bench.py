@@ -454,6 +454,52 @@ def run_matrix_free_cfg5():
     return out
 
 
+def run_gemv_case():
+    """G x and G^T y alone at the 40,804 x 196,608 (configs[2]-sized) G, every
+    storage kind: 3 warm-up + 10 timed calls each, CUDA events on the context
+    stream; G (16-64 GB) is far larger than L2."""
+    import ctypes
+
+    import torch
+
+    from graada3d_gb300 import Fwd, mesh
+
+    prisms = mesh.regular_mesh((0.0, 10000.0), 64, (0.0, 10000.0), 64, (0.0, 5000.0), 48)
+    obs = mesh.observation_grid(101, 0.0, 10000.0, 101, 0.0, 10000.0, -100.0)
+    f = Fwd(prisms, obs, 0x072)
+    lib, h = f.ctx.lib, f.ctx.handle
+    stream = torch.cuda.ExternalStream(f.ctx.stream)
+    dev = torch.device("cuda")
+    x = torch.randn(f.Nm, dtype=torch.float64, device=dev)
+    y = torch.randn(f.ld, dtype=torch.float64, device=dev)
+    ox = torch.empty(f.Nm, dtype=torch.float64, device=dev)
+    oy = torch.empty(f.ld, dtype=torch.float64, device=dev)
+    peak = json.loads((REPO / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs") \
+        if (REPO / "MEASURED_PEAKS.json").exists() else None
+    res = {"case": "gemv", "rows": f.Nd, "cols": f.Nm, "hbm_peak_GBps": peak}
+    for st, bpe in (("fp64", 8), ("fp32", 4), ("fp16", 2), ("bf16", 2)):
+        f.compute_G(st)
+        gbytes = f.ld * f.Nm * bpe + 8 * (f.Nd + f.Nm)
+        for name, fn, a, b in (("G_x", lib.grada_G_vec_mul_dev, x, oy),
+                               ("GT_y", lib.grada_GT_vec_mul_dev, y, ox)):
+            for _ in range(3):
+                fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(10):
+                fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / 10
+            r = {"ms": ms, "GBps": gbytes / ms / 1e6}
+            if peak:
+                r["frac_of_hbm"] = r["GBps"] / peak
+            res[f"{st}_{name}"] = r
+    f.ctx.close()
+    return res
+
+
 def run_profile_case(args):
     """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
     50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
@@ -479,7 +525,8 @@ def run_profile_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-cfg1",
-                                                         "inversion-cfg3", "matrix-free-cfg5"])
+                                                         "inversion-cfg3", "matrix-free-cfg5",
+                                                         "gemv"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -490,6 +537,8 @@ def main():
     args = ap.parse_args()
     if args.case == "profile":
         run_profile_case(args)
+    elif args.case == "gemv":
+        print(json.dumps(run_gemv_case()))
     elif args.case == "matrix-free-cfg5":
         print(json.dumps(run_matrix_free_cfg5()))
     elif args.case.startswith("inversion-"):
