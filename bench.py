@@ -500,6 +500,72 @@ def run_gemv_case():
     return res
 
 
+def run_batched_cfg4(n_problems: int = 64):
+    """BASELINE configs[3] part 2: independent inversions of uneven size (uniform
+    meshes nx = ny, nz = nx/2 with 4k-60k cells, square point grids of 400-5,000
+    points, gz + Tzz, seeded models, seeds 100..163), run one after the other and
+    then as one concurrent batch (one context, host thread and stream each)."""
+    import torch
+
+    from graada3d_gb300 import Context, mesh
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.inversion import GaussNewtonInversion, compute_G_batch, invert_batch
+
+    prm = dict(max_lambda=1e-1, n_lambda=30, rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6,
+               cg_factor=50, gn_iter=10, lp=[2, 2, 2, 2, 2], eps2=1e-9)
+    invs, args, sizes = [], [], []
+    for k in range(n_problems):
+        rng = np.random.default_rng(100 + k)
+        cells = int(rng.integers(4000, 60001))
+        nx = max(4, int(round((2 * cells) ** (1 / 3))))
+        nz = max(2, nx // 2)
+        pts = int(rng.integers(400, 5001))
+        no = max(2, int(round(pts ** 0.5)))
+        L = 10000.0
+        prisms = mesh.regular_mesh((0.0, L), nx, (0.0, L), nx, (0.0, L / 2), nz)
+        obs = mesh.observation_grid(no, 0.0, L, no, 0.0, L, -100.0)
+        boxes = []
+        for v in (300.0, -200.0):
+            s_ = rng.uniform(1000, 3000, 3)
+            x0, y0, z0 = rng.uniform(0, L - s_[0]), rng.uniform(0, L - s_[1]), rng.uniform(0, L / 2 - s_[2])
+            boxes.append([x0, x0 + s_[0], y0, y0 + s_[1], z0, z0 + s_[2], v])
+        rho = mesh.set_boxes(prisms, boxes)
+        inv = GaussNewtonInversion(prisms, obs, 0x012, ctx=Context(0))
+        inv.compute_G("fp64")
+        d = inv.G_vec_mul(rho)
+        dobs = d + 0.02 * np.abs(d) * rng.standard_normal(d.size)
+        inv.set_cross_gradient(False)
+        inv.set_operators(reg.regular_mesh_operators((nx, nx, nz), prisms, obs, 1.5))
+        inv.set_dobs(dobs, reg.data_weights(dobs, [0.02, 0.02], [1e-3, 1e-2], obs.shape[0]))
+        invs.append(inv)
+        nm = inv.Nm
+        args.append((np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0)))
+        sizes.append((nm, obs.shape[0]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for inv in invs:
+        inv.compute_G("fp64")
+    seq = [inv.invert(prm, *a) for inv, a in zip(invs, args)]
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    compute_G_batch(invs, "fp64")
+    bat = invert_batch(invs, [prm] * n_problems, [a[0] for a in args], [a[1] for a in args],
+                       [a[2] for a in args])
+    torch.cuda.synchronize()
+    t_bat = time.perf_counter() - t0
+    same = all(np.array_equal(a[0], b[0]) for a, b in zip(seq, bat))
+    reached = sum(1 for _, r in bat if r["final_misfit"] < 1.0)
+    for inv in invs:
+        inv.ctx.close()
+    return {"case": "batched-cfg4", "problems": n_problems,
+            "cells_range": [min(s[0] for s in sizes), max(s[0] for s in sizes)],
+            "points_range": [min(s[1] for s in sizes), max(s[1] for s in sizes)],
+            "sequential_s": t_seq, "batched_s": t_bat, "speedup": t_seq / t_bat,
+            "identical_models": same, "chi2_reached": reached,
+            "cg_iterations": int(sum(r["cg_iterations"] for _, r in bat))}
+
+
 def run_profile_case(args):
     """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
     50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
@@ -526,7 +592,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-cfg1",
                                                          "inversion-cfg3", "matrix-free-cfg5",
-                                                         "gemv"])
+                                                         "gemv", "batched-cfg4"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -537,6 +603,8 @@ def main():
     args = ap.parse_args()
     if args.case == "profile":
         run_profile_case(args)
+    elif args.case == "batched-cfg4":
+        print(json.dumps(run_batched_cfg4()))
     elif args.case == "gemv":
         print(json.dumps(run_gemv_case()))
     elif args.case == "matrix-free-cfg5":

@@ -59,6 +59,10 @@ SIGNATURES = {
     "grada_get_iterations": (c_int, [c_void_p, _dp, c_int64, _ip64]),
     "grada_G_vec_mul_noalloc": (c_int, [c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p,
                                         c_void_p]),
+    "grada_compute_G_batch": (c_int, [c_int, POINTER(c_void_p), c_int, c_int, POINTER(c_int)]),
+    "grada_invert_batch": (c_int, [c_int, POINTER(c_void_p), c_void_p, POINTER(_dp), POINTER(_dp),
+                                   POINTER(_dp), POINTER(_dp), POINTER(_dp), c_void_p, c_int,
+                                   POINTER(c_int)]),
 }
 
 

@@ -3,9 +3,11 @@
 // flag, and the dense sensitivity matrix it owns (src/Forward_modelling/Fwd.h:14-94).
 // Every entry point converts internal errors into a status code and keeps
 // the message for grada_last_error().
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/grada_gpu.h"
@@ -253,6 +255,33 @@ int guarded(grada_ctx *ctx, F &&f) {
 
 }  // namespace
 
+namespace {
+
+// Runs job(k) for k in [0, n) on up to max_threads host threads; each k is
+// taken by exactly one thread, so each context is driven by one thread.
+template <class F>
+int run_batch(int n, int max_threads, int *statuses, F &&job) {
+  if (n <= 0) return GRADA_OK;
+  int nt = (max_threads <= 0 || max_threads > n) ? n : max_threads;
+  std::atomic<int> next(0);
+  std::vector<int> st(n, GRADA_OK);
+  auto worker = [&]() {
+    for (int k = next++; k < n; k = next++) st[k] = job(k);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; t++) pool.emplace_back(worker);
+  worker();
+  for (auto &th : pool) th.join();
+  int first = GRADA_OK;
+  for (int k = 0; k < n; k++) {
+    if (statuses) statuses[k] = st[k];
+    if (first == GRADA_OK && st[k] != GRADA_OK) first = st[k];
+  }
+  return first;
+}
+
+}  // namespace
+
 extern "C" {
 
 int grada_version(void) { return 100; }
@@ -491,6 +520,26 @@ int grada_get_trials(const grada_ctx *ctx, double *rows, int64_t cap, int64_t *n
     o[4] = t.cg_error;
   }
   return GRADA_OK;
+}
+
+int grada_compute_G_batch(int n, grada_ctx *const *ctxs, int storage, int max_threads,
+                          int *statuses) {
+  if (n < 0 || (n > 0 && !ctxs)) return GRADA_ERR_INVALID_ARGUMENT;
+  return run_batch(n, max_threads, statuses,
+                   [&](int k) { return grada_compute_G(ctxs[k], storage); });
+}
+
+int grada_invert_batch(int n, grada_ctx *const *ctxs, const grada_invert_params *params,
+                       const double *const *m_ini, const double *const *m_min,
+                       const double *const *m_max, const double *const *m0s,
+                       double *const *m_out, grada_invert_report *reports, int max_threads,
+                       int *statuses) {
+  if (n < 0 || (n > 0 && (!ctxs || !params || !m_ini || !m_min || !m_max || !m_out)))
+    return GRADA_ERR_INVALID_ARGUMENT;
+  return run_batch(n, max_threads, statuses, [&](int k) {
+    return grada_invert(ctxs[k], &params[k], m_ini[k], m_min[k], m_max[k], m0s ? m0s[k] : nullptr,
+                        m_out[k], reports ? &reports[k] : nullptr);
+  });
 }
 
 int grada_get_iterations(const grada_ctx *ctx, double *rows, int64_t cap, int64_t *n) {

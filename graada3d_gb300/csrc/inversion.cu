@@ -314,6 +314,13 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
     sync();
     return res;
   }
+  // A zero right-hand side (A^T s = 0 already, e.g. no data signal and m at the
+  // reference) is solved by dx = 0; the reference would divide 0 by 0 in its
+  // first step.  Return the exact solution instead of a breakdown.
+  GRADA_CUDA_CHECK(cudaMemcpyAsync(h_scal, scal, sizeof(double) * CG_NSCALARS,
+                                   cudaMemcpyDeviceToHost, stream));
+  sync();
+  if (h_scal[CG_R2] == 0.0) return res;
   // Device-side stopping: the beta kernel counts iterations and raises
   // ctl[CTL_DONE] on err < tol (or maxit, breakdown, non-finite scalar);
   // every kernel of an iteration returns at once while it is raised, so a

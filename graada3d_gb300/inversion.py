@@ -84,19 +84,7 @@ class GaussNewtonInversion(Fwd):
         """invert_with_own_CG on the current G.  prm keys as oracle.inversion.invert
         (max_lambda, n_lambda, rate, target, stag, cg_tol, cg_factor, gn_iter,
         lp[5], eps2, start_from_reference).  Returns (m, report)."""
-        p = InvertParams()
-        p.max_lambda = prm["max_lambda"]
-        p.n_lambda = prm["n_lambda"]
-        p.lambda_decreasing_rate = prm["rate"]
-        p.target_misfit = prm["target"]
-        p.stag_tol = prm["stag"]
-        p.cg_tol = prm["cg_tol"]
-        p.cg_iteration_factor = prm["cg_factor"]
-        p.gn_iterations = prm["gn_iter"]
-        p.lp_s, p.lp_x, p.lp_y, p.lp_z, p.lp_t = (int(v) for v in prm["lp"])
-        p.epsilon2 = prm["eps2"]
-        p.start_from_reference = int(bool(prm.get("start_from_reference", False)))
-        p.fp64_refinement = int(bool(fp64_refinement))
+        p = _params(prm, fp64_refinement)
         vecs = [np.ascontiguousarray(v, dtype=np.float64) for v in (m_ini, m_min, m_max)]
         m0a = None if m0 is None else np.ascontiguousarray(m0, dtype=np.float64)
         out = np.empty(self.Nm)
@@ -123,3 +111,70 @@ class GaussNewtonInversion(Fwd):
         self.ctx.check(self.ctx.lib.grada_get_iterations(self.ctx.handle, _ptr(out), n.value,
                                                          ctypes.byref(n)))
         return out
+
+
+def _params(prm: dict, fp64_refinement: bool) -> InvertParams:
+    p = InvertParams()
+    p.max_lambda = prm["max_lambda"]
+    p.n_lambda = prm["n_lambda"]
+    p.lambda_decreasing_rate = prm["rate"]
+    p.target_misfit = prm["target"]
+    p.stag_tol = prm["stag"]
+    p.cg_tol = prm["cg_tol"]
+    p.cg_iteration_factor = prm["cg_factor"]
+    p.gn_iterations = prm["gn_iter"]
+    p.lp_s, p.lp_x, p.lp_y, p.lp_z, p.lp_t = (int(v) for v in prm["lp"])
+    p.epsilon2 = prm["eps2"]
+    p.start_from_reference = int(bool(prm.get("start_from_reference", False)))
+    p.fp64_refinement = int(bool(fp64_refinement))
+    return p
+
+
+def compute_G_batch(invs, storage="fp64", max_threads: int = 0) -> None:
+    """grada_compute_G_batch over the contexts of several Fwd/GaussNewtonInversion objects."""
+    from .fwd import STORAGE
+
+    lib = invs[0].ctx.lib
+    n = len(invs)
+    ctxs = (ctypes.c_void_p * n)(*[i.ctx.handle.value for i in invs])
+    st = (ctypes.c_int * n)()
+    s = STORAGE[storage] if isinstance(storage, str) else int(storage)
+    rc = lib.grada_compute_G_batch(n, ctxs, s, int(max_threads), st)
+    if rc != 0:
+        bad = [k for k in range(n) if st[k] != 0]
+        invs[bad[0]].ctx.check(st[bad[0]])
+
+
+def invert_batch(invs, prms, m_inis, m_mins, m_maxs, m0s=None, fp64_refinement=False,
+                 max_threads: int = 0):
+    """grada_invert_batch: the inversions of several GaussNewtonInversion objects run
+    concurrently.  Returns [(m, report)] in input order."""
+    lib = invs[0].ctx.lib
+    n = len(invs)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ctxs = (ctypes.c_void_p * n)(*[i.ctx.handle.value for i in invs])
+    params = (InvertParams * n)(*[_params(p, fp64_refinement) for p in prms])
+    keep = []
+
+    def arr(vs):
+        out = (dp * n)()
+        for k, v in enumerate(vs):
+            if v is None:
+                out[k] = dp()
+            else:
+                a = np.ascontiguousarray(v, dtype=np.float64)
+                keep.append(a)
+                out[k] = _ptr(a)
+        return out
+
+    outs = [np.empty(i.Nm) for i in invs]
+    reports = (InvertReport * n)()
+    st = (ctypes.c_int * n)()
+    rc = lib.grada_invert_batch(n, ctxs, params, arr(m_inis), arr(m_mins), arr(m_maxs),
+                                arr(m0s if m0s is not None else [None] * n), arr(outs), reports,
+                                int(max_threads), st)
+    if rc != 0:
+        bad = [k for k in range(n) if st[k] != 0]
+        invs[bad[0]].ctx.check(st[bad[0]])
+    return [(outs[k], {f: getattr(reports[k], f) for f, _ in InvertReport._fields_})
+            for k in range(n)]

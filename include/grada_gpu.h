@@ -260,6 +260,26 @@ int grada_invert(grada_ctx *ctx, const grada_invert_params *params, const double
 int grada_get_trials(const grada_ctx *ctx, double *rows, int64_t cap, int64_t *n);
 int grada_get_iterations(const grada_ctx *ctx, double *rows, int64_t cap, int64_t *n);
 
+/*
+ * Many independent problems at once (no reference counterpart; the reference
+ * runs one inversion per process).  Each context must be set up as for the
+ * single calls; the batch runs them concurrently, one host thread per context
+ * (at most max_threads, 0 = one per context) and each context on its own
+ * stream, so small problems that cannot fill the GPU alone overlap on it.
+ * statuses[n] gets each problem's status; the call returns GRADA_OK if all
+ * succeeded, else the first failing status.
+ *  grada_compute_G_batch: grada_compute_G(ctxs[k], storage) for every k.
+ *  grada_invert_batch: grada_invert(ctxs[k], params[k], ...) for every k, the
+ *  vectors given per problem (m0s[k] may be NULL, as may m0s itself).
+ */
+int grada_compute_G_batch(int n, grada_ctx *const *ctxs, int storage, int max_threads,
+                          int *statuses);
+int grada_invert_batch(int n, grada_ctx *const *ctxs, const grada_invert_params *params,
+                       const double *const *m_ini, const double *const *m_min,
+                       const double *const *m_max, const double *const *m0s,
+                       double *const *m_out, grada_invert_report *reports, int max_threads,
+                       int *statuses);
+
 #ifdef __cplusplus
 }
 #endif
