@@ -566,6 +566,133 @@ def run_batched_cfg4(n_problems: int = 64):
             "cg_iterations": int(sum(r["cg_iterations"] for _, r in bat))}
 
 
+def sweep_problem():
+    """BASELINE configs[3] part 1 geometry: configs[1]'s mesh (64 x 64 x 32 =
+    131,072 cells over [0, 20 km]^2 x [0, 8 km]) and points (101 x 101 at 50 m),
+    the gz + Tzz rows of its G (20,402 x 131,072), its 20-box model, data with 2 %
+    seeded noise."""
+    from graada3d_gb300 import regularization as reg
+
+    prisms, obs, rho = build_problem()
+    ops = reg.regular_mesh_operators((64, 64, 32), prisms, obs, 1.5)
+    return prisms, obs, rho, ops
+
+
+def _peak_gbs():
+    p = REPO / "MEASURED_PEAKS.json"
+    return json.loads(p.read_text()).get("hbm_gbs") if p.exists() else None
+
+
+def run_block_gemm_case():
+    """The 16-column block products G X and G^T Y against sixteen single products,
+    on the 20,402 x 131,072 gz + Tzz G of configs[1]'s geometry, each storage:
+    3 warm-up + 10 timed calls, CUDA events on the context stream.  G (5-21 GB)
+    is far larger than L2."""
+    import ctypes
+
+    import torch
+
+    from graada3d_gb300 import Fwd
+
+    prisms, obs, rho, _ = sweep_problem()
+    f = Fwd(prisms, obs, 0x012)
+    lib, h = f.ctx.lib, f.ctx.handle
+    stream = torch.cuda.ExternalStream(f.ctx.stream)
+    dev = torch.device("cuda")
+    X = torch.randn(f.Nm * 16, dtype=torch.float64, device=dev)
+    Y = torch.randn(f.ld * 16, dtype=torch.float64, device=dev)
+    oX = torch.empty(f.Nm * 16, dtype=torch.float64, device=dev)
+    oY = torch.empty(f.ld * 16, dtype=torch.float64, device=dev)
+    x1 = torch.randn(f.Nm, dtype=torch.float64, device=dev)
+    y1 = torch.randn(f.ld, dtype=torch.float64, device=dev)
+    o1 = torch.empty(max(f.Nm, f.ld), dtype=torch.float64, device=dev)
+    peak = _peak_gbs()
+    res = {"case": "block-gemm", "rows": f.Nd, "cols": f.Nm, "rhs": 16, "hbm_peak_GBps": peak}
+
+    def timed(fn, a, b, reps=10):
+        for _ in range(3):
+            f.ctx.check(fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr())))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    for st, bpe in (("fp32", 4), ("bf16", 2), ("fp16", 2), ("fp64", 8)):
+        f.compute_G(st)
+        gbytes = f.ld * f.Nm * bpe
+        flops = 2.0 * f.Nd * f.Nm * 16
+        for name, fb, a, b, fs, a1 in (("G_X", lib.grada_G_block_mul_dev, X, oY, lib.grada_G_vec_mul_dev, x1),
+                                        ("GT_Y", lib.grada_GT_block_mul_dev, Y, oX, lib.grada_GT_vec_mul_dev, y1)):
+            ms = timed(fb, a, b, reps=10 if st != "fp64" else 3)
+            ms1 = timed(fs, a1, o1)
+            r = {"ms": ms, "GBps": gbytes / ms / 1e6, "TFLOPs": flops / ms / 1e9,
+                 "single_product_ms": ms1, "speedup_vs_16_single": 16 * ms1 / ms}
+            if peak:
+                r["frac_of_hbm"] = r["GBps"] / peak
+            res[f"{st}_{name}"] = r
+    f.ctx.close()
+    return res
+
+
+def run_sweep_cfg4(n_lambda: int = 16, gn_iter: int = 5):
+    """BASELINE configs[3] part 1: a 16-value regularisation sweep (lambda
+    log-spaced 1e-3 .. 1e1) on the shared gz + Tzz G of configs[1]'s geometry,
+    each lambda a fixed-lambda Gauss-Newton run (L2, CG <= 50, up to gn_iter
+    iterations), run as one block (block CG, tensor-core products) and, for
+    comparison, as 16 separate inversions."""
+    import torch
+
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.inversion import GaussNewtonInversion
+
+    prisms, obs, rho, ops = sweep_problem()
+    inv = GaussNewtonInversion(prisms, obs, 0x012)
+    inv.compute_G("fp64")
+    d = inv.G_vec_mul(rho)
+    dobs = d + 0.02 * np.abs(d) * np.random.default_rng(3).standard_normal(d.size)
+    wd = reg.data_weights(dobs, [0.02, 0.02], [1e-3, 1e-2], obs.shape[0])
+    inv.set_cross_gradient(False)
+    inv.set_operators(ops)
+    inv.set_dobs(dobs, wd)
+    nm = inv.Nm
+    lam = np.logspace(-3, 1, n_lambda)
+    prm = dict(max_lambda=1e-1, n_lambda=1, rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6,
+               cg_factor=50, gn_iter=gn_iter, lp=[2, 2, 2, 2, 2], eps2=1e-9)
+    args = (np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0))
+    out = {"case": "sweep-cfg4", "cells": nm, "data": inv.Nd, "lambdas": n_lambda,
+           "gn_iter_max": gn_iter}
+    models = {}
+    for st in ("fp64", "fp32", "bf16"):
+        if st != "fp64":
+            inv.compute_G(st)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m, reps = inv.lambda_sweep(prm, lam, *args, fp64_refinement=(st != "fp64"))
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        models[st] = m
+        r = {"block_s": t, "misfits": [round(x["final_misfit"], 4) for x in reps],
+             "cg_iterations": int(sum(x["cg_iterations"] for x in reps)),
+             "gn_iterations": [int(x["gn_iterations"]) for x in reps]}
+        if st != "fp64":
+            rel = [float(np.linalg.norm(m[:, c] - models["fp64"][:, c]) /
+                         max(np.linalg.norm(models["fp64"][:, c]), 1e-30)) for c in range(n_lambda)]
+            r["model_rel_diff_vs_fp64_max"] = max(rel)
+            t0 = time.perf_counter()
+            for c in range(n_lambda):
+                inv.invert(dict(prm, max_lambda=float(lam[c])), *args, fp64_refinement=True)
+            torch.cuda.synchronize()
+            r["sequential_s"] = time.perf_counter() - t0
+            r["speedup_block_vs_sequential"] = r["sequential_s"] / t
+        out[st] = r
+    inv.ctx.close()
+    return out
+
+
 def run_profile_case(args):
     """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
     50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
@@ -592,7 +719,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-cfg1",
                                                          "inversion-cfg3", "matrix-free-cfg5",
-                                                         "gemv", "batched-cfg4"])
+                                                         "gemv", "batched-cfg4", "block-gemm",
+                                                         "sweep-cfg4"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -603,6 +731,10 @@ def main():
     args = ap.parse_args()
     if args.case == "profile":
         run_profile_case(args)
+    elif args.case == "block-gemm":
+        print(json.dumps(run_block_gemm_case()))
+    elif args.case == "sweep-cfg4":
+        print(json.dumps(run_sweep_cfg4()))
     elif args.case == "batched-cfg4":
         print(json.dumps(run_batched_cfg4()))
     elif args.case == "gemv":

@@ -63,6 +63,15 @@ SIGNATURES = {
     "grada_invert_batch": (c_int, [c_int, POINTER(c_void_p), c_void_p, POINTER(_dp), POINTER(_dp),
                                    POINTER(_dp), POINTER(_dp), POINTER(_dp), c_void_p, c_int,
                                    POINTER(c_int)]),
+    "grada_G_mat_mul": (c_int, [c_void_p, c_int, _dp, _dp]),
+    "grada_GT_mat_mul": (c_int, [c_void_p, c_int, _dp, _dp]),
+    "grada_G_block_mul_dev": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "grada_GT_block_mul_dev": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "grada_solve_cg_block": (c_int, [c_void_p, c_double, c_int, c_int, _dp, _dp, _dp, _dp,
+                                     POINTER(_dp), _dp, _dp, POINTER(c_int)]),
+    "grada_lambda_sweep": (c_int, [c_void_p, c_void_p, c_int, _dp, _dp, _dp, _dp, _dp, _dp,
+                                   c_void_p]),
+    "grada_get_sweep_trials": (c_int, [c_void_p, c_int, _dp, c_int64, _ip64]),
 }
 
 

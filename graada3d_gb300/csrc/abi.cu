@@ -556,4 +556,62 @@ int grada_get_iterations(const grada_ctx *ctx, double *rows, int64_t cap, int64_
   return GRADA_OK;
 }
 
+int grada_G_mat_mul(grada_ctx *ctx, int n_rhs, const double *X, double *Y) {
+  return guarded(ctx, [&] { ctx->G_mat_mul_host(n_rhs, X, Y, false); });
+}
+
+int grada_GT_mat_mul(grada_ctx *ctx, int n_rhs, const double *Y, double *X) {
+  return guarded(ctx, [&] { ctx->G_mat_mul_host(n_rhs, Y, X, true); });
+}
+
+int grada_G_block_mul_dev(grada_ctx *ctx, const double *d_X, double *d_Y) {
+  return guarded(ctx, [&] {
+    ctx->ensure_block_scratch(false);
+    ctx->apply_G_block(d_X, d_Y, grada::GemvOpts());
+  });
+}
+
+int grada_GT_block_mul_dev(grada_ctx *ctx, const double *d_Y, double *d_X) {
+  return guarded(ctx, [&] {
+    ctx->ensure_block_scratch(false);
+    ctx->apply_GT_block(d_Y, d_X, grada::GemvOpts());
+  });
+}
+
+int grada_solve_cg_block(grada_ctx *ctx, double tol, int maxit, int n_rhs, const double *lambda,
+                         const double *mk, const double *mref, const double *P,
+                         const double *const WL[7], double *dx, double *err, int *iterations) {
+  return guarded(ctx, [&] {
+    ctx->solve_cg_block_host(tol, maxit, n_rhs, lambda, mk, mref, P, WL, dx, err, iterations);
+  });
+}
+
+int grada_lambda_sweep(grada_ctx *ctx, const grada_invert_params *prm, int n_lambda,
+                       const double *lambdas, const double *m_ini, const double *m_min,
+                       const double *m_max, const double *m0, double *m_out,
+                       grada_invert_report *reports) {
+  if (!prm) return GRADA_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    ctx->lambda_sweep(*prm, n_lambda, lambdas, m_ini, m_min, m_max, m0, m_out, reports);
+  });
+}
+
+int grada_get_sweep_trials(const grada_ctx *ctx, int column, double *rows, int64_t cap,
+                           int64_t *n) {
+  if (!ctx || column < 0 || column >= (int)ctx->sweep_trials.size())
+    return GRADA_ERR_INVALID_ARGUMENT;
+  const std::vector<grada::TrialRecord> &tr = ctx->sweep_trials[column];
+  const int64_t total = (int64_t)tr.size();
+  if (n) *n = total;
+  for (int64_t k = 0; k < total && k < cap && rows; k++) {
+    double *o = rows + 5 * k;
+    o[0] = tr[k].gn_iteration;
+    o[1] = tr[k].lambda;
+    o[2] = tr[k].misfit;
+    o[3] = tr[k].cg_iterations;
+    o[4] = tr[k].cg_error;
+  }
+  return GRADA_OK;
+}
+
 }  // extern "C"

@@ -100,4 +100,67 @@ void launch_irls_weight(const double *v, int64_t n, double eps2, double expo, do
 void launch_sub(const double *a, const double *b, int64_t n, double *out, cudaStream_t s);
 void launch_add(const double *a, const double *b, int64_t n, double *out, cudaStream_t s);
 
+// ---- block solves (cg_block.cu) ---------------------------------------------
+// A block vector holds kBW right-hand sides row-interleaved: element (i, c) of
+// an n x kBW block is at [i * kBW + c], so the kBW values of one row share a
+// 128-byte line and every per-row kernel is coalesced across the columns.
+constexpr int kBW = 16;
+
+// Per-column scalar slots: column c's CG_* scalars at scal[c * CG_NSCALARS + slot].
+// Control block of a block solve (ints): [CTLB_ALL] = every column stopped,
+// column c's CTL_* slots at [CTLB_COL + c * CTL_NINTS + slot].
+enum : int { CTLB_ALL = 0, CTLB_COL = 4, CTLB_NINTS = 4 + kBW * CTL_NINTS };
+
+// out = c[col] * wl .* (A x)   for up to 7 terms; wl a block or null
+struct BForwardTerms {
+  DevCSR A[7];
+  double c[7][kBW];
+  const double *wl[7];
+  double *out[7];
+  int count = 0;
+};
+// contribution c[col] * A^T (wl .* s) per term, A^T given as CSR
+struct BAdjointTerms {
+  DevCSR AT[7];
+  double c[7][kBW];
+  const double *wl[7];
+  const double *s[7];
+  int count = 0;
+};
+
+// y = c[col] * wl .* (A (x - xs)); x and y blocks, xs a plain vector or null.
+void launch_bcsr_apply(const DevCSR &A, const double *x, const double *xs, const double *c,
+                       const double *wl, double *y, cudaStream_t s);
+void launch_bmulti_forward(const BForwardTerms &T, int64_t n, const double *x, cudaStream_t s,
+                           const int *skip);
+void launch_badjoint(const BAdjointTerms &T, int64_t n, const double *P, const double *gtw,
+                     double sign_g, double *r, cudaStream_t s, const int *skip);
+// Per-column dot products of two blocks (b null: a.a) into scal[c*CG_NSCALARS + slot].
+void launch_bdot(const double *a, const double *b, int64_t n, double *partial, int nblocks,
+                 double *scal, int slot, cudaStream_t s, const int *skip);
+void launch_bmisfit_sq(const double *g, const double *dobs, const double *wd, int64_t n,
+                       double *partial, int nblocks, double *scal, int slot, cudaStream_t s);
+void launch_bdata_residual(const double *dobs, const double *g, const double *wd, int64_t n,
+                           double *b0, double *s0, cudaStream_t s);
+// out(i, c) = w_i * a(i, c)
+void launch_bscale_rows(const double *a, const double *w, int64_t n, double *out, cudaStream_t s);
+void launch_bp_update(const double *r, const double *P, const double *scal, int64_t n, double *p,
+                      double *pp, cudaStream_t s, const int *skip);
+void launch_baxpy(const double *t, const double *p, const double *scal, int64_t nrow, int64_t n,
+                  double *sv, double *dx, cudaStream_t s, const int *skip);
+void launch_balpha(double *scal, int *ctl, cudaStream_t s);
+void launch_bbeta(double *scal, int *ctl, cudaStream_t s);
+// Bound transform per column; guard and mt_old are blocks, any_guard holds
+// kBW ints (pinned host copy in h_any_guard).
+void launch_bbound_update(const double *m, const double *dx, const double *mmin,
+                          const double *mmax, int64_t n, double *mt, const double *mt_old,
+                          int *guard, int *any_guard, int *h_any_guard, cudaStream_t s);
+void launch_bp_diag(const double *m, const double *mmin, const double *mmax, int64_t n, double *P,
+                    cudaStream_t s);
+// dst(:, c) = src(:, c) for the columns whose bit is set in mask.
+void launch_bcopy_columns(const double *src, int64_t n, uint32_t mask, double *dst, cudaStream_t s);
+// Block <-> column-major host layout (n x ncol, leading dimension n) on the device.
+void launch_bpack(const double *colmajor, int64_t n, int ncol, double *block, cudaStream_t s);
+void launch_bunpack(const double *block, int64_t n, int ncol, double *colmajor, cudaStream_t s);
+
 }  // namespace grada

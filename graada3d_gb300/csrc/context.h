@@ -115,6 +115,18 @@ struct Context {
   std::vector<TrialRecord> trials;
   std::vector<IterationRecord> iterations;
 
+  // Block solves and the lambda sweep (sweep.cu).  Block vectors hold kBW
+  // columns row-interleaved (cg_kernels.h).
+  DevBuf bscratch, tc_err;
+  DevBuf bk_b, bk_s, bk_t, bk_p, bk_pp, bk_r, bk_atb, bk_gtw, bk_gx, bk_tmpd, bk_scal, bk_part,
+      bk_ctl, bk_coef;
+  DevBuf sw_m, sw_mt, sw_mt_old, sw_mopt, sw_dx, sw_P, sw_mmin, sw_mmax, sw_m0, sw_wl, sw_tmp,
+      sw_tmp2, sw_dpre, sw_d64, sw_mstart, sw_guard, sw_flag, sw_in, sw_out;
+  double *h_bscal = nullptr;  // pinned, kBW * CG_NSCALARS
+  int *h_bctl = nullptr;      // pinned, CTLB_NINTS
+  int *h_bflag = nullptr;     // pinned, kBW + 1
+  std::vector<std::vector<TrialRecord>> sweep_trials;
+
   void release_all();
 
   // inversion.cu
@@ -153,6 +165,27 @@ struct Context {
   void apply_GT(const double *y, double *x, const GemvOpts &o);
   void forward_field_dev(const double *d_rho, double *d_fields);
   void expand_G(int64_t n_split, const int64_t *parent, const double *children);  // expand.cu
+
+  // sweep.cu: block products (kBW columns) for every storage, the block CG
+  // solve and the fixed-lambda sweep.
+  void ensure_block_scratch(bool fp64_forward);
+  void apply_G_block(const double *X, double *Y, const GemvOpts &o);
+  void apply_GT_block(const double *Y, double *X, const GemvOpts &o);
+  void check_tc_error();
+  void ensure_block_workspace(int nterms);
+  void block_prediction(const double *m, const double *m_start, const double *d64, double *out);
+  void block_misfits(const double *m, const double *m_start, const double *d64, double *out);
+  void solve_cg_block_dev(const double *lambda, uint32_t active, double tol, int maxit,
+                          const double *mk, const double *mref, const double *P,
+                          const double *const WL[7], double *dx, const double *d64,
+                          const double *m_start, CgResult *res);
+  void G_mat_mul_host(int n, const double *X, double *Y, bool transpose);
+  void solve_cg_block_host(double tol, int maxit, int n, const double *lambda, const double *mk,
+                           const double *mref, const double *P, const double *const WL[7],
+                           double *dx, double *err, int *iters);
+  void lambda_sweep(const grada_invert_params &prm, int n, const double *lambdas,
+                    const double *m_ini, const double *mmin, const double *mmax, const double *m0,
+                    double *m_out, grada_invert_report *reps);
 };
 
 }  // namespace grada

@@ -59,14 +59,25 @@ void Context::release_all() {
   DevBuf *bufs[] = {&dobs, &wd, &cg_b, &cg_s, &cg_t, &cg_p, &cg_pp, &cg_r, &cg_atb, &cg_gtw,
                     &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &cg_ctl, &iv_m, &iv_mt, &iv_mt_old,
                     &iv_mopt, &iv_dx, &iv_P, &iv_mmin, &iv_mmax, &iv_m0, &iv_wl, &iv_tmp, &iv_tmp2,
-                    &iv_dpre, &iv_d64, &iv_mstart, &iv_guard, &iv_flag};
+                    &iv_dpre, &iv_d64, &iv_mstart, &iv_guard, &iv_flag,
+                    &bscratch, &tc_err, &bk_b, &bk_s, &bk_t, &bk_p, &bk_pp, &bk_r, &bk_atb,
+                    &bk_gtw, &bk_gx, &bk_tmpd, &bk_scal, &bk_part, &bk_ctl, &bk_coef, &sw_m, &sw_mt,
+                    &sw_mt_old, &sw_mopt, &sw_dx, &sw_P, &sw_mmin, &sw_mmax, &sw_m0, &sw_wl,
+                    &sw_tmp, &sw_tmp2, &sw_dpre, &sw_d64, &sw_mstart, &sw_guard, &sw_flag, &sw_in,
+                    &sw_out};
   for (DevBuf *b : bufs) b->release();
   if (h_scal) cudaFreeHost(h_scal);
   if (h_flag) cudaFreeHost(h_flag);
   if (h_ctl) cudaFreeHost(h_ctl);
+  if (h_bscal) cudaFreeHost(h_bscal);
+  if (h_bctl) cudaFreeHost(h_bctl);
+  if (h_bflag) cudaFreeHost(h_bflag);
   h_scal = nullptr;
   h_flag = nullptr;
   h_ctl = nullptr;
+  h_bscal = nullptr;
+  h_bctl = nullptr;
+  h_bflag = nullptr;
 }
 
 namespace {

@@ -81,6 +81,36 @@ void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratc
 // out (ld x nc, column-major).
 void launch_widen_columns(const DevG &G, int64_t c0, int64_t nc, double *out, cudaStream_t s);
 
+// ---- block products (block_gemm.cu, tc_gemm.cu) -------------------------
+// Y = G X and X = G^T Y for blocks of kBW = 16 right-hand sides, row-
+// interleaved ([row * 16 + col], see cg_kernels.h).  Y has nd rows (rows
+// nd..ld-1 are neither read nor written).  GemvOpts as for the products
+// above, per row.  FP64 G runs on the FP64 pipe; FP32 and 16-bit G run on the
+// tensor cores (tc_gemm.cu).  `err` is a device int that a tensor-core
+// launch raises (bit flags) when one of its bounded waits gives up.
+int64_t block_scratch_bytes(const DevG &G, int sm_count);
+void launch_G_mat_mul(const DevG &G, const double *X, double *Y, void *scratch, int sm_count,
+                      cudaStream_t s, const GemvOpts &o, int *err);
+void launch_GT_mat_mul(const DevG &G, const double *Y, double *X, void *scratch, int sm_count,
+                       cudaStream_t s, const GemvOpts &o, int *err);
+
+// Tensor-core implementation for FP32 (3xTF32 split) and 16-bit G (A exact,
+// right-hand sides split into two 16-bit parts).
+bool tc_supported(const DevG &G);
+int64_t tc_scratch_bytes(const DevG &G, int sm_count);
+void launch_tc_G_mat_mul(const DevG &G, const double *X, double *Y, void *scratch, int sm_count,
+                         cudaStream_t s, const GemvOpts &o, int *err);
+void launch_tc_GT_mat_mul(const DevG &G, const double *Y, double *X, void *scratch, int sm_count,
+                          cudaStream_t s, const GemvOpts &o, int *err);
+
+// Matrix-free block products: every (point, cell) pair evaluated once for all
+// 16 right-hand sides (FP64).
+int64_t mf_block_scratch_doubles(const DevGeometry &g, int sm_count);
+void launch_forward_field_block(const DevGeometry &g, const double *X, double *Y, double *scratch,
+                                int sm_count, cudaStream_t s, const GemvOpts &o);
+void launch_adjoint_field_block(const DevGeometry &g, const double *Y, double *X, double *scratch,
+                                int sm_count, cudaStream_t s, const GemvOpts &o);
+
 // ---- diagnostics (diag.cu) ----------------------------------------------
 double measure_fp64_fma_rate(int sm_count, cudaStream_t s);
 

@@ -172,6 +172,20 @@ class Fwd:
         self.ctx.check(self.ctx.lib.grada_GT_vec_mul(self.ctx.handle, _ptr(y), _ptr(x)))
         return x
 
+    def G_mat_mul(self, X) -> np.ndarray:
+        """Y = G X for a block of right-hand sides X (Nm x n); n x G_vec_mul."""
+        X = np.asfortranarray(np.asarray(X, dtype=np.float64).reshape(self.Nm, -1))
+        Y = np.empty((self.Nd, X.shape[1]), dtype=np.float64, order="F")
+        self.ctx.check(self.ctx.lib.grada_G_mat_mul(self.ctx.handle, X.shape[1], _ptr(X), _ptr(Y)))
+        return Y
+
+    def GT_mat_mul(self, Y) -> np.ndarray:
+        """X = G^T Y for a block Y (Nd x n); n x GT_vec_mul."""
+        Y = np.asfortranarray(np.asarray(Y, dtype=np.float64).reshape(self.Nd, -1))
+        X = np.empty((self.Nm, Y.shape[1]), dtype=np.float64, order="F")
+        self.ctx.check(self.ctx.lib.grada_GT_mat_mul(self.ctx.handle, Y.shape[1], _ptr(Y), _ptr(X)))
+        return X
+
     def expand_G(self, parent_index, children=None) -> None:
         """AdaptiveInversion::expand_G: replace each listed cell (ascending
         indices) by its 8 children (x outer, y, z inner; split at the centre when

@@ -94,6 +94,61 @@ class GaussNewtonInversion(Fwd):
             None if m0a is None else _ptr(m0a), _ptr(out), ctypes.byref(rep)))
         return out, {f: getattr(rep, f) for f, _ in InvertReport._fields_}
 
+    def solve_cg_block(self, tol, maxit, lambdas, mk, mref, P, WL=None):
+        """Several solve_cg systems at once (grada_solve_cg_block): column c has
+        lambdas[c], mk[:, c], P[:, c] and WL[key][:, c] (Nm x n arrays; a WL entry
+        may also be None).  Returns (dx (Nm x n), err (n), iterations (n))."""
+        lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+        n = lam.size
+        blk = lambda a: np.asfortranarray(np.broadcast_to(
+            np.asarray(a, dtype=np.float64).reshape(self.Nm, -1), (self.Nm, n)))
+        mk_b, P_b = blk(mk), blk(P)
+        mref_v = np.ascontiguousarray(mref, dtype=np.float64)
+        arr = (ctypes.POINTER(ctypes.c_double) * 7)()
+        keep = []
+        for k, key in enumerate(WL_ORDER):
+            w = None if WL is None else WL.get(key)
+            if w is None:
+                arr[k] = ctypes.POINTER(ctypes.c_double)()
+            else:
+                wb = blk(w)
+                keep.append(wb)
+                arr[k] = _ptr(wb)
+        dx = np.empty((self.Nm, n), order="F")
+        err = np.empty(n)
+        it = (ctypes.c_int * n)()
+        self.ctx.check(self.ctx.lib.grada_solve_cg_block(
+            self.ctx.handle, float(tol), int(maxit), n, _ptr(lam), _ptr(mk_b), _ptr(mref_v),
+            _ptr(P_b), arr, _ptr(dx), _ptr(err), it))
+        return dx, err, np.array(it[:], dtype=int)
+
+    def lambda_sweep(self, prm: dict, lambdas, m_ini, m_min, m_max, m0=None,
+                     fp64_refinement: bool = False):
+        """grada_lambda_sweep: for each lambda the fixed-lambda Gauss-Newton run
+        (invert with n_lambda = 1, max_lambda = lambda), all lambdas advancing
+        together with block CG solves.  Returns (models (Nm x n), [report])."""
+        lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+        n = lam.size
+        p = _params(dict(prm, max_lambda=float(lam[0]), n_lambda=1), fp64_refinement)
+        vecs = [np.ascontiguousarray(v, dtype=np.float64) for v in (m_ini, m_min, m_max)]
+        m0a = None if m0 is None else np.ascontiguousarray(m0, dtype=np.float64)
+        out = np.empty((self.Nm, n), order="F")
+        reps = (InvertReport * n)()
+        self.ctx.check(self.ctx.lib.grada_lambda_sweep(
+            self.ctx.handle, ctypes.byref(p), n, _ptr(lam), _ptr(vecs[0]), _ptr(vecs[1]),
+            _ptr(vecs[2]), None if m0a is None else _ptr(m0a), _ptr(out), reps))
+        return out, [{f: getattr(reps[k], f) for f, _ in InvertReport._fields_} for k in range(n)]
+
+    def sweep_trials(self, column: int) -> np.ndarray:
+        """(n, 5) trial records of one column of the last lambda_sweep."""
+        n = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.grada_get_sweep_trials(self.ctx.handle, int(column), None, 0,
+                                                           ctypes.byref(n)))
+        out = np.empty((n.value, 5))
+        self.ctx.check(self.ctx.lib.grada_get_sweep_trials(self.ctx.handle, int(column),
+                                                           _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
     def trials(self) -> np.ndarray:
         """(n, 5): gn_iteration, lambda, misfit, cg_iterations, cg_error."""
         n = ctypes.c_int64()

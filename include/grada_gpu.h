@@ -280,6 +280,52 @@ int grada_invert_batch(int n, grada_ctx *const *ctxs, const grada_invert_params 
                        double *const *m_out, grada_invert_report *reports, int max_threads,
                        int *statuses);
 
+/*
+ * Blocks of right-hand sides on one G (no single reference counterpart: each
+ * column equals one call of the single entry point named).  Column-major host
+ * arrays; n_rhs >= 1 columns are processed sixteen at a time, and each group
+ * of sixteen reads G once per product (FP32 and 16-bit G on the tensor cores,
+ * FP64 G on the FP64 pipe, matrix-free G with one prism evaluation per pair).
+ *  grada_G_mat_mul:  Y[Nd x n] = G X[Nm x n]     (n x Fwd::G_vec_mul, Fwd.cpp:114-146)
+ *  grada_GT_mat_mul: X[Nm x n] = G^T Y[Nd x n]   (n x Fwd::GT_vec_mul, Fwd.cpp:80-112)
+ */
+int grada_G_mat_mul(grada_ctx *ctx, int n_rhs, const double *X, double *Y);
+int grada_GT_mat_mul(grada_ctx *ctx, int n_rhs, const double *Y, double *X);
+/* Device-pointer forms for exactly 16 columns in the library's block layout
+ * (element (i, c) at [i * 16 + c]): d_Y is Nd x 16, d_X is Nm x 16.  Enqueued
+ * on the context stream; no synchronisation. */
+int grada_G_block_mul_dev(grada_ctx *ctx, const double *d_X, double *d_Y);
+int grada_GT_block_mul_dev(grada_ctx *ctx, const double *d_Y, double *d_X);
+
+/*
+ * n_rhs solve_cg systems that share G, the data and the operators
+ * (GaussNewtonInversion::solve_cg, GaussNewtonInversion.cpp:1417-1698, once
+ * per column): column c has its own lambda[c], model mk[:, c], P[:, c] and
+ * weights WL[k][:, c] (WL[k] NULL = identity for every column); mref is
+ * shared.  mk, P, WL[k], dx are Nm x n_rhs column-major.  Each column stops
+ * on its own test; err[c] and iterations[c] are the single call's outputs.
+ */
+int grada_solve_cg_block(grada_ctx *ctx, double tol, int maxit, int n_rhs, const double *lambda,
+                         const double *mk, const double *mref, const double *P,
+                         const double *const WL[7], double *dx, double *err, int *iterations);
+
+/*
+ * Regularisation sweep: for each lambdas[c], the inversion grada_invert runs
+ * with n_lambda = 1 and max_lambda = lambdas[c] (a fixed-lambda
+ * Gauss-Newton run, invert_with_own_CG, GaussNewtonInversion.cpp:815-1103),
+ * all lambda values advancing together so that their CG solves run as one
+ * block per Gauss-Newton iteration.  prm->n_lambda and prm->max_lambda are
+ * ignored.  m_out is Nm x n_lambda column-major; reports[c] as grada_invert's.
+ * grada_get_sweep_trials gives column c's trial records (the rows of
+ * grada_get_trials) of the last sweep.
+ */
+int grada_lambda_sweep(grada_ctx *ctx, const grada_invert_params *prm, int n_lambda,
+                       const double *lambdas, const double *m_ini, const double *m_min,
+                       const double *m_max, const double *m0, double *m_out,
+                       grada_invert_report *reports);
+int grada_get_sweep_trials(const grada_ctx *ctx, int column, double *rows, int64_t cap,
+                           int64_t *n);
+
 #ifdef __cplusplus
 }
 #endif
