@@ -479,7 +479,7 @@ def run_gemv_case():
     res = {"case": "gemv", "rows": f.Nd, "cols": f.Nm, "hbm_peak_GBps": peak}
     for st, bpe in (("fp64", 8), ("fp32", 4), ("fp16", 2), ("bf16", 2)):
         f.compute_G(st)
-        gbytes = f.ld * f.Nm * bpe + 8 * (f.Nd + f.Nm)
+        gbytes = f.Nd * f.Nm * bpe + 8 * (f.Nd + f.Nm)
         for name, fn, a, b in (("G_x", lib.grada_G_vec_mul_dev, x, oy),
                                ("GT_y", lib.grada_GT_vec_mul_dev, y, ox)):
             for _ in range(3):
@@ -623,7 +623,7 @@ def run_block_gemm_case():
 
     for st, bpe in (("fp32", 4), ("bf16", 2), ("fp16", 2), ("fp64", 8)):
         f.compute_G(st)
-        gbytes = f.ld * f.Nm * bpe
+        gbytes = f.Nd * f.Nm * bpe
         flops = 2.0 * f.Nd * f.Nm * 16
         for name, fb, a, b, fs, a1 in (("G_X", lib.grada_G_block_mul_dev, X, oY, lib.grada_G_vec_mul_dev, x1),
                                         ("GT_Y", lib.grada_GT_block_mul_dev, Y, oX, lib.grada_GT_vec_mul_dev, y1)):
@@ -638,7 +638,38 @@ def run_block_gemm_case():
     return res
 
 
-def run_sweep_cfg4(n_lambda: int = 16, gn_iter: int = 5):
+def run_block_gemm_profile():
+    """Fixed small case for ncu captures of the tensor-core block products:
+    gz + Tzz rows of a 32 x 32 x 32 = 32,768-cell mesh under the 101 x 101
+    points (20,402 x 32,768; FP32 G 2.7 GB, larger than L2), FP32 then bf16,
+    two G X and two G^T Y calls each."""
+    import ctypes
+
+    import torch
+
+    from graada3d_gb300 import Fwd, mesh
+
+    prisms = mesh.regular_mesh((0.0, 20000.0), 32, (0.0, 20000.0), 32, (0.0, 8000.0), 32)
+    obs = mesh.observation_grid(101, 0.0, 20000.0, 101, 0.0, 20000.0, -50.0)
+    f = Fwd(prisms, obs, 0x012)
+    lib, h = f.ctx.lib, f.ctx.handle
+    dev = torch.device("cuda")
+    X = torch.randn(f.Nm * 16, dtype=torch.float64, device=dev)
+    Y = torch.randn(f.ld * 16, dtype=torch.float64, device=dev)
+    oX = torch.empty(f.Nm * 16, dtype=torch.float64, device=dev)
+    oY = torch.empty(f.ld * 16, dtype=torch.float64, device=dev)
+    for st in ("fp32", "bf16"):
+        f.compute_G(st)
+        for _ in range(2):
+            f.ctx.check(lib.grada_G_block_mul_dev(h, ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(oY.data_ptr())))
+            f.ctx.check(lib.grada_GT_block_mul_dev(h, ctypes.c_void_p(Y.data_ptr()), ctypes.c_void_p(oX.data_ptr())))
+        torch.cuda.synchronize()
+    f.ctx.close()
+    print(json.dumps({"case": "block-gemm-profile", "rows": f.Nd, "cols": f.Nm}))
+
+
+def run_sweep_cfg4(n_lambda: int = 16, gn_iter: int = 5, storages=("fp64", "fp32", "bf16"),
+                   sequential: bool = True):
     """BASELINE configs[3] part 1: a 16-value regularisation sweep (lambda
     log-spaced 1e-3 .. 1e1) on the shared gz + Tzz G of configs[1]'s geometry,
     each lambda a fixed-lambda Gauss-Newton run (L2, CG <= 50, up to gn_iter
@@ -666,9 +697,8 @@ def run_sweep_cfg4(n_lambda: int = 16, gn_iter: int = 5):
     out = {"case": "sweep-cfg4", "cells": nm, "data": inv.Nd, "lambdas": n_lambda,
            "gn_iter_max": gn_iter}
     models = {}
-    for st in ("fp64", "fp32", "bf16"):
-        if st != "fp64":
-            inv.compute_G(st)
+    for st in storages:
+        inv.compute_G(st)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         m, reps = inv.lambda_sweep(prm, lam, *args, fp64_refinement=(st != "fp64"))
@@ -678,10 +708,11 @@ def run_sweep_cfg4(n_lambda: int = 16, gn_iter: int = 5):
         r = {"block_s": t, "misfits": [round(x["final_misfit"], 4) for x in reps],
              "cg_iterations": int(sum(x["cg_iterations"] for x in reps)),
              "gn_iterations": [int(x["gn_iterations"]) for x in reps]}
-        if st != "fp64":
+        if st != "fp64" and "fp64" in models:
             rel = [float(np.linalg.norm(m[:, c] - models["fp64"][:, c]) /
                          max(np.linalg.norm(models["fp64"][:, c]), 1e-30)) for c in range(n_lambda)]
             r["model_rel_diff_vs_fp64_max"] = max(rel)
+        if st != "fp64" and sequential:
             t0 = time.perf_counter()
             for c in range(n_lambda):
                 inv.invert(dict(prm, max_lambda=float(lam[c])), *args, fp64_refinement=True)
@@ -720,7 +751,7 @@ def main():
     ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-cfg1",
                                                          "inversion-cfg3", "matrix-free-cfg5",
                                                          "gemv", "batched-cfg4", "block-gemm",
-                                                         "sweep-cfg4"])
+                                                         "sweep-cfg4", "block-gemm-profile"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -728,13 +759,18 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-inversion", action="store_true")
+    ap.add_argument("--sweep-storages", default="fp64,fp32,bf16")
+    ap.add_argument("--no-sequential", action="store_true")
     args = ap.parse_args()
     if args.case == "profile":
         run_profile_case(args)
     elif args.case == "block-gemm":
         print(json.dumps(run_block_gemm_case()))
+    elif args.case == "block-gemm-profile":
+        run_block_gemm_profile()
     elif args.case == "sweep-cfg4":
-        print(json.dumps(run_sweep_cfg4()))
+        print(json.dumps(run_sweep_cfg4(storages=tuple(args.sweep_storages.split(",")),
+                                        sequential=not args.no_sequential)))
     elif args.case == "batched-cfg4":
         print(json.dumps(run_batched_cfg4()))
     elif args.case == "gemv":

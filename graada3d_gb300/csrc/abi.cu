@@ -125,7 +125,9 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
   mask = fmask;
   n_fields = __builtin_popcount(fmask);
   nd = (int64_t)n_fields * no;
-  ld = round_up(nd, 8);
+  // columns start on 128-byte boundaries for 16-bit entries (and 256/512 B for
+  // FP32/FP64), so tile loads of a column never straddle an extra sector
+  ld = round_up(nd, 64);
   if (!math_tables.ptr) {
     std::vector<double> tab(math_table_size());
     build_math_tables_host(tab.data());
@@ -141,6 +143,13 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
   sync();
 }
 
+// Rows nd..ld-1 of every column (the padding) set to zero: one 2-D memset.
+void Context::zero_padding_rows(void *base, size_t esz) {
+  if (ld <= nd) return;
+  GRADA_CUDA_CHECK(cudaMemset2DAsync(static_cast<char *>(base) + esz * nd, esz * ld, 0,
+                                     esz * (ld - nd), n_cells, stream));
+}
+
 void Context::compute_G(int storage) {
   require_geometry();
   if (storage < GRADA_G_FP64 || storage > GRADA_G_MATRIX_FREE)
@@ -153,17 +162,17 @@ void Context::compute_G(int storage) {
     // does not fit in HBM)
   } else if (storage == GRADA_G_FP64) {
     G.alloc(this, n_entries * sizeof(double));
-    if (ld > nd)
-      GRADA_CUDA_CHECK(cudaMemsetAsync(G.ptr, 0, n_entries * sizeof(double), stream));
+    zero_padding_rows(G.ptr, sizeof(double));
     launch_assemble_fp64(g, g.prisms, n_cells, nullptr, 0, G.as<double>(), ld, stream);
   } else if (storage == GRADA_G_FP32) {
     G.alloc(this, n_entries * sizeof(float));
-    if (ld > nd) GRADA_CUDA_CHECK(cudaMemsetAsync(G.ptr, 0, n_entries * sizeof(float), stream));
+    zero_padding_rows(G.ptr, sizeof(float));
     launch_assemble_fp32(g, g.prisms, n_cells, nullptr, 0, G.as<float>(), ld, stream);
   } else {
+    // FP32 staging copy; the quantiser reads its rows < nd and writes zero
+    // padding rows itself
     DevBuf tmp;
     tmp.alloc(this, n_entries * sizeof(float));
-    if (ld > nd) GRADA_CUDA_CHECK(cudaMemsetAsync(tmp.ptr, 0, n_entries * sizeof(float), stream));
     launch_assemble_fp32(g, g.prisms, n_cells, nullptr, 0, tmp.as<float>(), ld, stream);
     G.alloc(this, n_entries * sizeof(uint16_t));
     row_scale.alloc(this, sizeof(float) * (size_t)nd);

@@ -155,6 +155,7 @@ struct Context {
   void set_geometry(const double *h_prisms, int64_t nc, const double *h_obs, int64_t no,
                     uint32_t fmask);
   void compute_G(int storage);
+  void zero_padding_rows(void *base, size_t esz);
   void G_vec_mul_dev(const double *d_x, double *d_y);
   void GT_vec_mul_dev(const double *d_y, double *d_x);
   // y = G x and x = G^T y for every storage, matrix-free included (GemvOpts

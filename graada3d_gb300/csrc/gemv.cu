@@ -7,7 +7,7 @@
 //
 // Both products stream G once from HBM with 16-byte vector loads and are
 // bound by HBM bandwidth.  G is column-major with leading dimension ld (a
-// multiple of 8, padding rows zero), so:
+// multiple of 64, padding rows zero), so:
 //  * G^T y: a block owns COLS consecutive columns; each thread walks the rows
 //    with 16-byte loads, multiplies by y (loaded once per row chunk and reused
 //    for the block's COLS columns) and the block reduces COLS sums with warp

@@ -12,10 +12,15 @@
 // Precision.  The MMA multiplies 32-bit-container TF32 (FP32 G) or 16-bit
 // operands and accumulates in FP32 in tensor memory:
 //  * FP32 G: split precision.  Each staged tile of G is split in shared
-//    memory into big = tf32(g) and small = tf32(g - big), each right-hand
-//    side likewise into two TF32 parts; one MMA with N = 32 multiplies a
-//    G part by both right-hand-side parts, so big*x_big + big*x_small +
-//    small*x_big (+ small*x_small) recovers an FP32-accurate product.
+//    memory into big + small TF32 parts, each right-hand side likewise into
+//    two TF32 parts; one MMA with N = 32 multiplies a G part by both
+//    right-hand-side parts, so big*x_big + big*x_small + small*x_big
+//    (+ small*x_small) recovers an FP32-accurate product.  The tensor core
+//    reads an FP32 bit pattern as TF32 by truncation (checked on GB300), so
+//    where the staged tile is already K-major (G^T Y) it is the big part
+//    itself, big = trunc(g), and only small = rna(g - big) is written; for
+//    G X the tile must be transposed to K-major (TF32 operands cannot be
+//    MN-major) and big = rna(g), small = rna(g - big) are both written.
 //  * 16-bit G: the stored entries are exact MMA operands; each right-hand
 //    side is split into hi + lo 16-bit parts (N = 32 again).  Each column
 //    is first scaled by a power of two so that its largest entry is in
@@ -64,6 +69,9 @@ constexpr int A_BYTES = TC_M * SWB;       // 16 KB per stage, both modes
 constexpr int B_BYTES = TC_N * SWB;       // 4 KB per stage
 constexpr int TMEM_COLS = 2 * TC_N;       // two accumulators
 constexpr uint64_t kWaitLimitNs = 1000000000ull;  // 1 s per wait
+// try_wait suspends the thread until the phase completes or this many ns
+// pass, so waiting warps do not spin on the issue slots
+constexpr uint32_t kSuspendHintNs = 200000u;
 
 // err bits
 enum : int {
@@ -85,12 +93,13 @@ struct EltCfg {
   // TMA ring: A tile + right-hand-side tile per stage
   static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
   static constexpr int STAGES = split_a ? 6 : 10;
-  // TF32 only: ring of converted slots (K-major big and small parts of A and a
-  // copy of the right-hand-side tile), read by the MMAs
-  static constexpr int CSLOT_BYTES = 2 * A_BYTES + B_BYTES;
-  static constexpr int CSLOTS = split_a ? 2 : 0;
-  static constexpr int THREADS = split_a ? 320 : 192;
-  static constexpr int W_EPI0 = split_a ? 6 : 2;  // first epilogue warp
+  // TF32 only: ring of converted slots (K-major big and small parts of A),
+  // read by the MMAs together with the right-hand-side tile of the TMA stage
+  static constexpr int CSLOT_BYTES = 2 * A_BYTES;
+  static constexpr int CSLOTS = split_a ? 3 : 0;
+  static constexpr int NCONV_WARPS = split_a ? 8 : 0;
+  static constexpr int THREADS = 64 + 32 * NCONV_WARPS + 128;
+  static constexpr int W_EPI0 = 2 + NCONV_WARPS;  // first epilogue warp
   static constexpr int SMEM = STAGES * STAGE_BYTES + CSLOTS * CSLOT_BYTES + 1024;
   static constexpr int ATOM_M = SWB / bytes;     // MN-major atom: rows of G per 128 B
 };
@@ -136,10 +145,10 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(bar), "r"(parity)
+      : "r"(bar), "r"(parity), "r"(kSuspendHintNs)
       : "memory");
   return ok != 0;
 }
@@ -223,10 +232,13 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+// FP32 -> TF32, round to nearest with ties away from zero (the rounding of
+// cvt.rna.tf32.f32) on the integer pipe: adding half a TF32 ulp (bit 12) to
+// the sign-magnitude bit pattern carries into the kept bits exactly when the
+// dropped 13 bits are >= half an ulp.  Conversions run on a narrow pipe on
+// this GPU; two integer operations do not.
 __device__ __forceinline__ uint32_t f32_to_tf32(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return r;
+  return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u;
 }
 
 // 32 lanes x 32 columns of FP32 from TMEM (this warp's lane quarter).
@@ -271,18 +283,16 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
   const uint32_t cbase = base + (uint32_t)C::STAGES * C::STAGE_BYTES;
   auto cslot_big = [&](int c) { return cbase + (uint32_t)c * C::CSLOT_BYTES; };
   auto cslot_small = [&](int c) { return cslot_big(c) + A_BYTES; };
-  auto cslot_b = [&](int c) { return cslot_big(c) + 2 * A_BYTES; };
   uint8_t *base_ptr = smem_raw + (base - smem_u32(smem_raw));
 
   if (threadIdx.x == 0) {
     abort_flag = 0;
     for (int s = 0; s < C::STAGES; s++) {
       mbar_init(smem_u32(&bar_full[s]), 1);
-      // freed by the MMA commit, or (TF32) by the four split warps once copied
-      mbar_init(smem_u32(&bar_empty[s]), C::split_a ? 4 : 1);
+      mbar_init(smem_u32(&bar_empty[s]), 1);  // freed by the MMA commit
     }
     for (int c = 0; c < NCS; c++) {
-      mbar_init(smem_u32(&bar_cfull[c]), 4);
+      mbar_init(smem_u32(&bar_cfull[c]), C::NCONV_WARPS > 0 ? C::NCONV_WARPS : 1);
       mbar_init(smem_u32(&bar_cempty[c]), 1);
     }
     for (int a = 0; a < 2; a++) {
@@ -383,37 +393,48 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
         unit_kst(u, k0, k1);
         uint32_t accum = 0;
         for (int ks = k0; ks < k1; ks++, it++) {
-          int s;
-          uint32_t ph, wb, a_s, b_s, free_bar;
+          const int s = (int)(it % C::STAGES);
+          uint32_t ph, wb, a_s;
+          const uint32_t b_s = stage_b(s);
+          int c = 0;
           if constexpr (C::split_a) {
-            s = (int)(it % NCS);
+            c = (int)(it % NCS);
             ph = (it / NCS) & 1u;
-            wb = smem_u32(&bar_cfull[s]);
-            a_s = cslot_big(s);
-            b_s = cslot_b(s);
-            free_bar = smem_u32(&bar_cempty[s]);
+            wb = smem_u32(&bar_cfull[c]);  // implies the stage's TMA completed
+            a_s = cslot_big(c);
           } else {
-            s = (int)(it % C::STAGES);
             ph = (it / C::STAGES) & 1u;
             wb = smem_u32(&bar_full[s]);
             a_s = stage_a(s);
-            b_s = stage_b(s);
-            free_bar = smem_u32(&bar_empty[s]);
           }
           if (!mbar_wait(wb, ph, &abort_flag, p.err, TCERR_MMA_FULL)) {
             ok = false;
             break;
           }
+          if constexpr (C::split_a) {
+            // the right-hand-side tile comes straight from the TMA stage
+            if (!mbar_wait(smem_u32(&bar_full[s]), (it / C::STAGES) & 1u, &abort_flag, p.err,
+                           TCERR_MMA_FULL)) {
+              ok = false;
+              break;
+            }
+          }
           tc_fence_after();
+          // TF32: the big part is the converted slot's (G X) or, for G^T Y, the
+          // staged FP32 tile itself, which the tensor core reads truncated to
+          // TF32; the small part is always the slot's
+          uint32_t a_big = a_s;
+          if constexpr (C::split_a && MODE == MODE_GTY) a_big = stage_a(s);
 #pragma unroll
           for (int st = 0; st < C::STEPS; st++) {
             const uint64_t bd = sdesc(b_s + st * b_step, 16u, 1024u);
-            mma<ELT>(dt, sdesc(a_s + st * a_step, a_lbo, a_sbo), bd, id, accum);
+            mma<ELT>(dt, sdesc(a_big + st * a_step, a_lbo, a_sbo), bd, id, accum);
             accum = 1;
             if constexpr (C::split_a)
               mma<ELT>(dt, sdesc(a_s + A_BYTES + st * a_step, a_lbo, a_sbo), bd, id, 1);
           }
-          mma_commit(free_bar);  // stage / slot free once these MMAs are done
+          mma_commit(smem_u32(&bar_empty[s]));  // stage free once these MMAs are done
+          if constexpr (C::split_a) mma_commit(smem_u32(&bar_cempty[c]));
         }
         if (!ok) break;
         mma_commit(smem_u32(&bar_acc_full[acc]));
@@ -424,11 +445,12 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
     }
   } else if (C::split_a && warp < C::W_EPI0) {
     // ---------------- TF32 split (and K-major transpose) of the G tile ----------
-    // A TMA stage is read once and released; the big and small TF32 parts go to
-    // a converted slot in the K-major 128B-swizzled layout (row m of 128 B
-    // holds k = 0..31; 16-byte chunk j of row m at chunk j ^ (m & 7)), with a
-    // copy of the right-hand-side tile.
-    const int ct = threadIdx.x - 64;  // 0..127
+    // The big and small TF32 parts of a TMA stage's A tile go to a converted
+    // slot in the K-major 128B-swizzled layout (row m of 128 B holds k =
+    // 0..31; 16-byte chunk j of row m at chunk j ^ (m & 7)); the MMAs read the
+    // right-hand-side tile from the TMA stage, which their commit frees.
+    constexpr int NCT = 32 * C::NCONV_WARPS;
+    const int ct = threadIdx.x - 64;  // 0..NCT-1
     uint32_t it = 0;
     bool ok = true;
     for (int u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
@@ -459,10 +481,13 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
         };
         if constexpr (MODE == MODE_GX) {
           // raw: 4 MN-major atoms (32 rows x 32 k, row k of 128 B holds 32 m);
-          // thread = row m of the K-major result
-          const int m = ct, atom = m >> 5, mm = m & 31;
+          // thread = row m of the K-major result, NCT / 128 threads per row
+          // sharing its eight 16-byte chunks
+          constexpr int TPR = NCT / TC_M;
+          const int m = ct % TC_M, atom = m >> 5, mm = m & 31;
 #pragma unroll
-          for (int j = 0; j < 8; j++) {
+          for (int jj = 0; jj < 8 / TPR; jj++) {
+            const int j = jj * TPR + ct / TC_M;
             float v[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
@@ -474,28 +499,27 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
             split4(v, (m * SWB + ((j ^ (m & 7)) << 4)) >> 4);
           }
         } else {
-          // raw is already K-major: element-wise
+          // raw is already K-major and serves as the big part (read truncated
+          // to TF32 by the tensor core): only small = rna(g - trunc(g)) is
+          // written, element-wise
           const float4 *r4 = reinterpret_cast<const float4 *>(raw);
 #pragma unroll
-          for (int j = 0; j < A_BYTES / 16 / 128; j++) {
-            const int idx = ct + 128 * j;
+          for (int j = 0; j < A_BYTES / 16 / NCT; j++) {
+            const int idx = ct + NCT * j;
             const float4 v4 = r4[idx];
             const float v[4] = {v4.x, v4.y, v4.z, v4.w};
-            split4(v, idx);
-          }
-        }
-        {
-          const float4 *bs = reinterpret_cast<const float4 *>(base_ptr + (stage_b(s) - base));
-          float4 *bd = reinterpret_cast<float4 *>(base_ptr + (cslot_b(c) - base));
+            float sm[4];
 #pragma unroll
-          for (int j = 0; j < B_BYTES / 16 / 128; j++) bd[ct + 128 * j] = bs[ct + 128 * j];
+            for (int q = 0; q < 4; q++) {
+              const float t = __uint_as_float(__float_as_uint(v[q]) & 0xFFFFE000u);
+              sm[q] = __uint_as_float(f32_to_tf32(v[q] - t));
+            }
+            small[idx] = make_float4(sm[0], sm[1], sm[2], sm[3]);
+          }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncwarp();
-        if (lane == 0) {
-          mbar_arrive(smem_u32(&bar_empty[s]));
-          mbar_arrive(smem_u32(&bar_cfull[c]));
-        }
+        if (lane == 0) mbar_arrive(smem_u32(&bar_cfull[c]));
       }
     }
   } else if (warp >= C::W_EPI0) {
