@@ -167,6 +167,12 @@ def max_over_ranks(world, v: float) -> float:
     return float(t.item())
 
 
+def shard_units(n: int, world: int, rank: int) -> list[int]:
+    """Indices of the independent units (problems, lambda values) this rank runs
+    when replicas share a batch: round-robin, disjoint, covering 0..n-1."""
+    return list(range(rank, n, world))
+
+
 def run_reference(args):
     world, rank, _ = dist_init()
     if rank != 0:
@@ -504,17 +510,23 @@ def run_batched_cfg4(n_problems: int = 64):
     """BASELINE configs[3] part 2: independent inversions of uneven size (uniform
     meshes nx = ny, nz = nx/2 with 4k-60k cells, square point grids of 400-5,000
     points, gz + Tzz, seeded models, seeds 100..163), run one after the other and
-    then as one concurrent batch (one context, host thread and stream each)."""
+    then as one concurrent batch (one context, host thread and stream each).
+    Under torchrun the problems are sharded over the ranks (replicas, one GPU
+    each); times are the max over ranks."""
     import torch
 
     from graada3d_gb300 import Context, mesh
     from graada3d_gb300 import regularization as reg
     from graada3d_gb300.inversion import GaussNewtonInversion, compute_G_batch, invert_batch
 
+    world, rank, local = dist_init()
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
     prm = dict(max_lambda=1e-1, n_lambda=30, rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6,
                cg_factor=50, gn_iter=10, lp=[2, 2, 2, 2, 2], eps2=1e-9)
     invs, args, sizes = [], [], []
-    for k in range(n_problems):
+    mine = shard_units(n_problems, world, rank)
+    for k in mine:
         rng = np.random.default_rng(100 + k)
         cells = int(rng.integers(4000, 60001))
         nx = max(4, int(round((2 * cells) ** (1 / 3))))
@@ -530,7 +542,7 @@ def run_batched_cfg4(n_problems: int = 64):
             x0, y0, z0 = rng.uniform(0, L - s_[0]), rng.uniform(0, L - s_[1]), rng.uniform(0, L / 2 - s_[2])
             boxes.append([x0, x0 + s_[0], y0, y0 + s_[1], z0, z0 + s_[2], v])
         rho = mesh.set_boxes(prisms, boxes)
-        inv = GaussNewtonInversion(prisms, obs, 0x012, ctx=Context(0))
+        inv = GaussNewtonInversion(prisms, obs, 0x012, ctx=Context(local))
         inv.compute_G("fp64")
         d = inv.G_vec_mul(rho)
         dobs = d + 0.02 * np.abs(d) * rng.standard_normal(d.size)
@@ -550,7 +562,7 @@ def run_batched_cfg4(n_problems: int = 64):
     t_seq = time.perf_counter() - t0
     t0 = time.perf_counter()
     compute_G_batch(invs, "fp64")
-    bat = invert_batch(invs, [prm] * n_problems, [a[0] for a in args], [a[1] for a in args],
+    bat = invert_batch(invs, [prm] * len(invs), [a[0] for a in args], [a[1] for a in args],
                        [a[2] for a in args])
     torch.cuda.synchronize()
     t_bat = time.perf_counter() - t0
@@ -558,12 +570,15 @@ def run_batched_cfg4(n_problems: int = 64):
     reached = sum(1 for _, r in bat if r["final_misfit"] < 1.0)
     for inv in invs:
         inv.ctx.close()
-    return {"case": "batched-cfg4", "problems": n_problems,
+    t_seq, t_bat = max_over_ranks(world, t_seq), max_over_ranks(world, t_bat)
+    reached = int(-max_over_ranks(world, -float(reached))) if world > 1 else reached
+    return {"case": "batched-cfg4", "problems": n_problems, "ranks": world,
+            "problems_per_rank": len(mine),
             "cells_range": [min(s[0] for s in sizes), max(s[0] for s in sizes)],
             "points_range": [min(s[1] for s in sizes), max(s[1] for s in sizes)],
             "sequential_s": t_seq, "batched_s": t_bat, "speedup": t_seq / t_bat,
-            "identical_models": same, "chi2_reached": reached,
-            "cg_iterations": int(sum(r["cg_iterations"] for _, r in bat))}
+            "identical_models": same, "chi2_reached_rank0": reached,
+            "cg_iterations_rank0": int(sum(r["cg_iterations"] for _, r in bat))}
 
 
 def sweep_problem():
@@ -772,7 +787,9 @@ def main():
         print(json.dumps(run_sweep_cfg4(storages=tuple(args.sweep_storages.split(",")),
                                         sequential=not args.no_sequential)))
     elif args.case == "batched-cfg4":
-        print(json.dumps(run_batched_cfg4()))
+        res = run_batched_cfg4()
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps(res))
     elif args.case == "gemv":
         print(json.dumps(run_gemv_case()))
     elif args.case == "matrix-free-cfg5":
