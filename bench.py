@@ -571,7 +571,6 @@ def run_batched_cfg4(n_problems: int = 64):
     for inv in invs:
         inv.ctx.close()
     t_seq, t_bat = max_over_ranks(world, t_seq), max_over_ranks(world, t_bat)
-    reached = int(-max_over_ranks(world, -float(reached))) if world > 1 else reached
     return {"case": "batched-cfg4", "problems": n_problems, "ranks": world,
             "problems_per_rank": len(mine),
             "cells_range": [min(s[0] for s in sizes), max(s[0] for s in sizes)],
