@@ -139,8 +139,31 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
   obs.alloc(this, sizeof(double) * 3 * no);
   upload(prisms.ptr, h_prisms, sizeof(double) * 6 * nc);
   host_prisms.assign(h_prisms, h_prisms + 6 * nc);
+  plan_valid = false;
   upload(obs.ptr, h_obs, sizeof(double) * 3 * no);
   sync();
+}
+
+// The assembly's tile plan for the current cell list (rebuilt after a change
+// of the cells).
+TilePlan Context::tile_plan() {
+  if (!plan_valid) {
+    std::vector<int32_t> tiles;
+    std::vector<int64_t> runs;
+    build_tile_plan(host_prisms.data(), n_cells, tiles, runs);
+    plan_tiles.alloc(this, sizeof(int32_t) * tiles.size());
+    plan_runs.alloc(this, sizeof(int64_t) * runs.size());
+    upload(plan_tiles.ptr, tiles.data(), sizeof(int32_t) * tiles.size());
+    upload(plan_runs.ptr, runs.data(), sizeof(int64_t) * runs.size());
+    sync();
+    plan_n_tiles = (int64_t)tiles.size() / 4;
+    plan_valid = true;
+  }
+  TilePlan p;
+  p.tiles = plan_tiles.as<int32_t>();
+  p.run_start = plan_runs.as<int64_t>();
+  p.n_tiles = plan_n_tiles;
+  return p;
 }
 
 // Rows nd..ld-1 of every column (the padding) set to zero: one 2-D memset.
@@ -163,17 +186,17 @@ void Context::compute_G(int storage) {
   } else if (storage == GRADA_G_FP64) {
     G.alloc(this, n_entries * sizeof(double));
     zero_padding_rows(G.ptr, sizeof(double));
-    launch_assemble_fp64(g, g.prisms, n_cells, nullptr, 0, G.as<double>(), ld, stream);
+    launch_assemble_tiled_fp64(g, tile_plan(), G.as<double>(), ld, stream);
   } else if (storage == GRADA_G_FP32) {
     G.alloc(this, n_entries * sizeof(float));
     zero_padding_rows(G.ptr, sizeof(float));
-    launch_assemble_fp32(g, g.prisms, n_cells, nullptr, 0, G.as<float>(), ld, stream);
+    launch_assemble_tiled_fp32(g, tile_plan(), G.as<float>(), ld, stream);
   } else {
     // FP32 staging copy; the quantiser reads its rows < nd and writes zero
     // padding rows itself
     DevBuf tmp;
     tmp.alloc(this, n_entries * sizeof(float));
-    launch_assemble_fp32(g, g.prisms, n_cells, nullptr, 0, tmp.as<float>(), ld, stream);
+    launch_assemble_tiled_fp32(g, tile_plan(), tmp.as<float>(), ld, stream);
     G.alloc(this, n_entries * sizeof(uint16_t));
     row_scale.alloc(this, sizeof(float) * (size_t)nd);
     launch_rowscale_16(tmp.as<float>(), nd, n_cells, ld, row_scale.as<float>(),

@@ -17,6 +17,8 @@
 #include "kernels.h"
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <vector>
 
 #include "prism.cuh"
 
@@ -75,6 +77,123 @@ void launch_assemble(const DevGeometry &g, const double *prisms, int64_t n_cells
   if (grid.y > 65535u) throw Error(-1, "too many observation points for one launch");
   assemble_kernel<OutT><<<grid, ASM_THREADS, 0, s>>>(g.obs, g.n_obs, prisms, n_cells, col_index,
                                                      col_offset, g.mask, g.tables, G, ld);
+  GRADA_LAUNCH_CHECK();
+}
+
+// ---- tiled assembly: cells shared in z and in y -----------------------------
+//
+// A tile is up to TL_COLS z-runs (vertical stacks of cells, consecutive in the
+// cell list) that are y-neighbours with identical levels: at every level the
+// cells of consecutive runs have the same x extent and z levels and the y0 of
+// one equals the y1 of the previous.  A thread (one observation point) walks
+// the tile level by level and, within a level, run by run, so the cell above
+// (same run, previous level) and the cell before it in y (previous run, same
+// level) are always done: their bottom and y1 faces are taken over
+// (prism_terms_tiled).  The z carries of the tile's runs live in shared
+// memory, the y carry in registers.  Regular meshes form tiles of TL_COLS full
+// columns; a refined mesh forms smaller ones (down to single runs).
+
+constexpr int TL_THREADS = 128;
+constexpr int TL_COLS = 8;
+constexpr int TL_LCH = 8;  // levels staged per pass
+constexpr int ZC_N = 9;    // doubles of a ZCarry
+
+template <typename OutT>
+__global__ void __launch_bounds__(TL_THREADS)
+    assemble_tiled_kernel(const double *__restrict__ obs, int64_t n_obs,
+                          const double *__restrict__ prisms, const int4 *__restrict__ tiles,
+                          const int64_t *__restrict__ run_start, uint32_t mask,
+                          const double *__restrict__ tables, OutT *__restrict__ G, int64_t ld) {
+  __shared__ double tab[kTabSize];
+  __shared__ double sc[TL_LCH][TL_COLS][6];
+  __shared__ int64_t rs[TL_COLS];
+  extern __shared__ double zsm[];  // [TL_COLS][ZC_N][TL_THREADS]
+  const int4 td = tiles[blockIdx.x];
+  const int ncols = td.y, nlev = td.z;
+  for (int t = threadIdx.x; t < kTabSize; t += TL_THREADS) tab[t] = tables[t];
+  if (threadIdx.x < ncols) rs[threadIdx.x] = run_start[td.x + threadIdx.x];
+  const int64_t i = (int64_t)blockIdx.y * TL_THREADS + threadIdx.x;
+  const bool active = i < n_obs;
+  double px = 0, py = 0, pz = 0;
+  if (active) {
+    px = obs[3 * i];
+    py = obs[3 * i + 1];
+    pz = obs[3 * i + 2];
+  }
+  const uint32_t fam = families_for_mask(mask);
+  auto zslot = [&](int a, int f) -> double & {
+    return zsm[((int64_t)a * ZC_N + f) * TL_THREADS + threadIdx.x];
+  };
+  for (int k0 = 0; k0 < nlev; k0 += TL_LCH) {
+    const int nl = min(TL_LCH, nlev - k0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nl * ncols * 6; t += TL_THREADS) {
+      const int k = t / (ncols * 6), a = (t / 6) % ncols, q = t % 6;
+      sc[k][a][q] = prisms[(rs[a] + k0 + k) * 6 + q];
+    }
+    __syncthreads();
+    if (!active) continue;
+    for (int kk = 0; kk < nl; kk++) {
+      const int k = k0 + kk;
+      YCarry yc;
+      for (int a = 0; a < ncols; a++) {
+        const double *p = sc[kk][a];
+        ZCarry zin, zout;
+        const bool top = k > 0;
+        if (top) {
+          zin.r[0][0] = zslot(a, 0); zin.r[0][1] = zslot(a, 1);
+          zin.r[1][0] = zslot(a, 2); zin.r[1][1] = zslot(a, 3);
+          zin.qx[0] = zslot(a, 4); zin.qx[1] = zslot(a, 5);
+          zin.qy[0] = zslot(a, 6); zin.qy[1] = zslot(a, 7);
+          zin.tz = zslot(a, 8);
+        }
+        YCarry yout;
+        PrismTerms t;
+        prism_terms_tiled(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, top, zin,
+                          a > 0, yc, zout, yout, t);
+        zslot(a, 0) = zout.r[0][0]; zslot(a, 1) = zout.r[0][1];
+        zslot(a, 2) = zout.r[1][0]; zslot(a, 3) = zout.r[1][1];
+        zslot(a, 4) = zout.qx[0]; zslot(a, 5) = zout.qx[1];
+        zslot(a, 6) = zout.qy[0]; zslot(a, 7) = zout.qy[1];
+        zslot(a, 8) = zout.tz;
+        yc = yout;
+        OutT *gcol = G + (rs[a] + k) * ld + i;
+        int slot = 0;
+#pragma unroll
+        for (int b = 0; b < 10; b++) {
+          if (mask & (1u << b)) {
+            store_entry(gcol + (int64_t)slot * n_obs, prism_component(t, b));
+            slot++;
+          }
+        }
+      }
+    }
+  }
+}
+
+template <typename OutT>
+void launch_assemble_tiled(const DevGeometry &g, const TilePlan &plan, OutT *G, int64_t ld,
+                           cudaStream_t s) {
+  if (plan.n_tiles <= 0 || g.n_obs <= 0) return;
+  static std::mutex mu;
+  static bool attr[64] = {};
+  const int smem = (int)(sizeof(double) * TL_COLS * ZC_N * TL_THREADS);
+  {
+    int dev = 0;
+    GRADA_CUDA_CHECK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64 || !attr[dev]) {
+      GRADA_CUDA_CHECK(cudaFuncSetAttribute(assemble_tiled_kernel<OutT>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      if (dev >= 0 && dev < 64) attr[dev] = true;
+    }
+  }
+  dim3 grid((unsigned)plan.n_tiles, (unsigned)ceil_div(g.n_obs, TL_THREADS));
+  if (grid.y > 65535u || plan.n_tiles > 0x7fffffff)
+    throw Error(-1, "too many observation points or tiles for one launch");
+  assemble_tiled_kernel<OutT><<<grid, TL_THREADS, smem, s>>>(
+      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(plan.tiles), plan.run_start,
+      g.mask, g.tables, G, ld);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -338,6 +457,61 @@ void launch_adjoint_field(const DevGeometry &g, const double *y, const double *p
 
 int math_table_size() { return kTabSize; }
 void build_math_tables_host(double *tab) { build_math_tables(tab); }
+
+int tile_max_cols() { return TL_COLS; }
+
+void build_tile_plan(const double *p, int64_t n, std::vector<int32_t> &tiles,
+                     std::vector<int64_t> &run_start) {
+  tiles.clear();
+  run_start.clear();
+  auto same = [](double a, double b) { return a == b; };
+  // z-runs: consecutive cells with equal x/y extents, each z0 the previous z1
+  std::vector<int64_t> rstart, rlen;
+  for (int64_t c = 0; c < n;) {
+    int64_t e = c;
+    while (e + 1 < n) {
+      const double *u = p + 6 * e, *v = p + 6 * (e + 1);
+      if (!(same(u[0], v[0]) && same(u[1], v[1]) && same(u[2], v[2]) && same(u[3], v[3]) &&
+            same(u[5], v[4])))
+        break;
+      e++;
+    }
+    rstart.push_back(c);
+    rlen.push_back(e - c + 1);
+    c = e + 1;
+  }
+  // runs that are y-neighbours level by level form a tile
+  auto ynext = [&](size_t a, size_t b) {
+    if (rlen[a] != rlen[b]) return false;
+    for (int64_t k = 0; k < rlen[a]; k++) {
+      const double *u = p + 6 * (rstart[a] + k), *v = p + 6 * (rstart[b] + k);
+      if (!(same(u[0], v[0]) && same(u[1], v[1]) && same(u[3], v[2]) && same(u[4], v[4]) &&
+            same(u[5], v[5])))
+        return false;
+    }
+    return true;
+  };
+  for (size_t r = 0; r < rstart.size();) {
+    size_t e = r;
+    while (e + 1 < rstart.size() && (int)(e + 1 - r) < TL_COLS && ynext(e, e + 1)) e++;
+    tiles.push_back((int32_t)run_start.size());
+    tiles.push_back((int32_t)(e - r + 1));
+    tiles.push_back((int32_t)rlen[r]);
+    tiles.push_back(0);
+    for (size_t q = r; q <= e; q++) run_start.push_back(rstart[q]);
+    r = e + 1;
+  }
+}
+
+void launch_assemble_tiled_fp64(const DevGeometry &g, const TilePlan &plan, double *G, int64_t ld,
+                                cudaStream_t s) {
+  launch_assemble_tiled<double>(g, plan, G, ld, s);
+}
+
+void launch_assemble_tiled_fp32(const DevGeometry &g, const TilePlan &plan, float *G, int64_t ld,
+                                cudaStream_t s) {
+  launch_assemble_tiled<float>(g, plan, G, ld, s);
+}
 
 void launch_assemble_fp64(const DevGeometry &g, const double *prisms, int64_t n_cells,
                           const int64_t *col_index, int64_t col_offset, double *G, int64_t ld,

@@ -85,6 +85,10 @@ struct Context {
   // Dense sensitivity matrix (Fwd::G), column-major, leading dimension ld.
   int g_storage = -1;
   DevBuf G, row_scale;
+  // Tile plan of the cell list for the assembly (built from host_prisms).
+  DevBuf plan_tiles, plan_runs;
+  int64_t plan_n_tiles = 0;
+  bool plan_valid = false;
 
   // Work space.
   DevBuf scratch, vx, vy;
@@ -156,6 +160,7 @@ struct Context {
                     uint32_t fmask);
   void compute_G(int storage);
   void zero_padding_rows(void *base, size_t esz);
+  TilePlan tile_plan();
   void G_vec_mul_dev(const double *d_x, double *d_y);
   void GT_vec_mul_dev(const double *d_y, double *d_x);
   // y = G x and x = G^T y for every storage, matrix-free included (GemvOpts

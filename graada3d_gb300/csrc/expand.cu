@@ -92,6 +92,7 @@ void Context::expand_G(int64_t n_split, const int64_t *parent, const double *chi
   if (matrix_free) {  // no matrix to splice: only the cell list changes
     n_cells = nm_new;
     host_prisms.swap(new_prisms);
+    plan_valid = false;
     prisms.alloc(this, sizeof(double) * 6 * nm_new);
     upload(prisms.ptr, host_prisms.data(), sizeof(double) * 6 * nm_new);
     sync();
@@ -129,6 +130,7 @@ void Context::expand_G(int64_t n_split, const int64_t *parent, const double *chi
   std::swap(G.bytes, newG.bytes);
   n_cells = nm_new;
   host_prisms.swap(new_prisms);
+  plan_valid = false;
   prisms.alloc(this, sizeof(double) * 6 * nm_new);
   upload(prisms.ptr, host_prisms.data(), sizeof(double) * 6 * nm_new);
   sync();

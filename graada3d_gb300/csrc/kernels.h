@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace grada {
 
 // Device-resident problem geometry (mesh leaf cells and observation points).
@@ -31,6 +33,22 @@ void launch_assemble_fp64(const DevGeometry &g, const double *prisms, int64_t n_
 void launch_assemble_fp32(const DevGeometry &g, const double *prisms, int64_t n_cells,
                           const int64_t *col_index, int64_t col_offset, float *G, int64_t ld,
                           cudaStream_t s);
+// Tiled assembly (regular parts of the mesh share faces in z and in y).  The
+// plan groups the cell list into tiles of up to tile_max_cols() z-runs: int4
+// {first run, runs, levels, 0} per tile, and the first cell of every run.
+struct TilePlan {
+  const int32_t *tiles = nullptr;    // n_tiles x 4
+  const int64_t *run_start = nullptr;
+  int64_t n_tiles = 0;
+};
+int tile_max_cols();
+void build_tile_plan(const double *prisms, int64_t n_cells, std::vector<int32_t> &tiles,
+                     std::vector<int64_t> &run_start);
+void launch_assemble_tiled_fp64(const DevGeometry &g, const TilePlan &plan, double *G, int64_t ld,
+                                cudaStream_t s);
+void launch_assemble_tiled_fp32(const DevGeometry &g, const TilePlan &plan, float *G, int64_t ld,
+                                cudaStream_t s);
+
 // Per-row maximum of |G| over the columns, then bf16 entries G/scale with the
 // FP32 scale per row (entries of an all-zero row get scale 1).
 // half16 = false: bf16; true: IEEE fp16 (entries in [-1, 1] after scaling).

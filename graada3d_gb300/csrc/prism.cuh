@@ -366,6 +366,163 @@ __device__ __forceinline__ void prism_terms(double px, double py, double pz, dou
   if (fam & FAM_AZ) carry.tz = t.tz[1];
 }
 
+// Quantities of a cell's y1 face that the next column of a tile (the cell at
+// the same level, same x extent and z levels, its y0 equal to this y1) needs
+// for its y0 face: corner distances, the x-edge log ratios on that face, the
+// z-edge log ratios along it and its angle sum.
+struct YCarry {
+  double r[2][2];  // [i][k]
+  double qx[2];    // [k]
+  double qz[2];    // [i]
+  double ty;
+};
+
+// prism_terms with both neighbours' faces available: `top` (the cell above in
+// the same column, ZCarry) and `yprev` (the cell of the previous column at the
+// same level, YCarry).  Shared quantities are taken over instead of being
+// recomputed; every computed quantity uses the same FP64 operands in the same
+// order as prism_terms, so the result is bitwise that of prism_terms.
+__device__ __forceinline__ void prism_terms_tiled(double px, double py, double pz, double x0,
+                                                  double x1, double y0, double y1, double z0,
+                                                  double z1, uint32_t fam,
+                                                  const double *__restrict__ tab, bool top,
+                                                  const ZCarry &zin, bool yprev,
+                                                  const YCarry &yin, ZCarry &zout, YCarry &yout,
+                                                  PrismTerms &t) {
+  t.X[0] = x0 - px; t.X[1] = x1 - px;
+  t.Y[0] = y0 - py; t.Y[1] = y1 - py;
+  t.Z[0] = z0 - pz; t.Z[1] = z1 - pz;
+  const double X2[2] = {t.X[0] * t.X[0], t.X[1] * t.X[1]};
+  const double Y2[2] = {t.Y[0] * t.Y[0], t.Y[1] * t.Y[1]};
+  const double Z2[2] = {t.Z[0] * t.Z[0], t.Z[1] * t.Z[1]};
+  double r[2][2][2];
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const double xy = X2[i] + Y2[j];
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        if (top && k == 0) r[i][j][k] = zin.r[i][j];
+        else if (yprev && j == 0) r[i][j][k] = yin.r[i][k];
+        else r[i][j][k] = sqrt(xy + Z2[k]);
+      }
+    }
+  if (fam & FAM_LX) {
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        if (top && k == 0) t.qx[j][k] = zin.qx[j];
+        else if (yprev && j == 0) t.qx[j][k] = yin.qx[k];
+        else
+          t.qx[j][k] = edge_log_ratio(t.X[0], t.X[1], r[0][j][k], r[1][j][k], Y2[j] + Z2[k], tab);
+      }
+  }
+  if (fam & FAM_LY) {
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        if (top && k == 0) t.qy[i][k] = zin.qy[i];
+        else
+          t.qy[i][k] = edge_log_ratio(t.Y[0], t.Y[1], r[i][0][k], r[i][1][k], X2[i] + Z2[k], tab);
+      }
+  }
+  if (fam & FAM_LZ) {
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        if (yprev && j == 0) t.qz[i][j] = yin.qz[i];
+        else
+          t.qz[i][j] = edge_log_ratio(t.Z[0], t.Z[1], r[i][j][0], r[i][j][1], X2[i] + Y2[j], tab);
+      }
+  }
+  if (fam & (FAM_AX | FAM_AY | FAM_AZ)) {
+    const float Xf[2] = {(float)t.X[0], (float)t.X[1]};
+    const float Yf[2] = {(float)t.Y[0], (float)t.Y[1]};
+    const float Zf[2] = {(float)t.Z[0], (float)t.Z[1]};
+    float rf[2][2][2];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+      for (int j = 0; j < 2; j++)
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+          rf[i][j][k] = sqrtf(fmaf(Xf[i], Xf[i], fmaf(Yf[j], Yf[j], Zf[k] * Zf[k])));
+    if (fam & FAM_AX) {
+      const double b[4] = {t.Y[0] * t.Z[0], t.Y[0] * t.Z[1], t.Y[1] * t.Z[0], t.Y[1] * t.Z[1]};
+      const float bf[4] = {Yf[0] * Zf[0], Yf[0] * Zf[1], Yf[1] * Zf[0], Yf[1] * Zf[1]};
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        const double a[4] = {t.X[i] * r[i][0][0], t.X[i] * r[i][0][1], t.X[i] * r[i][1][0],
+                             t.X[i] * r[i][1][1]};
+        const float af[4] = {Xf[i] * rf[i][0][0], Xf[i] * rf[i][0][1], Xf[i] * rf[i][1][0],
+                             Xf[i] * rf[i][1][1]};
+        t.tx[i] = face_atan_sum(a, b, af, bf, tab);
+      }
+    }
+    if (fam & FAM_AY) {
+      const double b[4] = {t.X[0] * t.Z[0], t.X[0] * t.Z[1], t.X[1] * t.Z[0], t.X[1] * t.Z[1]};
+      const float bf[4] = {Xf[0] * Zf[0], Xf[0] * Zf[1], Xf[1] * Zf[0], Xf[1] * Zf[1]};
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        if (yprev && j == 0) {
+          t.ty[0] = yin.ty;
+          continue;
+        }
+        const double a[4] = {t.Y[j] * r[0][j][0], t.Y[j] * r[0][j][1], t.Y[j] * r[1][j][0],
+                             t.Y[j] * r[1][j][1]};
+        const float af[4] = {Yf[j] * rf[0][j][0], Yf[j] * rf[0][j][1], Yf[j] * rf[1][j][0],
+                             Yf[j] * rf[1][j][1]};
+        t.ty[j] = face_atan_sum(a, b, af, bf, tab);
+      }
+    }
+    if (fam & FAM_AZ) {
+      const double b[4] = {t.X[0] * t.Y[0], t.X[0] * t.Y[1], t.X[1] * t.Y[0], t.X[1] * t.Y[1]};
+      const float bf[4] = {Xf[0] * Yf[0], Xf[0] * Yf[1], Xf[1] * Yf[0], Xf[1] * Yf[1]};
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        if (top && k == 0) {
+          t.tz[0] = zin.tz;
+          continue;
+        }
+        const double a[4] = {t.Z[k] * r[0][0][k], t.Z[k] * r[0][1][k], t.Z[k] * r[1][0][k],
+                             t.Z[k] * r[1][1][k]};
+        const float af[4] = {Zf[k] * rf[0][0][k], Zf[k] * rf[0][1][k], Zf[k] * rf[1][0][k],
+                             Zf[k] * rf[1][1][k]};
+        t.tz[k] = face_atan_sum(a, b, af, bf, tab);
+      }
+    }
+  }
+  // faces handed on: bottom (z1) down the column, y1 to the next column
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 2; j++) zout.r[i][j] = r[i][j][1];
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int k = 0; k < 2; k++) yout.r[i][k] = r[i][1][k];
+  if (fam & FAM_LX) {
+    zout.qx[0] = t.qx[0][1];
+    zout.qx[1] = t.qx[1][1];
+    yout.qx[0] = t.qx[1][0];
+    yout.qx[1] = t.qx[1][1];
+  }
+  if (fam & FAM_LY) {
+    zout.qy[0] = t.qy[0][1];
+    zout.qy[1] = t.qy[1][1];
+  }
+  if (fam & FAM_LZ) {
+    yout.qz[0] = t.qz[0][1];
+    yout.qz[1] = t.qz[1][1];
+  }
+  if (fam & FAM_AY) yout.ty = t.ty[1];
+  if (fam & FAM_AZ) zout.tz = t.tz[1];
+}
+
 // sum over two indices with signs sigma_a sigma_b of c_ab q_ab where
 // c_ab = u_a (or v_b); helpers keep the sign pattern (+,-,-,+) in one place.
 __device__ __forceinline__ double signed4(const double q[2][2]) {
