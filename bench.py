@@ -738,6 +738,26 @@ def run_sweep_cfg4(n_lambda: int = 16, gn_iter: int = 5, storages=("fp64", "fp32
     return out
 
 
+def run_mf_profile():
+    """Fixed small case for ncu captures of the matrix-free field sum and the
+    FP64 assembly with two components: 32 x 32 x 32 = 32,768 cells, gz + Tzz at
+    51 x 51 points (50 m over 20 km x 20 km); one FP64 assembly, one
+    matrix-free G x."""
+    from graada3d_gb300 import Fwd, mesh
+
+    prisms = mesh.regular_mesh((0.0, 20000.0), 32, (0.0, 20000.0), 32, (0.0, 8000.0), 32)
+    obs = mesh.observation_grid(51, 0.0, 20000.0, 51, 0.0, 20000.0, -50.0)
+    f = Fwd(prisms, obs, 0x012)
+    f.compute_G("fp64")
+    x = np.ones(f.Nm)
+    y64 = f.G_vec_mul(x)
+    f.compute_G("matrix_free")
+    y = f.G_vec_mul(x)
+    assert np.abs(y - y64).max() <= 1e-12 * np.abs(y64).max()
+    print(json.dumps({"case": "mf-profile", "pairs": f.N_obs * f.Nm}))
+    f.ctx.close()
+
+
 def run_profile_case(args):
     """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
     50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
@@ -765,7 +785,8 @@ def main():
     ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-cfg1",
                                                          "inversion-cfg3", "matrix-free-cfg5",
                                                          "gemv", "batched-cfg4", "block-gemm",
-                                                         "sweep-cfg4", "block-gemm-profile"])
+                                                         "sweep-cfg4", "block-gemm-profile",
+                                                         "mf-profile"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -780,6 +801,8 @@ def main():
         run_profile_case(args)
     elif args.case == "block-gemm":
         print(json.dumps(run_block_gemm_case()))
+    elif args.case == "mf-profile":
+        run_mf_profile()
     elif args.case == "block-gemm-profile":
         run_block_gemm_profile()
     elif args.case == "sweep-cfg4":

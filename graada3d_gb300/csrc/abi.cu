@@ -67,6 +67,9 @@ DevGeometry Context::geometry() const {
   g.mask = mask;
   g.n_fields = n_fields;
   g.tables = math_tables.as<double>();
+  g.plan.tiles = plan_tiles.as<int32_t>();
+  g.plan.run_start = plan_runs.as<int64_t>();
+  g.plan.n_tiles = plan_n_tiles;
   return g;
 }
 
@@ -142,6 +145,7 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
   plan_valid = false;
   upload(obs.ptr, h_obs, sizeof(double) * 3 * no);
   sync();
+  tile_plan();  // every kernel walking the cells uses it
 }
 
 // The assembly's tile plan for the current cell list (rebuilt after a change

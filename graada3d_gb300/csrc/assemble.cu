@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "prism.cuh"
+#include "tile_walk.cuh"
 
 namespace grada {
 
@@ -93,11 +94,6 @@ void launch_assemble(const DevGeometry &g, const double *prisms, int64_t n_cells
 // memory, the y carry in registers.  Regular meshes form tiles of TL_COLS full
 // columns; a refined mesh forms smaller ones (down to single runs).
 
-constexpr int TL_THREADS = 128;
-constexpr int TL_COLS = 8;
-constexpr int TL_LCH = 8;  // levels staged per pass
-constexpr int ZC_N = 9;    // doubles of a ZCarry
-
 template <typename OutT>
 __global__ void __launch_bounds__(TL_THREADS)
     assemble_tiled_kernel(const double *__restrict__ obs, int64_t n_obs,
@@ -105,13 +101,9 @@ __global__ void __launch_bounds__(TL_THREADS)
                           const int64_t *__restrict__ run_start, uint32_t mask,
                           const double *__restrict__ tables, OutT *__restrict__ G, int64_t ld) {
   __shared__ double tab[kTabSize];
-  __shared__ double sc[TL_LCH][TL_COLS][6];
-  __shared__ int64_t rs[TL_COLS];
-  extern __shared__ double zsm[];  // [TL_COLS][ZC_N][TL_THREADS]
-  const int4 td = tiles[blockIdx.x];
-  const int ncols = td.y, nlev = td.z;
+  __shared__ TileSmem ws;
+  extern __shared__ double zsm[];
   for (int t = threadIdx.x; t < kTabSize; t += TL_THREADS) tab[t] = tables[t];
-  if (threadIdx.x < ncols) rs[threadIdx.x] = run_start[td.x + threadIdx.x];
   const int64_t i = (int64_t)blockIdx.y * TL_THREADS + threadIdx.x;
   const bool active = i < n_obs;
   double px = 0, py = 0, pz = 0;
@@ -120,55 +112,18 @@ __global__ void __launch_bounds__(TL_THREADS)
     py = obs[3 * i + 1];
     pz = obs[3 * i + 2];
   }
-  const uint32_t fam = families_for_mask(mask);
-  auto zslot = [&](int a, int f) -> double & {
-    return zsm[((int64_t)a * ZC_N + f) * TL_THREADS + threadIdx.x];
-  };
-  for (int k0 = 0; k0 < nlev; k0 += TL_LCH) {
-    const int nl = min(TL_LCH, nlev - k0);
-    __syncthreads();
-    for (int t = threadIdx.x; t < nl * ncols * 6; t += TL_THREADS) {
-      const int k = t / (ncols * 6), a = (t / 6) % ncols, q = t % 6;
-      sc[k][a][q] = prisms[(rs[a] + k0 + k) * 6 + q];
-    }
-    __syncthreads();
-    if (!active) continue;
-    for (int kk = 0; kk < nl; kk++) {
-      const int k = k0 + kk;
-      YCarry yc;
-      for (int a = 0; a < ncols; a++) {
-        const double *p = sc[kk][a];
-        ZCarry zin, zout;
-        const bool top = k > 0;
-        if (top) {
-          zin.r[0][0] = zslot(a, 0); zin.r[0][1] = zslot(a, 1);
-          zin.r[1][0] = zslot(a, 2); zin.r[1][1] = zslot(a, 3);
-          zin.qx[0] = zslot(a, 4); zin.qx[1] = zslot(a, 5);
-          zin.qy[0] = zslot(a, 6); zin.qy[1] = zslot(a, 7);
-          zin.tz = zslot(a, 8);
-        }
-        YCarry yout;
-        PrismTerms t;
-        prism_terms_tiled(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, top, zin,
-                          a > 0, yc, zout, yout, t);
-        zslot(a, 0) = zout.r[0][0]; zslot(a, 1) = zout.r[0][1];
-        zslot(a, 2) = zout.r[1][0]; zslot(a, 3) = zout.r[1][1];
-        zslot(a, 4) = zout.qx[0]; zslot(a, 5) = zout.qx[1];
-        zslot(a, 6) = zout.qy[0]; zslot(a, 7) = zout.qy[1];
-        zslot(a, 8) = zout.tz;
-        yc = yout;
-        OutT *gcol = G + (rs[a] + k) * ld + i;
-        int slot = 0;
+  tile_walk(tiles[blockIdx.x], run_start, prisms, ws, zsm, active, px, py, pz,
+            families_for_mask(mask), tab, [&](int64_t cell, const PrismTerms &t) {
+              OutT *gcol = G + cell * ld + i;
+              int slot = 0;
 #pragma unroll
-        for (int b = 0; b < 10; b++) {
-          if (mask & (1u << b)) {
-            store_entry(gcol + (int64_t)slot * n_obs, prism_component(t, b));
-            slot++;
-          }
-        }
-      }
-    }
-  }
+              for (int b = 0; b < 10; b++) {
+                if (mask & (1u << b)) {
+                  store_entry(gcol + (int64_t)slot * n_obs, prism_component(t, b));
+                  slot++;
+                }
+              }
+            });
 }
 
 template <typename OutT>
@@ -177,7 +132,7 @@ void launch_assemble_tiled(const DevGeometry &g, const TilePlan &plan, OutT *G, 
   if (plan.n_tiles <= 0 || g.n_obs <= 0) return;
   static std::mutex mu;
   static bool attr[64] = {};
-  const int smem = (int)(sizeof(double) * TL_COLS * ZC_N * TL_THREADS);
+  const int smem = tile_walk_dyn_smem();
   {
     int dev = 0;
     GRADA_CUDA_CHECK(cudaGetDevice(&dev));
@@ -233,23 +188,25 @@ __global__ void quantize_16_kernel(const float *__restrict__ G, int64_t nd, int6
 
 // ---- matrix-free field sum ------------------------------------------------
 
-constexpr int FF_THREADS = 128;
-constexpr int FF_CHUNK = 32;
-
-__global__ void __launch_bounds__(FF_THREADS)
+// One block: TL_THREADS points x the tiles of one split; each thread sums
+// rho_j field_k(point, cell_j) over the split's cells (tile walk, faces shared
+// in z and y), the splits are added in order by a second pass.
+__global__ void __launch_bounds__(TL_THREADS)
     forward_field_kernel(const double *__restrict__ obs, int64_t n_obs,
-                         const double *__restrict__ prisms, const double *__restrict__ rho,
-                         int64_t n_cells, int64_t cells_per_split, uint32_t mask, int nf,
-                         const double *__restrict__ tables, double *__restrict__ partial,
+                         const double *__restrict__ prisms, const int4 *__restrict__ tiles,
+                         const int64_t *__restrict__ run_start, int64_t n_tiles,
+                         int64_t tiles_per_split, const double *__restrict__ rho, uint32_t mask,
+                         int nf, const double *__restrict__ tables, double *__restrict__ partial,
                          const int *__restrict__ skip) {
   if (skip && *skip) return;
-  __shared__ double sp[FF_CHUNK * 7];
   __shared__ double tab[kTabSize];
-  for (int t = threadIdx.x; t < kTabSize; t += FF_THREADS) tab[t] = tables[t];
+  __shared__ TileSmem ws;
+  extern __shared__ double zsm[];
+  for (int t = threadIdx.x; t < kTabSize; t += TL_THREADS) tab[t] = tables[t];
   const int64_t split = blockIdx.x;
-  const int64_t c_begin = split * cells_per_split;
-  const int64_t c_end = min(n_cells, c_begin + cells_per_split);
-  const int64_t i = (int64_t)blockIdx.y * FF_THREADS + threadIdx.x;
+  const int64_t t_begin = split * tiles_per_split;
+  const int64_t t_end = min(n_tiles, t_begin + tiles_per_split);
+  const int64_t i = (int64_t)blockIdx.y * TL_THREADS + threadIdx.x;
   const bool active = i < n_obs;
   double px = 0, py = 0, pz = 0;
   if (active) {
@@ -261,30 +218,14 @@ __global__ void __launch_bounds__(FF_THREADS)
   double acc[10];
 #pragma unroll
   for (int b = 0; b < 10; b++) acc[b] = 0.0;
-  ZCarry carry;
-  double prev[6] = {0, 0, 0, 0, 0, 0};
-  bool have_prev = false;
-  for (int64_t c0 = c_begin; c0 < c_end; c0 += FF_CHUNK) {
-    const int nc = (int)min((int64_t)FF_CHUNK, c_end - c0);
-    __syncthreads();
-    for (int t = threadIdx.x; t < nc * 6; t += FF_THREADS) sp[t] = prisms[c0 * 6 + t];
-    for (int t = threadIdx.x; t < nc; t += FF_THREADS) sp[FF_CHUNK * 6 + t] = rho[c0 + t];
-    __syncthreads();
-    if (!active) continue;
-    for (int c = 0; c < nc; c++) {
-      const double *p = sp + 6 * c;
-      const double w = sp[FF_CHUNK * 6 + c];
-      const bool reuse = have_prev && p[0] == prev[0] && p[1] == prev[1] && p[2] == prev[2] &&
-                         p[3] == prev[3] && p[4] == prev[5];
-      PrismTerms t;
-      prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, reuse, carry, t);
+  for (int64_t tl = t_begin; tl < t_end; tl++) {
+    tile_walk(tiles[tl], run_start, prisms, ws, zsm, active, px, py, pz, fam, tab,
+              [&](int64_t cell, const PrismTerms &t) {
+                const double w = __ldg(rho + cell);
 #pragma unroll
-      for (int q = 0; q < 6; q++) prev[q] = p[q];
-      have_prev = true;
-#pragma unroll
-      for (int b = 0; b < 10; b++)
-        if (mask & (1u << b)) acc[b] = fma(w, prism_component(t, b), acc[b]);
-    }
+                for (int b = 0; b < 10; b++)
+                  if (mask & (1u << b)) acc[b] = fma(w, prism_component(t, b), acc[b]);
+              });
   }
   if (!active) return;
   double *out = partial + split * n_obs * nf + i * nf;
@@ -317,69 +258,73 @@ __global__ void sum_splits_kernel(const double *__restrict__ partial, int n_spli
 
 // ---- matrix-free adjoint: x_j = sum_i sum_k G(k*n_obs+i, j) y(k*n_obs+i) ---
 
-constexpr int AD_THREADS = 128;
-constexpr int AD_CHUNK = 16;
-
-// One block: AD_CHUNK consecutive cells x the observation points of one
-// split.  Each thread evaluates its points against the chunk's cells and
-// keeps per-cell sums in shared memory; the block then reduces them over its
-// threads in a fixed order.  Splits are summed by a second pass.
-__global__ void __launch_bounds__(AD_THREADS)
-    adjoint_field_kernel(const double *__restrict__ obs, int64_t n_obs,
-                         const double *__restrict__ prisms, int64_t n_cells, uint32_t mask,
-                         const double *__restrict__ tables, const double *__restrict__ y,
-                         const double *__restrict__ pre_scale, int64_t obs_per_split,
-                         double *__restrict__ partial, const int *__restrict__ skip) {
+// Tiled G^T y: a block owns one tile and a range of point blocks.  For every
+// cell of the tile each thread forms its point's contribution
+// sum_k y(k*n_obs+i) field_k(point, cell); the warp adds its 32 with
+// shuffles and lane 0 accumulates the warp sum in shared memory, in point-
+// block order.  At the end the four warp sums of each cell are added in
+// order and written as the block's partial (no atomics: bit-reproducible).
+// Threads past n_obs walk observation 0 with weight 0, so every lane takes
+// part in the shuffles.
+__global__ void __launch_bounds__(TL_THREADS)
+    adjoint_field_tiled_kernel(const double *__restrict__ obs, int64_t n_obs,
+                               const double *__restrict__ prisms, const int4 *__restrict__ tiles,
+                               const int64_t *__restrict__ run_start, int64_t n_cells,
+                               uint32_t mask, const double *__restrict__ tables,
+                               const double *__restrict__ y, const double *__restrict__ pre_scale,
+                               int64_t pblocks_per_split, double *__restrict__ partial,
+                               const int *__restrict__ skip) {
   if (skip && *skip) return;
-  __shared__ double sp[AD_CHUNK * 6];
   __shared__ double tab[kTabSize];
-  __shared__ double acc[AD_CHUNK][AD_THREADS];
-  for (int t = threadIdx.x; t < kTabSize; t += AD_THREADS) tab[t] = tables[t];
-  const int64_t c0 = (int64_t)blockIdx.x * AD_CHUNK;
-  const int nc = (int)min((int64_t)AD_CHUNK, n_cells - c0);
-  for (int t = threadIdx.x; t < nc * 6; t += AD_THREADS) sp[t] = prisms[c0 * 6 + t];
-#pragma unroll
-  for (int c = 0; c < AD_CHUNK; c++) acc[c][threadIdx.x] = 0.0;
-  __syncthreads();
+  __shared__ TileSmem ws;
+  __shared__ double wacc[TL_THREADS / 32][TL_COLS * TL_MAXLEV];
+  extern __shared__ double zsm[];
+  for (int t = threadIdx.x; t < kTabSize; t += TL_THREADS) tab[t] = tables[t];
+  const int4 td = tiles[blockIdx.x];
+  const int ncells = td.y * td.z;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int q = lane; q < ncells; q += 32) wacc[warp][q] = 0.0;
   const uint32_t fam = families_for_mask(mask);
-  const int64_t i_begin = (int64_t)blockIdx.y * obs_per_split;
-  const int64_t i_end = min(n_obs, i_begin + obs_per_split);
-  for (int64_t i = i_begin + threadIdx.x; i < i_end; i += AD_THREADS) {
-    const double px = obs[3 * i], py = obs[3 * i + 1], pz = obs[3 * i + 2];
+  const int64_t n_pb = (n_obs + TL_THREADS - 1) / TL_THREADS;
+  const int64_t pb0 = (int64_t)blockIdx.y * pblocks_per_split;
+  const int64_t pb1 = min(n_pb, pb0 + pblocks_per_split);
+  for (int64_t pb = pb0; pb < pb1; pb++) {
+    const int64_t i = pb * TL_THREADS + threadIdx.x;
+    const bool real = i < n_obs;
+    const int64_t ii = real ? i : 0;
+    const double px = obs[3 * ii], py = obs[3 * ii + 1], pz = obs[3 * ii + 2];
     double w[10];
     int slot = 0;
 #pragma unroll
     for (int b = 0; b < 10; b++) {
       w[b] = 0.0;
       if (mask & (1u << b)) {
-        const int64_t r = (int64_t)slot * n_obs + i;
-        w[b] = pre_scale ? pre_scale[r] * y[r] : y[r];
+        const int64_t r = (int64_t)slot * n_obs + ii;
+        w[b] = real ? (pre_scale ? pre_scale[r] * y[r] : y[r]) : 0.0;
         slot++;
       }
     }
-    ZCarry carry;
-    for (int c = 0; c < nc; c++) {
-      const double *p = sp + 6 * c;
-      const bool reuse = c > 0 && p[0] == p[-6] && p[1] == p[-5] && p[2] == p[-4] &&
-                         p[3] == p[-3] && p[4] == p[-1];
-      PrismTerms t;
-      prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, reuse, carry, t);
-      double s = acc[c][threadIdx.x];
+    int q = 0;
+    tile_walk(td, run_start, prisms, ws, zsm, true, px, py, pz, fam, tab,
+              [&](int64_t, const PrismTerms &t) {
+                double c = 0.0;
 #pragma unroll
-      for (int b = 0; b < 10; b++)
-        if (mask & (1u << b)) s = fma(w[b], prism_component(t, b), s);
-      acc[c][threadIdx.x] = s;
-    }
+                for (int b = 0; b < 10; b++)
+                  if (mask & (1u << b)) c = fma(w[b], prism_component(t, b), c);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+                if (lane == 0) wacc[warp][q] += c;
+                q++;
+              });
   }
   __syncthreads();
-  // reduce each cell's AD_THREADS sums: warp w takes cells w, w + 4, ...
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c = warp; c < nc; c += AD_THREADS / 32) {
+  for (int qq = threadIdx.x; qq < ncells; qq += TL_THREADS) {
     double v = 0.0;
-    for (int t = lane; t < AD_THREADS; t += 32) v += acc[c][t];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) partial[(int64_t)blockIdx.y * n_cells + c0 + c] = v;
+    for (int w = 0; w < TL_THREADS / 32; w++) v += wacc[w][qq];
+    const int k = qq / td.y, a = qq % td.y;  // walk order: level-major, run-minor
+    const int64_t cell = run_start[td.x + a] + k;
+    partial[(int64_t)blockIdx.y * n_cells + cell] = v;
   }
 }
 
@@ -432,10 +377,10 @@ void build_math_tables(double *tab) {
 }
 
 int adjoint_field_splits(const DevGeometry &g, int sm_count) {
-  const int64_t chunks = ceil_div(g.n_cells, AD_CHUNK);
-  int64_t splits = ceil_div((int64_t)sm_count * 8, chunks);
-  const int64_t max_splits = ceil_div(g.n_obs, AD_THREADS);
-  if (splits > max_splits) splits = max_splits;
+  // ~16 waves of the 2 resident blocks per SM over (tiles x point ranges)
+  const int64_t n_pb = ceil_div(g.n_obs, TL_THREADS);
+  int64_t splits = ceil_div((int64_t)sm_count * 2 * 16, std::max<int64_t>(g.plan.n_tiles, 1));
+  if (splits > n_pb) splits = n_pb;
   if (splits < 1) splits = 1;
   if (splits > 65535) splits = 65535;
   return (int)splits;
@@ -445,10 +390,26 @@ void launch_adjoint_field(const DevGeometry &g, const double *y, const double *p
                           int n_split, double *partial, double *x, cudaStream_t s,
                           const int *skip) {
   if (g.n_cells <= 0) return;
-  const int64_t per = ceil_div(g.n_obs, n_split);
-  dim3 grid((unsigned)ceil_div(g.n_cells, AD_CHUNK), (unsigned)n_split);
-  adjoint_field_kernel<<<grid, AD_THREADS, 0, s>>>(g.obs, g.n_obs, g.prisms, g.n_cells, g.mask,
-                                                   g.tables, y, pre_scale, per, partial, skip);
+  const int64_t n_pb = ceil_div(g.n_obs, TL_THREADS);
+  const int64_t per = ceil_div(n_pb, n_split);
+  const int smem = tile_walk_dyn_smem();
+  {
+    static std::mutex mu;
+    static bool attr[64] = {};
+    int dev = 0;
+    GRADA_CUDA_CHECK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64 || !attr[dev]) {
+      GRADA_CUDA_CHECK(cudaFuncSetAttribute(adjoint_field_tiled_kernel,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      if (dev >= 0 && dev < 64) attr[dev] = true;
+    }
+  }
+  if (g.plan.n_tiles > 0x7fffffff) throw Error(-1, "too many tiles for one launch");
+  dim3 grid((unsigned)g.plan.n_tiles, (unsigned)n_split);
+  adjoint_field_tiled_kernel<<<grid, TL_THREADS, smem, s>>>(
+      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(g.plan.tiles), g.plan.run_start,
+      g.n_cells, g.mask, g.tables, y, pre_scale, per, partial, skip);
   GRADA_LAUNCH_CHECK();
   sum_cell_splits_kernel<<<(unsigned)ceil_div(g.n_cells, 256), 256, 0, s>>>(partial, n_split,
                                                                            g.n_cells, x, skip);
@@ -494,11 +455,14 @@ void build_tile_plan(const double *p, int64_t n, std::vector<int32_t> &tiles,
   for (size_t r = 0; r < rstart.size();) {
     size_t e = r;
     while (e + 1 < rstart.size() && (int)(e + 1 - r) < TL_COLS && ynext(e, e + 1)) e++;
-    tiles.push_back((int32_t)run_start.size());
-    tiles.push_back((int32_t)(e - r + 1));
-    tiles.push_back((int32_t)rlen[r]);
-    tiles.push_back(0);
-    for (size_t q = r; q <= e; q++) run_start.push_back(rstart[q]);
+    // runs longer than TL_MAXLEV levels go on in further tiles of the same runs
+    for (int64_t l0 = 0; l0 < rlen[r]; l0 += TL_MAXLEV) {
+      tiles.push_back((int32_t)run_start.size());
+      tiles.push_back((int32_t)(e - r + 1));
+      tiles.push_back((int32_t)std::min<int64_t>(TL_MAXLEV, rlen[r] - l0));
+      tiles.push_back(0);
+      for (size_t q = r; q <= e; q++) run_start.push_back(rstart[q] + l0);
+    }
     r = e + 1;
   }
 }
@@ -542,10 +506,12 @@ void launch_rowscale_16(const float *G32, int64_t nd, int64_t nm, int64_t ld, fl
 }
 
 int forward_field_splits(const DevGeometry &g, int sm_count) {
-  const int64_t obs_tiles = ceil_div(g.n_obs, FF_THREADS);
-  const int64_t want_blocks = (int64_t)sm_count * 8;
+  // ~16 waves of the 2 resident blocks per SM, so the last wave is a small
+  // part of the launch
+  const int64_t obs_tiles = ceil_div(g.n_obs, TL_THREADS);
+  const int64_t want_blocks = (int64_t)sm_count * 2 * 16;
   int64_t splits = ceil_div(want_blocks, obs_tiles);
-  const int64_t max_splits = ceil_div(g.n_cells, FF_CHUNK);
+  const int64_t max_splits = g.plan.n_tiles;
   if (splits > max_splits) splits = max_splits;
   if (splits < 1) splits = 1;
   if (splits > 65535) splits = 65535;
@@ -556,11 +522,25 @@ void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, 
                           double *fields, bool g_rows, cudaStream_t s, const double *post_scale,
                           const int *skip) {
   if (g.n_obs <= 0) return;
-  const int64_t per = round_up(ceil_div(g.n_cells, n_split), FF_CHUNK);
-  dim3 grid((unsigned)n_split, (unsigned)ceil_div(g.n_obs, FF_THREADS));
+  const int64_t per = ceil_div(g.plan.n_tiles, n_split);
+  dim3 grid((unsigned)n_split, (unsigned)ceil_div(g.n_obs, TL_THREADS));
   if (grid.y > 65535u) throw Error(-1, "too many observation points for one launch");
-  forward_field_kernel<<<grid, FF_THREADS, 0, s>>>(g.obs, g.n_obs, g.prisms, rho, g.n_cells, per,
-                                                   g.mask, g.n_fields, g.tables, partial, skip);
+  const int smem = tile_walk_dyn_smem();
+  {
+    static std::mutex mu;
+    static bool attr[64] = {};
+    int dev = 0;
+    GRADA_CUDA_CHECK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64 || !attr[dev]) {
+      GRADA_CUDA_CHECK(cudaFuncSetAttribute(forward_field_kernel,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      if (dev >= 0 && dev < 64) attr[dev] = true;
+    }
+  }
+  forward_field_kernel<<<grid, TL_THREADS, smem, s>>>(
+      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(g.plan.tiles), g.plan.run_start,
+      g.plan.n_tiles, per, rho, g.mask, g.n_fields, g.tables, partial, skip);
   GRADA_LAUNCH_CHECK();
   const int64_t n = g.n_obs * g.n_fields;
   sum_splits_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(

@@ -93,6 +93,7 @@ void Context::expand_G(int64_t n_split, const int64_t *parent, const double *chi
     n_cells = nm_new;
     host_prisms.swap(new_prisms);
     plan_valid = false;
+    tile_plan();
     prisms.alloc(this, sizeof(double) * 6 * nm_new);
     upload(prisms.ptr, host_prisms.data(), sizeof(double) * 6 * nm_new);
     sync();
@@ -134,6 +135,7 @@ void Context::expand_G(int64_t n_split, const int64_t *parent, const double *chi
   prisms.alloc(this, sizeof(double) * 6 * nm_new);
   upload(prisms.ptr, host_prisms.data(), sizeof(double) * 6 * nm_new);
   sync();
+  tile_plan();
   // the regularisation operators are Nm x Nm: the host rebuilds them after a refinement
   for (auto &o : ops) o.set = false;
   for (auto &o : crg) o.set = false;

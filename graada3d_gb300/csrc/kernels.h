@@ -9,6 +9,15 @@
 
 namespace grada {
 
+// Tiled assembly (regular parts of the mesh share faces in z and in y).  The
+// plan groups the cell list into tiles of up to tile_max_cols() z-runs: int4
+// {first run, runs, levels, 0} per tile, and the first cell of every run.
+struct TilePlan {
+  const int32_t *tiles = nullptr;    // n_tiles x 4
+  const int64_t *run_start = nullptr;
+  int64_t n_tiles = 0;
+};
+
 // Device-resident problem geometry (mesh leaf cells and observation points).
 struct DevGeometry {
   const double *prisms = nullptr;  // n_cells x 6: x0 x1 y0 y1 z0 z1
@@ -18,6 +27,7 @@ struct DevGeometry {
   uint32_t mask = 0;
   int n_fields = 0;
   const double *tables = nullptr;  // math tables of prism.cuh (kTabSize doubles)
+  TilePlan plan;                   // the cell list as assembly tiles
 };
 
 // Number of doubles of the math tables and their host-side construction.
@@ -33,14 +43,6 @@ void launch_assemble_fp64(const DevGeometry &g, const double *prisms, int64_t n_
 void launch_assemble_fp32(const DevGeometry &g, const double *prisms, int64_t n_cells,
                           const int64_t *col_index, int64_t col_offset, float *G, int64_t ld,
                           cudaStream_t s);
-// Tiled assembly (regular parts of the mesh share faces in z and in y).  The
-// plan groups the cell list into tiles of up to tile_max_cols() z-runs: int4
-// {first run, runs, levels, 0} per tile, and the first cell of every run.
-struct TilePlan {
-  const int32_t *tiles = nullptr;    // n_tiles x 4
-  const int64_t *run_start = nullptr;
-  int64_t n_tiles = 0;
-};
 int tile_max_cols();
 void build_tile_plan(const double *prisms, int64_t n_cells, std::vector<int32_t> &tiles,
                      std::vector<int64_t> &run_start);

@@ -7,12 +7,11 @@
 // The prism terms cost several hundred FP64 instructions per pair; the 16
 // multiply-adds per component that a block adds are a small fraction of
 // that, so a block costs little more than one single product.
-//  * G X: one thread per observation point, cells streamed in chunks through
-//    shared memory with their 16 model values; accumulators per component
-//    and right-hand side stay in registers, RG right-hand sides per pass
-//    (RG = 16 for up to 2 components, fewer passes' worth of registers for
-//    more components).  Cell ranges (splits) give partial sums added in
-//    order by a second pass.
+//  * G X: one thread per observation point walking the assembly tiles (faces
+//    shared in z and y, tile_walk.cuh); accumulators per component and
+//    right-hand side stay in registers, RG right-hand sides per pass (RG = 16
+//    for up to 2 components, fewer for more components).  Tile ranges
+//    (splits) give partial sums added in order by a second pass.
 //  * G^T Y: one thread per cell, observation points (coordinates and the 16
 //    weighted data values per component) streamed through shared memory;
 //    the thread's 16 sums stay in registers.  Point ranges (splits) give
@@ -23,13 +22,12 @@
 #include "common.cuh"
 #include "kernels.h"
 #include "prism.cuh"
+#include "tile_walk.cuh"
 
 namespace grada {
 
 namespace {
 
-constexpr int FB_THREADS = 128;
-constexpr int FB_CHUNK = 32;
 constexpr int AB_THREADS = 128;
 constexpr int AB_CHUNK = 32;
 
@@ -40,24 +38,25 @@ __device__ __forceinline__ void slot_bits(uint32_t mask, int *bits) {
 }
 
 template <int RG>
-__global__ void __launch_bounds__(FB_THREADS)
+__global__ void __launch_bounds__(TL_THREADS)
     forward_field_block_kernel(const double *__restrict__ obs, int64_t n_obs,
-                               const double *__restrict__ prisms, const double *__restrict__ X,
-                               int64_t n_cells, int64_t cells_per_split, uint32_t mask, int nf,
-                               const double *__restrict__ tables, int r0,
+                               const double *__restrict__ prisms, const int4 *__restrict__ tiles,
+                               const int64_t *__restrict__ run_start, int64_t n_tiles,
+                               int64_t tiles_per_split, const double *__restrict__ X,
+                               uint32_t mask, int nf, const double *__restrict__ tables, int r0,
                                double *__restrict__ partial, const int *__restrict__ skip) {
   constexpr int NFMAX = (RG >= 16) ? 2 : (RG >= 8 ? 4 : (RG >= 4 ? 8 : 10));
   if (skip && *skip) return;
-  __shared__ double sp[FB_CHUNK * 6];
-  __shared__ double xs[FB_CHUNK][RG];
   __shared__ double tab[kTabSize];
+  __shared__ TileSmem ws;
   __shared__ int bits[10];
-  for (int t = threadIdx.x; t < kTabSize; t += FB_THREADS) tab[t] = tables[t];
+  extern __shared__ double zsm[];
+  for (int t = threadIdx.x; t < kTabSize; t += TL_THREADS) tab[t] = tables[t];
   if (threadIdx.x == 0) slot_bits(mask, bits);
   const int64_t split = blockIdx.x;
-  const int64_t c_begin = split * cells_per_split;
-  const int64_t c_end = min(n_cells, c_begin + cells_per_split);
-  const int64_t i = (int64_t)blockIdx.y * FB_THREADS + threadIdx.x;
+  const int64_t t_begin = split * tiles_per_split;
+  const int64_t t_end = min(n_tiles, t_begin + tiles_per_split);
+  const int64_t i = (int64_t)blockIdx.y * TL_THREADS + threadIdx.x;
   const bool active = i < n_obs;
   double px = 0, py = 0, pz = 0;
   if (active) {
@@ -71,35 +70,19 @@ __global__ void __launch_bounds__(FB_THREADS)
   for (int s = 0; s < NFMAX; s++)
 #pragma unroll
     for (int r = 0; r < RG; r++) acc[s][r] = 0.0;
-  ZCarry carry;
-  double prev[6] = {0, 0, 0, 0, 0, 0};
-  bool have_prev = false;
-  for (int64_t c0 = c_begin; c0 < c_end; c0 += FB_CHUNK) {
-    const int nc = (int)min((int64_t)FB_CHUNK, c_end - c0);
-    __syncthreads();
-    for (int t = threadIdx.x; t < nc * 6; t += FB_THREADS) sp[t] = prisms[c0 * 6 + t];
-    for (int t = threadIdx.x; t < nc * RG; t += FB_THREADS)
-      xs[t / RG][t % RG] = X[(c0 + t / RG) * kBW + r0 + t % RG];
-    __syncthreads();
-    if (!active) continue;
-    for (int c = 0; c < nc; c++) {
-      const double *p = sp + 6 * c;
-      const bool reuse = have_prev && p[0] == prev[0] && p[1] == prev[1] && p[2] == prev[2] &&
-                         p[3] == prev[3] && p[4] == prev[5];
-      PrismTerms t;
-      prism_terms(px, py, pz, p[0], p[1], p[2], p[3], p[4], p[5], fam, tab, reuse, carry, t);
+  for (int64_t tl = t_begin; tl < t_end; tl++) {
+    tile_walk(tiles[tl], run_start, prisms, ws, zsm, active, px, py, pz, fam, tab,
+              [&](int64_t cell, const PrismTerms &t) {
+                const double *xc = X + cell * kBW + r0;  // same address in every thread
 #pragma unroll
-      for (int q = 0; q < 6; q++) prev[q] = p[q];
-      have_prev = true;
+                for (int s = 0; s < NFMAX; s++) {
+                  if (s < nf) {
+                    const double v = prism_component(t, bits[s]);
 #pragma unroll
-      for (int s = 0; s < NFMAX; s++) {
-        if (s < nf) {
-          const double v = prism_component(t, bits[s]);
-#pragma unroll
-          for (int r = 0; r < RG; r++) acc[s][r] = fma(v, xs[c][r], acc[s][r]);
-        }
-      }
-    }
+                    for (int r = 0; r < RG; r++) acc[s][r] = fma(v, __ldg(xc + r), acc[s][r]);
+                  }
+                }
+              });
   }
   if (!active) return;
   // partial[split][i][s][16]
@@ -200,9 +183,9 @@ __global__ void adjoint_block_sum_kernel(const double *__restrict__ partial, int
 }
 
 int fwd_splits(const DevGeometry &g, int sm_count) {
-  const int64_t obs_tiles = ceil_div(g.n_obs, FB_THREADS);
-  int64_t s = ceil_div((int64_t)sm_count * 8, obs_tiles);
-  const int64_t max_s = ceil_div(g.n_cells, FB_CHUNK);
+  const int64_t obs_tiles = ceil_div(g.n_obs, TL_THREADS);
+  int64_t s = ceil_div((int64_t)sm_count * 2 * 16, obs_tiles);  // ~16 waves
+  const int64_t max_s = g.plan.n_tiles;
   if (s > max_s) s = max_s;
   if (s < 1) s = 1;
   if (s > 65535) s = 65535;
@@ -222,9 +205,23 @@ int adj_splits(const DevGeometry &g, int sm_count) {
 template <int RG>
 void fwd_pass(const DevGeometry &g, const double *X, int splits, int64_t per, int r0,
               double *partial, cudaStream_t s, const int *skip) {
-  dim3 grid((unsigned)splits, (unsigned)ceil_div(g.n_obs, FB_THREADS));
-  forward_field_block_kernel<RG><<<grid, FB_THREADS, 0, s>>>(
-      g.obs, g.n_obs, g.prisms, X, g.n_cells, per, g.mask, g.n_fields, g.tables, r0, partial, skip);
+  const int smem = tile_walk_dyn_smem();
+  {
+    static std::mutex mu;
+    static bool attr[64] = {};
+    int dev = 0;
+    GRADA_CUDA_CHECK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64 || !attr[dev]) {
+      GRADA_CUDA_CHECK(cudaFuncSetAttribute(forward_field_block_kernel<RG>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      if (dev >= 0 && dev < 64) attr[dev] = true;
+    }
+  }
+  dim3 grid((unsigned)splits, (unsigned)ceil_div(g.n_obs, TL_THREADS));
+  forward_field_block_kernel<RG><<<grid, TL_THREADS, smem, s>>>(
+      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(g.plan.tiles), g.plan.run_start,
+      g.plan.n_tiles, per, X, g.mask, g.n_fields, g.tables, r0, partial, skip);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -239,9 +236,9 @@ int64_t mf_block_scratch_doubles(const DevGeometry &g, int sm_count) {
 void launch_forward_field_block(const DevGeometry &g, const double *X, double *Y, double *scratch,
                                 int sm_count, cudaStream_t s, const GemvOpts &o) {
   if (g.n_obs <= 0) return;
-  if (ceil_div(g.n_obs, FB_THREADS) > 65535) throw Error(-1, "too many observation points for one launch");
+  if (ceil_div(g.n_obs, TL_THREADS) > 65535) throw Error(-1, "too many observation points for one launch");
   const int splits = fwd_splits(g, sm_count);
-  const int64_t per = round_up(ceil_div(g.n_cells, splits), FB_CHUNK);
+  const int64_t per = ceil_div(g.plan.n_tiles, splits);
   const int nf = g.n_fields;
   if (nf <= 2) {
     fwd_pass<16>(g, X, splits, per, 0, scratch, s, o.skip);
