@@ -11,7 +11,10 @@
 namespace grada {
 
 constexpr int TL_THREADS = 128;  // points per block
-constexpr int TL_COLS = 8;       // runs per tile
+#ifndef GRADA_TILE_COLS
+#define GRADA_TILE_COLS 8
+#endif
+constexpr int TL_COLS = GRADA_TILE_COLS;  // runs per tile
 constexpr int TL_LCH = 8;        // levels staged per pass
 constexpr int ZC_N = 9;          // doubles of a ZCarry
 constexpr int TL_MAXLEV = 64;    // levels per tile (longer runs continue in the next tile)
