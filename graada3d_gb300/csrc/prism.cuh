@@ -26,8 +26,12 @@
 //    A+r = rho^2/(r-A), rho^2 the squared distance to the edge line);
 //  * the four-term sums of atan per face are the argument of a product of four
 //    complex numbers (Z r + i X Y or its conjugate), so each face costs one
-//    atan2; the 2*pi branch of that argument is picked with a cheap FP32
-//    estimate of the same sum (6 FP64 atan2 per prism instead of 24 atan).
+//    argument evaluation (6 per prism instead of 24 atan), done by the
+//    table rotation below; the 2*pi branch is picked with a cheap FP32
+//    estimate of the same sum;
+//  * faces shared by neighbouring cells (a column in z, and with
+//    prism_terms_tiled also the previous column in y) are taken over from the
+//    neighbour instead of being evaluated again.
 // Every quantity that reaches a result is computed in FP64.
 #pragma once
 
