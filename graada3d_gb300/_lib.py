@@ -72,6 +72,7 @@ SIGNATURES = {
     "grada_lambda_sweep": (c_int, [c_void_p, c_void_p, c_int, _dp, _dp, _dp, _dp, _dp, _dp,
                                    c_void_p]),
     "grada_get_sweep_trials": (c_int, [c_void_p, c_int, _dp, c_int64, _ip64]),
+    "grada_inject_fault": (c_int, [c_void_p, c_int]),
 }
 
 

@@ -35,6 +35,11 @@ void DevBuf::alloc(Context *ctx, size_t nbytes) {
   release();
   owner = ctx;
   if (nbytes == 0) return;
+  if (ctx->inject_alloc_failure) {  // grada_inject_fault(GRADA_FAULT_ALLOC)
+    ctx->inject_alloc_failure = false;
+    throw Error(GRADA_ERR_OUT_OF_MEMORY,
+                "cudaMalloc of " + std::to_string(nbytes) + " bytes: injected failure");
+  }
   cudaError_t e = cudaMalloc(&ptr, nbytes);
   if (e != cudaSuccess) {
     ptr = nullptr;
@@ -178,6 +183,7 @@ void Context::zero_padding_rows(void *base, size_t esz) {
 }
 
 void Context::compute_G(int storage) {
+  NvtxRange nvtx("grada compute_G");
   require_geometry();
   if (storage < GRADA_G_FP64 || storage > GRADA_G_MATRIX_FREE)
     throw Error(GRADA_ERR_INVALID_ARGUMENT, "unknown G storage");
@@ -648,6 +654,25 @@ int grada_get_sweep_trials(const grada_ctx *ctx, int column, double *rows, int64
     o[4] = tr[k].cg_error;
   }
   return GRADA_OK;
+}
+
+int grada_inject_fault(grada_ctx *ctx, int fault) {
+  return guarded(ctx, [&] {
+    if (fault == GRADA_FAULT_ALLOC) {
+      ctx->inject_alloc_failure = true;
+    } else if (fault == GRADA_FAULT_TC_TIMEOUT) {
+      // the flag a tensor-core product raises when one of its bounded waits
+      // expires; the next block product's host check reports it
+      ctx->tc_err.alloc(ctx, sizeof(int) * 4);
+      const int flag = 1;
+      ctx->upload(ctx->tc_err.ptr, &flag, sizeof(int));
+      ctx->sync();
+    } else if (fault != GRADA_FAULT_NONE) {
+      throw grada::Error(GRADA_ERR_INVALID_ARGUMENT, "unknown fault kind");
+    } else {
+      ctx->inject_alloc_failure = false;
+    }
+  });
 }
 
 }  // extern "C"

@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <stdexcept>
 #include <string>
 
@@ -31,6 +33,15 @@ struct Error : public std::runtime_error {
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
+
+// NVTX range around a host-side operation (visible in Nsight timelines; a
+// no-op without a tool attached).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Store helpers used by the G writers.
 __device__ __forceinline__ void store_entry(double *p, double v) { *p = v; }

@@ -73,6 +73,7 @@ struct Context {
   cudaStream_t stream = nullptr;
   std::string last_error;
   int64_t bytes_held = 0;
+  bool inject_alloc_failure = false;  // grada_inject_fault
 
   // Geometry (Fwd::mesh leaf cells, Fwd::ob, Fwd::field_flag) and the
   // prism kernels' math tables.

@@ -242,6 +242,7 @@ double Context::misfit_of(const double *m, const double *m_start, const double *
 CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const double *mk,
                                const double *mref, const double *P, const double *const WL[7],
                                double *dx, const double *d64, const double *m_start) {
+  NvtxRange nvtx("grada solve_cg");
   require_G();
   if (!data_set) throw Error(GRADA_ERR_STATE, "observed data not set (grada_set_data)");
   for (int t = 0; t < 4; t++)
@@ -410,6 +411,7 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
 void Context::invert(const grada_invert_params &prm, const double *h_m_ini, const double *h_mmin,
                      const double *h_mmax, const double *h_m0, double *h_m_out,
                      grada_invert_report &rep) {
+  NvtxRange nvtx("grada invert");
   require_G();
   if (!data_set) throw Error(GRADA_ERR_STATE, "observed data not set (grada_set_data)");
   if (!h_m_ini || !h_mmin || !h_mmax || !h_m_out)

@@ -127,6 +127,7 @@ void Context::solve_cg_block_dev(const double *lambda, uint32_t active, double t
                                  const double *mk, const double *mref, const double *P,
                                  const double *const WL[7], double *dx, const double *d64,
                                  const double *m_start, CgResult *res) {
+  NvtxRange nvtx("grada solve_cg_block");
   require_G();
   if (!data_set) throw Error(GRADA_ERR_STATE, "observed data not set (grada_set_data)");
   for (int t = 0; t < 4; t++)
@@ -374,6 +375,7 @@ void Context::solve_cg_block_host(double tol, int maxit, int n, const double *la
 void Context::lambda_sweep(const grada_invert_params &prm, int n, const double *lambdas,
                            const double *h_m_ini, const double *h_mmin, const double *h_mmax,
                            const double *h_m0, double *h_m_out, grada_invert_report *reps) {
+  NvtxRange nvtx("grada lambda_sweep");
   require_G();
   if (!data_set) throw Error(GRADA_ERR_STATE, "observed data not set (grada_set_data)");
   if (n < 1 || !lambdas || !h_m_ini || !h_mmin || !h_mmax || !h_m_out || !reps)

@@ -326,6 +326,19 @@ int grada_lambda_sweep(grada_ctx *ctx, const grada_invert_params *prm, int n_lam
 int grada_get_sweep_trials(const grada_ctx *ctx, int column, double *rows, int64_t cap,
                            int64_t *n);
 
+/*
+ * Fault injection for tests (no reference counterpart; nothing faults on the
+ * GPU).  GRADA_FAULT_ALLOC: the context's next device allocation fails with
+ * GRADA_ERR_OUT_OF_MEMORY.  GRADA_FAULT_TC_TIMEOUT: raises the flag a
+ * tensor-core block product sets when one of its bounded waits expires, so
+ * the next block product returns GRADA_ERR_CUDA.  GRADA_FAULT_NONE clears a
+ * pending allocation fault.  The context stays usable after either.
+ */
+#define GRADA_FAULT_NONE 0
+#define GRADA_FAULT_ALLOC 1
+#define GRADA_FAULT_TC_TIMEOUT 2
+int grada_inject_fault(grada_ctx *ctx, int fault);
+
 #ifdef __cplusplus
 }
 #endif
