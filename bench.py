@@ -54,6 +54,11 @@ UNIT = "entries/s"
 # profiles/assemble_fp64_9comp.md.  Re-measured whenever the kernel changes.
 FP64_FLOPS_PER_PAIR = 767.4
 
+# DRAM bytes (read + write) of one assembly launch on this workload, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of the full-size
+# launch; see profiles/assemble_fp64_9comp.md.  The algorithmic G write is 96.3 GB.
+ASSEMBLY_DRAM_BYTES_PER_LAUNCH = 4_772_644_608 + 98_347_602_688
+
 
 def build_problem():
     from graada3d_gb300 import mesh
@@ -274,7 +279,10 @@ def run_gpu(args):
     if FP64_FLOPS_PER_PAIR:
         achieved = FP64_FLOPS_PER_PAIR * pairs / per_launch
         roofline = {"bound": "fp64", "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
-                    "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                    "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                    "traffic": ASSEMBLY_DRAM_BYTES_PER_LAUNCH,
+                    "traffic_unit": "bytes per launch (ncu, full-size launch)",
+                    "algorithmic_flops_per_pair": FP64_FLOPS_PER_PAIR,
                     "peak_source": "DFMA loop measured in this run (grada_measure_fp64_peak)"}
     else:
         roofline = {"bound": "fp64", "achieved": None, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
@@ -315,6 +323,8 @@ def run_gpu(args):
             "hbm_write": hbm,
             "clocks": clk,
         }
+        if world == 1 and not args.no_block:
+            line["block_products"] = block_products_summary()
         if world == 1 and not args.no_inversion:
             # second half of the metric: inversion time to chi^2 = N, mixed precision vs
             # all-FP64 (configs[0] sizes; the 196,608-cell configs[2] run is --case inversion-cfg3)
@@ -682,6 +692,50 @@ def run_block_gemm_profile():
     print(json.dumps({"case": "block-gemm-profile", "rows": f.Nd, "cols": f.Nm}))
 
 
+def block_products_summary():
+    """Tensor-core block products (16 right-hand sides) on the gz + Tzz rows of the
+    bench geometry (20,402 x 131,072), FP32 (3xTF32) and bf16 G: ms per product
+    (3 warm-up + 10 timed, CUDA events) and the fraction of the measured HBM copy
+    peak the algorithmic bytes (Nd x Nm x bytes/entry) reach."""
+    import ctypes
+
+    import torch
+
+    from graada3d_gb300 import Fwd
+
+    prisms, obs, _ = build_problem()
+    f = Fwd(prisms, obs, 0x012)
+    lib, h = f.ctx.lib, f.ctx.handle
+    stream = torch.cuda.ExternalStream(f.ctx.stream)
+    dev = torch.device("cuda")
+    X = torch.randn(f.Nm * 16, dtype=torch.float64, device=dev)
+    Y = torch.randn(f.ld * 16, dtype=torch.float64, device=dev)
+    oX = torch.empty(f.Nm * 16, dtype=torch.float64, device=dev)
+    oY = torch.empty(f.ld * 16, dtype=torch.float64, device=dev)
+    peak = _peak_gbs()
+    out = {"rows": f.Nd, "cols": f.Nm, "rhs": 16}
+    for st, bpe in (("fp32", 4), ("bf16", 2)):
+        f.compute_G(st)
+        for name, fn, a, b in (("G_X", lib.grada_G_block_mul_dev, X, oY),
+                               ("GT_Y", lib.grada_GT_block_mul_dev, Y, oX)):
+            for _ in range(3):
+                f.ctx.check(fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr())))
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(10):
+                fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / 10
+            r = {"ms": round(ms, 4), "GBps": round(f.Nd * f.Nm * bpe / ms / 1e6, 1)}
+            if peak:
+                r["frac_of_hbm"] = round(r["GBps"] / peak, 3)
+            out[f"{st}_{name}"] = r
+    f.ctx.close()
+    return out
+
+
 def run_sweep_cfg4(n_lambda: int = 16, gn_iter: int = 5, storages=("fp64", "fp32", "bf16"),
                    sequential: bool = True):
     """BASELINE configs[3] part 1: a 16-value regularisation sweep (lambda
@@ -794,6 +848,7 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-inversion", action="store_true")
+    ap.add_argument("--no-block", action="store_true")
     ap.add_argument("--sweep-storages", default="fp64,fp32,bf16")
     ap.add_argument("--no-sequential", action="store_true")
     args = ap.parse_args()

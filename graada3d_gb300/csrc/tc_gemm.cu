@@ -97,11 +97,37 @@ struct EltCfg {
   // read by the MMAs together with the right-hand-side tile of the TMA stage
   static constexpr int CSLOT_BYTES = 2 * A_BYTES;
   static constexpr int CSLOTS = split_a ? 3 : 0;
-  static constexpr int NCONV_WARPS = split_a ? 8 : 0;
+#ifndef GRADA_TC_CONV_WARPS
+#define GRADA_TC_CONV_WARPS 8
+#endif
+  static constexpr int NCONV_WARPS = split_a ? GRADA_TC_CONV_WARPS : 0;
   static constexpr int THREADS = 64 + 32 * NCONV_WARPS + 128;
   static constexpr int W_EPI0 = 2 + NCONV_WARPS;  // first epilogue warp
   static constexpr int SMEM = STAGES * STAGE_BYTES + CSLOTS * CSLOT_BYTES + 1024;
   static constexpr int ATOM_M = SWB / bytes;     // MN-major atom: rows of G per 128 B
+};
+
+// Ring sizes per product.  TF32 G^T Y keeps only the small part in a
+// converted slot (the staged tile is the big part), so its slots are half the
+// size and the TMA ring gets the room; TF32 G X keeps both parts.
+#ifndef GRADA_TC_GX_STAGES
+#define GRADA_TC_GX_STAGES 6
+#endif
+#ifndef GRADA_TC_GX_SLOTS
+#define GRADA_TC_GX_SLOTS 3
+#endif
+#ifndef GRADA_TC_GTY_STAGES
+#define GRADA_TC_GTY_STAGES 8
+#endif
+template <int MODE, int ELT>
+struct Cfg : EltCfg<ELT> {
+  using E = EltCfg<ELT>;
+  static constexpr int STAGES =
+      !E::split_a ? E::STAGES : (MODE == 0 ? GRADA_TC_GX_STAGES : GRADA_TC_GTY_STAGES);
+  static constexpr int CSLOT_BYTES = (MODE == 0 ? 2 : 1) * A_BYTES;
+  static constexpr int CSLOTS = !E::split_a ? 0 : (MODE == 0 ? GRADA_TC_GX_SLOTS : 3);
+  static constexpr int SMEM = STAGES * E::STAGE_BYTES + CSLOTS * CSLOT_BYTES + 1024;
+  static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
 struct TcParams {
@@ -266,7 +292,7 @@ template <int MODE, int ELT>
 __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const TcParams p) {
-  using C = EltCfg<ELT>;
+  using C = Cfg<MODE, ELT>;
   if (p.skip && *p.skip) return;
   extern __shared__ uint8_t smem_raw[];
   constexpr int NCS = C::CSLOTS > 0 ? C::CSLOTS : 1;
@@ -282,7 +308,8 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
   auto stage_b = [&](int s) { return stage_a(s) + A_BYTES; };
   const uint32_t cbase = base + (uint32_t)C::STAGES * C::STAGE_BYTES;
   auto cslot_big = [&](int c) { return cbase + (uint32_t)c * C::CSLOT_BYTES; };
-  auto cslot_small = [&](int c) { return cslot_big(c) + A_BYTES; };
+  // G X slots: [big][small]; G^T Y slots: [small]
+  auto cslot_small = [&](int c) { return cslot_big(c) + (MODE == MODE_GX ? A_BYTES : 0); };
   uint8_t *base_ptr = smem_raw + (base - smem_u32(smem_raw));
 
   if (threadIdx.x == 0) {
@@ -431,7 +458,7 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
             mma<ELT>(dt, sdesc(a_big + st * a_step, a_lbo, a_sbo), bd, id, accum);
             accum = 1;
             if constexpr (C::split_a)
-              mma<ELT>(dt, sdesc(a_s + A_BYTES + st * a_step, a_lbo, a_sbo), bd, id, 1);
+              mma<ELT>(dt, sdesc(cslot_small(c) + st * a_step, a_lbo, a_sbo), bd, id, 1);
           }
           mma_commit(smem_u32(&bar_empty[s]));  // stage free once these MMAs are done
           if constexpr (C::split_a) mma_commit(smem_u32(&bar_cempty[c]));
@@ -776,7 +803,7 @@ CUtensorMap make_map(const void *ptr, int elt, uint64_t dim0, uint64_t dim1, uin
 template <int MODE, int ELT>
 void launch_kernel(const CUtensorMap &a, const CUtensorMap &b, const TcParams &p, int grid,
                    cudaStream_t s) {
-  using C = EltCfg<ELT>;
+  using C = Cfg<MODE, ELT>;
   static std::mutex mu;
   static bool attr_set[64] = {};
   int dev = 0;
