@@ -237,13 +237,63 @@ def ref_fields() -> None:
     np.savez_compressed(HERE / "ref_fields.npz", **out)
 
 
+def ref_expand() -> None:
+    """ref_expand.npz: the reference's own refinement path on a 6 x 5 x 4 regular mesh
+    (Fwd::compute_G, Mesh::refinement of six cells, Mesh::rearrange_id,
+    AdaptiveInversion::expand_G, run by oracle/_ref/ref_expand): the expanded G
+    (nine components at 6 x 4 points), the refined leaf list and each split
+    parent's children in Cell::child_cells order."""
+    from graada3d_gb300 import mesh as gm
+
+    exe = REF_BIN / "ref_expand"
+    nx, ny, nz = 6, 5, 4
+    xl, yl, zl = (0.0, 600.0), (0.0, 500.0), (0.0, 400.0)
+    obs = gm.observation_grid(6, -50.0, 650.0, 4, -50.0, 550.0, -5.0)
+    mask = 0x3FE
+    parents = np.array([0, 3, 17, 18, 50, 119], dtype=np.int64)
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
+        with open(fin, "wb") as fh:
+            np.array([nx, ny, nz], dtype=np.int64).tofile(fh)
+            np.array([*xl, *yl, *zl], dtype=np.float64).tofile(fh)
+            np.array([obs.shape[0]], dtype=np.int64).tofile(fh)
+            obs.astype(np.float64).tofile(fh)
+            np.array([mask], dtype=np.uint32).tofile(fh)
+            np.array([parents.size], dtype=np.int64).tofile(fh)
+            parents.tofile(fh)
+        subprocess.run([str(exe), str(fin), str(fout)], check=True, cwd=td)
+        raw = np.fromfile(fout, dtype=np.uint8)
+    off = 0
+
+    def take(n, dt):
+        nonlocal off
+        a = raw[off:off + n * np.dtype(dt).itemsize].view(dt)
+        off += n * np.dtype(dt).itemsize
+        return a
+
+    rows, cols = take(2, np.int64)
+    G = take(rows * cols, np.float64).reshape(cols, rows).T
+    n_leaf = int(take(1, np.int64)[0])
+    leaf = take(6 * n_leaf, np.float64).reshape(n_leaf, 6)
+    n_split = int(take(1, np.int64)[0])
+    idx, kids = [], []
+    for _ in range(n_split):
+        idx.append(int(take(1, np.int64)[0]))
+        kids.append(take(48, np.float64).reshape(8, 6))
+    prisms = gm.regular_mesh(xl, nx, yl, ny, zl, nz)
+    np.savez_compressed(HERE / "ref_expand.npz", prisms=prisms, obs=obs, mask=np.int64(mask),
+                        parents=parents, G=G, leaf=leaf, split_index=np.array(idx),
+                        children=np.array(kids))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
     ref = Path(a.ref)
-    jobs = {"forward_models": lambda: forward_models(ref), "ref_fields": ref_fields}
+    jobs = {"forward_models": lambda: forward_models(ref), "ref_fields": ref_fields,
+            "ref_expand": ref_expand}
     try:
         from inversion_cases import inversion_fixtures  # noqa: E402
         jobs["ref_inversion"] = inversion_fixtures

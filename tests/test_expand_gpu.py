@@ -61,3 +61,39 @@ def test_expand_G_rejects_bad_input(gpu_ctx):
     f.compute_G("bf16")
     with pytest.raises(GradaError):
         f.expand_G([1])
+
+
+# ---- pinned to the reference's own refinement path --------------------------
+# tests/golden/ref_expand.npz: Mesh::refinement of six cells of a 6 x 5 x 4 mesh,
+# Mesh::rearrange_id and AdaptiveInversion::expand_G run by the compiled
+# reference (oracle/refdrv/ref_expand.cpp).
+
+def _ref_expand(golden):
+    return golden("ref_expand.npz")
+
+
+def test_children_and_leaf_order_match_reference(golden):
+    r = _ref_expand(golden)
+    np.testing.assert_array_equal(r["split_index"], r["parents"])
+    np.testing.assert_array_equal(split_cells(r["prisms"][r["parents"]]), r["children"])
+    refined = []
+    pk = {int(p): k for k, p in enumerate(r["parents"])}
+    for j in range(r["prisms"].shape[0]):
+        refined.extend(r["children"][pk[j]] if j in pk else [r["prisms"][j]])
+    np.testing.assert_array_equal(np.array(refined), r["leaf"])
+
+
+@pytest.mark.gpu
+def test_expand_G_matches_reference_expand_G(gpu_ctx, golden):
+    r = _ref_expand(golden)
+    f = Fwd(r["prisms"], r["obs"], int(r["mask"]), ctx=gpu_ctx)
+    f.compute_G("fp64")
+    f.expand_G(r["parents"], r["children"])
+    np.testing.assert_array_equal(f.prisms, r["leaf"])
+    G = f.get_G()[: f.Nd]
+    ref = r["G"]
+    assert G.shape == ref.shape
+    n = r["obs"].shape[0]
+    for k in range(ref.shape[0] // n):  # per component, relative to its largest entry
+        blk = slice(k * n, (k + 1) * n)
+        assert np.abs(G[blk] - ref[blk]).max() <= 1e-10 * np.abs(ref[blk]).max(), k
