@@ -286,6 +286,44 @@ def ref_expand() -> None:
                         children=np.array(kids))
 
 
+def ref_padded() -> None:
+    """ref_padded.npz: the reference's padded mesh (Mesh::generate_regular_mesh_with_padding:
+    6 x 5 x 4 cells of interest over [0, 3 km]^2 x [0, 1.5 km] with 4 padding cells on each
+    x/y side and 3 below, stretch 1.8) and its Fwd::compute_G for nine components at 5 x 4
+    points, run by oracle/_ref/ref_padded.  Stored compactly: the leaf cells, a seeded
+    density model with the reference's G rho, and twelve whole columns of G (cells of
+    interest and the largest, farthest padding cells)."""
+    exe = REF_BIN / "ref_padded"
+    from graada3d_gb300 import mesh as gm
+
+    obs = gm.observation_grid(5, -500.0, 3500.0, 4, -500.0, 3500.0, -10.0)
+    mask = 0x3FE
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
+        with open(fin, "wb") as fh:
+            np.array([6, 5, 4], dtype=np.int64).tofile(fh)
+            np.array([0.0, 3000.0, 0.0, 3000.0, 0.0, 1500.0], dtype=np.float64).tofile(fh)
+            np.array([4, 4, 3], dtype=np.int64).tofile(fh)
+            np.array([1.8, 1.8, 1.8], dtype=np.float64).tofile(fh)
+            np.array([obs.shape[0]], dtype=np.int64).tofile(fh)
+            obs.astype(np.float64).tofile(fh)
+            np.array([mask], dtype=np.uint32).tofile(fh)
+        subprocess.run([str(exe), str(fin), str(fout)], check=True, cwd=td)
+        raw = np.fromfile(fout, dtype=np.uint8)
+    n_leaf = int(raw[:8].view(np.int64)[0])
+    leaf = raw[8:8 + 48 * n_leaf].view(np.float64).reshape(n_leaf, 6)
+    off = 8 + 48 * n_leaf
+    rows, cols = raw[off:off + 16].view(np.int64)
+    G = raw[off + 16:off + 16 + 8 * rows * cols].view(np.float64).reshape(cols, rows).T
+    rng = np.random.default_rng(31)
+    rho = rng.uniform(-300.0, 300.0, n_leaf)
+    vol = (leaf[:, 1] - leaf[:, 0]) * (leaf[:, 3] - leaf[:, 2]) * (leaf[:, 5] - leaf[:, 4])
+    cols_pick = np.unique(np.concatenate([np.argsort(vol)[-6:], np.argsort(vol)[:3],
+                                          [0, n_leaf // 2, n_leaf - 1]]))
+    np.savez_compressed(HERE / "ref_padded.npz", leaf=leaf, obs=obs, mask=np.int64(mask),
+                        rho=rho, d=G @ rho, cols=cols_pick, G_cols=G[:, cols_pick])
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -293,7 +331,7 @@ def main() -> None:
     a = ap.parse_args()
     ref = Path(a.ref)
     jobs = {"forward_models": lambda: forward_models(ref), "ref_fields": ref_fields,
-            "ref_expand": ref_expand}
+            "ref_expand": ref_expand, "ref_padded": ref_padded}
     try:
         from inversion_cases import inversion_fixtures  # noqa: E402
         jobs["ref_inversion"] = inversion_fixtures
