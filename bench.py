@@ -327,8 +327,8 @@ def run_gpu(args):
             line["block_products"] = block_products_summary()
         if world == 1 and not args.no_inversion:
             # second half of the metric: inversion time to chi^2 = N, mixed precision vs
-            # all-FP64 (configs[0] sizes; the 196,608-cell configs[2] run is --case inversion-cfg3)
-            line["inversion"] = run_inversion("cfg1")
+            # all-FP64 (16,384 cells; the 196,608-cell L1 run is --case inversion-l1-196k)
+            line["inversion"] = run_inversion("l2_16k")
         if world == 1 and not args.no_cpu_baseline:
             cb = cpu_sample(prisms, obs, target_s=args.ref_seconds)
             cb.pop("seconds", None)
@@ -338,14 +338,14 @@ def run_gpu(args):
 
 
 INVERSION_CASES = {
-    # BASELINE configs[0]: 32 x 32 x 16 cells over [0,10 km]^2 x [0,5 km], gz + Tzz at
+    # 32 x 32 x 16 cells over [0,10 km]^2 x [0,5 km], gz + Tzz at
     # 41 x 41 points 100 m above, L2, lambda0 = 0.1, 30 lambdas, rate 0.6, CG max 50
-    "cfg1": dict(cells=(32, 32, 16), domain=(10000.0, 10000.0, 5000.0), obs=(41, 41), height=100.0,
-                 mask=0x012, lp=[2, 2, 2, 2, 2], eps2=1e-9, boxes="cfg1", gn_iter=10),
-    # BASELINE configs[2] on a uniform stand-in mesh of 196,608 cells (64 x 64 x 48 over the
+    "l2_16k": dict(cells=(32, 32, 16), domain=(10000.0, 10000.0, 5000.0), obs=(41, 41), height=100.0,
+                 mask=0x012, lp=[2, 2, 2, 2, 2], eps2=1e-9, boxes="two_boxes", gn_iter=10),
+    # L1 IRLS on a uniform stand-in for a ~200k-leaf refined mesh: 196,608 cells (64 x 64 x 48 over the
     # same domain; the reference refines to ~200k leaves on the host): gz, Tzz, Txz, Tyz at
     # 101 x 101 points 100 m above, two dykes of +400 kg/m^3, L1 IRLS
-    "cfg3": dict(cells=(64, 64, 48), domain=(10000.0, 10000.0, 5000.0), obs=(101, 101),
+    "l1_196k": dict(cells=(64, 64, 48), domain=(10000.0, 10000.0, 5000.0), obs=(101, 101),
                  height=100.0, mask=0x072, lp=[1, 1, 1, 1, 2], eps2=1e-10, boxes="dykes",
                  gn_iter=10),
 }
@@ -360,8 +360,8 @@ def inversion_problem(name: str):
     Lx, Ly, Lz = c["domain"]
     prisms = mesh.regular_mesh((0.0, Lx), nx, (0.0, Ly), ny, (0.0, Lz), nz)
     obs = mesh.observation_grid(c["obs"][0], 0.0, Lx, c["obs"][1], 0.0, Ly, -c["height"])
-    rng = np.random.default_rng(1 if c["boxes"] == "cfg1" else 4)
-    if c["boxes"] == "cfg1":
+    rng = np.random.default_rng(1 if c["boxes"] == "two_boxes" else 4)
+    if c["boxes"] == "two_boxes":
         boxes = []
         for v in (300.0, -200.0):
             sx, sy, sz = rng.uniform(1000, 3000, 3)
@@ -390,7 +390,7 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16")):
     inv = GaussNewtonInversion(prisms, obs, c["mask"])
     inv.compute_G("fp64")
     d = inv.G_vec_mul(rho)
-    dobs = d + 0.02 * np.abs(d) * np.random.default_rng(2 if name == "cfg1" else 5).standard_normal(d.size)
+    dobs = d + 0.02 * np.abs(d) * np.random.default_rng(2 if name == "l2_16k" else 5).standard_normal(d.size)
     wd = reg.data_weights(dobs, rel, absf, obs.shape[0])
     inv.set_cross_gradient(False)
     inv.set_operators(ops)
@@ -429,8 +429,8 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16")):
     return out
 
 
-def run_matrix_free_cfg5():
-    """One matrix-free G x and G^T y at BASELINE configs[4] size: 128 x 128 x 64 =
+def run_matrix_free_1m():
+    """One matrix-free G x and G^T y with 128 x 128 x 64 =
     1,048,576 cells over [0, 20 km]^2 x [0, 8 km], gz + Tzz at 201 x 201 points
     50 m above (G would be 80,802 x 1,048,576 = 678 GB in FP64, beyond HBM)."""
     import torch
@@ -451,7 +451,7 @@ def run_matrix_free_cfg5():
     dout = torch.empty(inv.ld, dtype=torch.float64, device=dev)
     xout = torch.empty(inv.Nm, dtype=torch.float64, device=dev)
     stream = torch.cuda.ExternalStream(inv.ctx.stream)
-    out = {"case": "matrix-free-cfg5", "cells": inv.Nm, "points": inv.N_obs, "rows": inv.Nd,
+    out = {"case": "matrix-free-1m", "cells": inv.Nm, "points": inv.N_obs, "rows": inv.Nd,
            "pairs_per_product": inv.N_obs * inv.Nm}
     for name, fn, a, b in (("G_x", lib.grada_G_vec_mul_dev, x, dout),
                            ("GT_y", lib.grada_GT_vec_mul_dev, y, xout)):
@@ -471,7 +471,7 @@ def run_matrix_free_cfg5():
 
 
 def run_gemv_case():
-    """G x and G^T y alone at the 40,804 x 196,608 (configs[2]-sized) G, every
+    """G x and G^T y alone with a 40,804 x 196,608 G (4 components at 101 x 101 points over 196,608 cells), every
     storage kind: 3 warm-up + 10 timed calls each, CUDA events on the context
     stream; G (16-64 GB) is far larger than L2."""
     import ctypes
@@ -516,8 +516,8 @@ def run_gemv_case():
     return res
 
 
-def run_batched_cfg4(n_problems: int = 64):
-    """BASELINE configs[3] part 2: independent inversions of uneven size (uniform
+def run_batched_64(n_problems: int = 64):
+    """Independent inversions of uneven size (uniform
     meshes nx = ny, nz = nx/2 with 4k-60k cells, square point grids of 400-5,000
     points, gz + Tzz, seeded models, seeds 100..163), run one after the other and
     then as one concurrent batch (one context, host thread and stream each).
@@ -581,7 +581,7 @@ def run_batched_cfg4(n_problems: int = 64):
     for inv in invs:
         inv.ctx.close()
     t_seq, t_bat = max_over_ranks(world, t_seq), max_over_ranks(world, t_bat)
-    return {"case": "batched-cfg4", "problems": n_problems, "ranks": world,
+    return {"case": "batched-64", "problems": n_problems, "ranks": world,
             "problems_per_rank": len(mine),
             "cells_range": [min(s[0] for s in sizes), max(s[0] for s in sizes)],
             "points_range": [min(s[1] for s in sizes), max(s[1] for s in sizes)],
@@ -591,7 +591,7 @@ def run_batched_cfg4(n_problems: int = 64):
 
 
 def sweep_problem():
-    """BASELINE configs[3] part 1 geometry: configs[1]'s mesh (64 x 64 x 32 =
+    """The 64 x 64 x 32 mesh of the assembly benchmark (64 x 64 x 32 =
     131,072 cells over [0, 20 km]^2 x [0, 8 km]) and points (101 x 101 at 50 m),
     the gz + Tzz rows of its G (20,402 x 131,072), its 20-box model, data with 2 %
     seeded noise."""
@@ -609,7 +609,7 @@ def _peak_gbs():
 
 def run_block_gemm_case():
     """The 16-column block products G X and G^T Y against sixteen single products,
-    on the 20,402 x 131,072 gz + Tzz G of configs[1]'s geometry, each storage:
+    on the 20,402 x 131,072 gz + Tzz G of the assembly benchmark's geometry, each storage:
     3 warm-up + 10 timed calls, CUDA events on the context stream.  G (5-21 GB)
     is far larger than L2."""
     import ctypes
@@ -736,10 +736,10 @@ def block_products_summary():
     return out
 
 
-def run_sweep_cfg4(n_lambda: int = 16, gn_iter: int = 5, storages=("fp64", "fp32", "bf16"),
+def run_lambda_sweep_16(n_lambda: int = 16, gn_iter: int = 5, storages=("fp64", "fp32", "bf16"),
                    sequential: bool = True):
-    """BASELINE configs[3] part 1: a 16-value regularisation sweep (lambda
-    log-spaced 1e-3 .. 1e1) on the shared gz + Tzz G of configs[1]'s geometry,
+    """A 16-value regularisation sweep (lambda
+    log-spaced 1e-3 .. 1e1) on the shared gz + Tzz G of the assembly benchmark's geometry,
     each lambda a fixed-lambda Gauss-Newton run (L2, CG <= 50, up to gn_iter
     iterations), run as one block (block CG, tensor-core products) and, for
     comparison, as 16 separate inversions."""
@@ -762,7 +762,7 @@ def run_sweep_cfg4(n_lambda: int = 16, gn_iter: int = 5, storages=("fp64", "fp32
     prm = dict(max_lambda=1e-1, n_lambda=1, rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6,
                cg_factor=50, gn_iter=gn_iter, lp=[2, 2, 2, 2, 2], eps2=1e-9)
     args = (np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0))
-    out = {"case": "sweep-cfg4", "cells": nm, "data": inv.Nd, "lambdas": n_lambda,
+    out = {"case": "lambda-sweep-16", "cells": nm, "data": inv.Nd, "lambdas": n_lambda,
            "gn_iter_max": gn_iter}
     models = {}
     for st in storages:
@@ -836,10 +836,10 @@ def run_profile_case(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-cfg1",
-                                                         "inversion-cfg3", "matrix-free-cfg5",
-                                                         "gemv", "batched-cfg4", "block-gemm",
-                                                         "sweep-cfg4", "block-gemm-profile",
+    ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-l2-16k",
+                                                         "inversion-l1-196k", "matrix-free-1m",
+                                                         "gemv", "batched-64", "block-gemm",
+                                                         "lambda-sweep-16", "block-gemm-profile",
                                                          "mf-profile"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -860,19 +860,19 @@ def main():
         run_mf_profile()
     elif args.case == "block-gemm-profile":
         run_block_gemm_profile()
-    elif args.case == "sweep-cfg4":
-        print(json.dumps(run_sweep_cfg4(storages=tuple(args.sweep_storages.split(",")),
+    elif args.case == "lambda-sweep-16":
+        print(json.dumps(run_lambda_sweep_16(storages=tuple(args.sweep_storages.split(",")),
                                         sequential=not args.no_sequential)))
-    elif args.case == "batched-cfg4":
-        res = run_batched_cfg4()
+    elif args.case == "batched-64":
+        res = run_batched_64()
         if int(os.environ.get("RANK", "0")) == 0:
             print(json.dumps(res))
     elif args.case == "gemv":
         print(json.dumps(run_gemv_case()))
-    elif args.case == "matrix-free-cfg5":
-        print(json.dumps(run_matrix_free_cfg5()))
+    elif args.case == "matrix-free-1m":
+        print(json.dumps(run_matrix_free_1m()))
     elif args.case.startswith("inversion-"):
-        print(json.dumps(run_inversion(args.case.split("-", 1)[1])))
+        print(json.dumps(run_inversion(args.case.split("-", 1)[1].replace("-", "_"))))
     elif args.impl == "reference":
         run_reference(args)
     else:
