@@ -656,6 +656,11 @@ int grada_get_sweep_trials(const grada_ctx *ctx, int column, double *rows, int64
   return GRADA_OK;
 }
 
+int grada_refinement_indicator(grada_ctx *ctx, const double *m, const int64_t *rowptr,
+                               const int64_t *neighbour, const double *area, double *indicator) {
+  return guarded(ctx, [&] { ctx->refinement_indicator(m, rowptr, neighbour, area, indicator); });
+}
+
 int grada_inject_fault(grada_ctx *ctx, int fault) {
   return guarded(ctx, [&] {
     if (fault == GRADA_FAULT_ALLOC) {

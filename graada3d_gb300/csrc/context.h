@@ -172,6 +172,8 @@ struct Context {
   void apply_GT(const double *y, double *x, const GemvOpts &o);
   void forward_field_dev(const double *d_rho, double *d_fields);
   void expand_G(int64_t n_split, const int64_t *parent, const double *children);  // expand.cu
+  void refinement_indicator(const double *m, const int64_t *rowptr, const int64_t *nb,
+                            const double *area, double *out);  // refine.cu
 
   // sweep.cu: block products (kBW columns) for every storage, the block CG
   // solve and the fixed-lambda sweep.

@@ -149,6 +149,21 @@ class GaussNewtonInversion(Fwd):
                                                            _ptr(out), n.value, ctypes.byref(n)))
         return out
 
+    def indicator_calculator(self, m, rowptr, neighbour, area) -> np.ndarray:
+        """AdaptiveInversion::indicator_calculator on the device: per cell the sum
+        of (m[neighbour] - m[cell])^2 * area over its (neighbour, area) list (CSR,
+        in the reference's face order)."""
+        mv = np.ascontiguousarray(m, dtype=np.float64)
+        rp = np.ascontiguousarray(rowptr, dtype=np.int64)
+        nb = np.ascontiguousarray(neighbour, dtype=np.int64)
+        ar = np.ascontiguousarray(area, dtype=np.float64)
+        out = np.empty(self.Nm)
+        p64 = ctypes.POINTER(ctypes.c_int64)
+        self.ctx.check(self.ctx.lib.grada_refinement_indicator(
+            self.ctx.handle, _ptr(mv), rp.ctypes.data_as(p64), nb.ctypes.data_as(p64), _ptr(ar),
+            _ptr(out)))
+        return out
+
     def trials(self) -> np.ndarray:
         """(n, 5): gn_iteration, lambda, misfit, cg_iterations, cg_error."""
         n = ctypes.c_int64()

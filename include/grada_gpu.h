@@ -327,6 +327,19 @@ int grada_get_sweep_trials(const grada_ctx *ctx, int column, double *rows, int64
                            int64_t *n);
 
 /*
+ * Replaces AdaptiveInversion::indicator_calculator (AdaptiveInversion.cpp:
+ * 108-204): indicator[i] = sum over k in [rowptr[i], rowptr[i+1]) of
+ * (m[neighbour[k]] - m[i])^2 * area[k], in that order and with the
+ * reference's rounding (bitwise equal).  The host builds each leaf cell's
+ * (neighbour, area) list from its mesh faces in the reference's order: for
+ * side j = 0, 1 the x, y, z faces; a leaf face with cells on both sides gives
+ * the cell across it and the cell's own face area, a split face its four
+ * child faces' cells and their face areas.  m, indicator: Nm; rowptr: Nm + 1.
+ */
+int grada_refinement_indicator(grada_ctx *ctx, const double *m, const int64_t *rowptr,
+                               const int64_t *neighbour, const double *area, double *indicator);
+
+/*
  * Fault injection for tests (no reference counterpart; nothing faults on the
  * GPU).  GRADA_FAULT_ALLOC: the context's next device allocation fails with
  * GRADA_ERR_OUT_OF_MEMORY.  GRADA_FAULT_TC_TIMEOUT: raises the flag a

@@ -324,6 +324,43 @@ def ref_padded() -> None:
                         rho=rho, d=G @ rho, cols=cols_pick, G_cols=G[:, cols_pick])
 
 
+def ref_indicator() -> None:
+    """ref_indicator.npz: the reference's refinement indicator
+    (AdaptiveInversion::indicator_calculator) on a 6 x 5 x 4 mesh refined at six cells,
+    for a seeded model, with the (neighbour, face area) list of every cell in the
+    order the reference adds them (oracle/_ref/ref_indicator)."""
+    exe = REF_BIN / "ref_indicator"
+    parents = np.array([0, 3, 17, 18, 50, 119], dtype=np.int64)
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
+        with open(fin, "wb") as fh:
+            np.array([6, 5, 4], dtype=np.int64).tofile(fh)
+            np.array([0.0, 600.0, 0.0, 500.0, 0.0, 400.0], dtype=np.float64).tofile(fh)
+            np.array([parents.size], dtype=np.int64).tofile(fh)
+            parents.tofile(fh)
+            np.array([12345], dtype=np.uint64).tofile(fh)
+        subprocess.run([str(exe), str(fin), str(fout)], check=True, cwd=td)
+        raw = np.fromfile(fout, dtype=np.uint8)
+    off = 0
+
+    def take(cnt, dt):
+        nonlocal off
+        a = raw[off:off + cnt * np.dtype(dt).itemsize].view(dt)
+        off += cnt * np.dtype(dt).itemsize
+        return a
+
+    n = int(take(1, np.int64)[0])
+    leaf = take(6 * n, np.float64).reshape(n, 6)
+    m = take(n, np.float64)
+    ind = take(n, np.float64)
+    nnz = int(take(1, np.int64)[0])
+    rowptr = take(n + 1, np.int64)
+    nb = take(nnz, np.int64)
+    area = take(nnz, np.float64)
+    np.savez_compressed(HERE / "ref_indicator.npz", leaf=leaf, m=m, indicator=ind,
+                        rowptr=rowptr, neighbour=nb, area=area)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -331,7 +368,8 @@ def main() -> None:
     a = ap.parse_args()
     ref = Path(a.ref)
     jobs = {"forward_models": lambda: forward_models(ref), "ref_fields": ref_fields,
-            "ref_expand": ref_expand, "ref_padded": ref_padded}
+            "ref_expand": ref_expand, "ref_padded": ref_padded,
+            "ref_indicator": ref_indicator}
     try:
         from inversion_cases import inversion_fixtures  # noqa: E402
         jobs["ref_inversion"] = inversion_fixtures
