@@ -812,6 +812,69 @@ def run_mf_profile():
     f.ctx.close()
 
 
+def refined_dyke_mesh(levels: int = 3):
+    """32 x 32 x 16 cells over [0, 10 km]^2 x [0, 5 km], refined `levels` times at the
+    cells that cross the boundary of two +400 kg/m^3 dykes (split at the centre,
+    children x outer, y, z inner, in place of the parent: the leaf order of
+    Mesh::refinement + rearrange_id).  Three levels give 190,012 leaves."""
+    from graada3d_gb300 import mesh
+    from graada3d_gb300.fwd import split_cells
+
+    cells = mesh.regular_mesh((0.0, 10000.0), 32, (0.0, 10000.0), 32, (0.0, 5000.0), 16)
+    dykes = [[2500, 3500, 1000, 9000, 500, 3500], [6000, 7000, 1000, 9000, 500, 3500]]
+    for _ in range(levels):
+        mark = np.zeros(len(cells), bool)
+        for b in dykes:
+            inter = ((cells[:, 0] < b[1]) & (cells[:, 1] > b[0]) & (cells[:, 2] < b[3]) &
+                     (cells[:, 3] > b[2]) & (cells[:, 4] < b[5]) & (cells[:, 5] > b[4]))
+            inside = ((cells[:, 0] >= b[0]) & (cells[:, 1] <= b[1]) & (cells[:, 2] >= b[2]) &
+                      (cells[:, 3] <= b[3]) & (cells[:, 4] >= b[4]) & (cells[:, 5] <= b[5]))
+            mark |= inter & ~inside
+        idx = np.nonzero(mark)[0]
+        kids = split_cells(cells[idx])
+        parts, prev = [], 0
+        for k, j in enumerate(idx):
+            parts.append(cells[prev:j])
+            parts.append(kids[k].reshape(8, 6))
+            prev = j + 1
+        parts.append(cells[prev:])
+        cells = np.vstack(parts)
+    return cells
+
+
+def run_assembly_refined():
+    """FP64 assembly of gz, Tzz, Txz, Tyz at 101 x 101 points 100 m above
+    [0, 10 km]^2 on the adaptively refined 190,012-leaf dyke mesh and on the
+    uniform 196,608-cell (64 x 64 x 48) mesh over the same domain: 3 warm-up and
+    5 timed assemblies each (CUDA events).  On the refined mesh fewer cells
+    share faces with a neighbour run in the assembly tiles."""
+    import torch
+
+    from graada3d_gb300 import Fwd, mesh
+
+    obs = mesh.observation_grid(101, 0.0, 10000.0, 101, 0.0, 10000.0, -100.0)
+    out = {"case": "assembly-refined", "points": obs.shape[0], "components": 4}
+    for name, cells in (("refined", refined_dyke_mesh()),
+                        ("uniform", mesh.regular_mesh((0.0, 10000.0), 64, (0.0, 10000.0), 64,
+                                                      (0.0, 5000.0), 48))):
+        f = Fwd(cells, obs, 0x072)
+        stream = torch.cuda.ExternalStream(f.ctx.stream)
+        for _ in range(3):
+            f.compute_G("fp64")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            f.compute_G("fp64")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        s = e0.elapsed_time(e1) / 5 * 1e-3
+        out[name] = {"cells": f.Nm, "s": s, "G_entries_per_s": f.Nd * f.Nm / s,
+                     "pairs_per_s": f.N_obs * f.Nm / s}
+        f.ctx.close()
+    return out
+
+
 def run_profile_case(args):
     """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
     50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
@@ -840,7 +903,7 @@ def main():
                                                          "inversion-l1-196k", "matrix-free-1m",
                                                          "gemv", "batched-64", "block-gemm",
                                                          "lambda-sweep-16", "block-gemm-profile",
-                                                         "mf-profile"])
+                                                         "mf-profile", "assembly-refined"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -856,6 +919,8 @@ def main():
         run_profile_case(args)
     elif args.case == "block-gemm":
         print(json.dumps(run_block_gemm_case()))
+    elif args.case == "assembly-refined":
+        print(json.dumps(run_assembly_refined()))
     elif args.case == "mf-profile":
         run_mf_profile()
     elif args.case == "block-gemm-profile":

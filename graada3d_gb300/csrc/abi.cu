@@ -73,7 +73,7 @@ DevGeometry Context::geometry() const {
   g.n_fields = n_fields;
   g.tables = math_tables.as<double>();
   g.plan.tiles = plan_tiles.as<int32_t>();
-  g.plan.run_start = plan_runs.as<int64_t>();
+  g.plan.cells = plan_cells.as<int64_t>();
   g.plan.n_tiles = plan_n_tiles;
   return g;
 }
@@ -158,19 +158,19 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
 TilePlan Context::tile_plan() {
   if (!plan_valid) {
     std::vector<int32_t> tiles;
-    std::vector<int64_t> runs;
-    build_tile_plan(host_prisms.data(), n_cells, tiles, runs);
+    std::vector<int64_t> cl;
+    build_tile_plan(host_prisms.data(), n_cells, tiles, cl);
     plan_tiles.alloc(this, sizeof(int32_t) * tiles.size());
-    plan_runs.alloc(this, sizeof(int64_t) * runs.size());
+    plan_cells.alloc(this, sizeof(int64_t) * cl.size());
     upload(plan_tiles.ptr, tiles.data(), sizeof(int32_t) * tiles.size());
-    upload(plan_runs.ptr, runs.data(), sizeof(int64_t) * runs.size());
+    upload(plan_cells.ptr, cl.data(), sizeof(int64_t) * cl.size());
     sync();
     plan_n_tiles = (int64_t)tiles.size() / 4;
     plan_valid = true;
   }
   TilePlan p;
   p.tiles = plan_tiles.as<int32_t>();
-  p.run_start = plan_runs.as<int64_t>();
+  p.cells = plan_cells.as<int64_t>();
   p.n_tiles = plan_n_tiles;
   return p;
 }

@@ -17,6 +17,7 @@
 #include "kernels.h"
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -83,22 +84,23 @@ void launch_assemble(const DevGeometry &g, const double *prisms, int64_t n_cells
 
 // ---- tiled assembly: cells shared in z and in y -----------------------------
 //
-// A tile is up to TL_COLS z-runs (vertical stacks of cells, consecutive in the
-// cell list) that are y-neighbours with identical levels: at every level the
-// cells of consecutive runs have the same x extent and z levels and the y0 of
-// one equals the y1 of the previous.  A thread (one observation point) walks
-// the tile level by level and, within a level, run by run, so the cell above
-// (same run, previous level) and the cell before it in y (previous run, same
-// level) are always done: their bottom and y1 faces are taken over
+// A tile is up to TL_COLS z-runs (vertical stacks of cells with equal x/y
+// extent, each on the one above) that are y-neighbours with identical levels:
+// at every level the cells of consecutive runs have the same x extent and z
+// levels and the y0 of one equals the y1 of the previous.  The host groups the
+// cell list into tiles geometrically (build_tile_plan), whatever its order, so
+// a refined mesh in octree leaf order still forms long runs wherever its cells
+// are regular.  A thread (one observation point) walks a tile level by level
+// and, within a level, run by run, so the cell above and the cell before it in
+// y are always done: their bottom and y1 faces are taken over
 // (prism_terms_tiled).  The z carries of the tile's runs live in shared
-// memory, the y carry in registers.  Regular meshes form tiles of TL_COLS full
-// columns; a refined mesh forms smaller ones (down to single runs).
+// memory, the y carry in registers.  Each cell still writes its own column.
 
 template <typename OutT>
 __global__ void __launch_bounds__(TL_THREADS)
     assemble_tiled_kernel(const double *__restrict__ obs, int64_t n_obs,
                           const double *__restrict__ prisms, const int4 *__restrict__ tiles,
-                          const int64_t *__restrict__ run_start, uint32_t mask,
+                          const int64_t *__restrict__ cells, uint32_t mask,
                           const double *__restrict__ tables, OutT *__restrict__ G, int64_t ld) {
   __shared__ double tab[kTabSize];
   __shared__ TileSmem ws;
@@ -112,7 +114,7 @@ __global__ void __launch_bounds__(TL_THREADS)
     py = obs[3 * i + 1];
     pz = obs[3 * i + 2];
   }
-  tile_walk(tiles[blockIdx.x], run_start, prisms, ws, zsm, active, px, py, pz,
+  tile_walk(tiles[blockIdx.x], cells, prisms, ws, zsm, active, px, py, pz,
             families_for_mask(mask), tab, [&](int64_t cell, const PrismTerms &t) {
               OutT *gcol = G + cell * ld + i;
               int slot = 0;
@@ -147,7 +149,7 @@ void launch_assemble_tiled(const DevGeometry &g, const TilePlan &plan, OutT *G, 
   if (grid.y > 65535u || plan.n_tiles > 0x7fffffff)
     throw Error(-1, "too many observation points or tiles for one launch");
   assemble_tiled_kernel<OutT><<<grid, TL_THREADS, smem, s>>>(
-      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(plan.tiles), plan.run_start,
+      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(plan.tiles), plan.cells,
       g.mask, g.tables, G, ld);
   GRADA_LAUNCH_CHECK();
 }
@@ -194,7 +196,7 @@ __global__ void quantize_16_kernel(const float *__restrict__ G, int64_t nd, int6
 __global__ void __launch_bounds__(TL_THREADS)
     forward_field_kernel(const double *__restrict__ obs, int64_t n_obs,
                          const double *__restrict__ prisms, const int4 *__restrict__ tiles,
-                         const int64_t *__restrict__ run_start, int64_t n_tiles,
+                         const int64_t *__restrict__ cells, int64_t n_tiles,
                          int64_t tiles_per_split, const double *__restrict__ rho, uint32_t mask,
                          int nf, const double *__restrict__ tables, double *__restrict__ partial,
                          const int *__restrict__ skip) {
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(TL_THREADS)
 #pragma unroll
   for (int b = 0; b < 10; b++) acc[b] = 0.0;
   for (int64_t tl = t_begin; tl < t_end; tl++) {
-    tile_walk(tiles[tl], run_start, prisms, ws, zsm, active, px, py, pz, fam, tab,
+    tile_walk(tiles[tl], cells, prisms, ws, zsm, active, px, py, pz, fam, tab,
               [&](int64_t cell, const PrismTerms &t) {
                 const double w = __ldg(rho + cell);
 #pragma unroll
@@ -269,7 +271,7 @@ __global__ void sum_splits_kernel(const double *__restrict__ partial, int n_spli
 __global__ void __launch_bounds__(TL_THREADS)
     adjoint_field_tiled_kernel(const double *__restrict__ obs, int64_t n_obs,
                                const double *__restrict__ prisms, const int4 *__restrict__ tiles,
-                               const int64_t *__restrict__ run_start, int64_t n_cells,
+                               const int64_t *__restrict__ cells, int64_t n_cells,
                                uint32_t mask, const double *__restrict__ tables,
                                const double *__restrict__ y, const double *__restrict__ pre_scale,
                                int64_t pblocks_per_split, double *__restrict__ partial,
@@ -305,7 +307,7 @@ __global__ void __launch_bounds__(TL_THREADS)
       }
     }
     int q = 0;
-    tile_walk(td, run_start, prisms, ws, zsm, true, px, py, pz, fam, tab,
+    tile_walk(td, cells, prisms, ws, zsm, true, px, py, pz, fam, tab,
               [&](int64_t, const PrismTerms &t) {
                 double c = 0.0;
 #pragma unroll
@@ -323,7 +325,7 @@ __global__ void __launch_bounds__(TL_THREADS)
 #pragma unroll
     for (int w = 0; w < TL_THREADS / 32; w++) v += wacc[w][qq];
     const int k = qq / td.y, a = qq % td.y;  // walk order: level-major, run-minor
-    const int64_t cell = run_start[td.x + a] + k;
+    const int64_t cell = cells[td.x + (int64_t)a * td.z + k];
     partial[(int64_t)blockIdx.y * n_cells + cell] = v;
   }
 }
@@ -408,7 +410,7 @@ void launch_adjoint_field(const DevGeometry &g, const double *y, const double *p
   if (g.plan.n_tiles > 0x7fffffff) throw Error(-1, "too many tiles for one launch");
   dim3 grid((unsigned)g.plan.n_tiles, (unsigned)n_split);
   adjoint_field_tiled_kernel<<<grid, TL_THREADS, smem, s>>>(
-      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(g.plan.tiles), g.plan.run_start,
+      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(g.plan.tiles), g.plan.cells,
       g.n_cells, g.mask, g.tables, y, pre_scale, per, partial, skip);
   GRADA_LAUNCH_CHECK();
   sum_cell_splits_kernel<<<(unsigned)ceil_div(g.n_cells, 256), 256, 0, s>>>(partial, n_split,
@@ -422,46 +424,72 @@ void build_math_tables_host(double *tab) { build_math_tables(tab); }
 int tile_max_cols() { return TL_COLS; }
 
 void build_tile_plan(const double *p, int64_t n, std::vector<int32_t> &tiles,
-                     std::vector<int64_t> &run_start) {
+                     std::vector<int64_t> &cells) {
   tiles.clear();
-  run_start.clear();
-  auto same = [](double a, double b) { return a == b; };
-  // z-runs: consecutive cells with equal x/y extents, each z0 the previous z1
-  std::vector<int64_t> rstart, rlen;
+  cells.clear();
+  // cells ordered by (x0, x1, y0, y1, z0): the stacks of a column become adjacent
+  std::vector<int64_t> ord(n);
+  for (int64_t i = 0; i < n; i++) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [p](int64_t a, int64_t b) {
+    const double *u = p + 6 * a, *v = p + 6 * b;
+    for (int q : {0, 1, 2, 3, 4})
+      if (u[q] != v[q]) return u[q] < v[q];
+    return a < b;
+  });
+  // z-runs: equal x/y extents, each z0 the previous z1
+  struct Run {
+    int64_t start, len;
+  };
+  std::vector<Run> runs;
   for (int64_t c = 0; c < n;) {
     int64_t e = c;
     while (e + 1 < n) {
-      const double *u = p + 6 * e, *v = p + 6 * (e + 1);
-      if (!(same(u[0], v[0]) && same(u[1], v[1]) && same(u[2], v[2]) && same(u[3], v[3]) &&
-            same(u[5], v[4])))
-        break;
+      const double *u = p + 6 * ord[e], *v = p + 6 * ord[e + 1];
+      if (!(u[0] == v[0] && u[1] == v[1] && u[2] == v[2] && u[3] == v[3] && u[5] == v[4])) break;
       e++;
     }
-    rstart.push_back(c);
-    rlen.push_back(e - c + 1);
+    runs.push_back({c, e - c + 1});
     c = e + 1;
   }
-  // runs that are y-neighbours level by level form a tile
-  auto ynext = [&](size_t a, size_t b) {
-    if (rlen[a] != rlen[b]) return false;
-    for (int64_t k = 0; k < rlen[a]; k++) {
-      const double *u = p + 6 * (rstart[a] + k), *v = p + 6 * (rstart[b] + k);
-      if (!(same(u[0], v[0]) && same(u[1], v[1]) && same(u[3], v[2]) && same(u[4], v[4]) &&
-            same(u[5], v[5])))
-        return false;
+  // runs ordered by (x0, x1, levels, y0): y-neighbours with identical levels
+  // become adjacent
+  auto cell_of = [&](const Run &r, int64_t k) { return p + 6 * ord[r.start + k]; };
+  auto level_cmp = [&](const Run &a, const Run &b) -> int {
+    if (a.len != b.len) return a.len < b.len ? -1 : 1;
+    for (int64_t k = 0; k < a.len; k++) {
+      const double za = cell_of(a, k)[4], zb = cell_of(b, k)[4];
+      if (za != zb) return za < zb ? -1 : 1;
     }
-    return true;
+    const double za = cell_of(a, a.len - 1)[5], zb = cell_of(b, b.len - 1)[5];
+    if (za != zb) return za < zb ? -1 : 1;
+    return 0;
   };
-  for (size_t r = 0; r < rstart.size();) {
+  std::sort(runs.begin(), runs.end(), [&](const Run &a, const Run &b) {
+    const double *u = cell_of(a, 0), *v = cell_of(b, 0);
+    if (u[0] != v[0]) return u[0] < v[0];
+    if (u[1] != v[1]) return u[1] < v[1];
+    const int c = level_cmp(a, b);
+    if (c != 0) return c < 0;
+    if (u[2] != v[2]) return u[2] < v[2];
+    return a.start < b.start;
+  });
+  auto ynext = [&](const Run &a, const Run &b) {
+    const double *u = cell_of(a, 0), *v = cell_of(b, 0);
+    return u[0] == v[0] && u[1] == v[1] && u[3] == v[2] && level_cmp(a, b) == 0;
+  };
+  for (size_t r = 0; r < runs.size();) {
     size_t e = r;
-    while (e + 1 < rstart.size() && (int)(e + 1 - r) < TL_COLS && ynext(e, e + 1)) e++;
+    while (e + 1 < runs.size() && (int)(e + 1 - r) < TL_COLS && ynext(runs[e], runs[e + 1])) e++;
+    const int64_t len = runs[r].len;
     // runs longer than TL_MAXLEV levels go on in further tiles of the same runs
-    for (int64_t l0 = 0; l0 < rlen[r]; l0 += TL_MAXLEV) {
-      tiles.push_back((int32_t)run_start.size());
+    for (int64_t l0 = 0; l0 < len; l0 += TL_MAXLEV) {
+      const int64_t nl = std::min<int64_t>(TL_MAXLEV, len - l0);
+      tiles.push_back((int32_t)cells.size());
       tiles.push_back((int32_t)(e - r + 1));
-      tiles.push_back((int32_t)std::min<int64_t>(TL_MAXLEV, rlen[r] - l0));
+      tiles.push_back((int32_t)nl);
       tiles.push_back(0);
-      for (size_t q = r; q <= e; q++) run_start.push_back(rstart[q] + l0);
+      for (size_t q = r; q <= e; q++)
+        for (int64_t k = 0; k < nl; k++) cells.push_back(ord[runs[q].start + l0 + k]);
     }
     r = e + 1;
   }
@@ -539,7 +567,7 @@ void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, 
     }
   }
   forward_field_kernel<<<grid, TL_THREADS, smem, s>>>(
-      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(g.plan.tiles), g.plan.run_start,
+      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(g.plan.tiles), g.plan.cells,
       g.plan.n_tiles, per, rho, g.mask, g.n_fields, g.tables, partial, skip);
   GRADA_LAUNCH_CHECK();
   const int64_t n = g.n_obs * g.n_fields;

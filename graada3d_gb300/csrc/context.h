@@ -87,7 +87,7 @@ struct Context {
   int g_storage = -1;
   DevBuf G, row_scale;
   // Tile plan of the cell list for the assembly (built from host_prisms).
-  DevBuf plan_tiles, plan_runs;
+  DevBuf plan_tiles, plan_cells;
   int64_t plan_n_tiles = 0;
   bool plan_valid = false;
 

@@ -9,12 +9,14 @@
 
 namespace grada {
 
-// Tiled assembly (regular parts of the mesh share faces in z and in y).  The
-// plan groups the cell list into tiles of up to tile_max_cols() z-runs: int4
-// {first run, runs, levels, 0} per tile, and the first cell of every run.
+// Assembly tiles (cells that share faces in z and in y).  The plan groups the
+// cell list, in any order, into tiles of up to tile_max_cols() z-runs (stacks
+// of cells with equal x/y extent, each on the one above) that are y-neighbours
+// level by level: int4 {offset, runs, levels, 0} per tile, and the cell index
+// of run a, level k at cells[offset + a * levels + k].
 struct TilePlan {
   const int32_t *tiles = nullptr;    // n_tiles x 4
-  const int64_t *run_start = nullptr;
+  const int64_t *cells = nullptr;
   int64_t n_tiles = 0;
 };
 
@@ -45,7 +47,7 @@ void launch_assemble_fp32(const DevGeometry &g, const double *prisms, int64_t n_
                           cudaStream_t s);
 int tile_max_cols();
 void build_tile_plan(const double *prisms, int64_t n_cells, std::vector<int32_t> &tiles,
-                     std::vector<int64_t> &run_start);
+                     std::vector<int64_t> &cells);
 void launch_assemble_tiled_fp64(const DevGeometry &g, const TilePlan &plan, double *G, int64_t ld,
                                 cudaStream_t s);
 void launch_assemble_tiled_fp32(const DevGeometry &g, const TilePlan &plan, float *G, int64_t ld,

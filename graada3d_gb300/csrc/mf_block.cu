@@ -41,7 +41,7 @@ template <int RG>
 __global__ void __launch_bounds__(TL_THREADS)
     forward_field_block_kernel(const double *__restrict__ obs, int64_t n_obs,
                                const double *__restrict__ prisms, const int4 *__restrict__ tiles,
-                               const int64_t *__restrict__ run_start, int64_t n_tiles,
+                               const int64_t *__restrict__ cells, int64_t n_tiles,
                                int64_t tiles_per_split, const double *__restrict__ X,
                                uint32_t mask, int nf, const double *__restrict__ tables, int r0,
                                double *__restrict__ partial, const int *__restrict__ skip) {
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(TL_THREADS)
 #pragma unroll
     for (int r = 0; r < RG; r++) acc[s][r] = 0.0;
   for (int64_t tl = t_begin; tl < t_end; tl++) {
-    tile_walk(tiles[tl], run_start, prisms, ws, zsm, active, px, py, pz, fam, tab,
+    tile_walk(tiles[tl], cells, prisms, ws, zsm, active, px, py, pz, fam, tab,
               [&](int64_t cell, const PrismTerms &t) {
                 const double *xc = X + cell * kBW + r0;  // same address in every thread
 #pragma unroll
@@ -220,7 +220,7 @@ void fwd_pass(const DevGeometry &g, const double *X, int splits, int64_t per, in
   }
   dim3 grid((unsigned)splits, (unsigned)ceil_div(g.n_obs, TL_THREADS));
   forward_field_block_kernel<RG><<<grid, TL_THREADS, smem, s>>>(
-      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(g.plan.tiles), g.plan.run_start,
+      g.obs, g.n_obs, g.prisms, reinterpret_cast<const int4 *>(g.plan.tiles), g.plan.cells,
       g.plan.n_tiles, per, X, g.mask, g.n_fields, g.tables, r0, partial, skip);
   GRADA_LAUNCH_CHECK();
 }

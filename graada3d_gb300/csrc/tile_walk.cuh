@@ -24,30 +24,30 @@ constexpr int tile_walk_dyn_smem() { return (int)sizeof(double) * TL_COLS * ZC_N
 
 struct TileSmem {
   double sc[TL_LCH][TL_COLS][6];
-  int64_t rs[TL_COLS];
+  int64_t ci[TL_LCH][TL_COLS];
 };
 
 // All threads of the block call it for the same tile (it synchronises);
 // threads without a point pass active = false.  f(cell, terms) is called for
 // every cell of the tile in walk order.
 template <class F>
-__device__ __forceinline__ void tile_walk(const int4 td, const int64_t *__restrict__ run_start,
+__device__ __forceinline__ void tile_walk(const int4 td, const int64_t *__restrict__ cells,
                                           const double *__restrict__ prisms, TileSmem &ws,
                                           double *__restrict__ zsm, bool active, double px,
                                           double py, double pz, uint32_t fam,
                                           const double *__restrict__ tab, F &&f) {
   const int ncols = td.y, nlev = td.z;
-  __syncthreads();  // the previous tile's readers are done with ws
-  if (threadIdx.x < ncols) ws.rs[threadIdx.x] = run_start[td.x + threadIdx.x];
   auto zslot = [&](int a, int q) -> double & {
     return zsm[((int64_t)a * ZC_N + q) * TL_THREADS + threadIdx.x];
   };
   for (int k0 = 0; k0 < nlev; k0 += TL_LCH) {
     const int nl = min(TL_LCH, nlev - k0);
-    __syncthreads();
+    __syncthreads();  // the previous chunk's (or tile's) readers are done with ws
     for (int t = threadIdx.x; t < nl * ncols * 6; t += TL_THREADS) {
       const int k = t / (ncols * 6), a = (t / 6) % ncols, q = t % 6;
-      ws.sc[k][a][q] = prisms[(ws.rs[a] + k0 + k) * 6 + q];
+      const int64_t cell = cells[td.x + (int64_t)a * nlev + k0 + k];
+      ws.sc[k][a][q] = prisms[cell * 6 + q];
+      if (q == 0) ws.ci[k][a] = cell;
     }
     __syncthreads();
     if (!active) continue;
@@ -75,7 +75,7 @@ __device__ __forceinline__ void tile_walk(const int4 td, const int64_t *__restri
         zslot(a, 6) = zout.qy[0]; zslot(a, 7) = zout.qy[1];
         zslot(a, 8) = zout.tz;
         yc = yout;
-        f(ws.rs[a] + k, t);
+        f(ws.ci[kk][a], t);
       }
     }
   }
