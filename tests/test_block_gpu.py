@@ -190,3 +190,22 @@ def test_lambda_sweep_matrix_free_matches_stored(gpu_ctx):
     for c in range(4):
         assert abs(rmf[c]["final_misfit"] - r64[c]["final_misfit"]) <= 1e-8 * r64[c]["final_misfit"]
         assert np.linalg.norm(mmf[:, c] - m64[:, c]) <= 1e-8 * max(np.linalg.norm(m64[:, c]), 1.0)
+
+
+@pytest.mark.parametrize("storage", ["fp64", "fp32", "bf16", "fp16", "matrix_free"])
+def test_block_products_tiny_problem(gpu_ctx, storage):
+    """3 cells, 2 points: one tensor-core tile mostly out of bounds (zero-filled),
+    a single assembly tile, 3 right-hand sides."""
+    prisms = mesh.regular_mesh((0.0, 300.0), 3, (0.0, 100.0), 1, (0.0, 100.0), 1)
+    obs = np.array([[50.0, 50.0, -10.0], [250.0, 40.0, -20.0]])
+    inv = GaussNewtonInversion(prisms, obs, 0x3FE, ctx=gpu_ctx)
+    inv.compute_G(storage)
+    rng = np.random.default_rng(2)
+    X = rng.standard_normal((inv.Nm, 3))
+    Y = rng.standard_normal((inv.Nd, 3))
+    GX, GTY = inv.G_mat_mul(X), inv.GT_mat_mul(Y)
+    tol = TOL_BLOCK[storage]
+    for c in range(3):
+        y1, x1 = inv.G_vec_mul(X[:, c]), inv.GT_vec_mul(Y[:, c])
+        assert np.abs(GX[:, c] - y1).max() <= tol * np.abs(y1).max()
+        assert np.abs(GTY[:, c] - x1).max() <= tol * np.abs(x1).max()

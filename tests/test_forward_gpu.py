@@ -182,3 +182,42 @@ def test_invalid_inputs_are_rejected(gpu_ctx):
     f = Fwd(np.array([[0.0, 1.0, 0, 1, 0, 1]]), np.array([[0.5, 0.5, -1.0]]), 0x2, ctx=gpu_ctx)
     with pytest.raises(GradaError):
         f.G_vec_mul(np.ones(1))  # G not assembled yet
+
+
+@pytest.mark.parametrize("shape", ["one_cell", "tall_column", "shuffled", "ragged_rows"])
+def test_G_tile_plan_edge_cases(gpu_ctx, shape):
+    """The assembly groups cells into tiles of y-adjacent z-runs with equal
+    levels; G must not depend on that grouping.  One cell; a 1x1x130 column
+    (runs split at the 64-level tile limit, ragged remainder); a mesh in
+    random cell order; a mesh whose y-rows end in partial tiles (ny = 11)."""
+    rng = np.random.default_rng(21)
+    if shape == "one_cell":
+        prisms = mesh.regular_mesh((0.0, 50.0), 1, (0.0, 70.0), 1, (0.0, 30.0), 1)
+    elif shape == "tall_column":
+        prisms = mesh.regular_mesh((0.0, 50.0), 1, (0.0, 50.0), 1, (0.0, 1300.0), 130)
+    elif shape == "shuffled":
+        prisms = mesh.regular_mesh((0.0, 900.0), 9, (0.0, 700.0), 7, (0.0, 500.0), 5)
+        prisms = prisms[rng.permutation(prisms.shape[0])]
+    else:
+        prisms = mesh.regular_mesh((0.0, 300.0), 3, (0.0, 1100.0), 11, (0.0, 300.0), 3)
+    n_obs = 37
+    obs = np.stack([rng.uniform(-100, 1000, n_obs), rng.uniform(-100, 1200, n_obs),
+                    -rng.uniform(0.5, 100, n_obs)], 1)
+    mask = 0x3FE
+    f = Fwd(prisms, obs, mask, ctx=gpu_ctx)
+    f.compute_G("fp64")
+    G_want = prism.compute_G(prisms, obs, mask)
+    _check_blocks(f.get_G(), G_want, n_obs, 9, TOL_FP64, shape)
+    # mixed-sign densities cancel (gx of the column is ~1e-3 of sum |G||rho|):
+    # the field is checked against that sum, per component
+    rho = rng.uniform(-400, 400, prisms.shape[0])
+    ff = f.forward_field(rho)
+    want = prism.forward_field(prisms, rho, obs, mask)
+    scale = (np.abs(G_want) @ np.abs(rho)).reshape(9, n_obs).max(axis=1)
+    assert (np.abs(ff - want).max(axis=0) / scale).max() < TOL_FP64
+    G = f.get_G()
+    f.compute_G("matrix_free")
+    x = rng.standard_normal(f.Nm)
+    y = rng.standard_normal(f.Nd)
+    np.testing.assert_allclose(f.G_vec_mul(x), G @ x, rtol=0, atol=1e-12 * np.abs(G).sum(1).max())
+    np.testing.assert_allclose(f.GT_vec_mul(y), G.T @ y, rtol=0, atol=1e-12 * np.abs(G).sum(0).max())
