@@ -107,8 +107,21 @@ constexpr int kTabSize = kTabConst + 4;
 // Fills `tab` (kTabSize doubles).  Host only.
 void build_math_tables(double *tab);
 
+// Sign tests on the bit pattern: integer instructions instead of FP64
+// compares, which would take FP64-pipe slots.  Exact for every non-NaN double
+// (-0.0 is not negative).
+__device__ __forceinline__ bool neg_strict(double v) {
+  return (unsigned long long)__double_as_longlong(v) > 0x8000000000000000ull;
+}
+__device__ __forceinline__ bool both_zero(double a, double b) {
+  return (((unsigned long long)__double_as_longlong(a) |
+           (unsigned long long)__double_as_longlong(b)) << 1) == 0ull;
+}
+
 __device__ __forceinline__ double fast_log(double q, const double *__restrict__ tab) {
-  if (!(q >= 2.2250738585072014e-308 && q <= 1.7976931348623157e308)) return log(q);
+  // q outside [DBL_MIN, DBL_MAX] (zero, subnormal, negative, inf, NaN), tested
+  // on the high word: the library log handles those
+  if ((unsigned)__double2hiint(q) - 0x00100000u >= 0x7FE00000u) return log(q);
   const long long bits = __double_as_longlong(q);
   const long long f = bits & 0x000FFFFFFFFFFFFFll;
   int e = (int)(bits >> 52) - 1023;
@@ -147,10 +160,10 @@ __device__ __forceinline__ double fast_log(double q, const double *__restrict__ 
 __device__ __forceinline__ double edge_log_ratio(double a0, double a1, double r0, double r1,
                                                  double perp2, const double *__restrict__ tab) {
   double num, den;
-  if (a0 >= 0.0) {
+  if (!neg_strict(a0)) {
     num = a1 + r1;
     den = a0 + r0;
-  } else if (a1 < 0.0) {
+  } else if (neg_strict(a1)) {
     num = r0 - a0;
     den = r1 - a1;
   } else {
@@ -163,8 +176,7 @@ __device__ __forceinline__ double edge_log_ratio(double a0, double a1, double r0
 // Normalises (a, b) so that arg(a + i b) equals atan(b / a) as the corner
 // formula uses it (a < 0 flips both parts; 0/0 at a corner on an edge line of
 // the face's axis is taken as 0, which cancels between the two faces it
-// touches).  Works for double and float alike, so the FP32 estimate sees the
-// same conventions as the FP64 value.
+// touches).  Applied to the FP32 estimate of a face sum.
 template <typename T>
 __device__ __forceinline__ void atan_factor(T &a, T &b) {
   if (a < T(0)) {
@@ -176,6 +188,11 @@ __device__ __forceinline__ void atan_factor(T &a, T &b) {
 
 // sum_c s_c atan(b_c / a_c) over the four corners of a face, signs (+,-,-,+)
 // for corners (00, 01, 10, 11).  (a, b) in FP64, (af, bf) the same in FP32.
+// The FP64 factors skip the sign normalisation of atan_factor (a < 0 flips
+// both parts): a flipped factor negates the product and so both rotated parts
+// xr, yr exactly (round-to-nearest is symmetric), leaving d = yr / xr
+// bitwise unchanged.  Only the FP32 estimate, which picks the table angle
+// and the 2*pi branch, needs the principal values.  The 0/0 rule stays.
 __device__ __forceinline__ double face_atan_sum(const double (&a)[4], const double (&b)[4],
                                                 const float (&af)[4], const float (&bf)[4],
                                                 const double *__restrict__ tab) {
@@ -183,9 +200,8 @@ __device__ __forceinline__ double face_atan_sum(const double (&a)[4], const doub
   float est = 0.f;
 #pragma unroll
   for (int c = 0; c < 4; c++) {
-    A[c] = a[c];
+    A[c] = both_zero(a[c], b[c]) ? 1.0 : a[c];
     B[c] = b[c];
-    atan_factor(A[c], B[c]);
     float x = af[c], y = bf[c];
     atan_factor(x, y);
     const bool neg = (c == 1 || c == 2);  // conjugate the negative-sign corners
