@@ -118,6 +118,36 @@ __device__ __forceinline__ bool both_zero(double a, double b) {
            (unsigned long long)__double_as_longlong(b)) << 1) == 0ull;
 }
 
+// Exact int -> double for |v| < 2^21 from integer instructions (the
+// conversion instruction would take an FP64-pipe slot): exponent from the
+// leading-zero count, the bits below the leading one as the fraction.
+__device__ __forceinline__ double small_int_to_double(int v) {
+  if (v == 0) return 0.0;
+  const unsigned s = v < 0 ? 0x80000000u : 0u;
+  const unsigned u = v < 0 ? 0u - (unsigned)v : (unsigned)v;
+  const int lz = __clz(u);  // 11..31
+  const unsigned hi = s | ((unsigned)(1054 - lz) << 20) | ((u ^ (0x80000000u >> lz)) << (lz - 11));
+  return __hiloint2double((int)hi, 0);
+}
+
+// double -> float rounded to nearest even, as the conversion instruction does,
+// from integer instructions where the result is a normal float; zero, and
+// anything that rounds to a subnormal, infinity or NaN, takes the instruction.
+__device__ __forceinline__ float double_to_float_rn(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned ex = (hi >> 20) & 0x7FFu;
+  if (ex - 897u > 253u) {  // float exponent ex - 896 outside [1, 254]
+    if ((b << 1) == 0ull) return __uint_as_float(hi & 0x80000000u);
+    return (float)v;
+  }
+  const unsigned long long mant = b & 0x000FFFFFFFFFFFFFull;
+  unsigned f = ((ex - 896u) << 23) | (unsigned)(mant >> 29);
+  const unsigned rem = (unsigned)mant & 0x1FFFFFFFu;
+  f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;  // carries into
+  return __uint_as_float((hi & 0x80000000u) | f);                          // the exponent
+}
+
 __device__ __forceinline__ double fast_log(double q, const double *__restrict__ tab) {
   // q outside [DBL_MIN, DBL_MAX] (zero, subnormal, negative, inf, NaN), tested
   // on the high word: the library log handles those
@@ -146,7 +176,7 @@ __device__ __forceinline__ double fast_log(double q, const double *__restrict__ 
   p = fma(p, t, 1.0 / 3.0);
   p = fma(p, t, -0.5);
   const double l1p = fma(t2, p, t);
-  const double ed = (double)e;
+  const double ed = small_int_to_double(e);
   const double hi = fma(ed, tab[kTabConst + 0], L[1]);
   const double lo = fma(ed, tab[kTabConst + 1], L[2]);
   return hi + (l1p + lo);
@@ -231,7 +261,7 @@ __device__ __forceinline__ double face_atan_sum(const double (&a)[4], const doub
   p = fma(p, d2, 1.0 / 5.0);
   p = fma(p, d2, -1.0 / 3.0);
   const double at = fma(d * d2, p, d);
-  const double jd = (double)j;
+  const double jd = small_int_to_double(j);
   return fma(jd, tab[kTabConst + 2], fma(jd, tab[kTabConst + 3], at));
 }
 
@@ -318,10 +348,10 @@ __device__ __forceinline__ void prism_terms(double px, double py, double pz, dou
     return;
   }
   // FP32 copies for the branch/rotation estimates of the face angle sums
-  // (6 conversions; everything else of the estimate stays on the FP32 pipe).
-  const float Xf[2] = {(float)t.X[0], (float)t.X[1]};
-  const float Yf[2] = {(float)t.Y[0], (float)t.Y[1]};
-  const float Zf[2] = {(float)t.Z[0], (float)t.Z[1]};
+  // (6 conversions, by integer instructions; the rest of the estimate runs on the FP32 pipe).
+  const float Xf[2] = {double_to_float_rn(t.X[0]), double_to_float_rn(t.X[1])};
+  const float Yf[2] = {double_to_float_rn(t.Y[0]), double_to_float_rn(t.Y[1])};
+  const float Zf[2] = {double_to_float_rn(t.Z[0]), double_to_float_rn(t.Z[1])};
   float rf[2][2][2];
 #pragma unroll
   for (int i = 0; i < 2; i++)
@@ -460,9 +490,9 @@ __device__ __forceinline__ void prism_terms_tiled(double px, double py, double p
       }
   }
   if (fam & (FAM_AX | FAM_AY | FAM_AZ)) {
-    const float Xf[2] = {(float)t.X[0], (float)t.X[1]};
-    const float Yf[2] = {(float)t.Y[0], (float)t.Y[1]};
-    const float Zf[2] = {(float)t.Z[0], (float)t.Z[1]};
+    const float Xf[2] = {double_to_float_rn(t.X[0]), double_to_float_rn(t.X[1])};
+    const float Yf[2] = {double_to_float_rn(t.Y[0]), double_to_float_rn(t.Y[1])};
+    const float Zf[2] = {double_to_float_rn(t.Z[0]), double_to_float_rn(t.Z[1])};
     float rf[2][2][2];
 #pragma unroll
     for (int i = 0; i < 2; i++)
