@@ -18,7 +18,9 @@
 #include <cmath>
 #include <cstring>
 #include <algorithm>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "prism.cuh"
@@ -82,19 +84,22 @@ void launch_assemble(const DevGeometry &g, const double *prisms, int64_t n_cells
   GRADA_LAUNCH_CHECK();
 }
 
-// ---- tiled assembly: cells shared in z and in y -----------------------------
+// ---- tiled assembly: cells shared in z, y and x ------------------------------
 //
 // A tile is up to TL_COLS z-runs (vertical stacks of cells with equal x/y
-// extent, each on the one above) that are y-neighbours with identical levels:
-// at every level the cells of consecutive runs have the same x extent and z
-// levels and the y0 of one equals the y1 of the previous.  The host groups the
-// cell list into tiles geometrically (build_tile_plan), whatever its order, so
-// a refined mesh in octree leaf order still forms long runs wherever its cells
+// extent, each on the one above) with identical levels, arranged as 1 or 2
+// runs across x times up to TL_COLS (or TL_COLS/2) y-neighbours: at every
+// level, consecutive runs in y have the same x extent and the y0 of one equals
+// the y1 of the previous, and the two runs across x have the same y extent and
+// the x0 of the second equals the x1 of the first.  The host groups the cell
+// list into tiles geometrically (build_tile_plan), whatever its order, so a
+// refined mesh in octree leaf order still forms long runs wherever its cells
 // are regular.  A thread (one observation point) walks a tile level by level
-// and, within a level, run by run, so the cell above and the cell before it in
-// y are always done: their bottom and y1 faces are taken over
-// (prism_terms_tiled).  The z carries of the tile's runs live in shared
-// memory, the y carry in registers.  Each cell still writes its own column.
+// and, within a level, y-row by y-row and run by run across x, so the cell
+// above, the cell before in y and the cell before in x are always done: their
+// bottom, y1 and x1 faces are taken over (prism_terms_tiled).  The z carries
+// of the tile's runs and the y carries of its columns live in shared memory,
+// the x carry in registers.  Each cell still writes its own column.
 
 template <typename OutT>
 __global__ void __launch_bounds__(TL_THREADS)
@@ -114,8 +119,8 @@ __global__ void __launch_bounds__(TL_THREADS)
     py = obs[3 * i + 1];
     pz = obs[3 * i + 2];
   }
-  tile_walk(tiles[blockIdx.x], cells, prisms, ws, zsm, active, px, py, pz,
-            families_for_mask(mask), tab, [&](int64_t cell, const PrismTerms &t) {
+  tile_walk<true>(tiles[blockIdx.x], cells, prisms, ws, zsm, active, px, py, pz,
+                  families_for_mask(mask), tab, [&](int64_t cell, int, const PrismTerms &t) {
               OutT *gcol = G + cell * ld + i;
               int slot = 0;
 #pragma unroll
@@ -134,7 +139,7 @@ void launch_assemble_tiled(const DevGeometry &g, const TilePlan &plan, OutT *G, 
   if (plan.n_tiles <= 0 || g.n_obs <= 0) return;
   static std::mutex mu;
   static bool attr[64] = {};
-  const int smem = tile_walk_dyn_smem();
+  const int smem = tile_walk_dyn_smem(true);
   {
     int dev = 0;
     GRADA_CUDA_CHECK(cudaGetDevice(&dev));
@@ -221,8 +226,8 @@ __global__ void __launch_bounds__(TL_THREADS)
 #pragma unroll
   for (int b = 0; b < 10; b++) acc[b] = 0.0;
   for (int64_t tl = t_begin; tl < t_end; tl++) {
-    tile_walk(tiles[tl], cells, prisms, ws, zsm, active, px, py, pz, fam, tab,
-              [&](int64_t cell, const PrismTerms &t) {
+    tile_walk<true>(tiles[tl], cells, prisms, ws, zsm, active, px, py, pz, fam, tab,
+                    [&](int64_t cell, int, const PrismTerms &t) {
                 const double w = __ldg(rho + cell);
 #pragma unroll
                 for (int b = 0; b < 10; b++)
@@ -306,9 +311,8 @@ __global__ void __launch_bounds__(TL_THREADS)
         slot++;
       }
     }
-    int q = 0;
-    tile_walk(td, cells, prisms, ws, zsm, true, px, py, pz, fam, tab,
-              [&](int64_t, const PrismTerms &t) {
+    tile_walk<false>(td, cells, prisms, ws, zsm, true, px, py, pz, fam, tab,
+                     [&](int64_t, int q, const PrismTerms &t) {
                 double c = 0.0;
 #pragma unroll
                 for (int b = 0; b < 10; b++)
@@ -316,7 +320,6 @@ __global__ void __launch_bounds__(TL_THREADS)
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
                 if (lane == 0) wacc[warp][q] += c;
-                q++;
               });
   }
   __syncthreads();
@@ -324,7 +327,7 @@ __global__ void __launch_bounds__(TL_THREADS)
     double v = 0.0;
 #pragma unroll
     for (int w = 0; w < TL_THREADS / 32; w++) v += wacc[w][qq];
-    const int k = qq / td.y, a = qq % td.y;  // walk order: level-major, run-minor
+    const int k = qq / td.y, a = qq % td.y;  // q = level * runs + run
     const int64_t cell = cells[td.x + (int64_t)a * td.z + k];
     partial[(int64_t)blockIdx.y * n_cells + cell] = v;
   }
@@ -394,7 +397,7 @@ void launch_adjoint_field(const DevGeometry &g, const double *y, const double *p
   if (g.n_cells <= 0) return;
   const int64_t n_pb = ceil_div(g.n_obs, TL_THREADS);
   const int64_t per = ceil_div(n_pb, n_split);
-  const int smem = tile_walk_dyn_smem();
+  const int smem = tile_walk_dyn_smem(false);
   {
     static std::mutex mu;
     static bool attr[64] = {};
@@ -477,21 +480,72 @@ void build_tile_plan(const double *p, int64_t n, std::vector<int32_t> &tiles,
     const double *u = cell_of(a, 0), *v = cell_of(b, 0);
     return u[0] == v[0] && u[1] == v[1] && u[3] == v[2] && level_cmp(a, b) == 0;
   };
-  for (size_t r = 0; r < runs.size();) {
-    size_t e = r;
-    while (e + 1 < runs.size() && (int)(e + 1 - r) < TL_COLS && ynext(runs[e], runs[e + 1])) e++;
-    const int64_t len = runs[r].len;
+  // x partner of a run: the run whose x0 is its x1, with the same y extent and
+  // levels (candidates looked up by x0, y0, y1, level count and first z0)
+  using Key = std::tuple<double, double, double, int64_t, double>;
+  std::map<Key, std::vector<size_t>> by_face;
+  for (size_t r = 0; r < runs.size(); r++) {
+    const double *u = cell_of(runs[r], 0);
+    by_face[Key(u[0], u[2], u[3], runs[r].len, u[4])].push_back(r);
+  }
+  std::vector<char> used(runs.size(), 0);
+  auto partner = [&](size_t r) -> int64_t {
+    const double *u = cell_of(runs[r], 0);
+    auto it = by_face.find(Key(u[1], u[2], u[3], runs[r].len, u[4]));
+    if (it == by_face.end()) return -1;
+    for (size_t q : it->second)
+      if (!used[q] && level_cmp(runs[r], runs[q]) == 0) return (int64_t)q;
+    return -1;
+  };
+  auto emit = [&](const std::vector<size_t> &order, int nx) {
+    const int64_t len = runs[order[0]].len;
     // runs longer than TL_MAXLEV levels go on in further tiles of the same runs
     for (int64_t l0 = 0; l0 < len; l0 += TL_MAXLEV) {
       const int64_t nl = std::min<int64_t>(TL_MAXLEV, len - l0);
       tiles.push_back((int32_t)cells.size());
-      tiles.push_back((int32_t)(e - r + 1));
+      tiles.push_back((int32_t)order.size());
       tiles.push_back((int32_t)nl);
-      tiles.push_back(0);
-      for (size_t q = r; q <= e; q++)
+      tiles.push_back(nx);
+      for (size_t q : order)
         for (int64_t k = 0; k < nl; k++) cells.push_back(ord[runs[q].start + l0 + k]);
     }
-    r = e + 1;
+  };
+  // Greedy in (x0, x1, levels, y0) order: a run with an x partner starts a
+  // 2 x m tile (m <= TL_COLS/2 y-neighbours, each with its partner, run order
+  // y-major, x-minor); one without starts a 1 x m tile (m <= TL_COLS) that
+  // stops before a run that could start a 2 x m tile.
+  for (size_t r = 0; r < runs.size(); r++) {
+    if (used[r]) continue;
+    std::vector<size_t> order;
+    const int64_t p0 = partner(r);
+    if (p0 >= 0) {
+      size_t e = r, pe = (size_t)p0;
+      used[e] = used[pe] = 1;
+      order.push_back(e);
+      order.push_back(pe);
+      while ((int)order.size() < TL_COLS && e + 1 < runs.size() && !used[e + 1] &&
+             ynext(runs[e], runs[e + 1])) {
+        const int64_t pn = partner(e + 1);
+        if (pn < 0 || !ynext(runs[pe], runs[(size_t)pn])) break;
+        e = e + 1;
+        pe = (size_t)pn;
+        used[e] = used[pe] = 1;
+        order.push_back(e);
+        order.push_back(pe);
+      }
+      emit(order, 2);
+    } else {
+      size_t e = r;
+      used[e] = 1;
+      order.push_back(e);
+      while ((int)order.size() < TL_COLS && e + 1 < runs.size() && !used[e + 1] &&
+             ynext(runs[e], runs[e + 1]) && partner(e + 1) < 0) {
+        e = e + 1;
+        used[e] = 1;
+        order.push_back(e);
+      }
+      emit(order, 1);
+    }
   }
 }
 
@@ -553,7 +607,7 @@ void launch_forward_field(const DevGeometry &g, const double *rho, int n_split, 
   const int64_t per = ceil_div(g.plan.n_tiles, n_split);
   dim3 grid((unsigned)n_split, (unsigned)ceil_div(g.n_obs, TL_THREADS));
   if (grid.y > 65535u) throw Error(-1, "too many observation points for one launch");
-  const int smem = tile_walk_dyn_smem();
+  const int smem = tile_walk_dyn_smem(true);
   {
     static std::mutex mu;
     static bool attr[64] = {};

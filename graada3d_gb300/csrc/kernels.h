@@ -9,11 +9,12 @@
 
 namespace grada {
 
-// Assembly tiles (cells that share faces in z and in y).  The plan groups the
+// Assembly tiles (cells that share faces in z, y and x).  The plan groups the
 // cell list, in any order, into tiles of up to tile_max_cols() z-runs (stacks
-// of cells with equal x/y extent, each on the one above) that are y-neighbours
-// level by level: int4 {offset, runs, levels, 0} per tile, and the cell index
-// of run a, level k at cells[offset + a * levels + k].
+// of cells with equal x/y extent, each on the one above) that are neighbours
+// level by level, nx = 1 or 2 across x times runs / nx along y: int4 {offset,
+// runs, levels, nx} per tile; run a sits at x = a % nx, y = a / nx and its
+// cell at level k is cells[offset + a * levels + k].
 struct TilePlan {
   const int32_t *tiles = nullptr;    // n_tiles x 4
   const int64_t *cells = nullptr;

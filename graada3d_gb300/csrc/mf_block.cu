@@ -71,8 +71,8 @@ __global__ void __launch_bounds__(TL_THREADS)
 #pragma unroll
     for (int r = 0; r < RG; r++) acc[s][r] = 0.0;
   for (int64_t tl = t_begin; tl < t_end; tl++) {
-    tile_walk(tiles[tl], cells, prisms, ws, zsm, active, px, py, pz, fam, tab,
-              [&](int64_t cell, const PrismTerms &t) {
+    tile_walk<false>(tiles[tl], cells, prisms, ws, zsm, active, px, py, pz, fam, tab,
+                     [&](int64_t cell, int, const PrismTerms &t) {
                 const double *xc = X + cell * kBW + r0;  // same address in every thread
 #pragma unroll
                 for (int s = 0; s < NFMAX; s++) {
@@ -205,7 +205,7 @@ int adj_splits(const DevGeometry &g, int sm_count) {
 template <int RG>
 void fwd_pass(const DevGeometry &g, const double *X, int splits, int64_t per, int r0,
               double *partial, cudaStream_t s, const int *skip) {
-  const int smem = tile_walk_dyn_smem();
+  const int smem = tile_walk_dyn_smem(false);
   {
     static std::mutex mu;
     static bool attr[64] = {};

@@ -30,8 +30,8 @@
 //    table rotation below; the 2*pi branch is picked with a cheap FP32
 //    estimate of the same sum;
 //  * faces shared by neighbouring cells (a column in z, and with
-//    prism_terms_tiled also the previous column in y) are taken over from the
-//    neighbour instead of being evaluated again.
+//    prism_terms_tiled also the previous cells in y and x) are taken over
+//    from the neighbour instead of being evaluated again.
 // Every quantity that reaches a result is computed in FP64.
 #pragma once
 
@@ -200,6 +200,23 @@ __device__ __forceinline__ double fast_rcp(double x) {
   return fma(y0, fma(e, e, e), y0);
 }
 
+// sqrt(x) the same way: seed y0 = rsqrt.approx.ftz.f64(x) (relative error
+// below 2^-20, measured as for the reciprocal), t = x y0 ~ sqrt(x) and
+// e = 1 - t y0 = 1 - x y0^2, then sqrt(x) = t (1 - e)^(-1/2) with the binomial
+// series t (1 + e/2 + 3e^2/8 + ...) cut after e^2 (|e| < 2^-19, truncation
+// below 2^-58; the rounding of t adds half of its own 2^-53).  Five FP64
+// instructions; x outside 2^-1000..2^1000 or negative takes sqrt().
+__device__ __forceinline__ double fast_sqrt(double x) {
+  const unsigned hx = (unsigned)__double2hiint(x);
+  if (hx - 0x01700000u >= 0x7D100000u) return sqrt(x);
+  double y0;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y0) : "d"(x));
+  const double t = x * y0;
+  const double e = fma(-t, y0, 1.0);
+  const double p = fma(e, 0.375, 0.5) * e;
+  return fma(t, p, t);
+}
+
 // ln((a1 + r1) / (a0 + r0)) along one edge, a0 <= a1 the edge's end
 // coordinates relative to the point, r0/r1 the corner distances, perp2 the
 // squared distance from the point to the edge line.  Each factor a + r with
@@ -321,8 +338,8 @@ __device__ __forceinline__ void prism_terms(double px, double py, double pz, dou
 #pragma unroll
     for (int j = 0; j < 2; j++) {
       const double xy = X2[i] + Y2[j];
-      r[i][j][0] = reuse_top ? carry.r[i][j] : sqrt(xy + Z2[0]);
-      r[i][j][1] = sqrt(xy + Z2[1]);
+      r[i][j][0] = reuse_top ? carry.r[i][j] : fast_sqrt(xy + Z2[0]);
+      r[i][j][1] = fast_sqrt(xy + Z2[1]);
     }
   if (fam & FAM_LX) {
 #pragma unroll
@@ -444,18 +461,31 @@ struct YCarry {
   double ty;
 };
 
-// prism_terms with both neighbours' faces available: `top` (the cell above in
-// the same column, ZCarry) and `yprev` (the cell of the previous column at the
-// same level, YCarry).  Shared quantities are taken over instead of being
-// recomputed; every computed quantity uses the same FP64 operands in the same
-// order as prism_terms, so the result is bitwise that of prism_terms.
+// The same for a cell's x1 face and the cell after it in x (same y extent and
+// z levels, its x0 equal to this x1).
+struct XCarry {
+  double r[2][2];  // [j][k]
+  double qy[2];    // [k]
+  double qz[2];    // [j]
+  double tx;
+};
+
+// prism_terms with the neighbours' faces available: `top` (the cell above in
+// the same column, ZCarry), `yprev` (the cell before it in y at the same
+// level, YCarry) and `xprev` (the cell before it in x, XCarry).  A quantity
+// on several shared faces is taken from the first of z, y, x; shared
+// quantities are taken over instead of being recomputed, and every computed
+// quantity uses the same FP64 operands in the same order as prism_terms, so
+// the result is bitwise that of prism_terms.  The faces this cell hands on
+// (bottom, y1, x1) are written to zout, yout, xout.
 __device__ __forceinline__ void prism_terms_tiled(double px, double py, double pz, double x0,
                                                   double x1, double y0, double y1, double z0,
                                                   double z1, uint32_t fam,
                                                   const double *__restrict__ tab, bool top,
                                                   const ZCarry &zin, bool yprev,
-                                                  const YCarry &yin, ZCarry &zout, YCarry &yout,
-                                                  PrismTerms &t) {
+                                                  const YCarry &yin, bool xprev,
+                                                  const XCarry &xin, ZCarry &zout, YCarry &yout,
+                                                  XCarry &xout, PrismTerms &t) {
   t.X[0] = x0 - px; t.X[1] = x1 - px;
   t.Y[0] = y0 - py; t.Y[1] = y1 - py;
   t.Z[0] = z0 - pz; t.Z[1] = z1 - pz;
@@ -472,10 +502,11 @@ __device__ __forceinline__ void prism_terms_tiled(double px, double py, double p
       for (int k = 0; k < 2; k++) {
         if (top && k == 0) r[i][j][k] = zin.r[i][j];
         else if (yprev && j == 0) r[i][j][k] = yin.r[i][k];
-        else r[i][j][k] = sqrt(xy + Z2[k]);
+        else if (xprev && i == 0) r[i][j][k] = xin.r[j][k];
+        else r[i][j][k] = fast_sqrt(xy + Z2[k]);
       }
     }
-  if (fam & FAM_LX) {
+  if (fam & FAM_LX) {  // x-edges lie on z and y faces
 #pragma unroll
     for (int j = 0; j < 2; j++)
 #pragma unroll
@@ -486,22 +517,24 @@ __device__ __forceinline__ void prism_terms_tiled(double px, double py, double p
           t.qx[j][k] = edge_log_ratio(t.X[0], t.X[1], r[0][j][k], r[1][j][k], Y2[j] + Z2[k], tab);
       }
   }
-  if (fam & FAM_LY) {
+  if (fam & FAM_LY) {  // y-edges lie on z and x faces
 #pragma unroll
     for (int i = 0; i < 2; i++)
 #pragma unroll
       for (int k = 0; k < 2; k++) {
         if (top && k == 0) t.qy[i][k] = zin.qy[i];
+        else if (xprev && i == 0) t.qy[i][k] = xin.qy[k];
         else
           t.qy[i][k] = edge_log_ratio(t.Y[0], t.Y[1], r[i][0][k], r[i][1][k], X2[i] + Z2[k], tab);
       }
   }
-  if (fam & FAM_LZ) {
+  if (fam & FAM_LZ) {  // z-edges lie on y and x faces
 #pragma unroll
     for (int i = 0; i < 2; i++)
 #pragma unroll
       for (int j = 0; j < 2; j++) {
         if (yprev && j == 0) t.qz[i][j] = yin.qz[i];
+        else if (xprev && i == 0) t.qz[i][j] = xin.qz[j];
         else
           t.qz[i][j] = edge_log_ratio(t.Z[0], t.Z[1], r[i][j][0], r[i][j][1], X2[i] + Y2[j], tab);
       }
@@ -523,6 +556,10 @@ __device__ __forceinline__ void prism_terms_tiled(double px, double py, double p
       const float bf[4] = {Yf[0] * Zf[0], Yf[0] * Zf[1], Yf[1] * Zf[0], Yf[1] * Zf[1]};
 #pragma unroll
       for (int i = 0; i < 2; i++) {
+        if (xprev && i == 0) {
+          t.tx[0] = xin.tx;
+          continue;
+        }
         const double a[4] = {t.X[i] * r[i][0][0], t.X[i] * r[i][0][1], t.X[i] * r[i][1][0],
                              t.X[i] * r[i][1][1]};
         const float af[4] = {Xf[i] * rf[i][0][0], Xf[i] * rf[i][0][1], Xf[i] * rf[i][1][0],
@@ -563,15 +600,18 @@ __device__ __forceinline__ void prism_terms_tiled(double px, double py, double p
       }
     }
   }
-  // faces handed on: bottom (z1) down the column, y1 to the next column
+  // faces handed on: bottom (z1) down the column, y1 and x1 to the next runs
 #pragma unroll
   for (int i = 0; i < 2; i++)
 #pragma unroll
     for (int j = 0; j < 2; j++) zout.r[i][j] = r[i][j][1];
 #pragma unroll
-  for (int i = 0; i < 2; i++)
+  for (int a = 0; a < 2; a++)
 #pragma unroll
-    for (int k = 0; k < 2; k++) yout.r[i][k] = r[i][1][k];
+    for (int k = 0; k < 2; k++) {
+      yout.r[a][k] = r[a][1][k];
+      xout.r[a][k] = r[1][a][k];
+    }
   if (fam & FAM_LX) {
     zout.qx[0] = t.qx[0][1];
     zout.qx[1] = t.qx[1][1];
@@ -581,11 +621,16 @@ __device__ __forceinline__ void prism_terms_tiled(double px, double py, double p
   if (fam & FAM_LY) {
     zout.qy[0] = t.qy[0][1];
     zout.qy[1] = t.qy[1][1];
+    xout.qy[0] = t.qy[1][0];
+    xout.qy[1] = t.qy[1][1];
   }
   if (fam & FAM_LZ) {
     yout.qz[0] = t.qz[0][1];
     yout.qz[1] = t.qz[1][1];
+    xout.qz[0] = t.qz[1][0];
+    xout.qz[1] = t.qz[1][1];
   }
+  if (fam & FAM_AX) xout.tx = t.tx[1];
   if (fam & FAM_AY) yout.ty = t.ty[1];
   if (fam & FAM_AZ) zout.tz = t.tz[1];
 }

@@ -133,32 +133,70 @@ def _prm(lp, gn=4):
                 cg_factor=40, gn_iter=gn, lp=[lp] * 5, eps2=1e-9)
 
 
+def _rounding_floor(inv, prm, args, m1, rep1, t1, n=3):
+    """How far the single inversion itself moves when the data are perturbed at
+    the rounding level (4e-16 relative): relative change of the first-trial
+    misfit, of every trial misfit, of the final misfit and of the model (max
+    over n perturbations).  Where the CG stops at its iteration cap on a weakly
+    regularised system the iterates carry the rounding differences amplified
+    many orders of magnitude; a different summation order (block vs single
+    products) is a perturbation of the same kind."""
+    d0, w0 = inv.dobs.copy(), inv.wd.copy()
+    first = trials = final = model = 0.0
+    for s in range(n):
+        inv.set_dobs(d0 * (1 + 4e-16 * np.random.default_rng(100 + s).standard_normal(d0.size)), w0)
+        m, rep = inv.invert(prm, *args)
+        t = inv.trials()
+        first = max(first, abs(t[0, 2] / t1[0, 2] - 1))
+        if t.shape == t1.shape:
+            trials = max(trials, (np.abs(t[:, 2] / t1[:, 2] - 1)).max())
+        else:
+            trials = np.inf
+        final = max(final, abs(rep["final_misfit"] / rep1["final_misfit"] - 1))
+        model = max(model, np.linalg.norm(m - m1) / max(np.linalg.norm(m1), 1.0))
+    inv.set_dobs(d0, w0)
+    return first, trials, final, model
+
+
 @pytest.mark.parametrize("lp", [2, 1])
 def test_lambda_sweep_matches_fixed_lambda_inversions(gpu_ctx, lp):
     """Column c of the sweep is grada_invert with n_lambda = 1 and max_lambda =
     lambda_c.  The block and the single products sum in different orders
-    (1e-16); 40 CG iterations on the weakly regularised columns (lambda =
-    1e-3) grow that to ~1e-6 in the first trial, and L1 IRLS weights
-    ((Wm)^2 + 1e-9)^(-1/4) amplify it further in later Gauss-Newton
-    iterations, so later trials are compared loosely for p = 1."""
+    (1e-16 relative).  Where the CG converges the two agree to 1e-7; on the
+    weakly regularised column (lambda = 1e-3) the CG stops at its 40-step cap
+    and the difference is amplified like any rounding-level perturbation, so
+    there it is bounded by 20 times the single inversion's own spread under
+    data perturbed by 4e-16 (measured).  L1 IRLS weights ((Wm)^2 + 1e-9)^(-1/4)
+    amplify it further in later Gauss-Newton iterations, so later trials are
+    compared loosely for p = 1."""
     inv, rho = _inversion_problem(gpu_ctx, "fp64")
     nm = inv.Nm
     lam = np.logspace(-3, 1, 16)
     args = (np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0))
     models, reps = inv.lambda_sweep(_prm(lp), lam, *args)
+    cap = _prm(lp)["cg_factor"]
     for c in [0, 5, 10, 15]:
-        m1, rep1 = inv.invert(dict(_prm(lp), max_lambda=float(lam[c])), *args)
+        prm = dict(_prm(lp), max_lambda=float(lam[c]))
+        m1, rep1 = inv.invert(prm, *args)
         t1 = inv.trials()
         tb = inv.sweep_trials(c)
         np.testing.assert_allclose(tb[0, 1], t1[0, 1], rtol=0, atol=0)  # lambda
-        np.testing.assert_allclose(tb[0, 2], t1[0, 2], rtol=1e-5)       # first misfit
+        assert tb[0, 3] == t1[0, 3]  # CG iterations of the first trial
+        if t1[0, 3] < cap:
+            f_first, f_trials, f_final, f_model = 0.0, 0.0, 0.0, 0.0
+        else:
+            f_first, f_trials, f_final, f_model = _rounding_floor(inv, prm, args, m1, rep1, t1)
+            assert f_first < 1e-3  # the problem stays meaningful
+        np.testing.assert_allclose(tb[0, 2], t1[0, 2], rtol=max(1e-7, 20 * f_first))
         assert reps[c]["final_lambda"] == rep1["final_lambda"]
         if lp == 2:
             assert reps[c]["gn_iterations"] == rep1["gn_iterations"]
             assert tb.shape == t1.shape
-            np.testing.assert_allclose(tb[:, 2], t1[:, 2], rtol=1e-4)
-            assert abs(reps[c]["final_misfit"] - rep1["final_misfit"]) <= 1e-4 * rep1["final_misfit"]
-            assert np.linalg.norm(models[:, c] - m1) <= 1e-3 * max(np.linalg.norm(m1), 1.0)
+            np.testing.assert_allclose(tb[:, 2], t1[:, 2], rtol=max(1e-6, 20 * f_trials))
+            assert abs(reps[c]["final_misfit"] - rep1["final_misfit"]) <= \
+                max(1e-6, 20 * f_final) * rep1["final_misfit"]
+            assert np.linalg.norm(models[:, c] - m1) <= \
+                max(1e-5, 20 * f_model) * max(np.linalg.norm(m1), 1.0)
         else:
             assert abs(reps[c]["gn_iterations"] - rep1["gn_iterations"]) <= 1
             assert abs(reps[c]["final_misfit"] - rep1["final_misfit"]) <= 0.1 * rep1["final_misfit"]

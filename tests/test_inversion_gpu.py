@@ -138,7 +138,11 @@ def test_mixed_precision_inversion_close_to_fp64(gpu_ctx, storage, p, tol):
     (FP32) / 5 % (bf16) for L2.  L1 IRLS amplifies any perturbation of the
     CG iterates (weights up to eps^-1/2 ~ 180; the FP64 reference itself
     changes its trial sequence with the OpenMP thread count), so there the
-    bounds are 5 % / 10 %."""
+    bounds are 5 % / 10 %.  Every trial of this configuration stops its CG at
+    the 50-step cap, and near the target misfit the discrete lambda search
+    makes even the all-FP64 run move by ~1 % (model) and ~3 % (final misfit)
+    when the data are perturbed at the rounding level (4e-16 relative), so the
+    bounds are at least 3 times that measured spread."""
     prisms, obs, rho, n, mask, rng = _l2_problem(mask=0x072)
     inv = GaussNewtonInversion(prisms, obs, mask, ctx=gpu_ctx)
     inv.compute_G("fp64")
@@ -155,15 +159,24 @@ def test_mixed_precision_inversion_close_to_fp64(gpu_ctx, storage, p, tol):
     nm = inv.Nm
     args = (np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0))
     m64, rep64 = inv.invert(prm, *args)
+    f_model = f_misfit = 0.0  # spread of the FP64 run under rounding-level data perturbations
+    for s in range(2):
+        inv.set_dobs(dobs * (1 + 4e-16 * np.random.default_rng(200 + s).standard_normal(d.size)), wd)
+        mp, repp = inv.invert(prm, *args)
+        f_model = max(f_model, np.linalg.norm(mp - m64) / np.linalg.norm(m64))
+        f_misfit = max(f_misfit, abs(repp["final_misfit"] / rep64["final_misfit"] - 1))
+    inv.set_dobs(dobs, wd)
+    assert f_model < 0.05 and f_misfit < 0.1  # the comparison stays meaningful
     inv.compute_G(storage)
     mlp, replp = inv.invert(prm, *args, fp64_refinement=True)
     assert replp["fp64_refinements"] >= 1
     rel = np.linalg.norm(mlp - m64) / np.linalg.norm(m64)
-    assert rel < tol, rel
+    assert rel < max(tol, 3 * f_model), (rel, f_model)
     if p == 2:
-        assert abs(replp["final_misfit"] - rep64["final_misfit"]) <= 0.02 * rep64["final_misfit"]
+        assert abs(replp["final_misfit"] - rep64["final_misfit"]) <= \
+            max(0.02, 3 * f_misfit) * rep64["final_misfit"], f_misfit
     else:  # the perturbed L1 run may well end lower; it must not end higher
-        assert replp["final_misfit"] <= 1.05 * rep64["final_misfit"]
+        assert replp["final_misfit"] <= max(1.05, 1 + 3 * f_misfit) * rep64["final_misfit"]
 
 
 def test_inversion_error_paths(gpu_ctx):
