@@ -48,16 +48,24 @@ MASK = 0x3FE
 METRIC = "G entries/s"
 UNIT = "entries/s"
 
-# FP64 floating-point operations per (observation, cell) pair of the assembly
-# kernel for the nine-component flag, counted from its SASS instruction mix by
-# ncu (DFMA = 2, DADD/DMUL = 1) on a 1,024-point x 4,096-cell case; see
-# profiles/assemble_fp64_9comp.md.  Re-measured whenever the kernel changes.
+# Algorithmic FP64 work per (observation, cell) pair for the nine-component
+# flag, frozen once: the corner-grouped closed form evaluated cell by cell with
+# only the faces of a vertical column shared, counted by ncu (DFMA = 2,
+# DADD/DMUL = 1 from the executed-instruction counters) on a 1,024-point x
+# 4,096-cell case; see profiles/assemble_fp64_9comp.md.  roofline.achieved is
+# this figure x pairs/s.
 FP64_FLOPS_PER_PAIR = 767.4
+
+# FP64 work the current kernel executes per pair on the same case (faces shared
+# with the cells above, before in y and before in x; seeded reciprocal and
+# square root): 137.35 DFMA + 53.35 DADD + 122.19 DMUL.  Re-measured whenever the
+# kernel changes; reported beside the algorithmic figure.
+FP64_FLOPS_EXECUTED_PER_PAIR = 450.2
 
 # DRAM bytes (read + write) of one assembly launch on this workload, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of the full-size
 # launch; see profiles/assemble_fp64_9comp.md.  The algorithmic G write is 96.3 GB.
-ASSEMBLY_DRAM_BYTES_PER_LAUNCH = 4_772_644_608 + 98_347_602_688
+ASSEMBLY_DRAM_BYTES_PER_LAUNCH = 4_868_535_552 + 98_280_925_696
 
 
 def build_problem():
@@ -283,6 +291,12 @@ def run_gpu(args):
                     "traffic": ASSEMBLY_DRAM_BYTES_PER_LAUNCH,
                     "traffic_unit": "bytes per launch (ncu, full-size launch)",
                     "algorithmic_flops_per_pair": FP64_FLOPS_PER_PAIR,
+                    "executed_flops_per_pair": FP64_FLOPS_EXECUTED_PER_PAIR,
+                    "executed_tflops": FP64_FLOPS_EXECUTED_PER_PAIR * pairs / per_launch / 1e12,
+                    "executed_frac": FP64_FLOPS_EXECUTED_PER_PAIR * pairs / per_launch / fp64_peak,
+                    "note": "algorithmic work is the frozen per-cell figure; the kernel shares "
+                            "faces between neighbouring cells and executes less, so frac can "
+                            "exceed 1 while executed_frac stays below it",
                     "peak_source": "DFMA loop measured in this run (grada_measure_fp64_peak)"}
     else:
         roofline = {"bound": "fp64", "achieved": None, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
