@@ -439,6 +439,7 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16")):
         for st in storages:
             if st != "fp64":
                 out[st]["invert_speedup_vs_fp64"] = out["fp64"]["invert_s"] / out[st]["invert_s"]
+                out[st]["wall_speedup_vs_fp64"] = out["fp64"]["total_s"] / out[st]["total_s"]
     inv.ctx.close()
     return out
 
