@@ -392,9 +392,10 @@ def inversion_problem(name: str):
     return c, prisms, obs, rho, rel, absf, ops, rng
 
 
-def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16")):
+def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16", "fp32+fp64", "fp16+fp64")):
     """Inversion to chi^2 = N (misfit < 1) on the GPU: all-FP64 vs reduced-precision
-    G with one FP64 residual refinement per Gauss-Newton iteration."""
+    G with one FP64 residual refinement per Gauss-Newton iteration; "X+fp64" keeps
+    the FP64 G beside the X one and predicts every trial with it (grada_keep_fp64_G)."""
     import torch
 
     from graada3d_gb300 import regularization as reg
@@ -418,7 +419,7 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16")):
     for st in storages:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        inv.compute_G(st)
+        inv.compute_G(st.split("+")[0], keep_fp64=st.endswith("+fp64"))
         torch.cuda.synchronize()
         t_asm = time.perf_counter() - t0
         t0 = time.perf_counter()

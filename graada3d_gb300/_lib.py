@@ -74,6 +74,7 @@ SIGNATURES = {
     "grada_get_sweep_trials": (c_int, [c_void_p, c_int, _dp, c_int64, _ip64]),
     "grada_inject_fault": (c_int, [c_void_p, c_int]),
     "grada_refinement_indicator": (c_int, [c_void_p, _dp, _ip64, _ip64, _dp, _dp]),
+    "grada_keep_fp64_G": (c_int, [c_void_p, c_int]),
 }
 
 

@@ -124,6 +124,7 @@ void Context::set_geometry(const double *h_prisms, int64_t nc, const double *h_o
   // mesh/observation set and must be set again (InversionBase::set_mesh and
   // set_observation reinitialise them the same way).
   g_storage = -1;
+  g64_valid = false;
   data_set = false;
   for (auto &o : ops) o.set = false;
   for (auto &o : crg) o.set = false;
@@ -190,6 +191,17 @@ void Context::compute_G(int storage) {
   const DevGeometry g = geometry();
   const size_t n_entries = (size_t)ld * (size_t)n_cells;
   g_storage = -1;
+  g64_valid = false;
+  const bool derive = keep_fp64 && storage != GRADA_G_FP64 && storage != GRADA_G_MATRIX_FREE;
+  if (derive) {
+    // FP64 G kept; the reduced entries are rounded from it below, bitwise what
+    // the FP32 assembly writes (it rounds the same FP64 values at the store)
+    G64.alloc(this, n_entries * sizeof(double));
+    zero_padding_rows(G64.ptr, sizeof(double));
+    launch_assemble_tiled_fp64(g, tile_plan(), G64.as<double>(), ld, stream);
+  } else if (G64.ptr) {
+    G64.release();
+  }
   if (storage == GRADA_G_MATRIX_FREE) {
     // nothing to assemble: products re-evaluate the prisms (cfg-5-sized G
     // does not fit in HBM)
@@ -199,14 +211,21 @@ void Context::compute_G(int storage) {
     launch_assemble_tiled_fp64(g, tile_plan(), G.as<double>(), ld, stream);
   } else if (storage == GRADA_G_FP32) {
     G.alloc(this, n_entries * sizeof(float));
-    zero_padding_rows(G.ptr, sizeof(float));
-    launch_assemble_tiled_fp32(g, tile_plan(), G.as<float>(), ld, stream);
+    if (derive) {
+      launch_round_to_fp32(G64.as<double>(), G.as<float>(), n_entries, stream);
+    } else {
+      zero_padding_rows(G.ptr, sizeof(float));
+      launch_assemble_tiled_fp32(g, tile_plan(), G.as<float>(), ld, stream);
+    }
   } else {
     // FP32 staging copy; the quantiser reads its rows < nd and writes zero
     // padding rows itself
     DevBuf tmp;
     tmp.alloc(this, n_entries * sizeof(float));
-    launch_assemble_tiled_fp32(g, tile_plan(), tmp.as<float>(), ld, stream);
+    if (derive)
+      launch_round_to_fp32(G64.as<double>(), tmp.as<float>(), n_entries, stream);
+    else
+      launch_assemble_tiled_fp32(g, tile_plan(), tmp.as<float>(), ld, stream);
     G.alloc(this, n_entries * sizeof(uint16_t));
     row_scale.alloc(this, sizeof(float) * (size_t)nd);
     launch_rowscale_16(tmp.as<float>(), nd, n_cells, ld, row_scale.as<float>(),
@@ -214,6 +233,21 @@ void Context::compute_G(int storage) {
     sync();
   }
   g_storage = storage;
+  g64_valid = derive;
+}
+
+DevG Context::devG64() const {
+  DevG d;
+  d.kind = GKind::FP64;
+  d.data = G64.ptr;
+  d.nd = nd;
+  d.nm = n_cells;
+  d.ld = ld;
+  return d;
+}
+
+bool Context::fp64_resident() const {
+  return g64_valid && G64.ptr && g_storage != GRADA_G_FP64 && g_storage != GRADA_G_MATRIX_FREE;
 }
 
 int64_t Context::product_scratch_doubles() {
@@ -535,6 +569,10 @@ int grada_solve_cg(grada_ctx *ctx, double tol, int maxit, double lambda, const d
     if (err) *err = r.err;
     if (iterations) *iterations = r.iterations;
   });
+}
+
+int grada_keep_fp64_G(grada_ctx *ctx, int keep) {
+  return guarded(ctx, [&] { ctx->keep_fp64 = keep != 0; });
 }
 
 int grada_invert(grada_ctx *ctx, const grada_invert_params *params, const double *m_ini,

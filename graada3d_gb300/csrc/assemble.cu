@@ -193,6 +193,13 @@ __global__ void quantize_16_kernel(const float *__restrict__ G, int64_t nd, int6
                     : __bfloat16_as_ushort(__float2bfloat16_rn(v));
 }
 
+__global__ void round_to_fp32_kernel(const double *__restrict__ in, float *__restrict__ out,
+                                     size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
 // ---- matrix-free field sum ------------------------------------------------
 
 // One block: TL_THREADS points x the tiles of one split; each thread sums
@@ -547,6 +554,13 @@ void build_tile_plan(const double *p, int64_t n, std::vector<int32_t> &tiles,
       emit(order, 1);
     }
   }
+}
+
+void launch_round_to_fp32(const double *in, float *out, size_t n, cudaStream_t s) {
+  if (n == 0) return;
+  const size_t blocks = std::min<size_t>((n + 255) / 256, (size_t)65535 * 16);
+  round_to_fp32_kernel<<<(unsigned)blocks, 256, 0, s>>>(in, out, n);
+  GRADA_LAUNCH_CHECK();
 }
 
 void launch_assemble_tiled_fp64(const DevGeometry &g, const TilePlan &plan, double *G, int64_t ld,

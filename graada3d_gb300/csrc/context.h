@@ -86,6 +86,13 @@ struct Context {
   // Dense sensitivity matrix (Fwd::G), column-major, leading dimension ld.
   int g_storage = -1;
   DevBuf G, row_scale;
+  // FP64 G kept beside a reduced-precision G (grada_keep_fp64_G): the reduced
+  // entries are rounded from it, and while an inversion runs with
+  // predict_fp64 every data prediction (CG right-hand side, trial misfit) is
+  // an FP64 product with it instead of d64 + G_lp (m - m_start).
+  DevBuf G64;
+  bool keep_fp64 = false, g64_valid = false, predict_fp64 = false;
+  int64_t fp64_products = 0;
   // Tile plan of the cell list for the assembly (built from host_prisms).
   DevBuf plan_tiles, plan_cells;
   int64_t plan_n_tiles = 0;
@@ -153,6 +160,8 @@ struct Context {
   void sync();
   DevGeometry geometry() const;
   DevG devG() const;
+  DevG devG64() const;          // the kept FP64 G
+  bool fp64_resident() const;   // a kept FP64 G beside a reduced-precision G
   double *scratch_doubles(int64_t n);
   void require_G() const;
   void require_geometry() const;

@@ -126,7 +126,9 @@ void Context::expand_G(int64_t n_split, const int64_t *parent, const double *chi
     launch_assemble_fp32(g, d_kids.as<double>(), 8 * n_split, d_cols.as<int64_t>(), 0,
                          newG.as<float>(), ld, stream);
   sync();
-  // swap in the new matrix and cell list
+  // swap in the new matrix and cell list; a kept FP64 G no longer matches
+  g64_valid = false;
+  G64.release();
   std::swap(G.ptr, newG.ptr);
   std::swap(G.bytes, newG.bytes);
   n_cells = nm_new;

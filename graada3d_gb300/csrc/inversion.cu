@@ -45,6 +45,8 @@ void Context::release_all() {
   math_tables.release();
   G.release();
   row_scale.release();
+  G64.release();
+  g64_valid = false;
   scratch.release();
   vx.release();
   vy.release();
@@ -217,7 +219,11 @@ void Context::ensure_cg_workspace(int nterms) {
 // carries the increment).
 void Context::data_prediction(const double *m, const double *m_start, const double *d64,
                               double *out) {
-  if (d64) {
+  if (predict_fp64) {  // FP64 product with the kept FP64 G
+    launch_G_vec_mul(devG64(), m, out, scratch_doubles(gemv_scratch_doubles(devG64(), sm_count)),
+                     sm_count, stream);
+    fp64_products++;
+  } else if (d64) {
     double *dm = dptr(iv_tmp2);
     launch_sub(m, m_start, n_cells, dm, stream);
     G_vec_mul_dev(dm, out);
@@ -449,6 +455,15 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
   iv_flag.alloc(this, sizeof(int) * 4);
   const bool refine =
       prm.fp64_refinement && g_storage != GRADA_G_FP64 && g_storage != GRADA_G_MATRIX_FREE;
+  // with a kept FP64 G every prediction is an FP64 product instead
+  struct PredictGuard {
+    Context *c;
+    ~PredictGuard() { c->predict_fp64 = false; }
+  } predict_guard{this};
+  predict_fp64 = refine && fp64_resident();
+  fp64_products = 0;
+  if (predict_fp64) scratch_doubles(std::max(product_scratch_doubles(),
+                                             gemv_scratch_doubles(devG64(), sm_count)));
   if (refine) iv_d64.alloc(this, sizeof(double) * ld);
   ensure_cg_workspace(crg_enabled ? 7 : 4);
   upload(iv_m.ptr, m.data(), vb);
@@ -481,7 +496,7 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
     GRADA_CUDA_CHECK(cudaMemcpyAsync(mstart, mref_point, vb, cudaMemcpyDeviceToDevice, stream));
     rep.fp64_refinements++;
   };
-  if (refine) refresh_fp64(dm);
+  if (refine && !predict_fp64) refresh_fp64(dm);
 
   double misfit = misfit_of(dm, mstart, d64);
   double misfit_last_iteration = 5 * misfit;
@@ -509,7 +524,7 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
     int cg_maxit = 0;
     if (prm.cg_iteration_factor < 1) cg_maxit = (int)(prm.cg_iteration_factor * Nm);
     else cg_maxit = (int)prm.cg_iteration_factor;
-    if (refine && i > 0) refresh_fp64(dm);
+    if (refine && !predict_fp64 && i > 0) refresh_fp64(dm);
     launch_p_diag(dm, dmin, dmax, Nm, dP, stream);
     for (j = 0; j < prm.n_lambda; j++) {
       CgResult cg = solve_cg_dev(lambda, prm.cg_tol, cg_maxit, dm, dm0, dP, WL, ddx, d64, mstart);
@@ -577,6 +592,7 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
   rep.final_lambda = lambda;
   rep.gn_iterations = (int)iterations.size();
   rep.n_trials = (int)trials.size();
+  if (predict_fp64) rep.fp64_refinements = fp64_products;
 }
 
 }  // namespace grada

@@ -100,6 +100,10 @@ void launch_G_vec_mul(const DevG &G, const double *x, double *y, double *scratch
                       cudaStream_t s, const GemvOpts &o = GemvOpts());
 void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratch, int sm_count,
                        cudaStream_t s, const GemvOpts &o = GemvOpts());
+// out[i] = (float)in[i] for i < n (round to nearest: the entries the FP32
+// assembly writes from the same FP64 values).
+void launch_round_to_fp32(const double *in, float *out, size_t n, cudaStream_t s);
+
 // Columns [c0, c0+nc) of G widened to FP64 (scale applied for bf16) into
 // out (ld x nc, column-major).
 void launch_widen_columns(const DevG &G, int64_t c0, int64_t nc, double *out, cudaStream_t s);

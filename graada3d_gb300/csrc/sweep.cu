@@ -35,6 +35,7 @@ void Context::ensure_block_scratch(bool fp64_forward) {
     bytes = mf_block_scratch_doubles(geometry(), sm_count) * (int64_t)sizeof(double);
   if (g_storage != GRADA_G_MATRIX_FREE)
     bytes = std::max(bytes, block_scratch_bytes(devG(), sm_count));
+  if (fp64_resident()) bytes = std::max(bytes, block_scratch_bytes(devG64(), sm_count));
   bscratch.alloc(this, (size_t)std::max<int64_t>(bytes, 256));
   if (!tc_err.ptr) {
     tc_err.alloc(this, sizeof(int) * 4);
@@ -98,7 +99,11 @@ void Context::ensure_block_workspace(int nterms) {
 // out = G m (block) in the precision of G; with d64: d64 + G (m - m_start).
 void Context::block_prediction(const double *m, const double *m_start, const double *d64,
                                double *out) {
-  if (d64) {
+  if (predict_fp64) {  // FP64 block product with the kept FP64 G
+    launch_G_mat_mul(devG64(), m, out, bscratch.ptr, sm_count, stream, GemvOpts(),
+                     tc_err.as<int>());
+    fp64_products++;
+  } else if (d64) {
     double *dm = dptr(sw_tmp2);
     launch_sub(m, m_start, n_cells * kBW, dm, stream);
     apply_G_block(dm, out, GemvOpts());
@@ -405,6 +410,12 @@ void Context::lambda_sweep(const grada_invert_params &prm, int n, const double *
   }
   const bool refine =
       prm.fp64_refinement && g_storage != GRADA_G_FP64 && g_storage != GRADA_G_MATRIX_FREE;
+  // with a kept FP64 G every prediction is an FP64 block product instead
+  struct PredictGuard {
+    Context *c;
+    ~PredictGuard() { c->predict_fp64 = false; }
+  } predict_guard{this};
+  predict_fp64 = refine && fp64_resident();
   const size_t bb = sizeof(double) * kBW * Nm;
   DevBuf *blocks[] = {&sw_m, &sw_mt, &sw_mt_old, &sw_mopt, &sw_dx, &sw_P, &sw_tmp, &sw_tmp2};
   for (DevBuf *b : blocks) b->alloc(this, bb);
@@ -421,7 +432,7 @@ void Context::lambda_sweep(const grada_invert_params &prm, int n, const double *
   }
   const int nterms = crg_enabled ? 7 : 4;
   ensure_block_workspace(nterms);
-  ensure_block_scratch(refine);
+  ensure_block_scratch(refine && !predict_fp64);
   upload(sw_mmin.ptr, mmin.data(), sizeof(double) * Nm);
   upload(sw_mmax.ptr, mmax.data(), sizeof(double) * Nm);
   upload(sw_m0.ptr, m0.data(), sizeof(double) * Nm);
@@ -465,7 +476,8 @@ void Context::lambda_sweep(const grada_invert_params &prm, int n, const double *
       GRADA_CUDA_CHECK(cudaMemcpyAsync(mstart, dm, bb, cudaMemcpyDeviceToDevice, stream));
       for (int c = 0; c < nc; c++) rp[c].fp64_refinements++;
     };
-    if (refine) refresh_fp64();
+    fp64_products = 0;
+    if (refine && !predict_fp64) refresh_fp64();
     double misfit[kBW], mli[kBW], trial_misfit[kBW];
     block_misfits(dm, mstart, d64, misfit);
     uint32_t active = (1u << nc) - 1u;
@@ -474,7 +486,7 @@ void Context::lambda_sweep(const grada_invert_params &prm, int n, const double *
     else cg_maxit = (int)prm.cg_iteration_factor;
     for (int i = 0; i < prm.gn_iterations && active; i++) {
       for (int c = 0; c < nc; c++) mli[c] = misfit[c];
-      if (refine && i > 0) refresh_fp64();
+      if (refine && !predict_fp64 && i > 0) refresh_fp64();
       launch_bp_diag(dm, dptr(sw_mmin), dptr(sw_mmax), Nm, dP, stream);
       CgResult res[kBW];
       solve_cg_block_dev(lam, active, prm.cg_tol, cg_maxit, dm, dptr(sw_m0), dP, WL, ddx, d64,
@@ -528,6 +540,8 @@ void Context::lambda_sweep(const grada_invert_params &prm, int n, const double *
       }
       active = next;
     }
+    if (predict_fp64)
+      for (int c = 0; c < nc; c++) rp[c].fp64_refinements = fp64_products;
     launch_bunpack(dm, Nm, nc, dtmp, stream);
     download(h_m_out + (int64_t)g0 * Nm, dtmp, sizeof(double) * Nm * nc);
     sync();

@@ -146,8 +146,13 @@ class Fwd:
     def get_n_fields(self) -> int:
         return self.n_fields
 
-    def compute_G(self, storage: str | int = "fp64") -> None:
+    def compute_G(self, storage: str | int = "fp64", keep_fp64: bool = False) -> None:
+        """Fwd::compute_G in the given storage.  keep_fp64: with a reduced
+        storage also keep the FP64 G, from which the reduced entries are
+        rounded and which mixed-precision inversions then predict with
+        (grada_keep_fp64_G)."""
         s = STORAGE[storage] if isinstance(storage, str) else int(storage)
+        self.ctx.check(self.ctx.lib.grada_keep_fp64_G(self.ctx.handle, int(bool(keep_fp64))))
         self.ctx.check(self.ctx.lib.grada_compute_G(self.ctx.handle, s))
 
     def get_G(self) -> np.ndarray:

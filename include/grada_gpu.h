@@ -252,6 +252,20 @@ int grada_invert(grada_ctx *ctx, const grada_invert_params *params, const double
                  const double *m_min, const double *m_max, const double *m0, double *m_out,
                  grada_invert_report *report);
 
+/*
+ * Keep the FP64 G beside a reduced-precision one (no counterpart in the
+ * reference, which has only FP64 G).  With keep != 0, the next
+ * grada_compute_G with FP32 / bf16 / fp16 storage assembles G in FP64, keeps
+ * it, and rounds the reduced entries from it (bitwise those of the direct
+ * assembly).  grada_invert and grada_lambda_sweep with fp64_refinement then
+ * predict the data with FP64 products of the kept G (CG right-hand sides and
+ * every trial misfit exact in FP64; only the CG operator runs in reduced
+ * precision) instead of one matrix-free FP64 residual per Gauss-Newton
+ * iteration; report.fp64_refinements counts those products.  Costs the FP64
+ * G's memory; dropped by grada_expand_G and grada_set_geometry.
+ */
+int grada_keep_fp64_G(grada_ctx *ctx, int keep);
+
 /* The records of the last grada_invert: trials as rows of 5 doubles
  * (gn_iteration, lambda, misfit, cg_iterations, cg_error) -- lambda_misfit_GN,
  * GaussNewtonInversion.cpp:921-923 -- and iterations as rows of 3 doubles
