@@ -752,13 +752,15 @@ def block_products_summary():
     return out
 
 
-def run_lambda_sweep_16(n_lambda: int = 16, gn_iter: int = 5, storages=("fp64", "fp32", "bf16"),
-                   sequential: bool = True):
+def run_lambda_sweep_16(n_lambda: int = 16, gn_iter: int = 5,
+                        storages=("fp64", "fp32", "bf16", "fp32+fp64", "bf16+fp64"),
+                        sequential: bool = True):
     """A 16-value regularisation sweep (lambda
     log-spaced 1e-3 .. 1e1) on the shared gz + Tzz G of the assembly benchmark's geometry,
     each lambda a fixed-lambda Gauss-Newton run (L2, CG <= 50, up to gn_iter
     iterations), run as one block (block CG, tensor-core products) and, for
-    comparison, as 16 separate inversions."""
+    comparison, as 16 separate inversions.  "X+fp64" keeps the FP64 G beside the X
+    one and predicts with it (grada_keep_fp64_G)."""
     import torch
 
     from graada3d_gb300 import regularization as reg
@@ -782,7 +784,7 @@ def run_lambda_sweep_16(n_lambda: int = 16, gn_iter: int = 5, storages=("fp64", 
            "gn_iter_max": gn_iter}
     models = {}
     for st in storages:
-        inv.compute_G(st)
+        inv.compute_G(st.split("+")[0], keep_fp64=st.endswith("+fp64"))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         m, reps = inv.lambda_sweep(prm, lam, *args, fp64_refinement=(st != "fp64"))
@@ -928,7 +930,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-inversion", action="store_true")
     ap.add_argument("--no-block", action="store_true")
-    ap.add_argument("--sweep-storages", default="fp64,fp32,bf16")
+    ap.add_argument("--sweep-storages", default="fp64,fp32,bf16,fp32+fp64,bf16+fp64")
     ap.add_argument("--no-sequential", action="store_true")
     args = ap.parse_args()
     if args.case == "profile":
