@@ -200,12 +200,15 @@ def _params(prm: dict, fp64_refinement: bool) -> InvertParams:
     return p
 
 
-def compute_G_batch(invs, storage="fp64", max_threads: int = 0) -> None:
-    """grada_compute_G_batch over the contexts of several Fwd/GaussNewtonInversion objects."""
+def compute_G_batch(invs, storage="fp64", max_threads: int = 0, keep_fp64: bool = False) -> None:
+    """grada_compute_G_batch over the contexts of several Fwd/GaussNewtonInversion objects
+    (keep_fp64: as Fwd.compute_G)."""
     from .fwd import STORAGE
 
     lib = invs[0].ctx.lib
     n = len(invs)
+    for i in invs:
+        i.ctx.check(lib.grada_keep_fp64_G(i.ctx.handle, int(bool(keep_fp64))))
     ctxs = (ctypes.c_void_p * n)(*[i.ctx.handle.value for i in invs])
     st = (ctypes.c_int * n)()
     s = STORAGE[storage] if isinstance(storage, str) else int(storage)
