@@ -75,6 +75,7 @@ SIGNATURES = {
     "grada_inject_fault": (c_int, [c_void_p, c_int]),
     "grada_refinement_indicator": (c_int, [c_void_p, _dp, _ip64, _ip64, _dp, _dp]),
     "grada_keep_fp64_G": (c_int, [c_void_p, c_int]),
+    "grada_G_column_norms": (c_int, [c_void_p, _dp]),
 }
 
 

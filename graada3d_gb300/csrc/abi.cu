@@ -571,6 +571,20 @@ int grada_solve_cg(grada_ctx *ctx, double tol, int maxit, double lambda, const d
   });
 }
 
+int grada_G_column_norms(grada_ctx *ctx, double *norms) {
+  return guarded(ctx, [&] {
+    ctx->require_G();
+    if (!norms) throw grada::Error(GRADA_ERR_INVALID_ARGUMENT, "null output");
+    if (ctx->g_storage == GRADA_G_MATRIX_FREE)
+      throw grada::Error(GRADA_ERR_STATE, "column norms need a stored G (not matrix-free)");
+    grada::DevBuf d;
+    d.alloc(ctx, sizeof(double) * (size_t)ctx->n_cells);
+    grada::launch_column_norms(ctx->devG(), d.as<double>(), ctx->stream);
+    ctx->download(norms, d.ptr, sizeof(double) * (size_t)ctx->n_cells);
+    ctx->sync();
+  });
+}
+
 int grada_keep_fp64_G(grada_ctx *ctx, int keep) {
   return guarded(ctx, [&] { ctx->keep_fp64 = keep != 0; });
 }

@@ -337,4 +337,59 @@ void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratc
   GRADA_LAUNCH_CHECK();
 }
 
+// ---- column norms ---------------------------------------------------------------
+
+namespace {
+
+// norms[j] = ||G(:, j)||_2 of the stored entries (16-bit ones times their row
+// scale), one warp per column, squares summed in FP64 in a fixed order.
+template <class L>
+__global__ void __launch_bounds__(GV_THREADS)
+    column_norms_kernel(const void *__restrict__ G, const float *__restrict__ row_scale, int64_t nd,
+                        int64_t nm, int64_t ld, double *__restrict__ norms) {
+  const int64_t col = (int64_t)blockIdx.x * (GV_THREADS / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (col >= nm) return;
+  double s = 0.0;
+  for (int64_t r = (int64_t)lane * L::VEC; r < ld; r += 32 * L::VEC) {
+    typename L::Acc v[L::VEC];
+    L::load(G, col * ld + r, v);
+#pragma unroll
+    for (int k = 0; k < L::VEC; k++) {
+      double e = (double)v[k];
+      if (row_scale) e *= (r + k < nd) ? (double)row_scale[r + k] : 0.0;
+      s = fma(e, e, s);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) norms[col] = sqrt(s);
+}
+
+}  // namespace
+
+void launch_column_norms(const DevG &G, double *norms, cudaStream_t s) {
+  if (G.nm <= 0) return;
+  const unsigned blocks = (unsigned)ceil_div(G.nm, GV_THREADS / 32);
+  switch (G.kind) {
+    case GKind::FP64:
+      column_norms_kernel<LoadF64><<<blocks, GV_THREADS, 0, s>>>(G.data, nullptr, G.nd, G.nm, G.ld, norms);
+      break;
+    case GKind::FP32:
+      column_norms_kernel<LoadF32><<<blocks, GV_THREADS, 0, s>>>(G.data, nullptr, G.nd, G.nm, G.ld, norms);
+      break;
+    case GKind::BF16:
+      column_norms_kernel<LoadBF16><<<blocks, GV_THREADS, 0, s>>>(G.data, G.row_scale, G.nd, G.nm,
+                                                                   G.ld, norms);
+      break;
+    case GKind::FP16:
+      column_norms_kernel<LoadF16><<<blocks, GV_THREADS, 0, s>>>(G.data, G.row_scale, G.nd, G.nm,
+                                                                  G.ld, norms);
+      break;
+    default:
+      throw Error(-4, "column norms need a stored G");
+  }
+  GRADA_LAUNCH_CHECK();
+}
+
 }  // namespace grada

@@ -100,6 +100,10 @@ void launch_G_vec_mul(const DevG &G, const double *x, double *y, double *scratch
                       cudaStream_t s, const GemvOpts &o = GemvOpts());
 void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratch, int sm_count,
                        cudaStream_t s, const GemvOpts &o = GemvOpts());
+// norms[j] = ||G(:, j)||_2 of the stored entries (16-bit ones with their row
+// scale), FP64 sums; stored storages only.
+void launch_column_norms(const DevG &G, double *norms, cudaStream_t s);
+
 // out[i] = (float)in[i] for i < n (round to nearest: the entries the FP32
 // assembly writes from the same FP64 values).
 void launch_round_to_fp32(const double *in, float *out, size_t n, cudaStream_t s);

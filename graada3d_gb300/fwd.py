@@ -161,6 +161,13 @@ class Fwd:
         self.ctx.check(self.ctx.lib.grada_get_G(self.ctx.handle, _ptr(out), self.ld))
         return out[: self.Nd, :]
 
+    def G_column_norms(self) -> np.ndarray:
+        """||G(:, j)||_2 for every cell j (grada_G_column_norms), the quantity
+        InversionBase::set_depth_weighting(beta, 1) takes from G's columns."""
+        out = np.empty(self.Nm, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.grada_G_column_norms(self.ctx.handle, _ptr(out)))
+        return out
+
     def G_vec_mul(self, vec) -> np.ndarray:
         x = np.ascontiguousarray(vec, dtype=np.float64)
         if x.shape != (self.Nm,):

@@ -266,6 +266,15 @@ int grada_invert(grada_ctx *ctx, const grada_invert_params *params, const double
  */
 int grada_keep_fp64_G(grada_ctx *ctx, int keep);
 
+/*
+ * Column norms of the stored G: norms[j] = ||G(:, j)||_2 (Nm doubles, host),
+ * FP64 sums of the stored entries (16-bit ones times their row scale).  Serves
+ * InversionBase::set_depth_weighting with flag 1 (InversionBase.cpp:521-527,
+ * Z_ii = sqrt(||G(:, i)|| / Nd)) without copying G to the host.
+ * GRADA_ERR_STATE for matrix-free G.
+ */
+int grada_G_column_norms(grada_ctx *ctx, double *norms);
+
 /* The records of the last grada_invert: trials as rows of 5 doubles
  * (gn_iteration, lambda, misfit, cg_iterations, cg_error) -- lambda_misfit_GN,
  * GaussNewtonInversion.cpp:921-923 -- and iterations as rows of 3 doubles

@@ -221,3 +221,23 @@ def test_G_tile_plan_edge_cases(gpu_ctx, shape):
     y = rng.standard_normal(f.Nd)
     np.testing.assert_allclose(f.G_vec_mul(x), G @ x, rtol=0, atol=1e-12 * np.abs(G).sum(1).max())
     np.testing.assert_allclose(f.GT_vec_mul(y), G.T @ y, rtol=0, atol=1e-12 * np.abs(G).sum(0).max())
+
+
+@pytest.mark.parametrize("storage", ["fp64", "fp32", "bf16", "fp16", "matrix_free"])
+def test_G_column_norms(gpu_ctx, storage):
+    """||G(:, j)|| of the stored entries (the quantity of the reference's
+    set_depth_weighting with flag 1, Z_jj = sqrt(||G(:, j)|| / Nd)) against the
+    norms of the entries get_G returns."""
+    from graada3d_gb300 import GradaError
+    prisms, obs = _random_problem(8)
+    f = Fwd(prisms, obs, 0x3FE, ctx=gpu_ctx)
+    f.compute_G(storage)
+    if storage == "matrix_free":
+        with pytest.raises(GradaError):
+            f.G_column_norms()
+        return
+    norms = f.G_column_norms()
+    np.testing.assert_allclose(norms, np.linalg.norm(f.get_G(), axis=0), rtol=1e-13, atol=0)
+    if storage == "fp64":
+        want = np.sqrt(np.linalg.norm(prism.compute_G(prisms, obs, 0x3FE), axis=0) / f.Nd)
+        np.testing.assert_allclose(np.sqrt(norms / f.Nd), want, rtol=1e-10)
