@@ -424,7 +424,7 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
     throw Error(GRADA_ERR_INVALID_ARGUMENT, "null model vector");
   if (prm.n_lambda < 1 || prm.gn_iterations < 1)
     throw Error(GRADA_ERR_INVALID_ARGUMENT, "n_lambda and gn_iterations must be >= 1");
-  const int64_t Nm = n_cells, Nd = nd;
+  const int64_t Nm = n_cells;
   std::memset(&rep, 0, sizeof(rep));
   trials.clear();
   iterations.clear();

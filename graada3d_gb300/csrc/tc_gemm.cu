@@ -476,7 +476,9 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
     // slot in the K-major 128B-swizzled layout (row m of 128 B holds k =
     // 0..31; 16-byte chunk j of row m at chunk j ^ (m & 7)); the MMAs read the
     // right-hand-side tile from the TMA stage, which their commit frees.
-    constexpr int NCT = 32 * C::NCONV_WARPS;
+    // (16-bit instantiations have no split warps and never get here; the
+    // floor of TC_M keeps their compile-time arithmetic defined)
+    constexpr int NCT = C::NCONV_WARPS > 0 ? 32 * C::NCONV_WARPS : TC_M;
     const int ct = threadIdx.x - 64;  // 0..NCT-1
     uint32_t it = 0;
     bool ok = true;
