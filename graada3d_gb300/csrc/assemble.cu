@@ -354,9 +354,9 @@ __global__ void sum_cell_splits_kernel(const double *__restrict__ partial, int n
 }  // namespace
 
 void build_math_tables(double *tab) {
-  // log bins: c_k ~ 1/(0.75 + k/128), ln(1/c_k) as a hi/lo pair
+  // log bins: c_k ~ 1/(0.75 + k/256), ln(1/c_k) as a hi/lo pair
   for (int k = 0; k < kLogBins; k++) {
-    const double c = (k == 32) ? 1.0 : 1.0 / (0.75 + k / 128.0);
+    const double c = (k == 64) ? 1.0 : 1.0 / (0.75 + k / 256.0);
     const long double L = -logl((long double)c);
     const double hi = (double)L;
     tab[kTabLog + 3 * k] = c;
@@ -364,8 +364,8 @@ void build_math_tables(double *tab) {
     tab[kTabLog + 3 * k + 2] = (double)(L - (long double)hi);
   }
   const long double pi = acosl(-1.0L);
-  for (int j = 0; j < 128; j++) {
-    const long double th = pi * (long double)j / 64.0L;
+  for (int j = 0; j < kRotSteps; j++) {
+    const long double th = pi * (long double)j / 128.0L;
     tab[kTabSinCos + 2 * j] = (double)cosl(th);
     tab[kTabSinCos + 2 * j + 1] = (double)sinl(th);
   }
@@ -382,10 +382,10 @@ void build_math_tables(double *tab) {
   const double ln2_hi = clear_low((double)ln2, 11);
   tab[kTabConst + 0] = ln2_hi;
   tab[kTabConst + 1] = (double)(ln2 - (long double)ln2_hi);
-  const long double pi64 = pi / 64.0L;
-  const double pi64_hi = clear_low((double)pi64, 9);
-  tab[kTabConst + 2] = pi64_hi;
-  tab[kTabConst + 3] = (double)(pi64 - (long double)pi64_hi);
+  const long double step = pi / 128.0L;
+  const double step_hi = clear_low((double)step, 9);
+  tab[kTabConst + 2] = step_hi;
+  tab[kTabConst + 3] = (double)(step - (long double)step_hi);
 }
 
 int adjoint_field_splits(const DevGeometry &g, int sm_count) {

@@ -82,27 +82,28 @@ __host__ __device__ inline uint32_t families_for_mask(uint32_t m) {
 // to spend FP64 instructions only where FP64 accuracy is needed:
 //  * log: table-driven reduction (P. T. P. Tang, "Table-driven implementation
 //    of the logarithm function in IEEE floating-point arithmetic", ACM TOMS
-//    16(4), 1990): q = 2^e m, m in [0.75, 1.5); the table entry c_k is near
-//    1/m (97 bins of width 1/128 centred on 0.75 + k/128; the bin of 1.0 has
-//    c = 1 exactly), so t = m c_k - 1 is one FMA, |t| < 0.0053, and
+//    16(4), 1990): q = 2^e m, m in [0.75, 1.5]; the table entry c_k is near
+//    1/m (193 bins of width 1/256 centred on 0.75 + k/256; the bin of 1.0 has
+//    c = 1 exactly), so t = m c_k - 1 is one FMA, |t| < 0.0027, and
 //    ln q = e ln2 + ln(1/c_k) + ln(1+t) with the Taylor series of ln(1+t) to
-//    t^7 (truncation < 1.3e-17 relative).  ln2 and ln(1/c_k) carry a low
+//    t^6 (truncation below 4.5e-17 relative).  ln2 and ln(1/c_k) carry a low
 //    part, so q near 1 keeps full relative accuracy.  The exponent and bin
 //    come from integer operations on the bits.
 //  * face angle sums: the FP32 estimate of the sum (which is needed anyway
-//    for the 2*pi branch) picks theta_j = j*pi/64 nearest to it; the FP64
+//    for the 2*pi branch) picks theta_j = j*pi/128 nearest to it; the FP64
 //    complex product is rotated by -theta_j (cos/sin table), leaving an
-//    argument below pi/128 + 1e-6 whose arctangent is a short odd series
-//    (to delta^9; the first term left out, delta^11/11, is below 7.5e-18 of
+//    argument below pi/256 + 1e-6 whose arctangent is a short odd series
+//    (to delta^7; the first term left out, delta^9/9, is below 5.4e-17 of
 //    delta).  Sum = theta_j + atan(delta).
 // The tables are built once per context on the host in extended precision
 // (build_math_tables) and staged into shared memory by each block.
 // ---------------------------------------------------------------------------
 
-constexpr int kLogBins = 97;                    // k = 0..96, centres 0.75 + k/128
+constexpr int kLogBins = 193;                   // k = 0..192, centres 0.75 + k/256
 constexpr int kTabLog = 0;                      // [c, ln(1/c) hi, ln(1/c) lo] x 97
-constexpr int kTabSinCos = kTabLog + 3 * kLogBins;  // [cos, sin] of j*pi/64, j = 0..127
-constexpr int kTabConst = kTabSinCos + 2 * 128; // ln2 hi/lo, pi/64 hi/lo
+constexpr int kRotSteps = 256;                  // table angles j*pi/128, j = 0..255
+constexpr int kTabSinCos = kTabLog + 3 * kLogBins;  // [cos, sin] of j*pi/128
+constexpr int kTabConst = kTabSinCos + 2 * kRotSteps;  // ln2 hi/lo, pi/128 hi/lo
 constexpr int kTabSize = kTabConst + 4;
 
 // Fills `tab` (kTabSize doubles).  Host only.
@@ -161,17 +162,16 @@ __device__ __forceinline__ double fast_log(double q, const double *__restrict__ 
   if (f >= (1ll << 51)) {  // m_raw >= 1.5: halve into [0.75, 1)
     mbits = (1022ll << 52) | f;
     e += 1;
-    k = (int)((f + (1ll << 45)) >> 46) - 32;
+    k = (int)((f + (1ll << 44)) >> 45) - 64;
   } else {
     mbits = (1023ll << 52) | f;
-    k = 32 + (int)((f + (1ll << 44)) >> 45);
+    k = 64 + (int)((f + (1ll << 43)) >> 44);
   }
   const double m = __longlong_as_double(mbits);
   const double *L = tab + kTabLog + 3 * k;
   const double t = fma(m, L[0], -1.0);
   const double t2 = t * t;
-  double p = 1.0 / 7.0;
-  p = fma(p, t, -1.0 / 6.0);
+  double p = -1.0 / 6.0;
   p = fma(p, t, 1.0 / 5.0);
   p = fma(p, t, -1.0 / 4.0);
   p = fma(p, t, 1.0 / 3.0);
@@ -283,15 +283,14 @@ __device__ __forceinline__ double face_atan_sum(const double (&a)[4], const doub
   const double re3 = fma(re2, A[3], -im2 * B[3]);
   const double im3 = fma(re2, B[3], im2 * A[3]);
   // rotate by -j*pi/64, j nearest to the FP32 estimate of the sum
-  const int j = __float2int_rn(est * 20.371832715762604f);  // 64/pi
-  const double *cs = tab + kTabSinCos + 2 * (j & 127);
+  const int j = __float2int_rn(est * 40.743665431525208f);  // 128/pi
+  const double *cs = tab + kTabSinCos + 2 * (j & (kRotSteps - 1));
   const double c = cs[0], s = cs[1];
   const double xr = fma(re3, c, im3 * s);
   const double yr = fma(im3, c, -re3 * s);
   const double d = yr * fast_rcp(xr);
   const double d2 = d * d;
-  double p = 1.0 / 9.0;
-  p = fma(p, d2, -1.0 / 7.0);
+  double p = -1.0 / 7.0;
   p = fma(p, d2, 1.0 / 5.0);
   p = fma(p, d2, -1.0 / 3.0);
   const double at = fma(d * d2, p, d);
