@@ -437,18 +437,44 @@ void build_tile_plan(const double *p, int64_t n, std::vector<int32_t> &tiles,
                      std::vector<int64_t> &cells) {
   tiles.clear();
   cells.clear();
-  // cells ordered by (x0, x1, y0, y1, z0): the stacks of a column become adjacent
-  std::vector<int64_t> ord(n);
-  for (int64_t i = 0; i < n; i++) ord[i] = i;
-  std::sort(ord.begin(), ord.end(), [p](int64_t a, int64_t b) {
+  // cells ordered by (x0, x1, y0, y1, z0): the stacks of a column become
+  // adjacent.  A regular mesh in the reference's leaf order (x outer, y, z
+  // inner) is already in this order, which one linear pass detects; otherwise
+  // the keys are copied into one contiguous array and sorted.
+  auto cell_less = [p](int64_t a, int64_t b) {
     const double *u = p + 6 * a, *v = p + 6 * b;
-    for (int q : {0, 1, 2, 3, 4})
+    for (int q = 0; q < 5; q++)
       if (u[q] != v[q]) return u[q] < v[q];
     return a < b;
-  });
-  // z-runs: equal x/y extents, each z0 the previous z1
+  };
+  std::vector<int64_t> ord((size_t)n);
+  bool sorted = true;
+  for (int64_t i = 0; i < n; i++) {
+    ord[(size_t)i] = i;
+    if (i > 0 && sorted && cell_less(i, i - 1)) sorted = false;
+  }
+  if (!sorted) {
+    struct CellKey {
+      double k[5];
+      int64_t id;
+    };
+    std::vector<CellKey> keys((size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+      for (int q = 0; q < 5; q++) keys[(size_t)i].k[q] = p[6 * i + q];
+      keys[(size_t)i].id = i;
+    }
+    std::sort(keys.begin(), keys.end(), [](const CellKey &a, const CellKey &b) {
+      for (int q = 0; q < 5; q++)
+        if (a.k[q] != b.k[q]) return a.k[q] < b.k[q];
+      return a.id < b.id;
+    });
+    for (int64_t i = 0; i < n; i++) ord[(size_t)i] = keys[(size_t)i].id;
+  }
+  // z-runs: equal x/y extents, each z0 the previous z1; sig is a hash of the
+  // run's levels (its z0 sequence and last z1) that orders runs cheaply
   struct Run {
     int64_t start, len;
+    uint64_t sig;
   };
   std::vector<Run> runs;
   for (int64_t c = 0; c < n;) {
@@ -458,34 +484,44 @@ void build_tile_plan(const double *p, int64_t n, std::vector<int32_t> &tiles,
       if (!(u[0] == v[0] && u[1] == v[1] && u[2] == v[2] && u[3] == v[3] && u[5] == v[4])) break;
       e++;
     }
-    runs.push_back({c, e - c + 1});
+    uint64_t h = 0x9E3779B97F4A7C15ull;  // multiply-xorshift over the boundaries' bits
+    auto mix = [&h](double z) {
+      uint64_t b;
+      memcpy(&b, &z, 8);
+      h = (h ^ b) * 0xBF58476D1CE4E5B9ull;
+      h ^= h >> 31;
+    };
+    for (int64_t k = c; k <= e; k++) mix(p[6 * ord[k] + 4]);
+    mix(p[6 * ord[e] + 5]);
+    runs.push_back({c, e - c + 1, h});
     c = e + 1;
   }
   // runs ordered by (x0, x1, levels, y0): y-neighbours with identical levels
-  // become adjacent
+  // become adjacent (equal levels share count and signature)
   auto cell_of = [&](const Run &r, int64_t k) { return p + 6 * ord[r.start + k]; };
-  auto level_cmp = [&](const Run &a, const Run &b) -> int {
-    if (a.len != b.len) return a.len < b.len ? -1 : 1;
-    for (int64_t k = 0; k < a.len; k++) {
-      const double za = cell_of(a, k)[4], zb = cell_of(b, k)[4];
-      if (za != zb) return za < zb ? -1 : 1;
-    }
-    const double za = cell_of(a, a.len - 1)[5], zb = cell_of(b, b.len - 1)[5];
-    if (za != zb) return za < zb ? -1 : 1;
-    return 0;
+  // equal level sequences: count and signature as a quick reject, then the
+  // levels themselves
+  auto level_eq = [&](const Run &a, const Run &b) -> bool {
+    if (a.len != b.len || a.sig != b.sig) return false;
+    for (int64_t k = 0; k < a.len; k++)
+      if (cell_of(a, k)[4] != cell_of(b, k)[4]) return false;
+    return cell_of(a, a.len - 1)[5] == cell_of(b, b.len - 1)[5];
   };
+  // (the sort uses the level count and signature only: runs with equal levels
+  // stay adjacent, and a signature collision could at most split a chain,
+  // since ynext and the x partners compare the levels themselves)
   std::sort(runs.begin(), runs.end(), [&](const Run &a, const Run &b) {
     const double *u = cell_of(a, 0), *v = cell_of(b, 0);
     if (u[0] != v[0]) return u[0] < v[0];
     if (u[1] != v[1]) return u[1] < v[1];
-    const int c = level_cmp(a, b);
-    if (c != 0) return c < 0;
+    if (a.len != b.len) return a.len < b.len;
+    if (a.sig != b.sig) return a.sig < b.sig;
     if (u[2] != v[2]) return u[2] < v[2];
     return a.start < b.start;
   });
   auto ynext = [&](const Run &a, const Run &b) {
     const double *u = cell_of(a, 0), *v = cell_of(b, 0);
-    return u[0] == v[0] && u[1] == v[1] && u[3] == v[2] && level_cmp(a, b) == 0;
+    return u[0] == v[0] && u[1] == v[1] && u[3] == v[2] && level_eq(a, b);
   };
   // x partner of a run: the run whose x0 is its x1, with the same y extent and
   // levels (candidates looked up by x0, y0, y1, level count and first z0)
@@ -501,7 +537,7 @@ void build_tile_plan(const double *p, int64_t n, std::vector<int32_t> &tiles,
     auto it = by_face.find(Key(u[1], u[2], u[3], runs[r].len, u[4]));
     if (it == by_face.end()) return -1;
     for (size_t q : it->second)
-      if (!used[q] && level_cmp(runs[r], runs[q]) == 0) return (int64_t)q;
+      if (!used[q] && level_eq(runs[r], runs[q])) return (int64_t)q;
     return -1;
   };
   auto emit = [&](const std::vector<size_t> &order, int nx) {
@@ -517,6 +553,8 @@ void build_tile_plan(const double *p, int64_t n, std::vector<int32_t> &tiles,
         for (int64_t k = 0; k < nl; k++) cells.push_back(ord[runs[q].start + l0 + k]);
     }
   };
+  tiles.reserve(4 * (size_t)(n / TL_MAXLEV + runs.size()) + 4);
+  cells.reserve((size_t)n);
   // Greedy in (x0, x1, levels, y0) order: a run with an x partner starts a
   // 2 x m tile (m <= TL_COLS/2 y-neighbours, each with its partner, run order
   // y-major, x-minor); one without starts a 1 x m tile (m <= TL_COLS) that
