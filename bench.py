@@ -363,6 +363,12 @@ INVERSION_CASES = {
     "l1_196k": dict(cells=(64, 64, 48), domain=(10000.0, 10000.0, 5000.0), obs=(101, 101),
                  height=100.0, mask=0x072, lp=[1, 1, 1, 1, 2], eps2=1e-10, boxes="dykes",
                  gn_iter=10),
+    # the same L1 problem on the 32 x 32 x 16 base refined 3 levels at the dyke boundaries
+    # with the reference's face-balance cascade (236,226 leaves), operators from the
+    # leaves' geometry
+    "l1_refined": dict(cells="dyke_refined", domain=(10000.0, 10000.0, 5000.0), obs=(101, 101),
+                       height=100.0, mask=0x072, lp=[1, 1, 1, 1, 2], eps2=1e-10, boxes="dykes",
+                       gn_iter=10),
 }
 
 
@@ -371,9 +377,12 @@ def inversion_problem(name: str):
     from graada3d_gb300 import regularization as reg
 
     c = INVERSION_CASES[name]
-    nx, ny, nz = c["cells"]
     Lx, Ly, Lz = c["domain"]
-    prisms = mesh.regular_mesh((0.0, Lx), nx, (0.0, Ly), ny, (0.0, Lz), nz)
+    if c["cells"] == "dyke_refined":
+        prisms = refined_dyke_mesh(3)
+    else:
+        nx, ny, nz = c["cells"]
+        prisms = mesh.regular_mesh((0.0, Lx), nx, (0.0, Ly), ny, (0.0, Lz), nz)
     obs = mesh.observation_grid(c["obs"][0], 0.0, Lx, c["obs"][1], 0.0, Ly, -c["height"])
     rng = np.random.default_rng(1 if c["boxes"] == "two_boxes" else 4)
     if c["boxes"] == "two_boxes":
@@ -389,7 +398,10 @@ def inversion_problem(name: str):
     nf = bin(c["mask"]).count("1")
     rel = [0.02] * nf
     absf = [1e-3 if (c["mask"] & 2) and k == 0 else 1e-2 for k in range(nf)]
-    ops = reg.regular_mesh_operators((nx, ny, nz), prisms, obs, 1.5)
+    if c["cells"] == "dyke_refined":
+        ops = reg.mesh_operators(prisms, obs, 1.5)
+    else:
+        ops = reg.regular_mesh_operators((nx, ny, nz), prisms, obs, 1.5)
     return c, prisms, obs, rho, rel, absf, ops, rng
 
 
@@ -847,39 +859,33 @@ def run_mf_profile():
     f.ctx.close()
 
 
+DYKES = [[2500, 3500, 1000, 9000, 500, 3500], [6000, 7000, 1000, 9000, 500, 3500]]
+
+
 def refined_dyke_mesh(levels: int = 3):
     """32 x 32 x 16 cells over [0, 10 km]^2 x [0, 5 km], refined `levels` times at the
-    cells that cross the boundary of two +400 kg/m^3 dykes (split at the centre,
-    children x outer, y, z inner, in place of the parent: the leaf order of
-    Mesh::refinement + rearrange_id).  Three levels give 190,012 leaves."""
+    leaves that cross the boundary of one of two +400 kg/m^3 dykes, with the
+    reference's face-balance cascade and leaf order (mesh.Octree, Mesh::refinement
+    + rearrange_id).  Three levels give 236,226 leaves."""
     from graada3d_gb300 import mesh
-    from graada3d_gb300.fwd import split_cells
 
-    cells = mesh.regular_mesh((0.0, 10000.0), 32, (0.0, 10000.0), 32, (0.0, 5000.0), 16)
-    dykes = [[2500, 3500, 1000, 9000, 500, 3500], [6000, 7000, 1000, 9000, 500, 3500]]
+    o = mesh.Octree.regular((0.0, 10000.0), 32, (0.0, 10000.0), 32, (0.0, 5000.0), 16)
     for _ in range(levels):
+        cells = o.leaves()
         mark = np.zeros(len(cells), bool)
-        for b in dykes:
+        for b in DYKES:
             inter = ((cells[:, 0] < b[1]) & (cells[:, 1] > b[0]) & (cells[:, 2] < b[3]) &
                      (cells[:, 3] > b[2]) & (cells[:, 4] < b[5]) & (cells[:, 5] > b[4]))
             inside = ((cells[:, 0] >= b[0]) & (cells[:, 1] <= b[1]) & (cells[:, 2] >= b[2]) &
                       (cells[:, 3] <= b[3]) & (cells[:, 4] >= b[4]) & (cells[:, 5] <= b[5]))
             mark |= inter & ~inside
-        idx = np.nonzero(mark)[0]
-        kids = split_cells(cells[idx])
-        parts, prev = [], 0
-        for k, j in enumerate(idx):
-            parts.append(cells[prev:j])
-            parts.append(kids[k].reshape(8, 6))
-            prev = j + 1
-        parts.append(cells[prev:])
-        cells = np.vstack(parts)
-    return cells
+        o.refine(np.nonzero(mark)[0])
+    return o.leaves()
 
 
 def run_assembly_refined():
     """FP64 assembly of gz, Tzz, Txz, Tyz at 101 x 101 points 100 m above
-    [0, 10 km]^2 on the adaptively refined 190,012-leaf dyke mesh and on the
+    [0, 10 km]^2 on the adaptively refined 236,226-leaf dyke mesh and on the
     uniform 196,608-cell (64 x 64 x 48) mesh over the same domain: 3 warm-up and
     5 timed assemblies each (CUDA events).  On the refined mesh fewer cells
     share faces with a neighbour run in the assembly tiles."""
@@ -935,7 +941,8 @@ def run_profile_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-l2-16k",
-                                                         "inversion-l1-196k", "matrix-free-1m",
+                                                         "inversion-l1-196k", "inversion-l1-refined",
+                                                         "matrix-free-1m",
                                                          "gemv", "batched-64", "block-gemm",
                                                          "lambda-sweep-16", "block-gemm-profile",
                                                          "mf-profile", "assembly-refined"])

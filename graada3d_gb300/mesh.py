@@ -12,6 +12,8 @@ reference would produce.
   cell takes a box's value when it lies entirely inside the box (1e-10
   tolerance); later boxes overwrite earlier ones.
 * ``observation_grid`` -- Observation::generate, Observation.cpp:48-77
+* ``Octree`` -- Mesh::refinement, Mesh.cpp:1462-1942: octant splits kept
+  face-balanced, leaves in the reference's leaf order.
   (x fastest).
 """
 from __future__ import annotations
@@ -80,3 +82,117 @@ def observation_grid(nx, x0, x1, ny, y0, y1, z0) -> np.ndarray:
         ys = (y1 - y0) / (ny - 1)
     iy, ix = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
     return np.stack([x0 + ix.ravel() * xs, y0 + iy.ravel() * ys, np.full(nx * ny, float(z0))], 1)
+
+
+def _halves(lo: float, hi: float, bit: int):
+    mid = 0.5 * (hi + lo)  # RectPrism::get_center, RectPrism.cpp:45-50
+    return (lo, mid) if bit == 0 else (mid, hi)
+
+
+class Octree:
+    """A regular base mesh refined by splitting leaf cells into octants the way
+    Mesh::refinement does it (Mesh.cpp:1462-1942).
+
+    * Face balance (Mesh.cpp:1474-1551): before a cell of level L splits, each
+      face neighbour of level L - 1 is split first, recursively, so that cells
+      sharing a face differ by one level at most.  Boundary faces impose
+      nothing.  The set of leaves this gives does not depend on the order of
+      the cascaded splits: it is the smallest face-balanced refinement that
+      splits every requested cell.
+    * Children (Mesh.cpp:1562-1600): split at the centre 0.5 (hi + lo), x
+      outermost, then y, z innermost.
+    * Leaf order (Mesh.cpp:830-847 for the base, 1930-1942 for a split): the
+      base cells x outermost, z innermost, each split cell replaced in place
+      by its eight children, i.e. a depth-first walk.
+
+    Cells are keyed (level, i, j, k) with i, j, k indices on the level's grid
+    of (nx, ny, nz) * 2**level cells.
+    """
+
+    def __init__(self, xs, ys, zs):
+        self.pts = [np.asarray(v, dtype=np.float64) for v in (xs, ys, zs)]
+        self.n = tuple(len(v) - 1 for v in self.pts)
+        self.split_cells: set = set()
+        self._bounds: dict = {}
+        self._leaves = None
+
+    @classmethod
+    def regular(cls, xlim, nx, ylim, ny, zlim, nz) -> "Octree":
+        return cls(*regular_mesh_points(xlim, nx, ylim, ny, zlim, nz))
+
+    def bounds(self, key) -> tuple:
+        """x0 x1 y0 y1 z0 z1 of a cell."""
+        L, i, j, k = key
+        if L == 0:
+            xs, ys, zs = self.pts
+            return (xs[i], xs[i + 1], ys[j], ys[j + 1], zs[k], zs[k + 1])
+        b = self._bounds.get(key)
+        if b is None:
+            p = self.bounds((L - 1, i >> 1, j >> 1, k >> 1))
+            b = (*_halves(p[0], p[1], i & 1), *_halves(p[2], p[3], j & 1),
+                 *_halves(p[4], p[5], k & 1))
+            self._bounds[key] = b
+        return b
+
+    def exists(self, key) -> bool:
+        L, i, j, k = key
+        if L == 0:
+            return 0 <= i < self.n[0] and 0 <= j < self.n[1] and 0 <= k < self.n[2]
+        return (L - 1, i >> 1, j >> 1, k >> 1) in self.split_cells
+
+    def is_leaf(self, key) -> bool:
+        return self.exists(key) and key not in self.split_cells
+
+    def _split(self, key) -> None:
+        L, i, j, k = key
+        if L > 0:
+            for a in range(3):
+                for step in (-1, 1):
+                    c = [i, j, k]
+                    c[a] += step
+                    if not 0 <= c[a] < (self.n[a] << L):
+                        continue  # boundary face
+                    nb = (L, c[0], c[1], c[2])
+                    if not self.exists(nb):
+                        coarse = (L - 1, c[0] >> 1, c[1] >> 1, c[2] >> 1)
+                        if self.is_leaf(coarse):
+                            self._split(coarse)
+        self.split_cells.add(key)
+        self._leaves = None
+
+    def refine(self, leaf_indices) -> int:
+        """Split the given leaves (indices into the current ``leaf_keys()``),
+        skipping those a cascade already split; returns the number of splits."""
+        keys = self.leaf_keys()
+        before = len(self.split_cells)
+        for t in sorted(int(v) for v in np.asarray(leaf_indices).ravel()):
+            if self.is_leaf(keys[t]):
+                self._split(keys[t])
+        return len(self.split_cells) - before
+
+    def leaf_keys(self) -> list:
+        if self._leaves is None:
+            out = []
+            nx, ny, nz = self.n
+            for i in range(nx):
+                for j in range(ny):
+                    for k in range(nz):
+                        stack = [(0, i, j, k)]
+                        while stack:
+                            key = stack.pop()
+                            if key in self.split_cells:
+                                L, a, b, c = key
+                                for o in range(7, -1, -1):
+                                    stack.append((L + 1, 2 * a + (o >> 2), 2 * b + ((o >> 1) & 1),
+                                                  2 * c + (o & 1)))
+                            else:
+                                out.append(key)
+            self._leaves = out
+        return self._leaves
+
+    def leaves(self) -> np.ndarray:
+        """(n, 6) leaf cells x0 x1 y0 y1 z0 z1 in leaf order."""
+        return np.array([self.bounds(k) for k in self.leaf_keys()], dtype=np.float64).reshape(-1, 6)
+
+    def levels(self) -> np.ndarray:
+        return np.array([k[0] for k in self.leaf_keys()], dtype=np.int64)

@@ -13,6 +13,9 @@ classes:
 * D_s = I; D_x1, D_y1, D_z1: forward difference to the +axis neighbour,
   backward difference for the last cell of a line, no row if the axis has
   one cell (z only)                        InversionBase::set_difference_matrix, :189-434
+  On a refined (face-balanced) mesh the neighbour across a face is a cell of
+  the same size, a coarser cell, or four finer cells that each take a
+  quarter of the off-diagonal weight (``difference_matrices``).
 * W_* = a_* S_* V D_* Z with S_* = I      GaussNewtonInversion.cpp:711-714
 * T_z = V (diag(D_y m0s) D_x - diag(D_x m0s) D_y), T_x, T_y cyclic
                                            InversionBase::set_Tmatrix, :468-495
@@ -51,19 +54,149 @@ def _difference(nx: int, ny: int, nz: int, sizes: np.ndarray, axis: int) -> sp.c
     return D
 
 
-def regular_mesh_operators(n, prisms, obs, beta: float, a_s=1.0, a_z=1.0, a_x=1.0, a_y=1.0):
-    """Ws, Wx, Wy, Wz (CSR) plus V, Z, D_x, D_y, D_z for a regular mesh."""
-    nx, ny, nz = n
+def _axis_lattice(lo: np.ndarray, hi: np.ndarray):
+    """Distinct bound coordinates of one axis (values closer than 1e-9 of the
+    extent merged) and each cell's [first, last) interval index range."""
+    v = np.unique(np.concatenate([lo, hi]))
+    tol = 1e-9 * max(float(v[-1] - v[0]), 1e-300)
+    v = v[np.concatenate([[True], np.diff(v) > tol])]
+    i0 = np.searchsorted(v, lo - tol)
+    i1 = np.searchsorted(v, hi - tol)
+    return v, i0, i1
+
+
+def _leaf_owner(pr: np.ndarray):
+    """Cell id of every interval box of the lattice the cells' bounds span.
+    Raises if the cells overlap or leave holes in their bounding box."""
+    lat = [_axis_lattice(pr[:, 2 * a], pr[:, 2 * a + 1]) for a in range(3)]
+    shape = tuple(len(l[0]) - 1 for l in lat)
+    if np.prod(shape, dtype=np.float64) > 2.0 ** 31:
+        raise ValueError(f"lattice of {shape} interval boxes is too large")
+    owner = np.full(shape, -1, dtype=np.int64)
+    lo = np.stack([l[1] for l in lat], 1)
+    span = np.stack([l[2] - l[1] for l in lat], 1)
+    if (span <= 0).any():
+        raise ValueError("cell with zero extent")
+    if int(np.prod(span, axis=1).sum()) != int(np.prod(shape)):
+        raise ValueError("cells overlap or do not fill their bounding box")
+    groups = {}
+    for c, s in enumerate(map(tuple, span)):
+        groups.setdefault(s, []).append(c)
+    for s, ids in groups.items():
+        ids = np.asarray(ids)
+        ox, oy, oz = (np.arange(s[a]) for a in range(3))
+        owner[(lo[ids, 0][:, None, None, None] + ox[None, :, None, None]),
+              (lo[ids, 1][:, None, None, None] + oy[None, None, :, None]),
+              (lo[ids, 2][:, None, None, None] + oz[None, None, None, :])] = ids[:, None, None, None]
+    if (owner < 0).any():
+        raise ValueError("cells overlap or do not fill their bounding box")
+    return owner, [l[0] for l in lat], lo, lo + span
+
+
+def _face_neighbours(pr, owner, lat, lo, hi, axis: int, side: int):
+    """Cells across each cell's face on `side` (+1 / -1) of `axis`, probed at
+    four points of the face at 0.3 / 0.7 of its two extents: (n, 4) ids, -1 on
+    the bounding box's boundary.  Four equal ids: one cell of the same or a
+    coarser level; four distinct ids: four finer cells, in the order of
+    Mesh::refinement's child faces (first transverse axis outer)."""
+    n = pr.shape[0]
+    t = [b for b in range(3) if b != axis]
+    ia = hi[:, axis] if side > 0 else lo[:, axis] - 1
+    inside = (ia >= 0) & (ia < owner.shape[axis])
+    out = np.full((n, 4), -1, dtype=np.int64)
+    probes = []
+    for b in t:
+        p0, p1 = pr[:, 2 * b], pr[:, 2 * b + 1]
+        probes.append([np.searchsorted(lat[b], p0 + f * (p1 - p0), side="right") - 1
+                       for f in (0.3, 0.7)])
+    q = 0
+    for u in range(2):
+        for w in range(2):
+            idx = [None, None, None]
+            idx[axis] = ia[inside]
+            idx[t[0]] = probes[0][u][inside]
+            idx[t[1]] = probes[1][w][inside]
+            out[inside, q] = owner[idx[0], idx[1], idx[2]]
+            q += 1
+    return out
+
+
+def difference_matrices(prisms) -> tuple:
+    """D_x1, D_y1, D_z1 (CSR) of InversionBase::set_difference_matrix
+    (InversionBase.cpp:189-434) from the leaf cells' bounds alone, for regular,
+    padded and octree-refined meshes.  Per cell and axis, with h the cells'
+    sizes along the axis and w = 1 / (0.5 (h0 + h1)):
+
+    * the +axis face has a neighbour (same or coarser level): -w on the
+      diagonal, +w to the neighbour (:208-220);
+    * the +axis face is split (four finer neighbours, h1 the size of the
+      first): -w on the diagonal, +w/4 to each (:251-263);
+    * the +axis face is on the boundary: the same with the -axis face and the
+      signs swapped (:223-249), no row if that face is on the boundary too
+      (:389 for z; the reference's x and y rows need two cells).
+
+    Raises if a face has a neighbour pattern a face-balanced octree cannot
+    have (two levels apart, or finer in one transverse direction only)."""
     pr = np.asarray(prisms, dtype=np.float64)
+    n = pr.shape[0]
+    sizes = np.abs(pr[:, 1::2] - pr[:, 0::2])
+    owner, lat, lo, hi = _leaf_owner(pr)
+    rows_all = np.arange(n)
+    mats = []
+    for axis in range(3):
+        t = [b for b in range(3) if b != axis]
+        rows, cols, vals = [], [], []
+        done = np.zeros(n, dtype=bool)
+        for side in (1, -1):
+            nb = _face_neighbours(pr, owner, lat, lo, hi, axis, side)
+            has = (nb[:, 0] >= 0) & ~done
+            one = has & (nb == nb[:, :1]).all(1)
+            four = has & ~one
+            if four.any():
+                k = nb[four]
+                if not all(len(set(r)) == 4 for r in k.tolist()):
+                    raise ValueError("face neighbours are not face-balanced")
+                half = sizes[four][:, t] * 0.5
+                for q in range(4):
+                    if not np.allclose(sizes[k[:, q]][:, t], half, rtol=1e-9, atol=0.0):
+                        raise ValueError("face neighbours are not face-balanced")
+            if one.any():
+                big = sizes[nb[one, 0]][:, t]
+                mine = sizes[one][:, t]
+                ok = np.isclose(big, mine, rtol=1e-9) | np.isclose(big, 2 * mine, rtol=1e-9)
+                if not ok.all():
+                    raise ValueError("face neighbours are not face-balanced")
+            h0 = sizes[:, axis]
+            i = rows_all[one]
+            w = 1.0 / (0.5 * (h0[i] + sizes[nb[one, 0], axis]))
+            rows += [i, i]
+            cols += [i, nb[one, 0]]
+            vals += [-side * w, side * w]
+            i = rows_all[four]
+            w = 1.0 / (0.5 * (h0[i] + sizes[nb[four, 0], axis]))
+            rows.append(i)
+            cols.append(i)
+            vals.append(-side * w)
+            for q in range(4):
+                rows.append(i)
+                cols.append(nb[four, q])
+                vals.append(side * w * 0.25)
+            done |= has
+        D = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                          shape=(n, n))
+        D.sort_indices()
+        mats.append(D)
+    return tuple(mats)
+
+
+def _operators(pr, obs, beta, D, a_s, a_z, a_x, a_y):
     sizes = np.abs(np.stack([pr[:, 1] - pr[:, 0], pr[:, 3] - pr[:, 2], pr[:, 5] - pr[:, 4]], 1))
     vol = sizes[:, 0] * sizes[:, 1] * sizes[:, 2]
     V = np.sqrt(vol)
     zp = np.asarray(obs, dtype=np.float64)[:, 2].sum() / obs.shape[0]
     zc = 0.5 * (pr[:, 4] + pr[:, 5])
     Z = 1.0 / np.abs(zp - zc) ** (beta * 0.5)
-    Dx = _difference(nx, ny, nz, sizes, 0)
-    Dy = _difference(nx, ny, nz, sizes, 1)
-    Dz = _difference(nx, ny, nz, sizes, 2)
+    Dx, Dy, Dz = D
     Ds = sp.identity(pr.shape[0], format="csr")
 
     def W(a, D):
@@ -74,6 +207,23 @@ def regular_mesh_operators(n, prisms, obs, beta: float, a_s=1.0, a_z=1.0, a_x=1.
 
     return {"Ws": W(a_s, Ds), "Wx": W(a_x, Dx), "Wy": W(a_y, Dy), "Wz": W(a_z, Dz),
             "V": V, "Z": Z, "Dx": Dx, "Dy": Dy, "Dz": Dz}
+
+
+def regular_mesh_operators(n, prisms, obs, beta: float, a_s=1.0, a_z=1.0, a_x=1.0, a_y=1.0):
+    """Ws, Wx, Wy, Wz (CSR) plus V, Z, D_x, D_y, D_z for a regular mesh."""
+    nx, ny, nz = n
+    pr = np.asarray(prisms, dtype=np.float64)
+    sizes = np.abs(np.stack([pr[:, 1] - pr[:, 0], pr[:, 3] - pr[:, 2], pr[:, 5] - pr[:, 4]], 1))
+    D = tuple(_difference(nx, ny, nz, sizes, a) for a in range(3))
+    return _operators(pr, obs, beta, D, a_s, a_z, a_x, a_y)
+
+
+def mesh_operators(prisms, obs, beta: float, a_s=1.0, a_z=1.0, a_x=1.0, a_y=1.0):
+    """Ws, Wx, Wy, Wz (CSR) plus V, Z, D_x, D_y, D_z for any leaf-cell list
+    (regular, padded or octree-refined), the differences from the cells'
+    bounds (``difference_matrices``)."""
+    pr = np.asarray(prisms, dtype=np.float64)
+    return _operators(pr, obs, beta, difference_matrices(pr), a_s, a_z, a_x, a_y)
 
 
 def cross_gradient_operators(n, prisms, m0s, ops) -> dict:

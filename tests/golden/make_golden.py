@@ -17,6 +17,8 @@ Fixtures written (all .npz):
                       oracle/_ref/ref_fields, on seeded geometries including
                       degenerate ones (points on cell-face planes and above
                       vertical edges, far-away cells).
+  ref_operators.npz   regularisation operators on an octree-refined mesh
+                      (oracle/_ref/ref_operators).
   ref_inversion_*.npz regular-mesh inversion problems with the reference's
                       G, host-built operators, one solve_cg call and a full
                       invert_with_own_CG run (oracle/_ref/ref_inversion).
@@ -361,6 +363,80 @@ def ref_indicator() -> None:
                         rowptr=rowptr, neighbour=nb, area=area)
 
 
+OPERATOR_ROUNDS = [
+    # round 1: three base cells, one at the +x and one at the +z boundary
+    [(150.0, 250.0, 150.0), (450.0, 250.0, 150.0), (250.0, 250.0, 250.0), (550.0, 50.0, 350.0)],
+    # round 2: level-1 cells against unrefined neighbours (face-balance cascades)
+    [(110.0, 210.0, 110.0), (590.0, 60.0, 390.0), (240.0, 240.0, 210.0)],
+    # round 3: a level-2 cell whose neighbours are level 1 (cascade of two levels)
+    [(101.0, 201.0, 101.0), (595.0, 55.0, 395.0)],
+]
+
+
+def ref_operators() -> None:
+    """ref_operators.npz: the reference's regularisation operators on a 6 x 5 x 4
+    mesh refined in three rounds by Mesh::refinement (cascades included): leaf
+    cells and levels, D_x1/D_y1/D_z1, V, Z, Ws/Wx/Wy/Wz and, for a seeded
+    structure model, T_x/T_y/T_z (oracle/_ref/ref_operators)."""
+    exe = REF_BIN / "ref_operators"
+    obs = np.array([[120.0, 80.0, -20.0], [300.0, 260.0, -35.0], [520.0, 430.0, -10.0],
+                    [80.0, 470.0, -25.0]])
+    alphas = np.array([1.0, 1.3, 0.7, 1.1])  # a_s, a_z, a_x, a_y
+    beta = 1.5
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
+        with open(fin, "wb") as fh:
+            np.array([6, 5, 4], dtype=np.int64).tofile(fh)
+            np.array([0.0, 600.0, 0.0, 500.0, 0.0, 400.0], dtype=np.float64).tofile(fh)
+            np.array([len(OPERATOR_ROUNDS)], dtype=np.int64).tofile(fh)
+            for r in OPERATOR_ROUNDS:
+                np.array([len(r)], dtype=np.int64).tofile(fh)
+                np.array(r, dtype=np.float64).tofile(fh)
+            np.array([obs.shape[0]], dtype=np.int64).tofile(fh)
+            obs.tofile(fh)
+            np.array([beta], dtype=np.float64).tofile(fh)
+            alphas.tofile(fh)
+            np.array([777], dtype=np.uint64).tofile(fh)
+        subprocess.run([str(exe), str(fin), str(fout)], check=True, cwd=td)
+        raw = np.fromfile(fout, dtype=np.uint8)
+    off = 0
+
+    def take(cnt, dt):
+        nonlocal off
+        a = raw[off:off + cnt * np.dtype(dt).itemsize].view(dt)
+        off += cnt * np.dtype(dt).itemsize
+        return a
+
+    out = {}
+
+    def csr(key):
+        n = int(take(1, np.int64)[0])
+        nnz = int(take(1, np.int64)[0])
+        out[key + "_indptr"] = take(n + 1, np.int64)
+        out[key + "_indices"] = take(nnz, np.int64)
+        out[key + "_data"] = take(nnz, np.float64)
+
+    n = int(take(1, np.int64)[0])
+    out["leaf"] = take(6 * n, np.float64).reshape(n, 6)
+    out["level"] = take(n, np.int64)
+    for key in ("Dx", "Dy", "Dz"):
+        csr(key)
+    out["V"] = take(n, np.float64)
+    out["Z"] = take(n, np.float64)
+    for key in ("Ws", "Wx", "Wy", "Wz"):
+        csr(key)
+    out["m0s"] = take(n, np.float64)
+    for key in ("Tx", "Ty", "Tz"):
+        csr(key)
+    assert off == raw.size
+    rounds = np.full((len(OPERATOR_ROUNDS), max(map(len, OPERATOR_ROUNDS)), 3), np.nan)
+    for k, r in enumerate(OPERATOR_ROUNDS):
+        rounds[k, :len(r)] = r
+    np.savez_compressed(HERE / "ref_operators.npz", n=np.array([6, 5, 4]),
+                        limits=np.array([0.0, 600.0, 0.0, 500.0, 0.0, 400.0]), rounds=rounds,
+                        obs=obs, beta=beta, alphas=alphas, **out)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -369,7 +445,7 @@ def main() -> None:
     ref = Path(a.ref)
     jobs = {"forward_models": lambda: forward_models(ref), "ref_fields": ref_fields,
             "ref_expand": ref_expand, "ref_padded": ref_padded,
-            "ref_indicator": ref_indicator}
+            "ref_indicator": ref_indicator, "ref_operators": ref_operators}
     try:
         from inversion_cases import inversion_fixtures  # noqa: E402
         jobs["ref_inversion"] = inversion_fixtures
