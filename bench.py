@@ -442,7 +442,8 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16", "fp32+fp6
              "misfit": rep["final_misfit"], "chi2_reached": rep["final_misfit"] < 1.0,
              "gn_iterations": rep["gn_iterations"], "trials": rep["n_trials"],
              "cg_iterations": int(rep["cg_iterations"]),
-             "ms_per_cg_iteration": 1e3 * t_inv / max(1, rep["cg_iterations"])}
+             "ms_per_cg_iteration": 1e3 * t_inv / max(1, rep["cg_iterations"]),
+             "gn_misfits": [float(v) for v in inv.iterations()[:, 2]]}
         if st == "fp64":
             m64 = m
         else:
