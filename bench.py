@@ -357,7 +357,7 @@ INVERSION_CASES = {
     # 41 x 41 points 100 m above, L2, lambda0 = 0.1, 30 lambdas, rate 0.6, CG max 50
     "l2_16k": dict(cells=(32, 32, 16), domain=(10000.0, 10000.0, 5000.0), obs=(41, 41), height=100.0,
                  mask=0x012, lp=[2, 2, 2, 2, 2], eps2=1e-9, boxes="two_boxes", gn_iter=10),
-    # L1 IRLS on a uniform stand-in for a ~200k-leaf refined mesh: 196,608 cells (64 x 64 x 48 over the
+    # L1 IRLS on a uniform mesh of about the refined one's size: 196,608 cells (64 x 64 x 48 over the
     # same domain; the reference refines to ~200k leaves on the host): gz, Tzz, Txz, Tyz at
     # 101 x 101 points 100 m above, two dykes of +400 kg/m^3, L1 IRLS
     "l1_196k": dict(cells=(64, 64, 48), domain=(10000.0, 10000.0, 5000.0), obs=(101, 101),
