@@ -14,6 +14,7 @@ import ctypes
 import numpy as np
 import scipy.sparse as sp
 
+from . import output
 from ._lib import InvertParams, InvertReport
 from .fwd import Fwd, _ptr
 
@@ -92,7 +93,49 @@ class GaussNewtonInversion(Fwd):
         self.ctx.check(self.ctx.lib.grada_invert(
             self.ctx.handle, ctypes.byref(p), _ptr(vecs[0]), _ptr(vecs[1]), _ptr(vecs[2]),
             None if m0a is None else _ptr(m0a), _ptr(out), ctypes.byref(rep)))
+        self.m = out
+        self.m0 = m0a
         return out, {f: getattr(rep, f) for f, _ in InvertReport._fields_}
+
+    # -- result writers (GraAda3D.cpp:792-806); the files are the reference's
+    #    byte for byte (graada3d_gb300.output)
+
+    def _model(self, m):
+        v = getattr(self, "m", None) if m is None else m
+        if v is None:
+            raise ValueError("no model: run invert() or pass m")
+        return np.asarray(v, dtype=np.float64)
+
+    def get_predicted_field(self, m=None) -> np.ndarray:
+        """G m on the device (InversionBase::get_predicted_field, InversionBase.cpp:696-708)."""
+        return self.G_vec_mul(self._model(m))
+
+    def result2text(self, filename: str, m=None) -> None:
+        """<filename>.txt (InversionBase::result2text, InversionBase.cpp:883-887)."""
+        output.write_model_txt(filename + ".txt", self.prisms, self._model(m))
+
+    def result2vtk(self, filename: str, m=None, m0=None, m0s=None) -> None:
+        """<filename>.vtk and <filename>_points.vtk with the model, the reference
+        model and the structure model (zero when not given, as the reference
+        initialises them; InversionBase::result2vtk, InversionBase.cpp:888-896)."""
+        zero = np.zeros(self.Nm)
+        m0 = getattr(self, "m0", None) if m0 is None else m0
+        params = [("model", self._model(m)), ("m0", zero if m0 is None else m0),
+                  ("m0s", zero if m0s is None else m0s)]
+        output.write_model_vtk(filename + ".vtk", self.prisms, params)
+        output.write_model_vtk_points(filename + "_points.vtk", self.prisms, params)
+
+    def output_obs_data(self, out_name: str) -> None:
+        output.write_data(out_name, self.obs, self.dobs, self.field_flag)
+
+    def output_predicted_data(self, out_name: str, m=None) -> None:
+        output.write_data(out_name, self.obs, self.get_predicted_field(m), self.field_flag)
+
+    def output_obs_data_vtk(self, filename: str) -> None:
+        output.write_data_vtk(filename, self.obs, self.dobs, self.field_flag)
+
+    def output_predicted_data_vtk(self, filename: str, m=None) -> None:
+        output.write_data_vtk(filename, self.obs, self.get_predicted_field(m), self.field_flag)
 
     def solve_cg_block(self, tol, maxit, lambdas, mk, mref, P, WL=None):
         """Several solve_cg systems at once (grada_solve_cg_block): column c has

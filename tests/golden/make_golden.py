@@ -19,6 +19,8 @@ Fixtures written (all .npz):
                       vertical edges, far-away cells).
   ref_operators.npz   regularisation operators on an octree-refined mesh
                       (oracle/_ref/ref_operators).
+  ref_output.npz      the files the reference's result writers produce, with
+                      their inputs (oracle/_ref/ref_output).
   ref_inversion_*.npz regular-mesh inversion problems with the reference's
                       G, host-built operators, one solve_cg call and a full
                       invert_with_own_CG run (oracle/_ref/ref_inversion).
@@ -437,6 +439,57 @@ def ref_operators() -> None:
                         obs=obs, beta=beta, alphas=alphas, **out)
 
 
+OUTPUT_FILES = ["model.txt", "model.vtk", "model_points.vtk", "dobs.vtk"] + \
+    [f"dobs_{c}" for c in ["g_z", "T_zz", "T_xz", "T_yz", "T_xx", "T_xy"]]
+
+
+def ref_output() -> None:
+    """ref_output.npz: the files the reference's own writers make (result2text,
+    result2vtk, output_obs_data, output_obs_data_vtk) for the refined mesh of
+    ref_operators.npz, seeded models m, m0, m0s and data for six components
+    (oracle/_ref/ref_output), with those inputs."""
+    exe = REF_BIN / "ref_output"
+    obs = np.array([[120.0, 80.0, -20.0], [300.0, 260.0, -35.0], [520.0, 430.0, -10.0],
+                    [80.0, 470.0, -25.5], [0.125, 1e-3, -1234.5678]])
+    mask = 0x1F2  # gz, Tzz, Txz, Tyz, Txx, Txy
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
+        with open(fin, "wb") as fh:
+            np.array([6, 5, 4], dtype=np.int64).tofile(fh)
+            np.array([0.0, 600.0, 0.0, 500.0, 0.0, 400.0], dtype=np.float64).tofile(fh)
+            np.array([len(OPERATOR_ROUNDS)], dtype=np.int64).tofile(fh)
+            for r in OPERATOR_ROUNDS:
+                np.array([len(r)], dtype=np.int64).tofile(fh)
+                np.array(r, dtype=np.float64).tofile(fh)
+            np.array([obs.shape[0]], dtype=np.int64).tofile(fh)
+            obs.tofile(fh)
+            np.array([mask], dtype=np.uint32).tofile(fh)
+            np.array([99], dtype=np.uint64).tofile(fh)
+        subprocess.run([str(exe), str(fin), str(fout)], check=True, cwd=td,
+                       stdout=subprocess.DEVNULL)
+        raw = np.fromfile(fout, dtype=np.uint8)
+        files = {f"file:{name}": np.frombuffer((Path(td) / name).read_bytes(), dtype=np.uint8)
+                 for name in OUTPUT_FILES}
+    off = 0
+
+    def take(cnt, dt):
+        nonlocal off
+        a = raw[off:off + cnt * np.dtype(dt).itemsize].view(dt)
+        off += cnt * np.dtype(dt).itemsize
+        return a
+
+    n = int(take(1, np.int64)[0])
+    leaf = take(6 * n, np.float64).reshape(n, 6)
+    m = take(n, np.float64)
+    m0 = take(n, np.float64)
+    m0s = take(n, np.float64)
+    nd = int(take(1, np.int64)[0])
+    dobs = take(nd, np.float64)
+    assert off == raw.size
+    np.savez_compressed(HERE / "ref_output.npz", leaf=leaf, obs=obs, mask=np.int64(mask), m=m,
+                        m0=m0, m0s=m0s, dobs=dobs, **files)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -445,7 +498,8 @@ def main() -> None:
     ref = Path(a.ref)
     jobs = {"forward_models": lambda: forward_models(ref), "ref_fields": ref_fields,
             "ref_expand": ref_expand, "ref_padded": ref_padded,
-            "ref_indicator": ref_indicator, "ref_operators": ref_operators}
+            "ref_indicator": ref_indicator, "ref_operators": ref_operators,
+            "ref_output": ref_output}
     try:
         from inversion_cases import inversion_fixtures  # noqa: E402
         jobs["ref_inversion"] = inversion_fixtures

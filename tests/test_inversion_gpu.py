@@ -229,7 +229,8 @@ def _refined_setup(ctx, p_mask=0x012):
     G = inv.get_G()
     d = G @ rho
     dobs = d + 0.02 * np.abs(d) * rng.standard_normal(d.size)
-    wd = reg.data_weights(dobs, [0.02], [1e-3], obs.shape[0])
+    nf = bin(mask).count("1")
+    wd = reg.data_weights(dobs, [0.02] * nf, [1e-3] + [1e-2] * (nf - 1), obs.shape[0])
     ops = reg.mesh_operators(prisms, obs, 1.5)
     assert (np.diff(ops["Wx"].indptr) == 5).any()
     inv.set_cross_gradient(False)
@@ -287,3 +288,41 @@ def test_invert_on_refined_mesh_matches_oracle(gpu_ctx, p):
     np.testing.assert_allclose(tr[:k, 2], to[:k, 2], rtol=max(1e-6, 3 * spread))
     assert spread < 0.01  # the comparison stays meaningful
     assert rep["final_misfit"] <= 1.1 * misfit_o
+
+
+def test_result_writers_take_device_results(gpu_ctx, tmp_path):
+    """result2text / result2vtk / output_*_data after an inversion on the
+    refined mesh: the files carry the inverted model and the device G m in
+    the reference's formats (the formats themselves are pinned byte for byte
+    on the CPU)."""
+    from graada3d_gb300 import output
+
+    inv, G, dobs, wd, ops, rng = _refined_setup(gpu_ctx)
+    prm = dict(max_lambda=1e-1, n_lambda=3, rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6,
+               cg_factor=20, gn_iter=1, lp=[2] * 5, eps2=1e-9)
+    nm = inv.Nm
+    m, rep = inv.invert(prm, np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0))
+    base = str(tmp_path / "result")
+    inv.result2text(base)
+    inv.result2vtk(base)
+    inv.output_obs_data(str(tmp_path / "dobs"))
+    inv.output_predicted_data(str(tmp_path / "dpre"))
+    inv.output_predicted_data_vtk(str(tmp_path / "dpre.vtk"))
+    txt = np.loadtxt(base + ".txt", comments="#")
+    np.testing.assert_allclose(txt[:, 9], m, rtol=1e-13, atol=1e-300)
+    np.testing.assert_allclose(txt[:, :6], inv.prisms, rtol=1e-15, atol=0)
+    d = (G @ m).reshape(2, -1)
+    for k, name in enumerate(["g_z", "T_zz"]):
+        dpre = np.loadtxt(tmp_path / f"dpre_{name}")
+        np.testing.assert_allclose(dpre[:, 3], d[k], rtol=1e-12, atol=1e-12 * np.abs(d[k]).max())
+    np.testing.assert_allclose(dpre[:, :3], inv.obs, rtol=1e-15, atol=0)
+    assert (tmp_path / "dobs_T_zz").read_bytes() == _written(output.write_data, tmp_path, inv.obs,
+                                                            dobs, inv.field_flag)
+    vtk = (tmp_path / "result.vtk").read_text()
+    assert vtk.count("SCALARS ") == 3 and f"CELL_TYPES\t{nm}" in vtk
+    assert (tmp_path / "dpre.vtk").read_text().count("SCALARS g_z double 1") == 2
+
+
+def _written(writer, tmp_path, obs, d, mask):
+    writer(str(tmp_path / "again"), obs, d, mask)
+    return (tmp_path / "again_T_zz").read_bytes()
