@@ -585,6 +585,16 @@ int grada_G_column_norms(grada_ctx *ctx, double *norms) {
   });
 }
 
+int grada_build_operators(grada_ctx *ctx, const int32_t *faces, double beta, int depth_flag,
+                          const double *alphas) {
+  return guarded(ctx, [&] { ctx->build_operators(faces, beta, depth_flag, alphas); });
+}
+
+int grada_get_operator(grada_ctx *ctx, int which, int64_t *nnz, int *rowptr, int *col,
+                       double *val) {
+  return guarded(ctx, [&] { ctx->get_operator(which, nnz, rowptr, col, val); });
+}
+
 int grada_keep_fp64_G(grada_ctx *ctx, int keep) {
   return guarded(ctx, [&] { ctx->keep_fp64 = keep != 0; });
 }

@@ -145,6 +145,9 @@ struct Context {
   void set_operator(int which, int64_t n, int64_t nnz, const int *rowptr, const int *col,
                     const double *val);
   void set_cross_gradient(int enabled, double a, const double *S);
+  // operators.cu
+  void build_operators(const int *faces, double beta, int depth_flag, const double *alphas);
+  void get_operator(int which, int64_t *nnz, int *rowptr, int *col, double *val);
   void set_data(const double *h_dobs, const double *h_wd);
   void ensure_cg_workspace(int nterms);
   void data_prediction(const double *m, const double *m_start, const double *d64, double *out);

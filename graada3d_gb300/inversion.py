@@ -51,6 +51,32 @@ class GaussNewtonInversion(Fwd):
             if name in ops and ops[name] is not None:
                 self.set_operator(name, ops[name])
 
+    def build_operators(self, faces, beta: float = 2.0, depth_flag: int = 0,
+                        alphas=(1.0, 1.0, 1.0, 1.0)) -> None:
+        """Ws, Wx, Wy, Wz built on the device from the face table
+        (``regularization.face_table``); alphas = (a_s, a_z, a_x, a_y)."""
+        f = np.ascontiguousarray(faces, dtype=np.int32)
+        if f.shape != (self.Nm, 3, 5):
+            raise ValueError(f"face table of shape ({self.Nm}, 3, 5) expected")
+        a = np.ascontiguousarray(alphas, dtype=np.float64)
+        if a.shape != (4,):
+            raise ValueError("four weights expected")
+        self.ctx.check(self.ctx.lib.grada_build_operators(
+            self.ctx.handle, f.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), float(beta),
+            int(depth_flag), _ptr(a)))
+
+    def get_operator(self, name: str) -> sp.csr_matrix:
+        """An operator as the device holds it."""
+        nnz = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.grada_get_operator(self.ctx.handle, OP_SLOTS[name],
+                                                       ctypes.byref(nnz), None, None, None))
+        rp = np.empty(self.Nm + 1, dtype=np.int32)
+        ci = np.empty(max(nnz.value, 1), dtype=np.int32)
+        v = np.empty(max(nnz.value, 1))
+        self.ctx.check(self.ctx.lib.grada_get_operator(
+            self.ctx.handle, OP_SLOTS[name], ctypes.byref(nnz), _iptr(rp), _iptr(ci), _ptr(v)))
+        return sp.csr_matrix((v[:nnz.value], ci[:nnz.value], rp), shape=(self.Nm, self.Nm))
+
     def set_cross_gradient(self, enabled: bool, a_crg: float = 1.0, S_crg=None) -> None:
         S = None
         if S_crg is not None:

@@ -121,31 +121,30 @@ def _face_neighbours(pr, owner, lat, lo, hi, axis: int, side: int):
     return out
 
 
-def difference_matrices(prisms) -> tuple:
-    """D_x1, D_y1, D_z1 (CSR) of InversionBase::set_difference_matrix
-    (InversionBase.cpp:189-434) from the leaf cells' bounds alone, for regular,
-    padded and octree-refined meshes.  Per cell and axis, with h the cells'
-    sizes along the axis and w = 1 / (0.5 (h0 + h1)):
+def face_table(prisms) -> np.ndarray:
+    """Per cell and axis the face InversionBase::set_difference_matrix
+    (InversionBase.cpp:189-434) differences against, from the leaf cells'
+    bounds alone (regular, padded and octree-refined meshes): an (n, 3, 5)
+    int32 table of [side, c0, c1, c2, c3].
 
-    * the +axis face has a neighbour (same or coarser level): -w on the
-      diagonal, +w to the neighbour (:208-220);
-    * the +axis face is split (four finer neighbours, h1 the size of the
-      first): -w on the diagonal, +w/4 to each (:251-263);
-    * the +axis face is on the boundary: the same with the -axis face and the
-      signs swapped (:223-249), no row if that face is on the boundary too
-      (:389 for z; the reference's x and y rows need two cells).
+    * side +1: the +axis face has cells across it (:208-220, :251-263);
+    * side -1: the +axis face is on the boundary, the -axis face has cells
+      across it (:223-249);
+    * side 0: both faces on the boundary, no row (:389 for z; the
+      reference's x and y rows need two cells).
 
+    c0..c3: one neighbour of the same or a coarser level (c1 = c2 = c3 = -1)
+    or four finer neighbours in the order of the reference's child faces.
     Raises if a face has a neighbour pattern a face-balanced octree cannot
     have (two levels apart, or finer in one transverse direction only)."""
     pr = np.asarray(prisms, dtype=np.float64)
     n = pr.shape[0]
     sizes = np.abs(pr[:, 1::2] - pr[:, 0::2])
     owner, lat, lo, hi = _leaf_owner(pr)
-    rows_all = np.arange(n)
-    mats = []
+    table = np.full((n, 3, 5), -1, dtype=np.int32)
+    table[:, :, 0] = 0
     for axis in range(3):
         t = [b for b in range(3) if b != axis]
-        rows, cols, vals = [], [], []
         done = np.zeros(n, dtype=bool)
         for side in (1, -1):
             nb = _face_neighbours(pr, owner, lat, lo, hi, axis, side)
@@ -166,22 +165,45 @@ def difference_matrices(prisms) -> tuple:
                 ok = np.isclose(big, mine, rtol=1e-9) | np.isclose(big, 2 * mine, rtol=1e-9)
                 if not ok.all():
                     raise ValueError("face neighbours are not face-balanced")
-            h0 = sizes[:, axis]
-            i = rows_all[one]
-            w = 1.0 / (0.5 * (h0[i] + sizes[nb[one, 0], axis]))
-            rows += [i, i]
-            cols += [i, nb[one, 0]]
-            vals += [-side * w, side * w]
-            i = rows_all[four]
-            w = 1.0 / (0.5 * (h0[i] + sizes[nb[four, 0], axis]))
-            rows.append(i)
-            cols.append(i)
-            vals.append(-side * w)
-            for q in range(4):
-                rows.append(i)
-                cols.append(nb[four, q])
-                vals.append(side * w * 0.25)
+            table[one, axis, 0] = side
+            table[one, axis, 1] = nb[one, 0]
+            table[four, axis, 0] = side
+            table[four, axis, 1:] = nb[four]
             done |= has
+    return table
+
+
+def difference_matrices(prisms, table=None) -> tuple:
+    """D_x1, D_y1, D_z1 (CSR) of InversionBase::set_difference_matrix from the
+    face table (``face_table`` of the cells unless given), with h the cells'
+    sizes along the axis and w = 1 / (0.5 (h0 + h1)), h1 that of c0:
+    -side w on the diagonal and side w to one neighbour, or side w / 4 to each
+    of four finer ones (:208-263, :223-249 for side -1)."""
+    pr = np.asarray(prisms, dtype=np.float64)
+    n = pr.shape[0]
+    sizes = np.abs(pr[:, 1::2] - pr[:, 0::2])
+    tab = face_table(pr) if table is None else np.asarray(table)
+    mats = []
+    for axis in range(3):
+        f = tab[:, axis]
+        side = f[:, 0].astype(np.float64)
+        rowsel = f[:, 0] != 0
+        one = rowsel & (f[:, 2] < 0)
+        four = rowsel & (f[:, 2] >= 0)
+        i = np.nonzero(rowsel)[0]
+        h1 = sizes[f[i, 1], axis]
+        w = np.zeros(n)
+        w[i] = 1.0 / (0.5 * (sizes[i, axis] + h1))
+        rows, cols, vals = [i], [i], [-side[i] * w[i]]
+        j = np.nonzero(one)[0]
+        rows.append(j)
+        cols.append(f[j, 1])
+        vals.append(side[j] * w[j])
+        j = np.nonzero(four)[0]
+        for q in range(4):
+            rows.append(j)
+            cols.append(f[j, 1 + q])
+            vals.append(side[j] * w[j] * 0.25)
         D = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
                           shape=(n, n))
         D.sort_indices()
@@ -193,7 +215,8 @@ def _operators(pr, obs, beta, D, a_s, a_z, a_x, a_y):
     sizes = np.abs(np.stack([pr[:, 1] - pr[:, 0], pr[:, 3] - pr[:, 2], pr[:, 5] - pr[:, 4]], 1))
     vol = sizes[:, 0] * sizes[:, 1] * sizes[:, 2]
     V = np.sqrt(vol)
-    zp = np.asarray(obs, dtype=np.float64)[:, 2].sum() / obs.shape[0]
+    # summed in order, as InversionBase.cpp:505-510 does
+    zp = np.cumsum(np.asarray(obs, dtype=np.float64)[:, 2])[-1] / obs.shape[0]
     zc = 0.5 * (pr[:, 4] + pr[:, 5])
     Z = 1.0 / np.abs(zp - zc) ** (beta * 0.5)
     Dx, Dy, Dz = D

@@ -189,6 +189,34 @@ int grada_set_operator(grada_ctx *ctx, int which, int64_t n, int64_t nnz, const 
                        const int *col, const double *val);
 
 /*
+ * Builds Ws, Wx, Wy, Wz on the device for the current cells, in place of the
+ * host rebuild after a refinement (InversionBase::init_matrices,
+ * InversionBase.cpp:146-187: set_Vmatrix :452-466, set_depth_weighting
+ * :497-529, set_difference_matrix :189-434; W_* = a_* S_* V D_* Z with S_* = I,
+ * GaussNewtonInversion.cpp:711-714), transposes included.
+ *   faces: n_cells x 3 x 5 int32, per cell and axis (x, y, z) the face the
+ *     reference differences against: [side, c0, c1, c2, c3].  side +1: the
+ *     +axis face (-w on the diagonal, +w to the neighbour); -1: the -axis face,
+ *     the +axis face being on the boundary (signs swapped); 0: no row.  One
+ *     neighbour (c1 = c2 = c3 = -1), of the same or a coarser level, or four
+ *     finer neighbours taking w/4 each.  w = 1 / (0.5 (h0 + h1)), h the sizes
+ *     along the axis, h1 that of c0.  Checked on the host before any launch.
+ *   depth_flag 0: Z_ii = 1 / |zp - zc_i|^(beta/2), zp the mean observation
+ *     height; 1: Z_ii = sqrt(||G(:, i)|| / Nd) from the stored G.
+ *   alphas: a_s, a_z, a_x, a_y.
+ * The values follow the reference's operations in its order; Z's power may
+ * differ from the host C library's in the last bits.
+ */
+int grada_build_operators(grada_ctx *ctx, const int32_t *faces, double beta, int depth_flag,
+                          const double *alphas);
+
+/* Reads an operator back (its rows as grada_set_operator takes them): *nnz
+ * always, rowptr (Nm + 1), col and val (nnz) when not NULL.
+ * GRADA_ERR_STATE if the slot is empty. */
+int grada_get_operator(grada_ctx *ctx, int which, int64_t *nnz, int *rowptr, int *col,
+                       double *val);
+
+/*
  * Cross-gradient coupling (use_cross_gradient_constraint, InversionBase.h:125):
  * when enabled the CG system gains the rows a_crg*S_crg*T_{z,x,y}
  * (GaussNewtonInversion.cpp:1445-1450).  S_crg: Nm diagonal, NULL = identity.
