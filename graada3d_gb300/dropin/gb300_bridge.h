@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "../../include/grada_gpu.h"
 
@@ -20,5 +21,11 @@ void release(const void *owner);
 
 // Throws std::runtime_error with the library's message on a failing status.
 void check(grada_ctx *ctx, int status, const char *what);
+
+// grada_build_operators' face table of a mesh (FaceTable_gb300.cpp).
+}  // namespace gb300
+class Mesh;
+namespace gb300 {
+void face_table(Mesh &mesh, std::vector<int32_t> &table);
 
 }  // namespace gb300

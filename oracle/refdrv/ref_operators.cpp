@@ -9,6 +9,11 @@
 // and, for a seeded structure model, T_x, T_y, T_z (InversionBase::set_Tmatrix,
 // InversionBase.cpp:468-495).
 //
+// Also dumps the face table of the drop-in's face_table
+// (graada3d_gb300/dropin/FaceTable_gb300.cpp, compiled in here) read from the
+// reference's own Face objects, the input a C++ host hands to
+// grada_build_operators.
+//
 // A round names points; the leaves that contain a point (strictly inside)
 // are refined in leaf order, skipping cells a cascade already split, as
 // AdaptiveInversion::refine_mesh does with its marked cells.
@@ -21,6 +26,7 @@
 #include <vector>
 
 #include "GaussNewtonInversion.h"
+#include "../../graada3d_gb300/dropin/FaceTable_gb300.cpp"
 
 namespace {
 
@@ -173,6 +179,9 @@ int main(int argc, char **argv) {
   out.csr(inv.Tx());
   out.csr(inv.Ty());
   out.csr(inv.Tz());
+  std::vector<int32_t> table;
+  gb300::face_table(m, table);
+  std::fwrite(table.data(), 4, table.size(), fo);
   std::fclose(fo);
   return 0;
 }

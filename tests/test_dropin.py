@@ -17,7 +17,8 @@ REF = Path(os.environ.get("GRADA_REFERENCE", "/root/reference"))
                     reason="reference headers not available")
 @pytest.mark.skipif(shutil.which("g++") is None, reason="no C++ compiler")
 @pytest.mark.parametrize("unit", ["gb300_bridge", "Fwd_gb300", "GaussNewtonInversion_gb300",
-                                  "InversionBase_gb300", "AdaptiveInversion_gb300"])
+                                  "InversionBase_gb300", "AdaptiveInversion_gb300",
+                                  "FaceTable_gb300"])
 def test_dropin_compiles_against_reference_headers(unit):
     lib = REF / "3rd_party_lib"
     cmd = ["g++", "-std=c++14", "-w", "-fsyntax-only",

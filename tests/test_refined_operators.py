@@ -71,6 +71,17 @@ def test_difference_matrices_match_reference():
     assert (np.diff(_csr(f, "Dz").indptr) == 5).sum() > 0
 
 
+def test_face_table_matches_the_reference_faces():
+    """The geometric face table equals the one the drop-in reads from the
+    reference's own Face objects (dropin/FaceTable_gb300.cpp run on the
+    reference's refined mesh): the same side, neighbours and child-face order
+    for every cell and axis, so either feeds grada_build_operators alike."""
+    f = _load()
+    t = reg.face_table(f["leaf"])
+    np.testing.assert_array_equal(t, f["face_table"])
+    assert (t[:, :, 0] == -1).any() and (t[:, :, 2] >= 0).any()
+
+
 def test_mesh_operators_match_reference():
     f = _load()
     a = f["alphas"]
