@@ -917,6 +917,44 @@ def run_assembly_refined():
     return out
 
 
+def run_operators_refined():
+    """Rebuild of the regularisation operators after a refinement on the
+    236,226-leaf dyke mesh: the face table from the leaves' geometry (host),
+    then Ws/Wx/Wy/Wz with their transposes either built on the host and
+    uploaded (grada_set_operator) or built on the device from the table
+    (grada_build_operators).  Host wall clock, 1 warm-up + 3 timed runs each."""
+    from graada3d_gb300 import mesh
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.inversion import GaussNewtonInversion
+
+    cells = refined_dyke_mesh(3)
+    obs = mesh.observation_grid(101, 0.0, 10000.0, 101, 0.0, 10000.0, -100.0)
+    inv = GaussNewtonInversion(cells, obs, 0x072)
+
+    def timed(fn, k=3):
+        fn()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            out = fn()
+        return (time.perf_counter() - t0) / k, out
+
+    t_table, table = timed(lambda: reg.face_table(cells))
+    t_host, ops = timed(lambda: reg._operators(cells, obs, 1.5, reg.difference_matrices(cells, table),
+                                               1.0, 1.0, 1.0, 1.0))
+    t_upload, _ = timed(lambda: inv.set_operators(ops))
+    t_dev, _ = timed(lambda: inv.build_operators(table, 1.5))
+    worst = 0.0
+    for key in ("Ws", "Wx", "Wy", "Wz"):
+        a, b = inv.get_operator(key), ops[key]
+        worst = max(worst, float(np.max(np.abs(a.data - b.data) / np.abs(b.data))))
+    out = {"case": "operators-refined", "cells": int(cells.shape[0]),
+           "nnz_W": int(sum(ops[k].nnz for k in ("Ws", "Wx", "Wy", "Wz"))),
+           "face_table_host_s": t_table, "W_host_build_s": t_host, "W_upload_s": t_upload,
+           "W_device_build_s": t_dev, "max_rel_diff_device_vs_host": worst}
+    inv.ctx.close()
+    return out
+
+
 def run_profile_case(args):
     """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
     50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
@@ -946,7 +984,8 @@ def main():
                                                          "matrix-free-1m",
                                                          "gemv", "batched-64", "block-gemm",
                                                          "lambda-sweep-16", "block-gemm-profile",
-                                                         "mf-profile", "assembly-refined"])
+                                                         "mf-profile", "assembly-refined",
+                                                         "operators-refined"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -964,6 +1003,8 @@ def main():
         print(json.dumps(run_block_gemm_case()))
     elif args.case == "assembly-refined":
         print(json.dumps(run_assembly_refined()))
+    elif args.case == "operators-refined":
+        print(json.dumps(run_operators_refined()))
     elif args.case == "mf-profile":
         run_mf_profile()
     elif args.case == "block-gemm-profile":
