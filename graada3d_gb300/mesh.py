@@ -190,6 +190,37 @@ class Octree:
             self._leaves = out
         return self._leaves
 
+    def wavelet_order(self) -> np.ndarray:
+        """Mesh::get_reordered_id for every position: the leaf index of the
+        i-th cell in the sequence the wavelet compression runs along
+        (ro_leaf_cells).  Base cells: x outermost, then y, with z running
+        forward and backward on alternate (x, y) lines (Mesh.cpp:855-892); a
+        split cell is replaced by its children in the order 0 2 6 4 5 7 3 1
+        when its line runs forward, 1 3 7 5 4 6 2 0 otherwise, the children
+        keeping the parent's direction (Mesh.cpp:1605, 1946-1960)."""
+        index = {k: t for t, k in enumerate(self.leaf_keys())}
+        fwd_kids = (0, 2, 6, 4, 5, 7, 3, 1)
+        bwd_kids = (1, 3, 7, 5, 4, 6, 2, 0)
+        out = []
+        nx, ny, nz = self.n
+        for i in range(nx):
+            for j in range(ny):
+                forward = (i * ny + j) % 2 == 0
+                kids = fwd_kids if forward else bwd_kids
+                for kk in range(nz):
+                    k = kk if forward else nz - 1 - kk
+                    stack = [(0, i, j, k)]
+                    while stack:
+                        key = stack.pop()
+                        if key in self.split_cells:
+                            L, a, b, c = key
+                            for o in reversed(kids):
+                                stack.append((L + 1, 2 * a + (o >> 2), 2 * b + ((o >> 1) & 1),
+                                              2 * c + (o & 1)))
+                        else:
+                            out.append(index[key])
+        return np.array(out, dtype=np.int64)
+
     def leaves(self) -> np.ndarray:
         """(n, 6) leaf cells x0 x1 y0 y1 z0 z1 in leaf order."""
         return np.array([self.bounds(k) for k in self.leaf_keys()], dtype=np.float64).reshape(-1, 6)

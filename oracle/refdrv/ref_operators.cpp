@@ -9,7 +9,8 @@
 // and, for a seeded structure model, T_x, T_y, T_z (InversionBase::set_Tmatrix,
 // InversionBase.cpp:468-495).
 //
-// Also dumps the face table of the drop-in's face_table
+// Also dumps Mesh::get_reordered_id of every position (the order the
+// wavelet compression runs along) and the face table of the drop-in's face_table
 // (graada3d_gb300/dropin/FaceTable_gb300.cpp, compiled in here) read from the
 // reference's own Face objects, the input a C++ host hands to
 // grada_build_operators.
@@ -182,6 +183,7 @@ int main(int argc, char **argv) {
   std::vector<int32_t> table;
   gb300::face_table(m, table);
   std::fwrite(table.data(), 4, table.size(), fo);
+  for (int64_t i = 0; i < n; i++) out.i64(m.get_reordered_id((unsigned)i));
   std::fclose(fo);
   return 0;
 }

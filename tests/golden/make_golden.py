@@ -379,8 +379,9 @@ def ref_operators() -> None:
     """ref_operators.npz: the reference's regularisation operators on a 6 x 5 x 4
     mesh refined in three rounds by Mesh::refinement (cascades included): leaf
     cells and levels, D_x1/D_y1/D_z1, V, Z, Ws/Wx/Wy/Wz, for a seeded
-    structure model T_x/T_y/T_z, and the face table the drop-in reads from the
-    reference's Face objects (oracle/_ref/ref_operators)."""
+    structure model T_x/T_y/T_z, the face table the drop-in reads from the
+    reference's Face objects and Mesh::get_reordered_id of every position
+    (oracle/_ref/ref_operators)."""
     exe = REF_BIN / "ref_operators"
     obs = np.array([[120.0, 80.0, -20.0], [300.0, 260.0, -35.0], [520.0, 430.0, -10.0],
                     [80.0, 470.0, -25.0]])
@@ -432,6 +433,7 @@ def ref_operators() -> None:
     for key in ("Tx", "Ty", "Tz"):
         csr(key)
     out["face_table"] = take(15 * n, np.int32).reshape(n, 3, 5)
+    out["reordered_id"] = take(n, np.int64)
     assert off == raw.size
     rounds = np.full((len(OPERATOR_ROUNDS), max(map(len, OPERATOR_ROUNDS)), 3), np.nan)
     for k, r in enumerate(OPERATOR_ROUNDS):

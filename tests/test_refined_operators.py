@@ -60,6 +60,16 @@ def test_octree_refinement_matches_reference_leaves():
     assert f["level"].max() == 3
 
 
+def test_wavelet_order_matches_reference():
+    """Octree.wavelet_order is Mesh::get_reordered_id after the reference's
+    refinements (the sequence the wavelet-compressed G runs along)."""
+    f = _load()
+    np.testing.assert_array_equal(_octree_of(f).wavelet_order(), f["reordered_id"])
+    # unrefined: the z snake over (x, y) lines
+    o = mesh.Octree.regular((0, 1), 2, (0, 1), 2, (0, 1), 3)
+    np.testing.assert_array_equal(o.wavelet_order(), [0, 1, 2, 5, 4, 3, 6, 7, 8, 11, 10, 9])
+
+
 def test_difference_matrices_match_reference():
     f = _load()
     Dx, Dy, Dz = reg.difference_matrices(f["leaf"])
