@@ -955,6 +955,93 @@ def run_operators_refined():
     return out
 
 
+def run_wavelet_case(rel: float = 5e-4):
+    """The reference's method_id 2 at the 32 x 32 x 16-cell size (16,384 cells over
+    [0, 10 km]^2 x [0, 5 km], gz + Tzz at 41 x 41 points 100 m above): FP64
+    assembly plus Daubechies-4 compression of every row at the relative threshold
+    of the reference's example configurations (5e-4), then G x and G^T y on the
+    compressed rows against the dense FP64 ones (CUDA events, 20 runs each), the
+    relative error of G x on the two-box model, and an L2 inversion to the
+    target misfit on each."""
+    import torch
+
+    from graada3d_gb300 import mesh
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.inversion import GaussNewtonInversion
+
+    c, prisms, obs, rho, rel_e, absf, ops, rng = inversion_problem("l2_16k")
+    o = mesh.Octree.regular((0.0, 10000.0), 32, (0.0, 10000.0), 32, (0.0, 5000.0), 16)
+    order = o.wavelet_order()
+    import ctypes
+
+    inv = GaussNewtonInversion(prisms, obs, c["mask"])
+    lib, h = inv.ctx.lib, inv.ctx.handle
+    stream = torch.cuda.ExternalStream(inv.ctx.stream)
+    x = torch.from_numpy(rho).cuda()
+    y = torch.empty(inv.ld, dtype=torch.float64, device="cuda")
+    r = torch.zeros(inv.ld, dtype=torch.float64, device="cuda")
+    r[:inv.Nd] = torch.from_numpy(np.random.default_rng(3).standard_normal(inv.Nd))
+    g = torch.empty(inv.Nm, dtype=torch.float64, device="cuda")
+
+    def products():
+        out = []
+        for fn, a, b in ((lib.grada_G_vec_mul_dev, x, y), (lib.grada_GT_vec_mul_dev, r, g)):
+            for _ in range(3):
+                inv.ctx.check(fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr())))
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(20):
+                fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1) / 20)
+        return out
+
+    t0 = time.perf_counter()
+    inv.compute_G("fp64")
+    torch.cuda.synchronize()
+    t_dense = time.perf_counter() - t0
+    d_dense = inv.G_vec_mul(rho)
+    ms_dense = products()
+    dobs = d_dense + 0.02 * np.abs(d_dense) * np.random.default_rng(2).standard_normal(d_dense.size)
+    wd = reg.data_weights(dobs, rel_e, absf, obs.shape[0])
+    inv.set_cross_gradient(False)
+    inv.set_operators(ops)
+    inv.set_dobs(dobs, wd)
+    nm = inv.Nm
+    prm = dict(max_lambda=1e-1, n_lambda=30, rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6,
+               cg_factor=50, gn_iter=c["gn_iter"], lp=c["lp"], eps2=c["eps2"])
+    args = (np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0))
+    t0 = time.perf_counter()
+    m64, rep64 = inv.invert(prm, *args)
+    t_inv64 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    inv.compute_G_wavelet(order, rel)
+    torch.cuda.synchronize()
+    t_wv = time.perf_counter() - t0
+    n_dy, rp, cols, vals = inv.get_wavelet_G()
+    d_wv = inv.G_vec_mul(rho)
+    ms_wv = products()
+    t0 = time.perf_counter()
+    mw, repw = inv.invert(prm, *args)
+    t_invw = time.perf_counter() - t0
+    out = {"case": "wavelet", "cells": nm, "data": inv.Nd, "threshold": rel, "n_dy": n_dy,
+           "kept": int(cols.size), "compression_ratio": inv.Nd * nm / cols.size,
+           "dense_assemble_s": t_dense, "wavelet_assemble_compress_s": t_wv,
+           "G_x_ms": {"dense_fp64": ms_dense[0], "wavelet": ms_wv[0]},
+           "GT_y_ms": {"dense_fp64": ms_dense[1], "wavelet": ms_wv[1]},
+           "G_x_rel_error": float(np.linalg.norm(d_wv - d_dense) / np.linalg.norm(d_dense)),
+           "invert": {"dense_fp64": {"s": t_inv64, "misfit": rep64["final_misfit"],
+                                     "trials": rep64["n_trials"]},
+                      "wavelet": {"s": t_invw, "misfit": repw["final_misfit"],
+                                  "trials": repw["n_trials"],
+                                  "model_rel_diff": float(np.linalg.norm(mw - m64)
+                                                          / np.linalg.norm(m64))}}}
+    inv.ctx.close()
+    return out
+
+
 def run_profile_case(args):
     """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
     50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
@@ -985,7 +1072,7 @@ def main():
                                                          "gemv", "batched-64", "block-gemm",
                                                          "lambda-sweep-16", "block-gemm-profile",
                                                          "mf-profile", "assembly-refined",
-                                                         "operators-refined"])
+                                                         "operators-refined", "wavelet"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -1005,6 +1092,8 @@ def main():
         print(json.dumps(run_assembly_refined()))
     elif args.case == "operators-refined":
         print(json.dumps(run_operators_refined()))
+    elif args.case == "wavelet":
+        print(json.dumps(run_wavelet_case()))
     elif args.case == "mf-profile":
         run_mf_profile()
     elif args.case == "block-gemm-profile":

@@ -79,6 +79,9 @@ DevGeometry Context::geometry() const {
 }
 
 DevG Context::devG() const {
+  if (g_storage == GRADA_G_WAVELET)
+    throw Error(GRADA_ERR_STATE,
+                "not available for the wavelet-compressed G (products and solve_cg/invert only)");
   DevG d;
   d.kind = (GKind)g_storage;
   d.data = G.ptr;
@@ -252,6 +255,7 @@ bool Context::fp64_resident() const {
 
 int64_t Context::product_scratch_doubles() {
   require_G();
+  if (g_storage == GRADA_G_WAVELET) return 3 * wv_ndy;
   if (g_storage == GRADA_G_MATRIX_FREE) {
     const DevGeometry g = geometry();
     const int64_t f = (int64_t)forward_field_splits(g, sm_count) * n_obs * n_fields;
@@ -263,7 +267,9 @@ int64_t Context::product_scratch_doubles() {
 
 void Context::apply_G(const double *x, double *y, const GemvOpts &o) {
   double *sc = scratch.as<double>();
-  if (g_storage == GRADA_G_MATRIX_FREE) {
+  if (g_storage == GRADA_G_WAVELET) {
+    apply_G_wavelet(x, y, o);
+  } else if (g_storage == GRADA_G_MATRIX_FREE) {
     const DevGeometry g = geometry();
     launch_forward_field(g, x, forward_field_splits(g, sm_count), sc, y, true, stream, o.scale,
                          o.skip);
@@ -274,7 +280,9 @@ void Context::apply_G(const double *x, double *y, const GemvOpts &o) {
 
 void Context::apply_GT(const double *y, double *x, const GemvOpts &o) {
   double *sc = scratch.as<double>();
-  if (g_storage == GRADA_G_MATRIX_FREE) {
+  if (g_storage == GRADA_G_WAVELET) {
+    apply_GT_wavelet(y, x, o);
+  } else if (g_storage == GRADA_G_MATRIX_FREE) {
     const DevGeometry g = geometry();
     launch_adjoint_field(g, y, o.scale, adjoint_field_splits(g, sm_count), sc, x, stream, o.skip);
   } else {
@@ -593,6 +601,15 @@ int grada_build_operators(grada_ctx *ctx, const int32_t *faces, double beta, int
 int grada_get_operator(grada_ctx *ctx, int which, int64_t *nnz, int *rowptr, int *col,
                        double *val) {
   return guarded(ctx, [&] { ctx->get_operator(which, nnz, rowptr, col, val); });
+}
+
+int grada_compute_G_wavelet(grada_ctx *ctx, const int64_t *order, double relative_threshold) {
+  return guarded(ctx, [&] { ctx->compute_G_wavelet(order, relative_threshold); });
+}
+
+int grada_get_wavelet_G(grada_ctx *ctx, int64_t *n_dy, int64_t *nnz, int64_t *rowptr, int32_t *col,
+                        double *val) {
+  return guarded(ctx, [&] { ctx->get_wavelet_G(n_dy, nnz, rowptr, col, val); });
 }
 
 int grada_keep_fp64_G(grada_ctx *ctx, int keep) {

@@ -145,6 +145,15 @@ struct Context {
   void set_operator(int which, int64_t n, int64_t nnz, const int *rowptr, const int *col,
                     const double *val);
   void set_cross_gradient(int enabled, double a, const double *S);
+  // wavelet.cu: the wavelet-compressed G (g_storage == GRADA_G_WAVELET): rows
+  // (CSR, coefficient index ascending), the coefficient-major copy, the cell
+  // order the rows run along
+  DevBuf wv_order, wv_rowptr, wv_col, wv_val, wv_trowptr, wv_trow, wv_tval;
+  int64_t wv_ndy = 0, wv_nnz = 0;
+  void compute_G_wavelet(const int64_t *order, double rel);
+  void apply_G_wavelet(const double *x, double *y, const GemvOpts &o);
+  void apply_GT_wavelet(const double *y, double *x, const GemvOpts &o);
+  void get_wavelet_G(int64_t *n_dy, int64_t *nnz, int64_t *rowptr, int *col, double *val);
   // operators.cu
   void build_operators(const int *faces, double beta, int depth_flag, const double *alphas);
   void get_operator(int which, int64_t *nnz, int *rowptr, int *col, double *val);

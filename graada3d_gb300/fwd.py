@@ -22,7 +22,7 @@ FIELD_BITS = {
 }
 FIELD_ORDER = ["V", "gz", "gx", "gy", "Tzz", "Txz", "Tyz", "Txx", "Txy", "Tyy"]
 
-G_FP64, G_FP32, G_BF16_ROWSCALE, G_FP16_ROWSCALE, G_MATRIX_FREE = 0, 1, 2, 3, 4
+G_FP64, G_FP32, G_BF16_ROWSCALE, G_FP16_ROWSCALE, G_MATRIX_FREE, G_WAVELET = 0, 1, 2, 3, 4, 5
 STORAGE = {"fp64": G_FP64, "fp32": G_FP32, "bf16": G_BF16_ROWSCALE, "fp16": G_FP16_ROWSCALE,
            "matrix_free": G_MATRIX_FREE}
 
@@ -154,6 +154,31 @@ class Fwd:
         s = STORAGE[storage] if isinstance(storage, str) else int(storage)
         self.ctx.check(self.ctx.lib.grada_keep_fp64_G(self.ctx.handle, int(bool(keep_fp64))))
         self.ctx.check(self.ctx.lib.grada_compute_G(self.ctx.handle, s))
+
+    def compute_G_wavelet(self, order, relative_threshold: float) -> None:
+        """Fwd::compute_G_wavelet: rows of G along ``order`` (Mesh::get_reordered_id,
+        e.g. ``mesh.Octree.wavelet_order()``) Daubechies-4 transformed and
+        thresholded; the products then use the compressed rows."""
+        o = np.ascontiguousarray(order, dtype=np.int64)
+        if o.shape != (self.Nm,):
+            raise ValueError(f"expected an order of {self.Nm} cells")
+        self.ctx.check(self.ctx.lib.grada_compute_G_wavelet(
+            self.ctx.handle, o.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            float(relative_threshold)))
+
+    def get_wavelet_G(self):
+        """(n_dy, rowptr, cols, vals) of the compressed rows."""
+        n_dy, nnz = ctypes.c_int64(), ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.grada_get_wavelet_G(self.ctx.handle, ctypes.byref(n_dy),
+                                                        ctypes.byref(nnz), None, None, None))
+        rp = np.empty(self.Nd + 1, dtype=np.int64)
+        ci = np.empty(max(nnz.value, 1), dtype=np.int32)
+        v = np.empty(max(nnz.value, 1))
+        self.ctx.check(self.ctx.lib.grada_get_wavelet_G(
+            self.ctx.handle, ctypes.byref(n_dy), ctypes.byref(nnz),
+            rp.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            ci.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _ptr(v)))
+        return n_dy.value, rp, ci[:nnz.value].astype(np.int64), v[:nnz.value]
 
     def get_G(self) -> np.ndarray:
         """G as an (Nd, Nm) float64 array in column-major (Fortran) order."""

@@ -65,6 +65,7 @@ extern "C" {
 #define GRADA_G_BF16_ROWSCALE 2 /* bf16 entries times an FP32 scale per row */
 #define GRADA_G_FP16_ROWSCALE 3 /* fp16 entries (|v| <= 1) times an FP32 scale per row */
 #define GRADA_G_MATRIX_FREE 4   /* nothing stored: each product re-evaluates the prisms (FP64) */
+#define GRADA_G_WAVELET 5       /* rows Daubechies-4 transformed and thresholded (grada_compute_G_wavelet) */
 
 typedef struct grada_ctx grada_ctx;
 
@@ -158,6 +159,27 @@ int grada_expand_G(grada_ctx *ctx, int64_t n_split, const int64_t *parent_index,
  */
 int grada_forward_field(grada_ctx *ctx, const double *rho, double *fields);
 int grada_forward_field_dev(grada_ctx *ctx, const double *d_rho, double *d_fields);
+
+/*
+ * Replaces Fwd::compute_G_wavelet (Fwd.cpp:148-219, method_id 2 of
+ * GaussNewtonInversion::invert): every row of G, its cells in `order`
+ * (order[j] = Mesh::get_reordered_id(j), a permutation of the Nm cells),
+ * zero-padded to the next power of two n_dy, is transformed with the periodic
+ * Daubechies-4 pyramid (the algorithm of gsl_wavelet_daubechies, member 4)
+ * and keeps the coefficients c with |c| > t or ||c| - t| < 1e-15,
+ * t = relative_threshold x the row's largest |c| (Fwd::compress_vec,
+ * :298-358).  The FP64 G is assembled on the device first (it must fit) and
+ * released afterwards.  Then grada_G_vec_mul / grada_GT_vec_mul (and their
+ * _dev forms), grada_solve_cg and grada_invert use the compressed rows, as
+ * the reference's G_vec_mul / GT_vec_mul do (:80-146); other G readers answer
+ * GRADA_ERR_STATE.  Needs Nm >= 2.
+ */
+int grada_compute_G_wavelet(grada_ctx *ctx, const int64_t *order, double relative_threshold);
+
+/* The compressed rows: *n_dy and *nnz always; rowptr (Nd + 1), col and val
+ * (nnz) when not NULL.  GRADA_ERR_STATE unless G is wavelet-compressed. */
+int grada_get_wavelet_G(grada_ctx *ctx, int64_t *n_dy, int64_t *nnz, int64_t *rowptr, int32_t *col,
+                        double *val);
 
 /*
  * Measures the FP64 fused-multiply-add rate of the device (FLOP/s, FMA = 2

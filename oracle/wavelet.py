@@ -1,0 +1,117 @@
+"""Test oracle (test infrastructure only): the reference's wavelet-compressed
+sensitivity matrix restated in NumPy.
+
+Follows Fwd::compute_G_wavelet (src/Forward_modelling/Fwd.cpp:148-219),
+Fwd::compress_vec (:298-358), Fwd::wavelet_transform_vec /
+inverse_wavelet_transform_vec (:257-296, :360-402) and the wavelet branches of
+Fwd::G_vec_mul / GT_vec_mul (:80-146).  The reference takes its transform from
+GSL (gsl_wavelet_daubechies, member 4, gsl_wavelet_transform_forward /
+_inverse, GSL 2.x), which is absent here; this restates the published
+periodic Daubechies-4 pyramid algorithm GSL implements: the four-tap scaling
+filter h of Daubechies (1988), the wavelet filter g_k = (-1)^k h_{3-k}, no
+offset, levels n = n_dy, n_dy / 2, ..., 2 (forward) with the approximations of
+a level in entries [0, n/2) and its details in [n/2, n), every sum accumulated
+in index order from zero.  Parity with GSL itself is unpinned; the device path
+is checked against this restatement, and the restatement against the
+transform's own properties (orthogonality, exact reconstruction, vanishing
+moments).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# (1 + sqrt 3, 3 + sqrt 3, 3 - sqrt 3, 1 - sqrt 3) / (4 sqrt 2), correctly rounded
+H = np.array([0.48296291314453416, 0.8365163037378079, 0.2241438680420134, -0.12940952255126037])
+G = np.array([H[3], -H[2], H[1], -H[0]])
+
+
+def padded_length(n: int) -> int:
+    """n when it is a power of two, else the next power of two (Fwd.cpp:302-312)."""
+    p = 1
+    while p < n:
+        p *= 2
+    return p
+
+
+def forward(data: np.ndarray) -> np.ndarray:
+    """Forward transform along the last axis (a power-of-two length)."""
+    a = np.array(data, dtype=np.float64, copy=True)
+    n = a.shape[-1]
+    while n >= 2:
+        nh = n // 2
+        ii = np.arange(nh)
+        h = np.zeros(a.shape[:-1] + (nh,))
+        g = np.zeros(a.shape[:-1] + (nh,))
+        for k in range(4):
+            v = a[..., (2 * ii + k) & (n - 1)]
+            h = h + H[k] * v
+            g = g + G[k] * v
+        a[..., :nh] = h
+        a[..., nh:n] = g
+        n = nh
+    return a
+
+
+def inverse(coef: np.ndarray) -> np.ndarray:
+    """Inverse transform along the last axis: levels n = 2, 4, ..., each output
+    accumulating its contributions in the order the pyramid visits them."""
+    a = np.array(coef, dtype=np.float64, copy=True)
+    total = a.shape[-1]
+    n = 2
+    while n <= total:
+        nh = n // 2
+        out = np.zeros(a.shape[:-1] + (n,))
+        for i in range(nh):
+            ai = a[..., i]
+            ai1 = a[..., i + nh]
+            for k in range(4):
+                jf = (2 * i + k) & (n - 1)
+                out[..., jf] = out[..., jf] + (H[k] * ai + G[k] * ai1)
+        a[..., :n] = out
+        n *= 2
+    return a
+
+
+def compress(Gd: np.ndarray, order: np.ndarray, rel: float):
+    """Rows of the dense G (Nd x Nm), cells in `order` (Mesh::get_reordered_id),
+    transformed and thresholded: (n_dy, rowptr, cols, vals)."""
+    nd, nm = Gd.shape
+    n_dy = padded_length(nm)
+    data = np.zeros((nd, n_dy))
+    data[:, :nm] = Gd[:, order]
+    c = forward(data)
+    rowptr = [0]
+    cols, vals = [], []
+    for r in range(nd):
+        a = np.abs(c[r])
+        thr = rel * a.max()
+        keep = np.nonzero((a > thr) | (np.abs(a - thr) < 1e-15))[0]
+        cols.append(keep)
+        vals.append(c[r, keep])
+        rowptr.append(rowptr[-1] + keep.size)
+    return n_dy, np.array(rowptr, dtype=np.int64), np.concatenate(cols), np.concatenate(vals)
+
+
+def G_vec_mul(comp, order: np.ndarray, x: np.ndarray) -> np.ndarray:
+    n_dy, rowptr, cols, vals = comp
+    w = np.zeros(n_dy)
+    w[:order.size] = x[order]
+    w = forward(w)
+    y = np.empty(rowptr.size - 1)
+    for r in range(y.size):
+        s = slice(rowptr[r], rowptr[r + 1])
+        p = vals[s] * w[cols[s]]
+        y[r] = np.cumsum(p)[-1] if p.size else 0.0
+    return y
+
+
+def GT_vec_mul(comp, order: np.ndarray, y: np.ndarray) -> np.ndarray:
+    n_dy, rowptr, cols, vals = comp
+    pw = np.zeros(n_dy)
+    for r in range(rowptr.size - 1):
+        s = slice(rowptr[r], rowptr[r + 1])
+        pw[cols[s]] = pw[cols[s]] + vals[s] * y[r]
+    pw = inverse(pw)
+    x = np.empty(order.size)
+    x[order] = pw[:order.size]
+    return x
