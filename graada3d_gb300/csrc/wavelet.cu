@@ -13,20 +13,28 @@
 // the coefficients with |c| > t or ||c| - t| < 1e-15, t = threshold x the
 // row's largest |c|, in coefficient order.
 //
-//   G x:   x reordered and padded, transformed; each row's kept coefficients
-//          dotted with it in stored order.
-//   G^T y: the kept coefficients gathered per coefficient index over the rows
-//          in ascending order (a stable sort by index gives that layout), the
-//          inverse pyramid (levels 2, 4, ..., n_dy), the result put back in
-//          cell order.
-// Every sum runs in the reference's order from zero, as explicit
-// round-to-nearest operations.  The compression assembles the FP64 G first
-// (it must fit on the device) and releases it afterwards.
+// Like the reference, the compression never holds the dense G: the rows are
+// assembled (FP64, the tiled assembly) for a batch of observation points at a
+// time, transformed and thresholded; a first pass counts each row's kept
+// coefficients, a second assembles again and fills them in.
+//
+//   G x:   x reordered and padded, transformed; one warp per row dots the
+//          row's kept coefficients with it, lane l summing entries l, l + 32,
+//          ... in order, then a fixed butterfly over the lanes.
+//   G^T y: rows in 304 consecutive blocks; a block adds its rows' scaled
+//          coefficients into its own partial vector, row after row; the
+//          partials are added in block order; then the inverse pyramid
+//          (levels 2, 4, ..., n_dy) and the cell order.
+// These fixed orders differ from the reference's sequential sums at the
+// rounding level; the oracle reproduces them.  Every operation is an explicit
+// round-to-nearest one.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
-#include <cub/device/device_radix_sort.cuh>
+#include <cub/block/block_reduce.cuh>
+#include <cub/block/block_scan.cuh>
 
 #include "common.cuh"
 #include "context.h"
@@ -36,6 +44,7 @@ namespace grada {
 namespace {
 
 constexpr int WV_THREADS = 256;
+constexpr int kGtBlocks = 304;  // row blocks of G^T y
 
 // (1 + sqrt 3, 3 + sqrt 3, 3 - sqrt 3, 1 - sqrt 3) / (4 sqrt 2), correctly rounded
 __constant__ double kH[4] = {0.48296291314453416, 0.8365163037378079, 0.2241438680420134,
@@ -45,39 +54,48 @@ __constant__ double kG[4] = {-0.12940952255126037, -0.2241438680420134, 0.836516
 
 unsigned grid_for(int64_t n) { return (unsigned)std::max<int64_t>(1, ceil_div(n, WV_THREADS)); }
 
-// P[j * B + r] = G(rows r0 + r, cell order[j]) for j < nm, zero beyond (and for
-// rows past nd).
-__global__ void load_rows_kernel(const double *__restrict__ G, int64_t ld, int64_t nd, int64_t r0,
-                                 int64_t B, const int *__restrict__ order, int64_t nm,
-                                 int64_t n_dy, double *__restrict__ P) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= B * n_dy) return;
-  const int64_t r = t % B, j = t / B;
-  double v = 0.0;
-  if (j < nm && r0 + r < nd) v = G[(int64_t)order[j] * ld + r0 + r];
-  P[t] = v;
+// P[r * n_dy + j] = Gb(r, order[j]) for j < nm, zero up to n_dy: a 32 x 32
+// tiled transpose (coalesced reads down G's columns, coalesced row writes).
+__global__ void load_rows_kernel(const double *__restrict__ Gb, int64_t ldb, int64_t rows,
+                                 const int *__restrict__ order, int64_t nm, int64_t n_dy,
+                                 double *__restrict__ P) {
+  __shared__ double tile[32][33];
+  const int64_t j0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int q = 0; q < 4; q++) {
+    const int64_t j = j0 + ty + 8 * q, r = r0 + tx;
+    double v = 0.0;
+    if (j < nm && r < rows) v = Gb[(int64_t)order[j] * ldb + r];
+    tile[ty + 8 * q][tx] = v;
+  }
+  __syncthreads();
+  for (int q = 0; q < 4; q++) {
+    const int64_t r = r0 + ty + 8 * q, j = j0 + tx;
+    if (r < rows && j < n_dy) P[r * n_dy + j] = tile[tx][ty + 8 * q];
+  }
 }
 
-// One forward level of length n on B interleaved vectors: approximations to
-// approx[ii * B + r], details to coef[(nh + ii) * B + r] (at n = 2 approx is
+// One forward level of length n on `rows` vectors of stride S: approximations
+// to approx[r * S + ii], details to coef[r * S + nh + ii] (at n = 2 approx is
 // coef itself: the two writes never meet).
 __global__ void forward_level_kernel(const double *__restrict__ src, double *approx, double *coef,
-                                     int64_t B, int64_t n,
+                                     int64_t rows, int64_t S, int64_t n,
                                      const int *__restrict__ skip) {
   if (skip && *skip) return;
   const int64_t nh = n >> 1;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= B * nh) return;
-  const int64_t r = t % B, ii = t / B;
+  if (t >= rows * nh) return;
+  const int64_t ii = t % nh, r = t / nh;
+  const double *a = src + r * S;
   double h = 0.0, g = 0.0;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    const double a = src[((2 * ii + k) & (n - 1)) * B + r];
-    h = __dadd_rn(h, __dmul_rn(kH[k], a));
-    g = __dadd_rn(g, __dmul_rn(kG[k], a));
+    const double v = a[(2 * ii + k) & (n - 1)];
+    h = __dadd_rn(h, __dmul_rn(kH[k], v));
+    g = __dadd_rn(g, __dmul_rn(kG[k], v));
   }
-  approx[ii * B + r] = h;
-  coef[(nh + ii) * B + r] = g;
+  approx[r * S + ii] = h;
+  coef[r * S + nh + ii] = g;
 }
 
 __device__ __forceinline__ bool kept(double c, double thr) {
@@ -85,72 +103,62 @@ __device__ __forceinline__ bool kept(double c, double thr) {
   return a > thr || fabs(__dsub_rn(a, thr)) < 1e-15;
 }
 
-__device__ double row_threshold(const double *__restrict__ coef, int64_t B, int64_t r,
-                                int64_t n_dy, double rel) {
-  double mx = fabs(coef[r]);
-  for (int64_t i = 1; i < n_dy; i++) mx = fmax(mx, fabs(coef[i * B + r]));
-  return __dmul_rn(rel, mx);
+// Global row of batch row r: component r / pb of point p0 + r % pb.
+__device__ __forceinline__ int64_t global_row(int64_t r, int64_t pb, int64_t p0, int64_t n_obs) {
+  return (r / pb) * n_obs + p0 + r % pb;
 }
 
-__global__ void count_rows_kernel(const double *__restrict__ coef, int64_t B, int64_t rows,
-                                  int64_t n_dy, double rel, int64_t *__restrict__ count) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
-  const double thr = row_threshold(coef, B, r, n_dy, rel);
-  int64_t c = 0;
-  for (int64_t i = 0; i < n_dy; i++) c += kept(coef[i * B + r], thr) ? 1 : 0;
-  count[r] = c;
+__device__ double block_row_threshold(const double *__restrict__ c, int64_t n_dy, double rel) {
+  using Reduce = cub::BlockReduce<double, WV_THREADS>;
+  __shared__ typename Reduce::TempStorage tmp;
+  __shared__ double thr;
+  double mx = 0.0;
+  for (int64_t i = threadIdx.x; i < n_dy; i += WV_THREADS) mx = fmax(mx, fabs(c[i]));
+  mx = Reduce(tmp).Reduce(mx, [](double a, double b) { return fmax(a, b); });
+  if (threadIdx.x == 0) thr = __dmul_rn(rel, mx);
+  __syncthreads();
+  return thr;
 }
 
-__global__ void fill_rows_kernel(const double *__restrict__ coef, int64_t B, int64_t rows,
-                                 int64_t n_dy, double rel, const int64_t *__restrict__ rowptr,
-                                 int *__restrict__ col, double *__restrict__ val) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
-  const double thr = row_threshold(coef, B, r, n_dy, rel);
-  int64_t p = rowptr[r];
-  for (int64_t i = 0; i < n_dy; i++) {
-    const double c = coef[i * B + r];
-    if (kept(c, thr)) {
-      col[p] = (int)i;
-      val[p] = c;
-      p++;
+// One block per batch row: the number of kept coefficients.
+__global__ void __launch_bounds__(WV_THREADS)
+    count_rows_kernel(const double *__restrict__ C, int64_t n_dy, double rel, int64_t pb,
+                      int64_t p0, int64_t n_obs, int64_t *__restrict__ count) {
+  using Reduce = cub::BlockReduce<int64_t, WV_THREADS>;
+  __shared__ typename Reduce::TempStorage tmp;
+  const int64_t r = blockIdx.x;
+  const double *c = C + r * n_dy;
+  const double thr = block_row_threshold(c, n_dy, rel);
+  int64_t k = 0;
+  for (int64_t i = threadIdx.x; i < n_dy; i += WV_THREADS) k += kept(c[i], thr) ? 1 : 0;
+  k = Reduce(tmp).Sum(k);
+  if (threadIdx.x == 0) count[global_row(r, pb, p0, n_obs)] = k;
+}
+
+// One block per batch row: the kept coefficients in index order.
+__global__ void __launch_bounds__(WV_THREADS)
+    fill_rows_kernel(const double *__restrict__ C, int64_t n_dy, double rel, int64_t pb,
+                     int64_t p0, int64_t n_obs, const int64_t *__restrict__ rowptr,
+                     int *__restrict__ col, double *__restrict__ val) {
+  using Scan = cub::BlockScan<int, WV_THREADS>;
+  __shared__ typename Scan::TempStorage tmp;
+  const int64_t r = blockIdx.x;
+  const double *c = C + r * n_dy;
+  const double thr = block_row_threshold(c, n_dy, rel);
+  int64_t base = rowptr[global_row(r, pb, p0, n_obs)];
+  for (int64_t i0 = 0; i0 < n_dy; i0 += WV_THREADS) {
+    const int64_t i = i0 + threadIdx.x;
+    const double v = i < n_dy ? c[i] : 0.0;
+    const int flag = (i < n_dy && kept(v, thr)) ? 1 : 0;
+    int pos, total;
+    Scan(tmp).ExclusiveSum(flag, pos, total);
+    if (flag) {
+      col[base + pos] = (int)i;
+      val[base + pos] = v;
     }
+    base += total;
+    __syncthreads();  // tmp is reused by the next chunk
   }
-}
-
-__global__ void row_of_entry_kernel(const int64_t *__restrict__ rowptr, int64_t nd,
-                                    int *__restrict__ row_of, int *__restrict__ seq) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nd) return;
-  for (int64_t k = rowptr[r]; k < rowptr[r + 1]; k++) {
-    row_of[k] = (int)r;
-    seq[k] = (int)k;
-  }
-}
-
-// t_rowptr[c] = first position of a key >= c in the sorted keys (c <= n_dy).
-__global__ void column_starts_kernel(const int *__restrict__ keys, int64_t nnz, int64_t n_dy,
-                                     int64_t *__restrict__ t_rowptr) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c > n_dy) return;
-  int64_t lo = 0, hi = nnz;
-  while (lo < hi) {
-    const int64_t mid = (lo + hi) >> 1;
-    if (keys[mid] < c) lo = mid + 1;
-    else hi = mid;
-  }
-  t_rowptr[c] = lo;
-}
-
-__global__ void gather_transpose_kernel(const int *__restrict__ perm, const int *__restrict__ row_of,
-                                        const double *__restrict__ val, int64_t nnz,
-                                        int *__restrict__ t_row, double *__restrict__ t_val) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nnz) return;
-  const int e = perm[p];
-  t_row[p] = row_of[e];
-  t_val[p] = val[e];
 }
 
 // ---- products --------------------------------------------------------------
@@ -169,27 +177,44 @@ __global__ void row_dot_kernel(const int64_t *__restrict__ rowptr, const int *__
                                int64_t nd, const double *__restrict__ scale,
                                double *__restrict__ y, const int *__restrict__ skip) {
   if (skip && *skip) return;
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (r >= nd) return;
   double s = 0.0;
-  for (int64_t k = rowptr[r]; k < rowptr[r + 1]; k++) s = __dadd_rn(s, __dmul_rn(val[k], w[col[k]]));
-  y[r] = scale ? __dmul_rn(s, scale[r]) : s;
+  for (int64_t k = rowptr[r] + lane; k < rowptr[r + 1]; k += 32)
+    s = __dadd_rn(s, __dmul_rn(val[k], w[col[k]]));
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) s = __dadd_rn(s, __shfl_xor_sync(0xffffffffu, s, off));
+  if (lane == 0) y[r] = scale ? __dmul_rn(s, scale[r]) : s;
 }
 
-__global__ void column_gather_kernel(const int64_t *__restrict__ t_rowptr,
-                                     const int *__restrict__ t_row, const double *__restrict__ t_val,
-                                     const double *__restrict__ y, const double *__restrict__ scale,
-                                     int64_t n_dy, double *__restrict__ w,
-                                     const int *__restrict__ skip) {
+// Block b adds rows [b R, (b + 1) R) into part[b * n_dy + c], row after row.
+__global__ void __launch_bounds__(WV_THREADS)
+    gt_partial_kernel(const int64_t *__restrict__ rowptr, const int *__restrict__ col,
+                      const double *__restrict__ val, const double *__restrict__ y,
+                      const double *__restrict__ scale, int64_t nd, int64_t R, int64_t n_dy,
+                      double *__restrict__ part, const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  double *p = part + (int64_t)blockIdx.x * n_dy;
+  const int64_t r_last = ((int64_t)blockIdx.x + 1) * R;
+  const int64_t r_end = r_last < nd ? r_last : nd;
+  for (int64_t r = (int64_t)blockIdx.x * R; r < r_end; r++) {
+    const double v = scale ? __dmul_rn(scale[r], y[r]) : y[r];
+    for (int64_t k = rowptr[r] + threadIdx.x; k < rowptr[r + 1]; k += WV_THREADS) {
+      const int c = col[k];
+      p[c] = __dadd_rn(p[c], __dmul_rn(val[k], v));
+    }
+    __syncthreads();  // the next row may touch the same entries
+  }
+}
+
+__global__ void gt_reduce_kernel(const double *__restrict__ part, int64_t nb, int64_t n_dy,
+                                 double *__restrict__ w, const int *__restrict__ skip) {
   if (skip && *skip) return;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n_dy) return;
   double s = 0.0;
-  for (int64_t p = t_rowptr[c]; p < t_rowptr[c + 1]; p++) {
-    const int r = t_row[p];
-    const double v = scale ? __dmul_rn(scale[r], y[r]) : y[r];
-    s = __dadd_rn(s, __dmul_rn(t_val[p], v));
-  }
+  for (int64_t b = 0; b < nb; b++) s = __dadd_rn(s, part[b * n_dy + c]);
   w[c] = s;
 }
 
@@ -204,9 +229,9 @@ __global__ void inverse_level_kernel(const double *__restrict__ a, const double 
   const int64_t nh = n >> 1;
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  const int k0 = (int)(j & 1);                   // k of the contribution from ii = j >> 1
+  const int k0 = (int)(j & 1);             // k of the contribution from ii = j >> 1
   const int64_t ia = j >> 1;
-  const int64_t ib = (ia + nh - 1) % nh;        // k0 + 2
+  const int64_t ib = (ia + nh - 1) % nh;  // the contribution with k0 + 2
   const double ca = __dadd_rn(__dmul_rn(kH[k0], a[ia]), __dmul_rn(kG[k0], coef[nh + ia]));
   const double cb =
       __dadd_rn(__dmul_rn(kH[k0 + 2], a[ib]), __dmul_rn(kG[k0 + 2], coef[nh + ib]));
@@ -221,6 +246,24 @@ __global__ void store_vec_kernel(const double *__restrict__ w, const int *__rest
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nm) return;
   x[order[j]] = w[j];
+}
+
+// Forward pyramid of `rows` vectors of stride n_dy held in P0; details land in
+// C, the last approximation in C[r * n_dy]; P0 and P1 take the intermediate
+// approximations in turn.
+void forward_pyramid(double *P0, double *P1, double *C, int64_t rows, int64_t n_dy,
+                     const int *skip, cudaStream_t s) {
+  const double *src = P0;
+  double *bufs[2] = {P1, P0};
+  int flip = 0;
+  for (int64_t n = n_dy; n >= 2; n >>= 1) {
+    double *dst = n == 2 ? C : bufs[flip];
+    forward_level_kernel<<<grid_for(rows * (n >> 1)), WV_THREADS, 0, s>>>(src, dst, C, rows, n_dy,
+                                                                          n, skip);
+    GRADA_LAUNCH_CHECK();
+    src = dst;
+    flip ^= 1;
+  }
 }
 
 }  // namespace
@@ -247,103 +290,78 @@ void Context::compute_G_wavelet(const int64_t *h_order, double rel) {
   int64_t n_dy = 1;
   while (n_dy < nm) n_dy <<= 1;
 
-  compute_G(GRADA_G_FP64);  // the rows to compress; released below
+  // the old G goes first: the compressed rows replace it
   g_storage = -1;
+  g64_valid = false;
+  G.release();
+  G64.release();
   wv_order.alloc(this, sizeof(int) * (size_t)nm);
   upload(wv_order.ptr, order.data(), sizeof(int) * (size_t)nm);
 
-  // rows in batches: three n_dy x B buffers of at most ~6 GB together
-  const int64_t budget = (int64_t)6 << 30;
-  int64_t B = std::max<int64_t>(32, (budget / (3 * 8 * n_dy)) / 32 * 32);
-  B = std::min(B, round_up(nd, 32));
-  DevBuf P0, P1, C, cnt;
-  P0.alloc(this, sizeof(double) * (size_t)(B * n_dy));
-  P1.alloc(this, sizeof(double) * (size_t)(B * std::max<int64_t>(n_dy / 2, 1)));
-  C.alloc(this, sizeof(double) * (size_t)(B * n_dy));
-  cnt.alloc(this, sizeof(int64_t) * (size_t)B);
-  const double *Gd = G.as<double>();
-  auto transform_batch = [&](int64_t r0) {
-    load_rows_kernel<<<grid_for(B * n_dy), WV_THREADS, 0, stream>>>(
-        Gd, ld, nd, r0, B, wv_order.as<int>(), nm, n_dy, P0.as<double>());
+  // points per batch: the batch's FP64 rows (ldb x nm) and three n_dy-long
+  // buffers per row within ~8 GB
+  const int64_t budget = (int64_t)8 << 30;
+  const int64_t per_row = 8 * (nm + 3 * n_dy);
+  int64_t pb = std::max<int64_t>(1, budget / (per_row * n_fields));
+  if (const char *e = std::getenv("GRADA_WAVELET_BATCH_POINTS"))  // smaller batches for tests
+    pb = std::max<int64_t>(1, std::atoll(e));
+  pb = std::min(pb, n_obs);
+  const int64_t rows_max = pb * n_fields, ldb = round_up(rows_max, 32);
+  DevBuf Gb, P0, P1, C, cnt;
+  Gb.alloc(this, sizeof(double) * (size_t)(ldb * nm));
+  P0.alloc(this, sizeof(double) * (size_t)(rows_max * n_dy));
+  P1.alloc(this, sizeof(double) * (size_t)(rows_max * n_dy));
+  C.alloc(this, sizeof(double) * (size_t)(rows_max * n_dy));
+  cnt.alloc(this, sizeof(int64_t) * (size_t)nd);
+  const DevGeometry g_all = geometry();
+  const TilePlan plan = tile_plan();
+  auto transform_batch = [&](int64_t p0, int64_t np) {
+    DevGeometry g = g_all;  // the batch's points only: rows k * np + i
+    g.obs = g_all.obs + 3 * p0;
+    g.n_obs = np;
+    launch_assemble_tiled_fp64(g, plan, Gb.as<double>(), ldb, stream);
+    const int64_t rows = np * n_fields;
+    dim3 grid((unsigned)ceil_div(n_dy, 32), (unsigned)ceil_div(rows, 32));
+    load_rows_kernel<<<grid, dim3(32, 8), 0, stream>>>(Gb.as<double>(), ldb, rows,
+                                                      wv_order.as<int>(), nm, n_dy,
+                                                      P0.as<double>());
     GRADA_LAUNCH_CHECK();
-    double *src = P0.as<double>();
-    double *bufs[2] = {P1.as<double>(), P0.as<double>()};
-    int flip = 0;
-    for (int64_t n = n_dy; n >= 2; n >>= 1) {
-      double *dst = n == 2 ? C.as<double>() : bufs[flip];
-      forward_level_kernel<<<grid_for(B * (n >> 1)), WV_THREADS, 0, stream>>>(
-          src, dst, C.as<double>(), B, n, nullptr);
-      GRADA_LAUNCH_CHECK();
-      src = dst;
-      flip ^= 1;
-    }
+    forward_pyramid(P0.as<double>(), P1.as<double>(), C.as<double>(), rows, n_dy, nullptr, stream);
+    return rows;
   };
-  // The level writing into P0 reads P1 and vice versa; P0 holds n_dy, P1 n_dy/2
-  // entries per row, enough for every level after the first.
-  std::vector<int64_t> rowptr((size_t)nd + 1, 0), part((size_t)B);
-  for (int64_t r0 = 0; r0 < nd; r0 += B) {
-    const int64_t rows = std::min(B, nd - r0);
-    transform_batch(r0);
-    count_rows_kernel<<<grid_for(rows), WV_THREADS, 0, stream>>>(C.as<double>(), B, rows, n_dy,
-                                                                 rel, cnt.as<int64_t>());
+  for (int64_t p0 = 0; p0 < n_obs; p0 += pb) {
+    const int64_t np = std::min(pb, n_obs - p0);
+    const int64_t rows = transform_batch(p0, np);
+    count_rows_kernel<<<(unsigned)rows, WV_THREADS, 0, stream>>>(C.as<double>(), n_dy, rel, np, p0,
+                                                                n_obs, cnt.as<int64_t>());
     GRADA_LAUNCH_CHECK();
-    download(part.data(), cnt.ptr, sizeof(int64_t) * (size_t)rows);
-    sync();
-    for (int64_t r = 0; r < rows; r++)
-      rowptr[(size_t)(r0 + r + 1)] = rowptr[(size_t)(r0 + r)] + part[(size_t)r];
   }
+  std::vector<int64_t> counts((size_t)nd), rowptr((size_t)nd + 1, 0);
+  download(counts.data(), cnt.ptr, sizeof(int64_t) * (size_t)nd);
+  sync();
+  for (int64_t r = 0; r < nd; r++) rowptr[(size_t)r + 1] = rowptr[(size_t)r] + counts[(size_t)r];
   const int64_t nnz = rowptr[(size_t)nd];
-  if (nnz >= ((int64_t)1 << 31) - 1)
-    throw Error(GRADA_ERR_INVALID_ARGUMENT, "too many kept coefficients (raise the threshold)");
   wv_rowptr.alloc(this, sizeof(int64_t) * ((size_t)nd + 1));
   wv_col.alloc(this, sizeof(int) * (size_t)std::max<int64_t>(nnz, 1));
   wv_val.alloc(this, sizeof(double) * (size_t)std::max<int64_t>(nnz, 1));
   upload(wv_rowptr.ptr, rowptr.data(), sizeof(int64_t) * ((size_t)nd + 1));
-  for (int64_t r0 = 0; r0 < nd; r0 += B) {
-    const int64_t rows = std::min(B, nd - r0);
-    transform_batch(r0);
-    fill_rows_kernel<<<grid_for(rows), WV_THREADS, 0, stream>>>(
-        C.as<double>(), B, rows, n_dy, rel, wv_rowptr.as<int64_t>() + r0, wv_col.as<int>(),
+  for (int64_t p0 = 0; p0 < n_obs; p0 += pb) {
+    const int64_t np = std::min(pb, n_obs - p0);
+    const int64_t rows = transform_batch(p0, np);
+    fill_rows_kernel<<<(unsigned)rows, WV_THREADS, 0, stream>>>(
+        C.as<double>(), n_dy, rel, np, p0, n_obs, wv_rowptr.as<int64_t>(), wv_col.as<int>(),
         wv_val.as<double>());
     GRADA_LAUNCH_CHECK();
   }
   sync();
+  Gb.release();
   P0.release();
   P1.release();
   C.release();
-  G.release();  // the reference drops the dense G too (Fwd.cpp:159)
-
-  // coefficient-major copy: a stable sort of the entries by coefficient index
-  DevBuf row_of, seq, keys_out, perm, sort_tmp;
-  const int64_t m = std::max<int64_t>(nnz, 1);
-  row_of.alloc(this, sizeof(int) * (size_t)m);
-  seq.alloc(this, sizeof(int) * (size_t)m);
-  keys_out.alloc(this, sizeof(int) * (size_t)m);
-  perm.alloc(this, sizeof(int) * (size_t)m);
-  row_of_entry_kernel<<<grid_for(nd), WV_THREADS, 0, stream>>>(wv_rowptr.as<int64_t>(), nd,
-                                                               row_of.as<int>(), seq.as<int>());
-  GRADA_LAUNCH_CHECK();
-  int end_bit = 1;
-  while (((int64_t)1 << end_bit) <= n_dy) end_bit++;
-  size_t sort_bytes = 0;
-  GRADA_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, wv_col.as<int>(),
-                                                   keys_out.as<int>(), seq.as<int>(), perm.as<int>(),
-                                                   (int)nnz, 0, end_bit, stream));
-  sort_tmp.alloc(this, std::max<size_t>(sort_bytes, 16));
-  GRADA_CUDA_CHECK(cub::DeviceRadixSort::SortPairs(sort_tmp.ptr, sort_bytes, wv_col.as<int>(),
-                                                   keys_out.as<int>(), seq.as<int>(), perm.as<int>(),
-                                                   (int)nnz, 0, end_bit, stream));
-  wv_trowptr.alloc(this, sizeof(int64_t) * ((size_t)n_dy + 1));
-  wv_trow.alloc(this, sizeof(int) * (size_t)m);
-  wv_tval.alloc(this, sizeof(double) * (size_t)m);
-  column_starts_kernel<<<grid_for(n_dy + 1), WV_THREADS, 0, stream>>>(
-      keys_out.as<int>(), nnz, n_dy, wv_trowptr.as<int64_t>());
-  GRADA_LAUNCH_CHECK();
-  gather_transpose_kernel<<<grid_for(nnz), WV_THREADS, 0, stream>>>(
-      perm.as<int>(), row_of.as<int>(), wv_val.as<double>(), nnz, wv_trow.as<int>(),
-      wv_tval.as<double>());
-  GRADA_LAUNCH_CHECK();
-  sync();
+  // G^T y's row blocks and their partial vectors
+  wv_rows_per_block = std::max<int64_t>(1, ceil_div(nd, kGtBlocks));
+  wv_blocks = ceil_div(nd, wv_rows_per_block);
+  wv_part.alloc(this, sizeof(double) * (size_t)(wv_blocks * n_dy));
   wv_ndy = n_dy;
   wv_nnz = nnz;
   g_storage = GRADA_G_WAVELET;
@@ -355,19 +373,9 @@ void Context::apply_G_wavelet(const double *x, double *y, const GemvOpts &o) {
   load_vec_kernel<<<grid_for(wv_ndy), WV_THREADS, 0, stream>>>(x, wv_order.as<int>(), n_cells,
                                                                wv_ndy, P0, o.skip);
   GRADA_LAUNCH_CHECK();
-  double *src = P0;
-  double *bufs[2] = {P1, P0};
-  int flip = 0;
-  for (int64_t n = wv_ndy; n >= 2; n >>= 1) {
-    double *dst = n == 2 ? W : bufs[flip];
-    forward_level_kernel<<<grid_for(n >> 1), WV_THREADS, 0, stream>>>(src, dst, W, 1, n, o.skip);
-    GRADA_LAUNCH_CHECK();
-    src = dst;
-    flip ^= 1;
-  }
-  row_dot_kernel<<<grid_for(nd), WV_THREADS, 0, stream>>>(wv_rowptr.as<int64_t>(), wv_col.as<int>(),
-                                                          wv_val.as<double>(), W, nd, o.scale, y,
-                                                          o.skip);
+  forward_pyramid(P0, P1, W, 1, wv_ndy, o.skip, stream);
+  row_dot_kernel<<<grid_for(nd * 32), WV_THREADS, 0, stream>>>(
+      wv_rowptr.as<int64_t>(), wv_col.as<int>(), wv_val.as<double>(), W, nd, o.scale, y, o.skip);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -375,9 +383,14 @@ void Context::apply_GT_wavelet(const double *y, double *x, const GemvOpts &o) {
   double *sc = scratch.as<double>();
   double *W = sc + 2 * wv_ndy;
   double *bufs[2] = {sc, sc + wv_ndy};
-  column_gather_kernel<<<grid_for(wv_ndy), WV_THREADS, 0, stream>>>(
-      wv_trowptr.as<int64_t>(), wv_trow.as<int>(), wv_tval.as<double>(), y, o.scale, wv_ndy, W,
-      o.skip);
+  GRADA_CUDA_CHECK(cudaMemsetAsync(wv_part.ptr, 0, sizeof(double) * (size_t)(wv_blocks * wv_ndy),
+                                   stream));
+  gt_partial_kernel<<<(unsigned)wv_blocks, WV_THREADS, 0, stream>>>(
+      wv_rowptr.as<int64_t>(), wv_col.as<int>(), wv_val.as<double>(), y, o.scale, nd,
+      wv_rows_per_block, wv_ndy, wv_part.as<double>(), o.skip);
+  GRADA_LAUNCH_CHECK();
+  gt_reduce_kernel<<<grid_for(wv_ndy), WV_THREADS, 0, stream>>>(wv_part.as<double>(), wv_blocks,
+                                                                wv_ndy, W, o.skip);
   GRADA_LAUNCH_CHECK();
   const double *a = W;  // the level-2 approximation is coef[0]
   int flip = 0;

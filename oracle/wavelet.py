@@ -11,7 +11,10 @@ periodic Daubechies-4 pyramid algorithm GSL implements: the four-tap scaling
 filter h of Daubechies (1988), the wavelet filter g_k = (-1)^k h_{3-k}, no
 offset, levels n = n_dy, n_dy / 2, ..., 2 (forward) with the approximations of
 a level in entries [0, n/2) and its details in [n/2, n), every sum accumulated
-in index order from zero.  Parity with GSL itself is unpinned; the device path
+in index order from zero.  The products sum in the device's fixed parallel
+orders (documented at G_vec_mul / GT_vec_mul), which differ from the
+reference's sequential sums at the rounding level.  Parity with GSL itself is
+unpinned; the device path
 is checked against this restatement, and the restatement against the
 transform's own properties (orthogonality, exact reconstruction, vanishing
 moments).
@@ -92,7 +95,24 @@ def compress(Gd: np.ndarray, order: np.ndarray, rel: float):
     return n_dy, np.array(rowptr, dtype=np.int64), np.concatenate(cols), np.concatenate(vals)
 
 
+GT_BLOCKS = 304  # row blocks of the device's G^T y
+
+
+def _warp_sum(p: np.ndarray) -> float:
+    """The device's row sum: lane l adds entries l, l + 32, ... in order from
+    zero, then lanes combine by a butterfly (xor 16, 8, 4, 2, 1)."""
+    lanes = np.zeros(32)
+    for l in range(min(32, p.size)):
+        lanes[l] = np.cumsum(p[l::32])[-1]
+    for off in (16, 8, 4, 2, 1):
+        lanes = lanes + lanes[np.arange(32) ^ off]
+    return float(lanes[0])
+
+
 def G_vec_mul(comp, order: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """Fwd::G_vec_mul's wavelet branch (Fwd.cpp:113-140): x reordered, padded
+    and transformed, each row's kept coefficients dotted with it (summed in the
+    device's fixed order instead of the reference's sequential one)."""
     n_dy, rowptr, cols, vals = comp
     w = np.zeros(n_dy)
     w[:order.size] = x[order]
@@ -100,17 +120,25 @@ def G_vec_mul(comp, order: np.ndarray, x: np.ndarray) -> np.ndarray:
     y = np.empty(rowptr.size - 1)
     for r in range(y.size):
         s = slice(rowptr[r], rowptr[r + 1])
-        p = vals[s] * w[cols[s]]
-        y[r] = np.cumsum(p)[-1] if p.size else 0.0
+        y[r] = _warp_sum(vals[s] * w[cols[s]])
     return y
 
 
 def GT_vec_mul(comp, order: np.ndarray, y: np.ndarray) -> np.ndarray:
+    """Fwd::GT_vec_mul's wavelet branch (Fwd.cpp:80-112): the kept coefficients
+    times y added per coefficient index -- the rows in consecutive blocks of
+    ceil(Nd / 304), each block's rows in order into its own partial vector, the
+    partials in block order -- then the inverse transform and the cell order."""
     n_dy, rowptr, cols, vals = comp
+    nd = rowptr.size - 1
+    R = max(1, -(-nd // GT_BLOCKS))
     pw = np.zeros(n_dy)
-    for r in range(rowptr.size - 1):
-        s = slice(rowptr[r], rowptr[r + 1])
-        pw[cols[s]] = pw[cols[s]] + vals[s] * y[r]
+    for b0 in range(0, nd, R):
+        part = np.zeros(n_dy)
+        for r in range(b0, min(nd, b0 + R)):
+            s = slice(rowptr[r], rowptr[r + 1])
+            part[cols[s]] = part[cols[s]] + vals[s] * y[r]
+        pw = pw + part
     pw = inverse(pw)
     x = np.empty(order.size)
     x[order] = pw[:order.size]

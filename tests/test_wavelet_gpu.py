@@ -1,7 +1,7 @@
 """The wavelet-compressed G on the device (grada_compute_G_wavelet) against
 the oracle's restatement of Fwd::compute_G_wavelet and the wavelet products,
 on the device's own FP64 G: the same kept coefficients, bitwise, and bitwise
-products (the device sums in the reference's order)."""
+products (the oracle reproduces the device's summation orders)."""
 import numpy as np
 import pytest
 
@@ -32,9 +32,14 @@ def _refined():
     return o, obs
 
 
-@pytest.mark.parametrize("case,rel", [("regular", 5e-4), ("regular", 0.0), ("refined", 5e-4),
-                                      ("refined", 1e-2)])
-def test_wavelet_rows_and_products_match_oracle(gpu_ctx, case, rel):
+@pytest.mark.parametrize("case,rel,batch", [("regular", 5e-4, None), ("regular", 0.0, None),
+                                            ("refined", 5e-4, None), ("refined", 1e-2, None),
+                                            ("regular", 5e-4, 7), ("refined", 5e-4, 50)])
+def test_wavelet_rows_and_products_match_oracle(gpu_ctx, monkeypatch, case, rel, batch):
+    """batch: observation points per assembly batch of the compression (the
+    rows of a batch interleave with other batches' in G's row order)."""
+    if batch is not None:
+        monkeypatch.setenv("GRADA_WAVELET_BATCH_POINTS", str(batch))
     o, obs = _regular() if case == "regular" else _refined()
     prisms, order = o.leaves(), o.wavelet_order()
     inv = GaussNewtonInversion(prisms, obs, 0x012, ctx=gpu_ctx)
