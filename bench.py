@@ -1042,6 +1042,74 @@ def run_wavelet_case(rel: float = 5e-4):
     return out
 
 
+def run_wavelet_1m(rel: float = 5e-4):
+    """The wavelet-compressed G at the matrix-free case's size: 128 x 128 x 64 =
+    1,048,576 cells over [0, 20 km]^2 x [0, 8 km], gz + Tzz at 201 x 201 points 50 m
+    above (the FP64 G would be 678 GB).  Compression at the reference's example
+    threshold (5e-4) in batches of points, never holding the dense G; then G x
+    and G^T y on the compressed rows (CUDA events, 5 runs each) against one
+    matrix-free FP64 product of each, and the relative error of the compressed
+    G x on a two-box model."""
+    import ctypes
+
+    import torch
+
+    from graada3d_gb300 import mesh
+    from graada3d_gb300.inversion import GaussNewtonInversion
+
+    o = mesh.Octree.regular((0.0, 20000.0), 128, (0.0, 20000.0), 128, (0.0, 8000.0), 64)
+    prisms = mesh.regular_mesh((0.0, 20000.0), 128, (0.0, 20000.0), 128, (0.0, 8000.0), 64)
+    order = o.wavelet_order()
+    obs = mesh.observation_grid(201, 0.0, 20000.0, 201, 0.0, 20000.0, -50.0)
+    rho = mesh.set_boxes(prisms, [[5000, 9000, 6000, 12000, 1000, 3000, 300.0],
+                                  [12000, 16000, 4000, 8000, 2000, 5000, -200.0]])
+    inv = GaussNewtonInversion(prisms, obs, 0x012)
+    lib, h = inv.ctx.lib, inv.ctx.handle
+    stream = torch.cuda.ExternalStream(inv.ctx.stream)
+    x = torch.from_numpy(rho).cuda()
+    y = torch.empty(inv.ld, dtype=torch.float64, device="cuda")
+    r = torch.zeros(inv.ld, dtype=torch.float64, device="cuda")
+    r[:inv.Nd] = torch.from_numpy(np.random.default_rng(3).standard_normal(inv.Nd))
+    g = torch.empty(inv.Nm, dtype=torch.float64, device="cuda")
+
+    def timed(fn, a, b, k):
+        inv.ctx.check(fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr())))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn(h, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k * 1e-3
+
+    out = {"case": "wavelet-1m", "cells": inv.Nm, "data": inv.Nd, "threshold": rel}
+    inv.compute_G("matrix_free")
+    out["matrix_free_s"] = {"G_x": timed(lib.grada_G_vec_mul_dev, x, y, 1),
+                            "GT_y": timed(lib.grada_GT_vec_mul_dev, r, g, 1)}
+    d_exact = y[:inv.Nd].cpu().numpy().copy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    inv.compute_G_wavelet(order, rel)
+    torch.cuda.synchronize()
+    out["compress_s"] = time.perf_counter() - t0
+    nnz = ctypes.c_int64()
+    n_dy = ctypes.c_int64()
+    inv.ctx.check(lib.grada_get_wavelet_G(h, ctypes.byref(n_dy), ctypes.byref(nnz), None, None,
+                                          None))
+    out["kept"] = nnz.value
+    out["compression_ratio"] = inv.Nd * n_dy.value / nnz.value
+    out["stored_GB"] = nnz.value * 12 / 1e9
+    out["wavelet_s"] = {"G_x": timed(lib.grada_G_vec_mul_dev, x, y, 5),
+                        "GT_y": timed(lib.grada_GT_vec_mul_dev, r, g, 5)}
+    d_wv = y[:inv.Nd].cpu().numpy()
+    out["G_x_rel_error"] = float(np.linalg.norm(d_wv - d_exact) / np.linalg.norm(d_exact))
+    out["cg_iteration_s"] = {k: out[k]["G_x"] + out[k]["GT_y"] for k in ("matrix_free_s",
+                                                                         "wavelet_s")}
+    inv.ctx.close()
+    return out
+
+
 def run_profile_case(args):
     """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
     50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
@@ -1072,7 +1140,8 @@ def main():
                                                          "gemv", "batched-64", "block-gemm",
                                                          "lambda-sweep-16", "block-gemm-profile",
                                                          "mf-profile", "assembly-refined",
-                                                         "operators-refined", "wavelet"])
+                                                         "operators-refined", "wavelet",
+                                                         "wavelet-1m"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -1094,6 +1163,8 @@ def main():
         print(json.dumps(run_operators_refined()))
     elif args.case == "wavelet":
         print(json.dumps(run_wavelet_case()))
+    elif args.case == "wavelet-1m":
+        print(json.dumps(run_wavelet_1m()))
     elif args.case == "mf-profile":
         run_mf_profile()
     elif args.case == "block-gemm-profile":
