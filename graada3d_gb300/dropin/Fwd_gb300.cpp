@@ -1,8 +1,10 @@
-// Drop-in bodies for the dense path of the reference's Fwd class
-// (src/Forward_modelling/Fwd.cpp:47-146), against the unchanged Fwd.h.
-// A maintainer removes Fwd::compute_G, Fwd::GT_vec_mul and Fwd::G_vec_mul from
-// Fwd.cpp (keeping the constructors and the wavelet members there) and links
-// this file, gb300_bridge.cpp and libgrada_gpu.so instead.
+// Drop-in bodies for the reference's Fwd class (src/Forward_modelling/Fwd.cpp:
+// 47-219), against the unchanged Fwd.h.  A maintainer removes Fwd::compute_G,
+// Fwd::GT_vec_mul, Fwd::G_vec_mul and Fwd::compute_G_wavelet from Fwd.cpp
+// (keeping the constructors and the wavelet helpers there) and links this file,
+// gb300_bridge.cpp and libgrada_gpu.so instead.  With the wavelet-compressed G
+// the library keeps the compressed rows and both products use them, as the
+// reference's G_vec_mul / GT_vec_mul do when use_wavelet is set.
 //
 // G is assembled and kept on the GPU.  Because the reference also reads the
 // member G directly (InversionBase::get_predicted_field, set_depth_weighting
@@ -68,4 +70,26 @@ void Fwd::G_vec_mul(const VectorXd &vec, VectorXd &product) const
   grada_ctx *ctx = gb300::context_for(this);
   product.resize(Nd);
   gb300::check(ctx, grada_G_vec_mul(ctx, vec.data(), product.data()), "grada_G_vec_mul");
+}
+
+// Fwd::compute_G_wavelet (Fwd.cpp:148-219): the rows along the mesh's
+// reordered sequence, compressed on the device at compression_threshold; the
+// member G is emptied as in the reference.
+void Fwd::compute_G_wavelet()
+{
+  assert(Nm > 0);
+  assert(N_obs > 0);
+  grada_ctx *ctx = gb300::context_for(this);
+  bind_geometry(ctx, mesh, ob, field_flag, Nm, N_obs);
+  std::vector<int64_t> order((size_t)Nm);
+  for (int j = 0; j < Nm; j++) order[(size_t)j] = mesh.get_reordered_id((unsigned)j);
+  gb300::check(ctx, grada_compute_G_wavelet(ctx, order.data(), compression_threshold),
+               "grada_compute_G_wavelet");
+  int64_t n_dy = 0, nnz = 0;
+  gb300::check(ctx, grada_get_wavelet_G(ctx, &n_dy, &nnz, nullptr, nullptr, nullptr),
+               "grada_get_wavelet_G");
+  n_dy_for_wavelet = (int)n_dy;
+  comp_col_ids.clear();
+  comp_G_coeffs.clear();
+  G.resize(0, 0);
 }
