@@ -148,8 +148,9 @@ struct Context {
   // wavelet.cu: the wavelet-compressed G (g_storage == GRADA_G_WAVELET): rows
   // (CSR, coefficient index ascending), the cell order the rows run along and
   // the partial vectors of G^T y's row blocks
-  DevBuf wv_order, wv_rowptr, wv_col, wv_val, wv_part;
-  int64_t wv_ndy = 0, wv_nnz = 0, wv_rows_per_block = 1, wv_blocks = 0;
+  DevBuf wv_order, wv_rowptr, wv_col, wv_val, wv_part, wv_segptr;
+  int64_t wv_ndy = 0, wv_nnz = 0, wv_rows_per_block = 1, wv_blocks = 0, wv_seg_len = 1,
+          wv_nseg = 0;
   void compute_G_wavelet(const int64_t *order, double rel);
   void apply_G_wavelet(const double *x, double *y, const GemvOpts &o);
   void apply_GT_wavelet(const double *y, double *x, const GemvOpts &o);

@@ -58,7 +58,7 @@ void Context::release_all() {
     o.rowptr.release(); o.col.release(); o.val.release();
     o.t_rowptr.release(); o.t_col.release(); o.t_val.release();
   }
-  for (DevBuf *b : {&wv_order, &wv_rowptr, &wv_col, &wv_val, &wv_part})
+  for (DevBuf *b : {&wv_order, &wv_rowptr, &wv_col, &wv_val, &wv_part, &wv_segptr})
     b->release();
   DevBuf *bufs[] = {&dobs, &wd, &cg_b, &cg_s, &cg_t, &cg_p, &cg_pp, &cg_r, &cg_atb, &cg_gtw,
                     &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &cg_ctl, &iv_m, &iv_mt, &iv_mt_old,

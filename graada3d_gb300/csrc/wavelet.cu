@@ -22,9 +22,10 @@
 //          row's kept coefficients with it, lane l summing entries l, l + 32,
 //          ... in order, then a fixed butterfly over the lanes.
 //   G^T y: rows in 304 consecutive blocks; a block adds its rows' scaled
-//          coefficients into its own partial vector, row after row; the
-//          partials are added in block order; then the inverse pyramid
-//          (levels 2, 4, ..., n_dy) and the cell order.
+//          coefficients into its own partial vector, row after row (a segment
+//          of 4096 columns at a time, in shared memory); the partials are
+//          added in block order; then the inverse pyramid (levels 2, 4, ...,
+//          n_dy) and the cell order.
 // These fixed orders differ from the reference's sequential sums at the
 // rounding level; the oracle reproduces them.  Every operation is an explicit
 // round-to-nearest one.
@@ -44,7 +45,8 @@ namespace grada {
 namespace {
 
 constexpr int WV_THREADS = 256;
-constexpr int kGtBlocks = 304;  // row blocks of G^T y
+constexpr int kGtBlocks = 304;       // row blocks of G^T y
+constexpr int64_t kGtSegment = 4096;  // columns a block of G^T y accumulates in shared memory
 
 // (1 + sqrt 3, 3 + sqrt 3, 3 - sqrt 3, 1 - sqrt 3) / (4 sqrt 2), correctly rounded
 __constant__ double kH[4] = {0.48296291314453416, 0.8365163037378079, 0.2241438680420134,
@@ -188,24 +190,52 @@ __global__ void row_dot_kernel(const int64_t *__restrict__ rowptr, const int *__
   if (lane == 0) y[r] = scale ? __dmul_rn(s, scale[r]) : s;
 }
 
-// Block b adds rows [b R, (b + 1) R) into part[b * n_dy + c], row after row.
+// seg[r * (S + 1) + s] = the first entry of row r with column >= s * SEG
+// (columns ascend within a row), s = 0..S.
+__global__ void segment_starts_kernel(const int64_t *__restrict__ rowptr,
+                                      const int *__restrict__ col, int64_t nd, int64_t S,
+                                      int64_t SEG, int64_t *__restrict__ seg) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nd * (S + 1)) return;
+  const int64_t r = t / (S + 1), s = t % (S + 1);
+  const int64_t c = s * SEG;
+  int64_t lo = rowptr[r], hi = rowptr[r + 1];
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (col[mid] < c) lo = mid + 1;
+    else hi = mid;
+  }
+  seg[t] = lo;
+}
+
+// Block (b, s) adds the entries of rows [b R, (b + 1) R) with columns in
+// segment s into a shared-memory accumulator, row after row, and writes it to
+// part[b * n_dy + s * SEG + i]: per column the rows of a block in ascending
+// order, as one pass over the whole row would add them.
 __global__ void __launch_bounds__(WV_THREADS)
-    gt_partial_kernel(const int64_t *__restrict__ rowptr, const int *__restrict__ col,
+    gt_partial_kernel(const int64_t *__restrict__ seg, const int *__restrict__ col,
                       const double *__restrict__ val, const double *__restrict__ y,
-                      const double *__restrict__ scale, int64_t nd, int64_t R, int64_t n_dy,
-                      double *__restrict__ part, const int *__restrict__ skip) {
+                      const double *__restrict__ scale, int64_t nd, int64_t R, int64_t S,
+                      int64_t SEG, int64_t n_dy, double *__restrict__ part,
+                      const int *__restrict__ skip) {
   if (skip && *skip) return;
-  double *p = part + (int64_t)blockIdx.x * n_dy;
-  const int64_t r_last = ((int64_t)blockIdx.x + 1) * R;
+  extern __shared__ double acc[];
+  const int64_t b = blockIdx.x, s = blockIdx.y, c0 = s * SEG;
+  for (int64_t i = threadIdx.x; i < SEG; i += WV_THREADS) acc[i] = 0.0;
+  __syncthreads();
+  const int64_t r_last = (b + 1) * R;
   const int64_t r_end = r_last < nd ? r_last : nd;
-  for (int64_t r = (int64_t)blockIdx.x * R; r < r_end; r++) {
+  for (int64_t r = b * R; r < r_end; r++) {
     const double v = scale ? __dmul_rn(scale[r], y[r]) : y[r];
-    for (int64_t k = rowptr[r] + threadIdx.x; k < rowptr[r + 1]; k += WV_THREADS) {
-      const int c = col[k];
-      p[c] = __dadd_rn(p[c], __dmul_rn(val[k], v));
+    const int64_t k1 = seg[r * (S + 1) + s + 1];
+    for (int64_t k = seg[r * (S + 1) + s] + threadIdx.x; k < k1; k += WV_THREADS) {
+      const int64_t c = col[k] - c0;
+      acc[c] = __dadd_rn(acc[c], __dmul_rn(val[k], v));
     }
     __syncthreads();  // the next row may touch the same entries
   }
+  double *p = part + b * n_dy + c0;
+  for (int64_t i = threadIdx.x; i < SEG; i += WV_THREADS) p[i] = acc[i];
 }
 
 __global__ void gt_reduce_kernel(const double *__restrict__ part, int64_t nb, int64_t n_dy,
@@ -358,10 +388,18 @@ void Context::compute_G_wavelet(const int64_t *h_order, double rel) {
   P0.release();
   P1.release();
   C.release();
-  // G^T y's row blocks and their partial vectors
+  // G^T y's row blocks, their partial vectors and the rows' column segments
   wv_rows_per_block = std::max<int64_t>(1, ceil_div(nd, kGtBlocks));
   wv_blocks = ceil_div(nd, wv_rows_per_block);
   wv_part.alloc(this, sizeof(double) * (size_t)(wv_blocks * n_dy));
+  wv_seg_len = std::min<int64_t>(kGtSegment, n_dy);
+  wv_nseg = n_dy / wv_seg_len;
+  wv_segptr.alloc(this, sizeof(int64_t) * (size_t)(nd * (wv_nseg + 1)));
+  segment_starts_kernel<<<grid_for(nd * (wv_nseg + 1)), WV_THREADS, 0, stream>>>(
+      wv_rowptr.as<int64_t>(), wv_col.as<int>(), nd, wv_nseg, wv_seg_len,
+      wv_segptr.as<int64_t>());
+  GRADA_LAUNCH_CHECK();
+  sync();
   wv_ndy = n_dy;
   wv_nnz = nnz;
   g_storage = GRADA_G_WAVELET;
@@ -383,11 +421,10 @@ void Context::apply_GT_wavelet(const double *y, double *x, const GemvOpts &o) {
   double *sc = scratch.as<double>();
   double *W = sc + 2 * wv_ndy;
   double *bufs[2] = {sc, sc + wv_ndy};
-  GRADA_CUDA_CHECK(cudaMemsetAsync(wv_part.ptr, 0, sizeof(double) * (size_t)(wv_blocks * wv_ndy),
-                                   stream));
-  gt_partial_kernel<<<(unsigned)wv_blocks, WV_THREADS, 0, stream>>>(
-      wv_rowptr.as<int64_t>(), wv_col.as<int>(), wv_val.as<double>(), y, o.scale, nd,
-      wv_rows_per_block, wv_ndy, wv_part.as<double>(), o.skip);
+  gt_partial_kernel<<<dim3((unsigned)wv_blocks, (unsigned)wv_nseg), WV_THREADS,
+                      sizeof(double) * (size_t)wv_seg_len, stream>>>(
+      wv_segptr.as<int64_t>(), wv_col.as<int>(), wv_val.as<double>(), y, o.scale, nd,
+      wv_rows_per_block, wv_nseg, wv_seg_len, wv_ndy, wv_part.as<double>(), o.skip);
   GRADA_LAUNCH_CHECK();
   gt_reduce_kernel<<<grid_for(wv_ndy), WV_THREADS, 0, stream>>>(wv_part.as<double>(), wv_blocks,
                                                                 wv_ndy, W, o.skip);
