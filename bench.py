@@ -939,8 +939,7 @@ def run_operators_refined():
         return (time.perf_counter() - t0) / k, out
 
     t_table, table = timed(lambda: reg.face_table(cells))
-    t_host, ops = timed(lambda: reg._operators(cells, obs, 1.5, reg.difference_matrices(cells, table),
-                                               1.0, 1.0, 1.0, 1.0))
+    t_host, ops = timed(lambda: reg.mesh_operators(cells, obs, 1.5, table=table))
     t_upload, _ = timed(lambda: inv.set_operators(ops))
     t_dev, _ = timed(lambda: inv.build_operators(table, 1.5))
     worst = 0.0

@@ -241,12 +241,13 @@ def regular_mesh_operators(n, prisms, obs, beta: float, a_s=1.0, a_z=1.0, a_x=1.
     return _operators(pr, obs, beta, D, a_s, a_z, a_x, a_y)
 
 
-def mesh_operators(prisms, obs, beta: float, a_s=1.0, a_z=1.0, a_x=1.0, a_y=1.0):
+def mesh_operators(prisms, obs, beta: float, a_s=1.0, a_z=1.0, a_x=1.0, a_y=1.0, table=None):
     """Ws, Wx, Wy, Wz (CSR) plus V, Z, D_x, D_y, D_z for any leaf-cell list
     (regular, padded or octree-refined), the differences from the cells'
-    bounds (``difference_matrices``)."""
+    bounds (``difference_matrices``; ``table``: a face table already built by
+    ``face_table``)."""
     pr = np.asarray(prisms, dtype=np.float64)
-    return _operators(pr, obs, beta, difference_matrices(pr), a_s, a_z, a_x, a_y)
+    return _operators(pr, obs, beta, difference_matrices(pr, table), a_s, a_z, a_x, a_y)
 
 
 def cross_gradient_operators(n, prisms, m0s, ops) -> dict:
