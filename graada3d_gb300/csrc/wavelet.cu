@@ -319,6 +319,8 @@ void Context::compute_G_wavelet(const int64_t *h_order, double rel) {
   }
   int64_t n_dy = 1;
   while (n_dy < nm) n_dy <<= 1;
+  if (n_dy / std::min<int64_t>(kGtSegment, n_dy) > 65535)
+    throw Error(GRADA_ERR_INVALID_ARGUMENT, "too many cells for the wavelet G (2^28 at most)");
 
   // the old G goes first: the compressed rows replace it
   g_storage = -1;
@@ -336,6 +338,7 @@ void Context::compute_G_wavelet(const int64_t *h_order, double rel) {
   if (const char *e = std::getenv("GRADA_WAVELET_BATCH_POINTS"))  // smaller batches for tests
     pb = std::max<int64_t>(1, std::atoll(e));
   pb = std::min(pb, n_obs);
+  pb = std::min<int64_t>(pb, std::max<int64_t>(1, (int64_t)65535 * 32 / n_fields));  // grid rows
   const int64_t rows_max = pb * n_fields, ldb = round_up(rows_max, 32);
   DevBuf Gb, P0, P1, C, cnt;
   Gb.alloc(this, sizeof(double) * (size_t)(ldb * nm));
