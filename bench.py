@@ -1041,14 +1041,15 @@ def run_wavelet_case(rel: float = 5e-4):
     return out
 
 
-def run_wavelet_1m(thresholds=(5e-4, 5e-5, 5e-6)):
+def run_wavelet_1m(variants=((5e-4, "fp64"), (5e-5, "fp64"), (5e-6, "fp64"), (5e-6, "fp32"))):
     """The wavelet-compressed G at the matrix-free case's size: 128 x 128 x 64 =
     1,048,576 cells over [0, 20 km]^2 x [0, 8 km], gz + Tzz at 201 x 201 points 50 m
     above (the FP64 G would be 678 GB).  Compression at the reference's example
-    threshold (5e-4) and two lower ones, in batches of points, never holding the
-    dense G; then G x and G^T y on the compressed rows (CUDA events, 5 runs
-    each) against one matrix-free FP64 product of each, and the relative error
-    of the compressed G x on a two-box model."""
+    threshold (5e-4) and two lower ones (values in FP64, and in FP32 at 5e-6), in
+    batches of points, never holding the dense G; then G x and G^T y on the
+    compressed rows (CUDA events, 5 runs each) against one matrix-free FP64
+    product of each, and the relative error of the compressed G x on a two-box
+    model."""
     import ctypes
 
     import torch
@@ -1088,10 +1089,10 @@ def run_wavelet_1m(thresholds=(5e-4, 5e-5, 5e-6)):
                             "GT_y": timed(lib.grada_GT_vec_mul_dev, r, g, 1)}
     d_exact = y[:inv.Nd].cpu().numpy().copy()
     out["matrix_free_s"]["cg_iteration"] = sum(out["matrix_free_s"].values())
-    for rel in thresholds:
+    for rel, values in variants:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        inv.compute_G_wavelet(order, rel)
+        inv.compute_G_wavelet(order, rel, values)
         torch.cuda.synchronize()
         res = {"compress_s": time.perf_counter() - t0}
         nnz = ctypes.c_int64()
@@ -1100,13 +1101,13 @@ def run_wavelet_1m(thresholds=(5e-4, 5e-5, 5e-6)):
                                               None, None))
         res["kept"] = nnz.value
         res["compression_ratio"] = inv.Nd * n_dy.value / nnz.value
-        res["stored_GB"] = nnz.value * 12 / 1e9
+        res["stored_GB"] = nnz.value * (12 if values == "fp64" else 8) / 1e9
         res["G_x_s"] = timed(lib.grada_G_vec_mul_dev, x, y, 5)
         res["GT_y_s"] = timed(lib.grada_GT_vec_mul_dev, r, g, 5)
         res["cg_iteration_s"] = res["G_x_s"] + res["GT_y_s"]
         d_wv = y[:inv.Nd].cpu().numpy()
         res["G_x_rel_error"] = float(np.linalg.norm(d_wv - d_exact) / np.linalg.norm(d_exact))
-        out[f"threshold_{rel:g}"] = res
+        out[f"threshold_{rel:g}_{values}"] = res
     inv.ctx.close()
     return out
 

@@ -78,6 +78,7 @@ SIGNATURES = {
     "grada_G_column_norms": (c_int, [c_void_p, _dp]),
     "grada_build_operators": (c_int, [c_void_p, POINTER(c_int), c_double, c_int, _dp]),
     "grada_compute_G_wavelet": (c_int, [c_void_p, _ip64, c_double]),
+    "grada_compute_G_wavelet_ex": (c_int, [c_void_p, _ip64, c_double, c_int]),
     "grada_get_wavelet_G": (c_int, [c_void_p, _ip64, _ip64, _ip64, POINTER(c_int), _dp]),
     "grada_get_operator": (c_int, [c_void_p, c_int, _ip64, POINTER(c_int), POINTER(c_int), _dp]),
 }

@@ -604,7 +604,13 @@ int grada_get_operator(grada_ctx *ctx, int which, int64_t *nnz, int *rowptr, int
 }
 
 int grada_compute_G_wavelet(grada_ctx *ctx, const int64_t *order, double relative_threshold) {
-  return guarded(ctx, [&] { ctx->compute_G_wavelet(order, relative_threshold); });
+  return guarded(ctx, [&] { ctx->compute_G_wavelet(order, relative_threshold, GRADA_G_FP64); });
+}
+
+int grada_compute_G_wavelet_ex(grada_ctx *ctx, const int64_t *order, double relative_threshold,
+                               int value_storage) {
+  return guarded(ctx,
+                 [&] { ctx->compute_G_wavelet(order, relative_threshold, value_storage); });
 }
 
 int grada_get_wavelet_G(grada_ctx *ctx, int64_t *n_dy, int64_t *nnz, int64_t *rowptr, int32_t *col,

@@ -151,7 +151,8 @@ struct Context {
   DevBuf wv_order, wv_rowptr, wv_col, wv_val, wv_part, wv_segptr;
   int64_t wv_ndy = 0, wv_nnz = 0, wv_rows_per_block = 1, wv_blocks = 0, wv_seg_len = 1,
           wv_nseg = 0;
-  void compute_G_wavelet(const int64_t *order, double rel);
+  bool wv_fp32 = false;
+  void compute_G_wavelet(const int64_t *order, double rel, int value_storage);
   void apply_G_wavelet(const double *x, double *y, const GemvOpts &o);
   void apply_GT_wavelet(const double *y, double *x, const GemvOpts &o);
   void get_wavelet_G(int64_t *n_dy, int64_t *nnz, int64_t *rowptr, int *col, double *val);

@@ -137,11 +137,13 @@ __global__ void __launch_bounds__(WV_THREADS)
   if (threadIdx.x == 0) count[global_row(r, pb, p0, n_obs)] = k;
 }
 
-// One block per batch row: the kept coefficients in index order.
+// One block per batch row: the kept coefficients in index order (as FP32,
+// rounded to nearest, when the values are stored in FP32).
+template <class V>
 __global__ void __launch_bounds__(WV_THREADS)
     fill_rows_kernel(const double *__restrict__ C, int64_t n_dy, double rel, int64_t pb,
                      int64_t p0, int64_t n_obs, const int64_t *__restrict__ rowptr,
-                     int *__restrict__ col, double *__restrict__ val) {
+                     int *__restrict__ col, V *__restrict__ val) {
   using Scan = cub::BlockScan<int, WV_THREADS>;
   __shared__ typename Scan::TempStorage tmp;
   const int64_t r = blockIdx.x;
@@ -156,7 +158,7 @@ __global__ void __launch_bounds__(WV_THREADS)
     Scan(tmp).ExclusiveSum(flag, pos, total);
     if (flag) {
       col[base + pos] = (int)i;
-      val[base + pos] = v;
+      val[base + pos] = (V)v;
     }
     base += total;
     __syncthreads();  // tmp is reused by the next chunk
@@ -174,8 +176,9 @@ __global__ void load_vec_kernel(const double *__restrict__ x, const int *__restr
   w[j] = j < nm ? x[order[j]] : 0.0;
 }
 
+template <class V>
 __global__ void row_dot_kernel(const int64_t *__restrict__ rowptr, const int *__restrict__ col,
-                               const double *__restrict__ val, const double *__restrict__ w,
+                               const V *__restrict__ val, const double *__restrict__ w,
                                int64_t nd, const double *__restrict__ scale,
                                double *__restrict__ y, const int *__restrict__ skip) {
   if (skip && *skip) return;
@@ -184,7 +187,7 @@ __global__ void row_dot_kernel(const int64_t *__restrict__ rowptr, const int *__
   if (r >= nd) return;
   double s = 0.0;
   for (int64_t k = rowptr[r] + lane; k < rowptr[r + 1]; k += 32)
-    s = __dadd_rn(s, __dmul_rn(val[k], w[col[k]]));
+    s = __dadd_rn(s, __dmul_rn((double)val[k], w[col[k]]));
 #pragma unroll
   for (int off = 16; off >= 1; off >>= 1) s = __dadd_rn(s, __shfl_xor_sync(0xffffffffu, s, off));
   if (lane == 0) y[r] = scale ? __dmul_rn(s, scale[r]) : s;
@@ -212,9 +215,10 @@ __global__ void segment_starts_kernel(const int64_t *__restrict__ rowptr,
 // segment s into a shared-memory accumulator, row after row, and writes it to
 // part[b * n_dy + s * SEG + i]: per column the rows of a block in ascending
 // order, as one pass over the whole row would add them.
+template <class V>
 __global__ void __launch_bounds__(WV_THREADS)
     gt_partial_kernel(const int64_t *__restrict__ seg, const int *__restrict__ col,
-                      const double *__restrict__ val, const double *__restrict__ y,
+                      const V *__restrict__ val, const double *__restrict__ y,
                       const double *__restrict__ scale, int64_t nd, int64_t R, int64_t S,
                       int64_t SEG, int64_t n_dy, double *__restrict__ part,
                       const int *__restrict__ skip) {
@@ -230,7 +234,7 @@ __global__ void __launch_bounds__(WV_THREADS)
     const int64_t k1 = seg[r * (S + 1) + s + 1];
     for (int64_t k = seg[r * (S + 1) + s] + threadIdx.x; k < k1; k += WV_THREADS) {
       const int64_t c = col[k] - c0;
-      acc[c] = __dadd_rn(acc[c], __dmul_rn(val[k], v));
+      acc[c] = __dadd_rn(acc[c], __dmul_rn((double)val[k], v));
     }
     __syncthreads();  // the next row may touch the same entries
   }
@@ -298,8 +302,11 @@ void forward_pyramid(double *P0, double *P1, double *C, int64_t rows, int64_t n_
 
 }  // namespace
 
-void Context::compute_G_wavelet(const int64_t *h_order, double rel) {
+void Context::compute_G_wavelet(const int64_t *h_order, double rel, int value_storage) {
   require_geometry();
+  if (value_storage != GRADA_G_FP64 && value_storage != GRADA_G_FP32)
+    throw Error(GRADA_ERR_INVALID_ARGUMENT, "wavelet values are stored in FP64 or FP32");
+  const bool f32 = value_storage == GRADA_G_FP32;
   if (!h_order) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null cell order");
   if (!std::isfinite(rel) || rel < 0.0)
     throw Error(GRADA_ERR_INVALID_ARGUMENT, "threshold must be finite and >= 0");
@@ -376,14 +383,19 @@ void Context::compute_G_wavelet(const int64_t *h_order, double rel) {
   const int64_t nnz = rowptr[(size_t)nd];
   wv_rowptr.alloc(this, sizeof(int64_t) * ((size_t)nd + 1));
   wv_col.alloc(this, sizeof(int) * (size_t)std::max<int64_t>(nnz, 1));
-  wv_val.alloc(this, sizeof(double) * (size_t)std::max<int64_t>(nnz, 1));
+  wv_val.alloc(this, (f32 ? sizeof(float) : sizeof(double)) * (size_t)std::max<int64_t>(nnz, 1));
   upload(wv_rowptr.ptr, rowptr.data(), sizeof(int64_t) * ((size_t)nd + 1));
   for (int64_t p0 = 0; p0 < n_obs; p0 += pb) {
     const int64_t np = std::min(pb, n_obs - p0);
     const int64_t rows = transform_batch(p0, np);
-    fill_rows_kernel<<<(unsigned)rows, WV_THREADS, 0, stream>>>(
-        C.as<double>(), n_dy, rel, np, p0, n_obs, wv_rowptr.as<int64_t>(), wv_col.as<int>(),
-        wv_val.as<double>());
+    if (f32)
+      fill_rows_kernel<float><<<(unsigned)rows, WV_THREADS, 0, stream>>>(
+          C.as<double>(), n_dy, rel, np, p0, n_obs, wv_rowptr.as<int64_t>(), wv_col.as<int>(),
+          wv_val.as<float>());
+    else
+      fill_rows_kernel<double><<<(unsigned)rows, WV_THREADS, 0, stream>>>(
+          C.as<double>(), n_dy, rel, np, p0, n_obs, wv_rowptr.as<int64_t>(), wv_col.as<int>(),
+          wv_val.as<double>());
     GRADA_LAUNCH_CHECK();
   }
   sync();
@@ -405,6 +417,7 @@ void Context::compute_G_wavelet(const int64_t *h_order, double rel) {
   sync();
   wv_ndy = n_dy;
   wv_nnz = nnz;
+  wv_fp32 = f32;
   g_storage = GRADA_G_WAVELET;
 }
 
@@ -415,8 +428,12 @@ void Context::apply_G_wavelet(const double *x, double *y, const GemvOpts &o) {
                                                                wv_ndy, P0, o.skip);
   GRADA_LAUNCH_CHECK();
   forward_pyramid(P0, P1, W, 1, wv_ndy, o.skip, stream);
-  row_dot_kernel<<<grid_for(nd * 32), WV_THREADS, 0, stream>>>(
-      wv_rowptr.as<int64_t>(), wv_col.as<int>(), wv_val.as<double>(), W, nd, o.scale, y, o.skip);
+  if (wv_fp32)
+    row_dot_kernel<float><<<grid_for(nd * 32), WV_THREADS, 0, stream>>>(
+        wv_rowptr.as<int64_t>(), wv_col.as<int>(), wv_val.as<float>(), W, nd, o.scale, y, o.skip);
+  else
+    row_dot_kernel<double><<<grid_for(nd * 32), WV_THREADS, 0, stream>>>(
+        wv_rowptr.as<int64_t>(), wv_col.as<int>(), wv_val.as<double>(), W, nd, o.scale, y, o.skip);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -424,10 +441,16 @@ void Context::apply_GT_wavelet(const double *y, double *x, const GemvOpts &o) {
   double *sc = scratch.as<double>();
   double *W = sc + 2 * wv_ndy;
   double *bufs[2] = {sc, sc + wv_ndy};
-  gt_partial_kernel<<<dim3((unsigned)wv_blocks, (unsigned)wv_nseg), WV_THREADS,
-                      sizeof(double) * (size_t)wv_seg_len, stream>>>(
-      wv_segptr.as<int64_t>(), wv_col.as<int>(), wv_val.as<double>(), y, o.scale, nd,
-      wv_rows_per_block, wv_nseg, wv_seg_len, wv_ndy, wv_part.as<double>(), o.skip);
+  const dim3 grid((unsigned)wv_blocks, (unsigned)wv_nseg);
+  const size_t smem = sizeof(double) * (size_t)wv_seg_len;
+  if (wv_fp32)
+    gt_partial_kernel<float><<<grid, WV_THREADS, smem, stream>>>(
+        wv_segptr.as<int64_t>(), wv_col.as<int>(), wv_val.as<float>(), y, o.scale, nd,
+        wv_rows_per_block, wv_nseg, wv_seg_len, wv_ndy, wv_part.as<double>(), o.skip);
+  else
+    gt_partial_kernel<double><<<grid, WV_THREADS, smem, stream>>>(
+        wv_segptr.as<int64_t>(), wv_col.as<int>(), wv_val.as<double>(), y, o.scale, nd,
+        wv_rows_per_block, wv_nseg, wv_seg_len, wv_ndy, wv_part.as<double>(), o.skip);
   GRADA_LAUNCH_CHECK();
   gt_reduce_kernel<<<grid_for(wv_ndy), WV_THREADS, 0, stream>>>(wv_part.as<double>(), wv_blocks,
                                                                 wv_ndy, W, o.skip);
@@ -452,7 +475,14 @@ void Context::get_wavelet_G(int64_t *n_dy, int64_t *nnz, int64_t *rowptr, int *c
   if (nnz) *nnz = wv_nnz;
   if (rowptr) download(rowptr, wv_rowptr.ptr, sizeof(int64_t) * ((size_t)nd + 1));
   if (col) download(col, wv_col.ptr, sizeof(int) * (size_t)wv_nnz);
-  if (val) download(val, wv_val.ptr, sizeof(double) * (size_t)wv_nnz);
+  if (val && wv_fp32) {
+    std::vector<float> tmp((size_t)wv_nnz);
+    download(tmp.data(), wv_val.ptr, sizeof(float) * (size_t)wv_nnz);
+    sync();
+    for (int64_t k = 0; k < wv_nnz; k++) val[k] = (double)tmp[(size_t)k];
+  } else if (val) {
+    download(val, wv_val.ptr, sizeof(double) * (size_t)wv_nnz);
+  }
   sync();
 }
 

@@ -155,16 +155,17 @@ class Fwd:
         self.ctx.check(self.ctx.lib.grada_keep_fp64_G(self.ctx.handle, int(bool(keep_fp64))))
         self.ctx.check(self.ctx.lib.grada_compute_G(self.ctx.handle, s))
 
-    def compute_G_wavelet(self, order, relative_threshold: float) -> None:
+    def compute_G_wavelet(self, order, relative_threshold: float, values: str = "fp64") -> None:
         """Fwd::compute_G_wavelet: rows of G along ``order`` (Mesh::get_reordered_id,
         e.g. ``mesh.Octree.wavelet_order()``) Daubechies-4 transformed and
-        thresholded; the products then use the compressed rows."""
+        thresholded; the products then use the compressed rows.  values: "fp64"
+        (the reference's) or "fp32" (kept coefficients rounded to FP32)."""
         o = np.ascontiguousarray(order, dtype=np.int64)
         if o.shape != (self.Nm,):
             raise ValueError(f"expected an order of {self.Nm} cells")
-        self.ctx.check(self.ctx.lib.grada_compute_G_wavelet(
+        self.ctx.check(self.ctx.lib.grada_compute_G_wavelet_ex(
             self.ctx.handle, o.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
-            float(relative_threshold)))
+            float(relative_threshold), STORAGE[values]))
 
     def get_wavelet_G(self):
         """(n_dy, rowptr, cols, vals) of the compressed rows."""

@@ -176,8 +176,15 @@ int grada_forward_field_dev(grada_ctx *ctx, const double *d_rho, double *d_field
  */
 int grada_compute_G_wavelet(grada_ctx *ctx, const int64_t *order, double relative_threshold);
 
+/* As grada_compute_G_wavelet, the kept coefficients stored in value_storage:
+ * GRADA_G_FP64 (the reference's) or GRADA_G_FP32 (rounded to nearest; 8 bytes
+ * per coefficient with its index instead of 12).  The products stay FP64. */
+int grada_compute_G_wavelet_ex(grada_ctx *ctx, const int64_t *order, double relative_threshold,
+                               int value_storage);
+
 /* The compressed rows: *n_dy and *nnz always; rowptr (Nd + 1), col and val
- * (nnz) when not NULL.  GRADA_ERR_STATE unless G is wavelet-compressed. */
+ * (nnz, widened to FP64 when stored in FP32) when not NULL.  GRADA_ERR_STATE
+ * unless G is wavelet-compressed. */
 int grada_get_wavelet_G(grada_ctx *ctx, int64_t *n_dy, int64_t *nnz, int64_t *rowptr, int32_t *col,
                         double *val);
 

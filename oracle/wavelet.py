@@ -75,9 +75,10 @@ def inverse(coef: np.ndarray) -> np.ndarray:
     return a
 
 
-def compress(Gd: np.ndarray, order: np.ndarray, rel: float):
+def compress(Gd: np.ndarray, order: np.ndarray, rel: float, fp32: bool = False):
     """Rows of the dense G (Nd x Nm), cells in `order` (Mesh::get_reordered_id),
-    transformed and thresholded: (n_dy, rowptr, cols, vals)."""
+    transformed and thresholded: (n_dy, rowptr, cols, vals); fp32: the kept
+    values rounded to FP32 (the device's optional value storage)."""
     nd, nm = Gd.shape
     n_dy = padded_length(nm)
     data = np.zeros((nd, n_dy))
@@ -92,7 +93,10 @@ def compress(Gd: np.ndarray, order: np.ndarray, rel: float):
         cols.append(keep)
         vals.append(c[r, keep])
         rowptr.append(rowptr[-1] + keep.size)
-    return n_dy, np.array(rowptr, dtype=np.int64), np.concatenate(cols), np.concatenate(vals)
+    vals = np.concatenate(vals)
+    if fp32:
+        vals = vals.astype(np.float32).astype(np.float64)
+    return n_dy, np.array(rowptr, dtype=np.int64), np.concatenate(cols), vals
 
 
 GT_BLOCKS = 304  # row blocks of the device's G^T y

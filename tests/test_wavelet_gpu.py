@@ -32,12 +32,15 @@ def _refined():
     return o, obs
 
 
-@pytest.mark.parametrize("case,rel,batch", [("regular", 5e-4, None), ("regular", 0.0, None),
-                                            ("refined", 5e-4, None), ("refined", 1e-2, None),
-                                            ("regular", 5e-4, 7), ("refined", 5e-4, 50)])
-def test_wavelet_rows_and_products_match_oracle(gpu_ctx, monkeypatch, case, rel, batch):
+@pytest.mark.parametrize("case,rel,batch,values", [
+    ("regular", 5e-4, None, "fp64"), ("regular", 0.0, None, "fp64"),
+    ("refined", 5e-4, None, "fp64"), ("refined", 1e-2, None, "fp64"),
+    ("regular", 5e-4, 7, "fp64"), ("refined", 5e-4, 50, "fp64"),
+    ("regular", 5e-4, None, "fp32"), ("refined", 5e-5, 9, "fp32")])
+def test_wavelet_rows_and_products_match_oracle(gpu_ctx, monkeypatch, case, rel, batch, values):
     """batch: observation points per assembly batch of the compression (the
-    rows of a batch interleave with other batches' in G's row order)."""
+    rows of a batch interleave with other batches' in G's row order); values:
+    the kept coefficients' storage."""
     if batch is not None:
         monkeypatch.setenv("GRADA_WAVELET_BATCH_POINTS", str(batch))
     o, obs = _regular() if case == "regular" else _refined()
@@ -45,8 +48,8 @@ def test_wavelet_rows_and_products_match_oracle(gpu_ctx, monkeypatch, case, rel,
     inv = GaussNewtonInversion(prisms, obs, 0x012, ctx=gpu_ctx)
     inv.compute_G("fp64")
     Gd = inv.get_G()
-    comp = wv.compress(Gd, order, rel)
-    inv.compute_G_wavelet(order, rel)
+    comp = wv.compress(Gd, order, rel, fp32=values == "fp32")
+    inv.compute_G_wavelet(order, rel, values)
     n_dy, rp, cols, vals = inv.get_wavelet_G()
     assert n_dy == comp[0]
     np.testing.assert_array_equal(rp, comp[1])
