@@ -36,7 +36,7 @@ def _refined():
     ("regular", 5e-4, None, "fp64"), ("regular", 0.0, None, "fp64"),
     ("refined", 5e-4, None, "fp64"), ("refined", 1e-2, None, "fp64"),
     ("regular", 5e-4, 7, "fp64"), ("refined", 5e-4, 50, "fp64"),
-    ("regular", 5e-4, None, "fp32"), ("refined", 5e-5, 9, "fp32")])
+    ("regular", 5e-4, None, "fp32"), ("refined", 5e-4, 9, "fp32")])
 def test_wavelet_rows_and_products_match_oracle(gpu_ctx, monkeypatch, case, rel, batch, values):
     """batch: observation points per assembly batch of the compression (the
     rows of a batch interleave with other batches' in G's row order); values:
