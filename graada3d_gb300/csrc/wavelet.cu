@@ -186,7 +186,11 @@ __global__ void row_dot_kernel(const int64_t *__restrict__ rowptr, const int *__
   const int lane = threadIdx.x & 31;
   if (r >= nd) return;
   double s = 0.0;
-  for (int64_t k = rowptr[r] + lane; k < rowptr[r + 1]; k += 32)
+  // unrolled so that the index loads and gathers of several entries are in
+  // flight together; the additions keep their order
+  const int64_t k1 = rowptr[r + 1];
+#pragma unroll 4
+  for (int64_t k = rowptr[r] + lane; k < k1; k += 32)
     s = __dadd_rn(s, __dmul_rn((double)val[k], w[col[k]]));
 #pragma unroll
   for (int off = 16; off >= 1; off >>= 1) s = __dadd_rn(s, __shfl_xor_sync(0xffffffffu, s, off));
@@ -232,6 +236,7 @@ __global__ void __launch_bounds__(WV_THREADS)
   for (int64_t r = b * R; r < r_end; r++) {
     const double v = scale ? __dmul_rn(scale[r], y[r]) : y[r];
     const int64_t k1 = seg[r * (S + 1) + s + 1];
+#pragma unroll 4
     for (int64_t k = seg[r * (S + 1) + s] + threadIdx.x; k < k1; k += WV_THREADS) {
       const int64_t c = col[k] - c0;
       acc[c] = __dadd_rn(acc[c], __dmul_rn((double)val[k], v));
