@@ -186,8 +186,7 @@ __global__ void row_dot_kernel(const int64_t *__restrict__ rowptr, const int *__
   const int lane = threadIdx.x & 31;
   if (r >= nd) return;
   double s = 0.0;
-  // unrolled so that the index loads and gathers of several entries are in
-  // flight together; the additions keep their order
+  // unrolled; the additions keep their order
   const int64_t k1 = rowptr[r + 1];
 #pragma unroll 4
   for (int64_t k = rowptr[r] + lane; k < k1; k += 32)
