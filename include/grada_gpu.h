@@ -168,11 +168,14 @@ int grada_forward_field_dev(grada_ctx *ctx, const double *d_rho, double *d_field
  * Daubechies-4 pyramid (the algorithm of gsl_wavelet_daubechies, member 4)
  * and keeps the coefficients c with |c| > t or ||c| - t| < 1e-15,
  * t = relative_threshold x the row's largest |c| (Fwd::compress_vec,
- * :298-358).  The FP64 G is assembled on the device first (it must fit) and
- * released afterwards.  Then grada_G_vec_mul / grada_GT_vec_mul (and their
+ * :298-358).  Like the reference it never holds the dense G: rows are
+ * assembled, transformed and thresholded a batch of points at a time.  Then
+ * grada_G_vec_mul / grada_GT_vec_mul (and their
  * _dev forms), grada_solve_cg and grada_invert use the compressed rows, as
  * the reference's G_vec_mul / GT_vec_mul do (:80-146); other G readers answer
- * GRADA_ERR_STATE.  Needs Nm >= 2.
+ * GRADA_ERR_STATE.  Needs 2 <= Nm <= 2^28.  The rows are assembled for batches of
+ * points within about 8 GB of scratch (the environment variable
+ * GRADA_WAVELET_BATCH_POINTS sets a smaller batch, for tests).
  */
 int grada_compute_G_wavelet(grada_ctx *ctx, const int64_t *order, double relative_threshold);
 

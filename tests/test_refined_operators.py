@@ -154,3 +154,21 @@ def test_dyke_mesh_is_face_balanced():
         assert (np.diff(M.indptr) >= 2).all()
         s = np.abs(M @ np.ones(cells.shape[0]))
         assert s.max() <= 1e-15 * np.abs(M).max()
+
+
+def test_octree_random_refinements_stay_face_balanced():
+    """Random rounds of splits (cascades included) keep every face between
+    cells at most one level apart, tile the domain, and give a wavelet order
+    that is a permutation of the leaves."""
+    rng = np.random.default_rng(17)
+    o = mesh.Octree.regular((0.0, 800.0), 4, (0.0, 600.0), 3, (0.0, 400.0), 2)
+    for _ in range(4):
+        n = len(o.leaf_keys())
+        o.refine(rng.choice(n, size=max(1, n // 10), replace=False))
+    cells = o.leaves()
+    vol = np.prod(cells[:, 1::2] - cells[:, 0::2], axis=1).sum()
+    assert abs(vol - 800.0 * 600.0 * 400.0) <= 1e-9 * vol
+    reg.face_table(cells)  # raises on a face between cells two levels apart
+    w = o.wavelet_order()
+    np.testing.assert_array_equal(np.sort(w), np.arange(cells.shape[0]))
+    assert o.levels().max() >= 3
