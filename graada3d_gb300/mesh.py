@@ -8,6 +8,7 @@ reference would produce.
 
 * ``regular_mesh`` -- Mesh.cpp:500-514 (grid points from Eigen's LinSpaced)
   and Mesh.cpp:830-847 (leaf order: x outermost, then y, z innermost).
+* ``padded_mesh`` -- Mesh::generate_regular_mesh_with_padding, Mesh.cpp:516-587.
 * ``set_boxes`` -- Mesh::set_parameter_in_a_region, Mesh.cpp:1079-1107: a
   cell takes a box's value when it lies entirely inside the box (1e-10
   tolerance); later boxes overwrite earlier ones.
@@ -51,6 +52,34 @@ def prisms_from_points(xs, ys, zs) -> np.ndarray:
 
 def regular_mesh(xlim, nx, ylim, ny, zlim, nz) -> np.ndarray:
     return prisms_from_points(*regular_mesh_points(xlim, nx, ylim, ny, zlim, nz))
+
+
+def padded_mesh_points(xlim, nx, ylim, ny, zlim, nz, npx, sx, npy, sy, npz, sz):
+    """Mesh::generate_regular_mesh_with_padding (Mesh.cpp:516-587): the regular
+    points of the area of interest, then npx / npy padding cells on both x / y
+    sides and npz below, each one `s` times wider than the one inside it
+    (starting from the first interior spacing)."""
+    xi, yi, zi = regular_mesh_points(xlim, nx, ylim, ny, zlim, nz)
+
+    def pad(inner, n, stretch, both):
+        lo = n if both else 0
+        pts = np.empty(inner.size + (2 * n if both else n))
+        pts[lo:lo + inner.size] = inner
+        d = inner[1] - inner[0]
+        top = lo + inner.size - 1
+        for i in range(n):
+            d *= stretch
+            pts[top + 1 + i] = pts[top + i] + d
+            if both:
+                pts[lo - 1 - i] = pts[lo - i] - d
+        return pts
+
+    return pad(xi, npx, sx, True), pad(yi, npy, sy, True), pad(zi, npz, sz, False)
+
+
+def padded_mesh(xlim, nx, ylim, ny, zlim, nz, npx, sx, npy, sy, npz, sz) -> np.ndarray:
+    return prisms_from_points(*padded_mesh_points(xlim, nx, ylim, ny, zlim, nz, npx, sx, npy, sy,
+                                                  npz, sz))
 
 
 def set_boxes(prisms: np.ndarray, boxes, values: np.ndarray | None = None) -> np.ndarray:

@@ -172,3 +172,21 @@ def test_octree_random_refinements_stay_face_balanced():
     w = o.wavelet_order()
     np.testing.assert_array_equal(np.sort(w), np.arange(cells.shape[0]))
     assert o.levels().max() >= 3
+
+
+def test_padded_mesh_matches_reference_leaves():
+    """mesh.padded_mesh is Mesh::generate_regular_mesh_with_padding bit for bit
+    (tests/golden/ref_padded.npz: 6 x 5 x 4 cells of interest, 4 padding cells
+    on each x / y side and 3 below, stretch 1.8); its operators build."""
+    f = np.load(GOLDEN / "ref_padded.npz")
+    pr = mesh.padded_mesh((0.0, 3000.0), 6, (0.0, 3000.0), 5, (0.0, 1500.0), 4, 4, 1.8, 4, 1.8, 3,
+                          1.8)
+    assert np.array_equal(pr.view(np.uint64), f["leaf"].view(np.uint64))
+    xs, ys, zs = mesh.padded_mesh_points((0.0, 3000.0), 6, (0.0, 3000.0), 5, (0.0, 1500.0), 4, 4,
+                                         1.8, 4, 1.8, 3, 1.8)
+    obs = mesh.observation_grid(3, 0.0, 3000.0, 3, 0.0, 3000.0, -10.0)
+    n = (len(xs) - 1, len(ys) - 1, len(zs) - 1)
+    want = reg.regular_mesh_operators(n, pr, obs, 1.5)
+    got = reg.mesh_operators(pr, obs, 1.5)
+    for key in ("Dx", "Dy", "Dz", "Wx", "Wy", "Wz"):
+        assert _same_csr(got[key], want[key]), key
