@@ -1,0 +1,58 @@
+"""One mesh refinement of the adaptive inversion, the reference's
+AdaptiveInversion::refine_mesh (src/Inversion/AdaptiveInversion.cpp:637-735)
+without the constraint-model re-interpolation:
+
+1. the refinement indicator of every leaf for the current model, on the
+   device (grada_refinement_indicator), over the (neighbour, area) list built
+   from the cells (``regularization.indicator_pairs``);
+2. the cells to split (``refinement_marks``, on the host);
+3. the split, face balance included (``mesh.Octree.refine``, on the host);
+4. G expanded in place on the device (grada_expand_G), the model inherited by
+   the children, and the regularisation operators rebuilt on the device
+   (grada_build_operators).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import regularization as reg
+
+
+def refinement_marks(indicator, prisms, fraction: float, min_size) -> np.ndarray:
+    """The leaves refine_mesh splits (AdaptiveInversion.cpp:639-683): none when
+    fraction < 0 or fraction x Nm < 1; else those whose indicator exceeds the
+    int(fraction x Nm)-th largest (0-based) and whose sizes are all above the
+    minimum (a size within 1e-7 of it counts as at the minimum).  Ascending."""
+    ind = np.asarray(indicator, dtype=np.float64)
+    nm = ind.size
+    if fraction < 0 or abs(fraction * nm) < 1:
+        return np.zeros(0, dtype=np.int64)
+    tol = np.sort(ind)[::-1][int(fraction * nm)]
+    pr = np.asarray(prisms, dtype=np.float64)
+    size = np.abs(pr[:, 1::2] - pr[:, 0::2])
+    mn = np.asarray(min_size, dtype=np.float64)
+    small = ((size < mn) | (np.abs(size - mn) < 1e-7)).any(1)
+    return np.nonzero((ind > tol) & ~small)[0].astype(np.int64)
+
+
+def refine_mesh(inv, octree, m, fraction: float, min_size, beta: float,
+                alphas=(1.0, 1.0, 1.0, 1.0), extra=()):
+    """One refinement of `inv` (a GaussNewtonInversion whose cells are
+    ``octree.leaves()``) for the model m.  Splits the marked cells, expands G
+    and rebuilds Ws/Wx/Wy/Wz on the device.  Returns the model on the new
+    cells and the other per-cell vectors in `extra` carried over the same way
+    (children take their parent's value), or m unchanged when nothing is
+    marked."""
+    prisms = octree.leaves()
+    indicator = inv.indicator_calculator(m, *reg.indicator_pairs(prisms))
+    marks = refinement_marks(indicator, prisms, fraction, min_size)
+    if marks.size == 0:
+        return (np.asarray(m), *extra)
+    n_old = prisms.shape[0]
+    split = octree.refine(marks)
+    parent = octree.parent_leaf(split, n_old)
+    inv.expand_G(split)
+    if not np.array_equal(inv.prisms.view(np.uint64), octree.leaves().view(np.uint64)):
+        raise RuntimeError("expanded cells differ from the refined mesh")
+    inv.build_operators(reg.face_table(inv.prisms), beta, 0, alphas)
+    return (np.asarray(m)[parent], *(np.asarray(v)[parent] for v in extra))

@@ -189,15 +189,31 @@ class Octree:
         self.split_cells.add(key)
         self._leaves = None
 
-    def refine(self, leaf_indices) -> int:
-        """Split the given leaves (indices into the current ``leaf_keys()``),
-        skipping those a cascade already split; returns the number of splits."""
+    def refine(self, leaf_indices) -> np.ndarray:
+        """Split the given leaves (indices into the current ``leaf_keys()``) in
+        ascending order, skipping those a cascade already split.  Returns the
+        indices, in the old leaf order and ascending, of every leaf split
+        (requested or cascaded): the parents AdaptiveInversion::expand_G
+        replaces by their children."""
         keys = self.leaf_keys()
-        before = len(self.split_cells)
+        before = set(self.split_cells)
         for t in sorted(int(v) for v in np.asarray(leaf_indices).ravel()):
             if self.is_leaf(keys[t]):
                 self._split(keys[t])
-        return len(self.split_cells) - before
+        new = self.split_cells - before
+        return np.array([t for t, k in enumerate(keys) if k in new], dtype=np.int64)
+
+    def parent_leaf(self, split: np.ndarray, n_old: int) -> np.ndarray:
+        """For each current leaf, the index of the old leaf it lies in, after a
+        refine() that split the old leaves `split` (children inherit their
+        parent's values, Mesh.cpp:1575-1590)."""
+        out, prev = [], 0
+        for j in np.asarray(split, dtype=np.int64):
+            out.extend(range(prev, int(j)))
+            out.extend([int(j)] * 8)
+            prev = int(j) + 1
+        out.extend(range(prev, n_old))
+        return np.array(out, dtype=np.int64)
 
     def leaf_keys(self) -> list:
         if self._leaves is None:

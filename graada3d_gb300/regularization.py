@@ -173,6 +173,48 @@ def face_table(prisms) -> np.ndarray:
     return table
 
 
+def indicator_pairs(prisms):
+    """The (neighbour, face area) list AdaptiveInversion::indicator_calculator
+    (AdaptiveInversion.cpp:108-204) sums over, from the leaf cells' bounds: for
+    each cell, for side j = -, + the x, y and z faces; a face with one cell
+    across it (same or coarser level) gives that cell and the cell's own face
+    area, a face with four finer cells across gives them in the reference's
+    child-face order with their face areas, a boundary face nothing.  Returns
+    (rowptr (Nm + 1), neighbour, area), the arguments of
+    grada_refinement_indicator."""
+    pr = np.asarray(prisms, dtype=np.float64)
+    n = pr.shape[0]
+    sizes = np.abs(pr[:, 1::2] - pr[:, 0::2])
+    owner, lat, lo, hi = _leaf_owner(pr)
+    blocks = []  # (count, neighbours, areas) per (side, axis), each (n, 4)
+    for side in (-1, 1):
+        for axis in range(3):
+            t = [b for b in range(3) if b != axis]
+            nb = _face_neighbours(pr, owner, lat, lo, hi, axis, side)
+            has = nb[:, 0] >= 0
+            one = has & (nb == nb[:, :1]).all(1)
+            cnt = np.where(one, 1, np.where(has, 4, 0))
+            own = sizes[:, t[0]] * sizes[:, t[1]]
+            kid = np.where(nb >= 0, sizes[np.maximum(nb, 0), t[0]] * sizes[np.maximum(nb, 0), t[1]],
+                           0.0)
+            area = np.where(one[:, None], own[:, None], kid)
+            blocks.append((cnt, nb, area))
+    counts = np.stack([b[0] for b in blocks], 1)  # (n, 6)
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    rowptr[1:] = np.cumsum(counts.sum(1))
+    total = int(rowptr[-1])
+    neighbour = np.empty(total, dtype=np.int64)
+    area = np.empty(total)
+    pos = rowptr[:-1].copy()
+    for cnt, nb, ar in blocks:
+        for q in range(4):
+            sel = cnt > q
+            neighbour[pos[sel]] = nb[sel, q]
+            area[pos[sel]] = ar[sel, q]
+            pos[sel] += 1
+    return rowptr, neighbour, area
+
+
 def difference_matrices(prisms, table=None) -> tuple:
     """D_x1, D_y1, D_z1 (CSR) of InversionBase::set_difference_matrix from the
     face table (``face_table`` of the cells unless given), with h the cells'

@@ -21,6 +21,8 @@ Fixtures written (all .npz):
                       (oracle/_ref/ref_operators).
   ref_output.npz      the files the reference's result writers produce, with
                       their inputs (oracle/_ref/ref_output).
+  ref_adapt.npz       one AdaptiveInversion::refine_mesh of the reference
+                      (oracle/_ref/ref_adapt).
   ref_inversion_*.npz regular-mesh inversion problems with the reference's
                       G, host-built operators, one solve_cg call and a full
                       invert_with_own_CG run (oracle/_ref/ref_inversion).
@@ -494,6 +496,48 @@ def ref_output() -> None:
                         m0=m0, m0s=m0s, dobs=dobs, **files)
 
 
+def ref_adapt() -> None:
+    """ref_adapt.npz: one AdaptiveInversion::refine_mesh(0.25) of the reference on a
+    6 x 5 x 4 mesh first refined at four cells (levels mixed), a seeded model and
+    minimum cell sizes of 20 m (level-2 cells still split, with face-balance
+    cascades): the leaves and model before, the indicator, the leaves and the
+    inherited model after (oracle/_ref/ref_adapt)."""
+    exe = REF_BIN / "ref_adapt"
+    pts = np.array(OPERATOR_ROUNDS[0], dtype=np.float64)
+    frac, min_size = 0.25, (20.0, 20.0, 20.0)
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
+        with open(fin, "wb") as fh:
+            np.array([6, 5, 4], dtype=np.int64).tofile(fh)
+            np.array([0.0, 600.0, 0.0, 500.0, 0.0, 400.0], dtype=np.float64).tofile(fh)
+            np.array([pts.shape[0]], dtype=np.int64).tofile(fh)
+            pts.tofile(fh)
+            np.array([frac, *min_size], dtype=np.float64).tofile(fh)
+            np.array([2024], dtype=np.uint64).tofile(fh)
+        subprocess.run([str(exe), str(fin), str(fout)], check=True, cwd=td,
+                       stdout=subprocess.DEVNULL)
+        raw = np.fromfile(fout, dtype=np.uint8)
+    off = 0
+
+    def take(cnt, dt):
+        nonlocal off
+        a = raw[off:off + cnt * np.dtype(dt).itemsize].view(dt)
+        off += cnt * np.dtype(dt).itemsize
+        return a
+
+    n0 = int(take(1, np.int64)[0])
+    leaf0 = take(6 * n0, np.float64).reshape(n0, 6)
+    m0 = take(n0, np.float64)
+    ind = take(n0, np.float64)
+    n1 = int(take(1, np.int64)[0])
+    leaf1 = take(6 * n1, np.float64).reshape(n1, 6)
+    m1 = take(n1, np.float64)
+    assert off == raw.size
+    np.savez_compressed(HERE / "ref_adapt.npz", pre_points=pts, fraction=frac,
+                        min_size=np.array(min_size), leaf0=leaf0, m0=m0, indicator=ind,
+                        leaf1=leaf1, m1=m1)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -503,7 +547,7 @@ def main() -> None:
     jobs = {"forward_models": lambda: forward_models(ref), "ref_fields": ref_fields,
             "ref_expand": ref_expand, "ref_padded": ref_padded,
             "ref_indicator": ref_indicator, "ref_operators": ref_operators,
-            "ref_output": ref_output}
+            "ref_output": ref_output, "ref_adapt": ref_adapt}
     try:
         from inversion_cases import inversion_fixtures  # noqa: E402
         jobs["ref_inversion"] = inversion_fixtures

@@ -22,3 +22,76 @@ def test_device_indicator_equals_reference(gpu_ctx, golden):
     inv = GaussNewtonInversion(r["leaf"], obs, 0x002, ctx=gpu_ctx)
     got = inv.indicator_calculator(r["m"], r["rowptr"], r["neighbour"], r["area"])
     np.testing.assert_array_equal(got, r["indicator"])
+
+
+def test_indicator_pairs_from_geometry_equal_reference(golden):
+    """regularization.indicator_pairs builds the reference's (neighbour, area)
+    list from the cells alone, in its order, bitwise."""
+    from graada3d_gb300 import regularization as reg
+
+    r = golden("ref_indicator.npz")
+    rp, nb, ar = reg.indicator_pairs(r["leaf"])
+    np.testing.assert_array_equal(rp, r["rowptr"])
+    np.testing.assert_array_equal(nb, r["neighbour"])
+    np.testing.assert_array_equal(ar.view(np.uint64), r["area"].view(np.uint64))
+
+
+def test_refine_mesh_steps_equal_reference(golden):
+    """One AdaptiveInversion::refine_mesh of the reference (ref_adapt.npz): the
+    indicator over the geometric pairs, the marks (fraction, minimum sizes), the
+    octree split and the model the children inherit all equal the reference's."""
+    from graada3d_gb300 import mesh
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.adaptive import refinement_marks
+
+    f = golden("ref_adapt.npz")
+    o = mesh.Octree.regular((0.0, 600.0), 6, (0.0, 500.0), 5, (0.0, 400.0), 4)
+    pts, c = f["pre_points"], o.leaves()
+    inside = ((pts[None, :, 0] > c[:, None, 0]) & (pts[None, :, 0] < c[:, None, 1])
+              & (pts[None, :, 1] > c[:, None, 2]) & (pts[None, :, 1] < c[:, None, 3])
+              & (pts[None, :, 2] > c[:, None, 4]) & (pts[None, :, 2] < c[:, None, 5]))
+    o.refine(np.nonzero(inside.any(1))[0])
+    assert np.array_equal(o.leaves().view(np.uint64), f["leaf0"].view(np.uint64))
+    ind = refinement.indicator(f["m0"], *reg.indicator_pairs(f["leaf0"]))
+    np.testing.assert_array_equal(ind, f["indicator"])
+    marks = refinement_marks(ind, f["leaf0"], float(f["fraction"]), f["min_size"])
+    assert marks.size > 0
+    n0 = f["leaf0"].shape[0]
+    split = o.refine(marks)
+    assert np.array_equal(o.leaves().view(np.uint64), f["leaf1"].view(np.uint64))
+    np.testing.assert_array_equal(f["m0"][o.parent_leaf(split, n0)], f["m1"])
+    # nothing to do for a fraction below one cell
+    assert refinement_marks(ind, f["leaf0"], 0.1 / n0, f["min_size"]).size == 0
+    assert refinement_marks(ind, f["leaf0"], -1.0, f["min_size"]).size == 0
+
+
+@pytest.mark.gpu
+def test_device_refine_mesh_step(gpu_ctx, golden):
+    """adaptive.refine_mesh on the device: the same leaves and inherited model
+    as the reference's refine_mesh, G expanded to the re-assembled G of the new
+    cells, the operators rebuilt to the host construction's."""
+    from graada3d_gb300 import adaptive, mesh
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.inversion import GaussNewtonInversion
+
+    f = golden("ref_adapt.npz")
+    o = mesh.Octree.regular((0.0, 600.0), 6, (0.0, 500.0), 5, (0.0, 400.0), 4)
+    pts, c = f["pre_points"], o.leaves()
+    inside = ((pts[None, :, 0] > c[:, None, 0]) & (pts[None, :, 0] < c[:, None, 1])
+              & (pts[None, :, 1] > c[:, None, 2]) & (pts[None, :, 1] < c[:, None, 3])
+              & (pts[None, :, 2] > c[:, None, 4]) & (pts[None, :, 2] < c[:, None, 5]))
+    o.refine(np.nonzero(inside.any(1))[0])
+    obs = np.array([[300.0, 250.0, -10.0], [120.0, 400.0, -15.0]])
+    inv = GaussNewtonInversion(o.leaves(), obs, 0x012, ctx=gpu_ctx)
+    inv.compute_G("fp64")
+    m1, = adaptive.refine_mesh(inv, o, f["m0"], float(f["fraction"]), f["min_size"], 1.5)
+    assert np.array_equal(inv.prisms.view(np.uint64), f["leaf1"].view(np.uint64))
+    np.testing.assert_array_equal(m1, f["m1"])
+    G_exp = inv.get_G()
+    inv.compute_G("fp64")
+    np.testing.assert_array_equal(G_exp, inv.get_G())
+    host = reg.mesh_operators(inv.prisms, obs, 1.5)
+    for key in ("Ws", "Wx", "Wy", "Wz"):
+        got, want = inv.get_operator(key), host[key]
+        assert np.array_equal(got.indices, want.indices)
+        np.testing.assert_allclose(got.data, want.data, rtol=2.4e-15, atol=0)
