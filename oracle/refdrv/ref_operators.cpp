@@ -1,5 +1,5 @@
 // Fixture driver (test infrastructure, built only in the oracle's _ref/ tree
-// from the reference sources).  Builds a regular mesh, refines it in rounds
+// from the reference sources).  Builds a regular mesh, refines it in passes
 // with the reference's own Mesh::refinement (face-balance cascade included,
 // Mesh.cpp:1462-1942) and Mesh::rearrange_id, rebuilds the inversion matrices
 // the way AdaptiveInversion does after a refinement (init_matrices,
@@ -15,7 +15,7 @@
 // reference's own Face objects, the input a C++ host hands to
 // grada_build_operators.
 //
-// A round names points; the leaves that contain a point (strictly inside)
+// A pass names points; the leaves that contain a point (strictly inside)
 // are refined in leaf order, skipping cells a cascade already split, as
 // AdaptiveInversion::refine_mesh does with its marked cells.
 //
@@ -106,9 +106,9 @@ int main(int argc, char **argv) {
   xl[0] = in.get<double>(); xl[1] = in.get<double>();
   yl[0] = in.get<double>(); yl[1] = in.get<double>();
   zl[0] = in.get<double>(); zl[1] = in.get<double>();
-  const int64_t n_rounds = in.get<int64_t>();
-  std::vector<std::vector<double>> rounds(n_rounds);
-  for (auto &r : rounds) {
+  const int64_t n_passes = in.get<int64_t>();
+  std::vector<std::vector<double>> passes(n_passes);
+  for (auto &r : passes) {
     const int64_t np = in.get<int64_t>();
     r.resize(3 * np);
     for (auto &v : r) v = in.get<double>();
@@ -128,7 +128,7 @@ int main(int argc, char **argv) {
   for (int64_t i = 0; i < n_obs; i++) ob.add_point(obs[3 * i], obs[3 * i + 1], obs[3 * i + 2]);
   Drv inv(mesh, ob, 0x002);
   Mesh &m = inv.mesh_();
-  for (const auto &r : rounds) {
+  for (const auto &r : passes) {
     std::vector<Cell *> marked;
     for (size_t i = 0; i < m.leaf_cells.size(); i++) {
       Cell *c = m.leaf_cells[i];

@@ -7,7 +7,7 @@
 //   InversionBase::output_obs_data      -> dobs_<component>  (InversionBase::out_data, :743-784)
 //   InversionBase::output_obs_data_vtk  -> dobs.vtk          (InversionBase::out_data_vtk, :798-880)
 // and dumps the inputs (leaf cells, observation points, m, m0, m0s, dobs) to
-// out.bin.  The mesh is refined as the operator driver does it: rounds of
+// out.bin.  The mesh is refined as the operator driver does it: passes of
 // points whose containing leaves are split with Mesh::refinement.
 //
 // Usage: ref_output <in.bin> <out.bin>
@@ -75,9 +75,9 @@ int main(int argc, char **argv) {
   xl[0] = in.get<double>(); xl[1] = in.get<double>();
   yl[0] = in.get<double>(); yl[1] = in.get<double>();
   zl[0] = in.get<double>(); zl[1] = in.get<double>();
-  const int64_t n_rounds = in.get<int64_t>();
-  std::vector<std::vector<double>> rounds(n_rounds);
-  for (auto &r : rounds) {
+  const int64_t n_passes = in.get<int64_t>();
+  std::vector<std::vector<double>> passes(n_passes);
+  for (auto &r : passes) {
     const int64_t np = in.get<int64_t>();
     r.resize(3 * np);
     for (auto &v : r) v = in.get<double>();
@@ -95,7 +95,7 @@ int main(int argc, char **argv) {
   for (int64_t i = 0; i < n_obs; i++) ob.add_point(obs[3 * i], obs[3 * i + 1], obs[3 * i + 2]);
   Drv inv(mesh, ob, mask);
   Mesh &m = inv.mesh_();
-  for (const auto &r : rounds) {
+  for (const auto &r : passes) {
     std::vector<Cell *> marked;
     for (size_t i = 0; i < m.leaf_cells.size(); i++) {
       Cell *c = m.leaf_cells[i];

@@ -367,19 +367,19 @@ def ref_indicator() -> None:
                         rowptr=rowptr, neighbour=nb, area=area)
 
 
-OPERATOR_ROUNDS = [
-    # round 1: three base cells, one at the +x and one at the +z boundary
+REFINE_PASSES = [
+    # first refinement pass: base cells, one at the +x and one at the +z boundary
     [(150.0, 250.0, 150.0), (450.0, 250.0, 150.0), (250.0, 250.0, 250.0), (550.0, 50.0, 350.0)],
-    # round 2: level-1 cells against unrefined neighbours (face-balance cascades)
+    # second pass: level-1 cells against unrefined neighbours (face-balance cascades)
     [(110.0, 210.0, 110.0), (590.0, 60.0, 390.0), (240.0, 240.0, 210.0)],
-    # round 3: a level-2 cell whose neighbours are level 1 (cascade of two levels)
+    # third pass: a level-2 cell whose neighbours are level 1 (cascade of two levels)
     [(101.0, 201.0, 101.0), (595.0, 55.0, 395.0)],
 ]
 
 
 def ref_operators() -> None:
     """ref_operators.npz: the reference's regularisation operators on a 6 x 5 x 4
-    mesh refined in three rounds by Mesh::refinement (cascades included): leaf
+    mesh refined in three passes by Mesh::refinement (cascades included): leaf
     cells and levels, D_x1/D_y1/D_z1, V, Z, Ws/Wx/Wy/Wz, for a seeded
     structure model T_x/T_y/T_z, the face table the drop-in reads from the
     reference's Face objects and Mesh::get_reordered_id of every position
@@ -394,8 +394,8 @@ def ref_operators() -> None:
         with open(fin, "wb") as fh:
             np.array([6, 5, 4], dtype=np.int64).tofile(fh)
             np.array([0.0, 600.0, 0.0, 500.0, 0.0, 400.0], dtype=np.float64).tofile(fh)
-            np.array([len(OPERATOR_ROUNDS)], dtype=np.int64).tofile(fh)
-            for r in OPERATOR_ROUNDS:
+            np.array([len(REFINE_PASSES)], dtype=np.int64).tofile(fh)
+            for r in REFINE_PASSES:
                 np.array([len(r)], dtype=np.int64).tofile(fh)
                 np.array(r, dtype=np.float64).tofile(fh)
             np.array([obs.shape[0]], dtype=np.int64).tofile(fh)
@@ -437,11 +437,11 @@ def ref_operators() -> None:
     out["face_table"] = take(15 * n, np.int32).reshape(n, 3, 5)
     out["reordered_id"] = take(n, np.int64)
     assert off == raw.size
-    rounds = np.full((len(OPERATOR_ROUNDS), max(map(len, OPERATOR_ROUNDS)), 3), np.nan)
-    for k, r in enumerate(OPERATOR_ROUNDS):
-        rounds[k, :len(r)] = r
+    passes = np.full((len(REFINE_PASSES), max(map(len, REFINE_PASSES)), 3), np.nan)
+    for k, r in enumerate(REFINE_PASSES):
+        passes[k, :len(r)] = r
     np.savez_compressed(HERE / "ref_operators.npz", n=np.array([6, 5, 4]),
-                        limits=np.array([0.0, 600.0, 0.0, 500.0, 0.0, 400.0]), rounds=rounds,
+                        limits=np.array([0.0, 600.0, 0.0, 500.0, 0.0, 400.0]), passes=passes,
                         obs=obs, beta=beta, alphas=alphas, **out)
 
 
@@ -463,8 +463,8 @@ def ref_output() -> None:
         with open(fin, "wb") as fh:
             np.array([6, 5, 4], dtype=np.int64).tofile(fh)
             np.array([0.0, 600.0, 0.0, 500.0, 0.0, 400.0], dtype=np.float64).tofile(fh)
-            np.array([len(OPERATOR_ROUNDS)], dtype=np.int64).tofile(fh)
-            for r in OPERATOR_ROUNDS:
+            np.array([len(REFINE_PASSES)], dtype=np.int64).tofile(fh)
+            for r in REFINE_PASSES:
                 np.array([len(r)], dtype=np.int64).tofile(fh)
                 np.array(r, dtype=np.float64).tofile(fh)
             np.array([obs.shape[0]], dtype=np.int64).tofile(fh)
@@ -503,7 +503,7 @@ def ref_adapt() -> None:
     cascades): the leaves and model before, the indicator, the leaves and the
     inherited model after (oracle/_ref/ref_adapt)."""
     exe = REF_BIN / "ref_adapt"
-    pts = np.array(OPERATOR_ROUNDS[0], dtype=np.float64)
+    pts = np.array(REFINE_PASSES[0], dtype=np.float64)
     frac, min_size = 0.25, (20.0, 20.0, 20.0)
     with tempfile.TemporaryDirectory() as td:
         fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"

@@ -39,7 +39,7 @@ def _octree_of(f):
     n = f["n"]
     lim = f["limits"]
     o = mesh.Octree.regular(lim[0:2], int(n[0]), lim[2:4], int(n[1]), lim[4:6], int(n[2]))
-    for r in f["rounds"]:
+    for r in f["passes"]:
         pts = r[~np.isnan(r[:, 0])]
         cells = o.leaves()
         inside = ((pts[None, :, 0] > cells[:, None, 0]) & (pts[None, :, 0] < cells[:, None, 1]) &
@@ -51,7 +51,7 @@ def _octree_of(f):
 
 def test_octree_refinement_matches_reference_leaves():
     """Same leaves, bitwise, in the same order, at the same levels, cascades
-    included (the fixture's rounds split level-1 and level-2 cells next to
+    included (the fixture's passes split level-1 and level-2 cells next to
     coarser ones)."""
     f = _load()
     o = _octree_of(f)
@@ -157,7 +157,7 @@ def test_dyke_mesh_is_face_balanced():
 
 
 def test_octree_random_refinements_stay_face_balanced():
-    """Random rounds of splits (cascades included) keep every face between
+    """Random passes of splits (cascades included) keep every face between
     cells at most one level apart, tile the domain, and give a wavelet order
     that is a permutation of the leaves."""
     rng = np.random.default_rng(17)
