@@ -95,3 +95,39 @@ def test_device_refine_mesh_step(gpu_ctx, golden):
         got, want = inv.get_operator(key), host[key]
         assert np.array_equal(got.indices, want.indices)
         np.testing.assert_allclose(got.data, want.data, rtol=2.4e-15, atol=0)
+
+
+def test_refinement_marks_rules():
+    """refine_mesh's rule (AdaptiveInversion.cpp:639-683): strictly above the
+    int(fraction Nm)-th largest indicator; a cell any of whose sizes is at (to
+    1e-7) or below the minimum is never split."""
+    from graada3d_gb300.adaptive import refinement_marks
+
+    cells = np.array([[0, 10, 0, 10, 0, 10], [10, 20, 0, 10, 0, 10], [20, 25, 0, 5, 0, 5],
+                      [25, 30, 0, 5, 0, 5], [30, 40, 0, 10, 0, 10.00000005]], dtype=float)
+    ind = np.array([5.0, 4.0, 9.0, 1.0, 8.0])
+    # fraction 0.4 of 5 cells: tol = 3rd largest = 5.0, so indicators 9 and 8 qualify
+    np.testing.assert_array_equal(refinement_marks(ind, cells, 0.4, (1.0, 1.0, 1.0)), [2, 4])
+    # minimum 5: cell 2 (5 m) is at the minimum
+    np.testing.assert_array_equal(refinement_marks(ind, cells, 0.4, (5.0, 5.0, 5.0)), [4])
+    # minimum 10.00000005 in z: cell 4 is within 1e-7 of it
+    np.testing.assert_array_equal(refinement_marks(ind, cells, 0.4, (1.0, 1.0, 10.00000005)), [])
+    # ties at the threshold are not split
+    np.testing.assert_array_equal(refinement_marks(np.ones(5), cells, 0.4, (1, 1, 1)), [])
+
+
+def test_parent_leaf_maps_children_into_their_parents():
+    from graada3d_gb300 import mesh
+
+    rng = np.random.default_rng(5)
+    o = mesh.Octree.regular((0.0, 400.0), 4, (0.0, 300.0), 3, (0.0, 200.0), 2)
+    for _ in range(3):
+        old = o.leaves()
+        split = o.refine(rng.choice(old.shape[0], size=old.shape[0] // 5, replace=False))
+        new = o.leaves()
+        parent = o.parent_leaf(split, old.shape[0])
+        assert parent.size == new.shape[0] == old.shape[0] + 7 * split.size
+        p = old[parent]
+        assert np.all(new[:, 0::2] >= p[:, 0::2]) and np.all(new[:, 1::2] <= p[:, 1::2])
+        kept = np.setdiff1d(np.arange(old.shape[0]), split)
+        assert np.isin(kept, parent).all()
