@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import numpy as np
 
+from . import mesh
 from . import regularization as reg
 
 
@@ -35,19 +36,34 @@ def refinement_marks(indicator, prisms, fraction: float, min_size) -> np.ndarray
     return np.nonzero((ind > tol) & ~small)[0].astype(np.int64)
 
 
+def carry_over(values, parent, split, new_cells, interpolator=None) -> np.ndarray:
+    """A per-cell vector on the refined cells: children take their parent's
+    value (Cell's constructor copies the parent's parameters, Mesh.cpp:1575-1590)
+    or, with an interpolator, its value at their centre -- what the
+    constrained refine_mesh variants do for the structure (cross-gradient) and
+    reference models (AdaptiveInversion.cpp:333-375); other cells keep theirs."""
+    out = np.asarray(values, dtype=np.float64)[parent].copy()
+    if interpolator is not None:
+        child = np.isin(parent, split)
+        out[child] = interpolator(mesh.cell_centres(np.asarray(new_cells)[child]))
+    return out
+
+
 def refine_mesh(inv, octree, m, fraction: float, min_size, beta: float,
                 alphas=(1.0, 1.0, 1.0, 1.0), extra=()):
     """One refinement of `inv` (a GaussNewtonInversion whose cells are
     ``octree.leaves()``) for the model m.  Splits the marked cells, expands G
     and rebuilds Ws/Wx/Wy/Wz on the device.  Returns the model on the new
-    cells and the other per-cell vectors in `extra` carried over the same way
-    (children take their parent's value), or m unchanged when nothing is
+    cells and the vectors of `extra` on them: each entry a per-cell vector
+    (children take the parent's value) or a (vector, interpolator) pair
+    (children take the interpolator's value at their centre, as the
+    constrained refine_mesh variants do).  Nothing changes when no cell is
     marked."""
     prisms = octree.leaves()
     indicator = inv.indicator_calculator(m, *reg.indicator_pairs(prisms))
     marks = refinement_marks(indicator, prisms, fraction, min_size)
     if marks.size == 0:
-        return (np.asarray(m), *extra)
+        return (np.asarray(m), *(v[0] if isinstance(v, tuple) else v for v in extra))
     n_old = prisms.shape[0]
     split = octree.refine(marks)
     parent = octree.parent_leaf(split, n_old)
@@ -55,4 +71,8 @@ def refine_mesh(inv, octree, m, fraction: float, min_size, beta: float,
     if not np.array_equal(inv.prisms.view(np.uint64), octree.leaves().view(np.uint64)):
         raise RuntimeError("expanded cells differ from the refined mesh")
     inv.build_operators(reg.face_table(inv.prisms), beta, 0, alphas)
-    return (np.asarray(m)[parent], *(np.asarray(v)[parent] for v in extra))
+    out = [np.asarray(m)[parent]]
+    for v in extra:
+        vec, interp = v if isinstance(v, tuple) else (v, None)
+        out.append(carry_over(vec, parent, split, inv.prisms, interp))
+    return tuple(out)

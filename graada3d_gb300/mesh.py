@@ -15,6 +15,8 @@ reference would produce.
 * ``observation_grid`` -- Observation::generate, Observation.cpp:48-77
 * ``Octree`` -- Mesh::refinement, Mesh.cpp:1462-1942: octant splits kept
   face-balanced, leaves in the reference's leaf order.
+* ``Multilinear`` -- the gridded-model interpolation of
+  InversionBase::create_crg_model_from_data / create_ref_model_from_data.
   (x fastest).
 """
 from __future__ import annotations
@@ -272,3 +274,67 @@ class Octree:
 
     def levels(self) -> np.ndarray:
         return np.array([k[0] for k in self.leaf_keys()], dtype=np.int64)
+
+
+class Multilinear:
+    """Multilinear interpolation of values on a rectilinear x, y, z grid, the
+    interpolator the reference builds from a gridded constraint model
+    (InversionBase.cpp:1305-1307, the vendored Linterp InterpMultilinear):
+
+    * per axis the cell is found by an upper bound in the grid; a coordinate
+      below the first grid point takes the first point's values, one at or
+      beyond the last takes the last's (no extrapolation), and inside the
+      fraction (x - g_c) / (g_c+1 - g_c) is clamped to [0, 1];
+    * the eight corner values are combined x first: lower + t_x (upper -
+      lower), each side combining y then z the same way.
+
+    values: (nx, ny, nz), x outermost."""
+
+    def __init__(self, grid_x, grid_y, grid_z, values):
+        self.grids = [np.asarray(g, dtype=np.float64) for g in (grid_x, grid_y, grid_z)]
+        self.values = np.asarray(values, dtype=np.float64).reshape([g.size for g in self.grids])
+        for g in self.grids:
+            if g.size < 1 or np.any(np.diff(g) <= 0):
+                raise ValueError("grid coordinates must increase")
+
+    def __call__(self, points) -> np.ndarray:
+        p = np.asarray(points, dtype=np.float64).reshape(-1, 3)
+        lo, hi, t = [], [], []
+        for d, g in enumerate(self.grids):
+            x = p[:, d]
+            n = g.size
+            c = np.searchsorted(g, x, side="right") - 1
+            c = np.where(x < g[0], -1, np.where(x >= g[-1], n - 1, c))
+            inner = (c >= 0) & (c < n - 1)
+            ci = np.clip(c, 0, max(n - 2, 0))
+            y = np.zeros(x.size)
+            if n >= 2:
+                with np.errstate(invalid="ignore", divide="ignore"):
+                    yy = (x - g[ci]) / (g[np.minimum(ci + 1, n - 1)] - g[ci])
+                y = np.where(inner, np.clip(yy, 0.0, 1.0), y)
+            y = np.where(c == -1, 1.0, y)
+            lo.append(np.where(c < 0, 0, np.where(c >= n - 1, n - 1, c)))
+            hi.append(np.where(c < 0, 0, np.where(c >= n - 1, n - 1, c + 1)))
+            t.append(y)
+        f = self.values
+
+        def corner(bx, by, bz):
+            return f[(hi[0] if bx else lo[0]), (hi[1] if by else lo[1]), (hi[2] if bz else lo[2])]
+
+        def along_z(bx, by):
+            a, b = corner(bx, by, 0), corner(bx, by, 1)
+            return a + t[2] * (b - a)
+
+        def along_y(bx):
+            a, b = along_z(bx, 0), along_z(bx, 1)
+            return a + t[1] * (b - a)
+
+        a, b = along_y(0), along_y(1)
+        return a + t[0] * (b - a)
+
+
+def cell_centres(cells) -> np.ndarray:
+    """RectPrism::get_center of each cell (RectPrism.cpp:45-50)."""
+    c = np.asarray(cells, dtype=np.float64).reshape(-1, 6)
+    return np.stack([0.5 * (c[:, 1] + c[:, 0]), 0.5 * (c[:, 3] + c[:, 2]),
+                     0.5 * (c[:, 5] + c[:, 4])], 1)

@@ -23,6 +23,8 @@ Fixtures written (all .npz):
                       their inputs (oracle/_ref/ref_output).
   ref_adapt.npz       one AdaptiveInversion::refine_mesh of the reference
                       (oracle/_ref/ref_adapt).
+  ref_interp.npz      the structure-model interpolation and a "crg" refinement
+                      (oracle/_ref/ref_interp).
   ref_inversion_*.npz regular-mesh inversion problems with the reference's
                       G, host-built operators, one solve_cg call and a full
                       invert_with_own_CG run (oracle/_ref/ref_inversion).
@@ -538,6 +540,61 @@ def ref_adapt() -> None:
                         leaf1=leaf1, m1=m1)
 
 
+def ref_interp() -> None:
+    """ref_interp.npz: the cross-gradient structure model read from a seeded
+    gridded file (InversionBase::create_crg_model_from_data, Linterp's
+    InterpMultilinear) on a 6 x 5 x 4 mesh first refined at four cells: its
+    cell-centre values, its values at probe points (inside, on grid points and
+    outside the grid on every side), and one refine_mesh(0.25, interpolator,
+    "crg") whose children take interpolated values (oracle/_ref/ref_interp)."""
+    exe = REF_BIN / "ref_interp"
+    rng = np.random.default_rng(77)
+    pts = np.array(REFINE_PASSES[0], dtype=np.float64)
+    grids = [np.sort(np.concatenate([[40.0, 560.0], rng.uniform(40.0, 560.0, 9)])),
+             np.sort(np.concatenate([[-20.0, 470.0], rng.uniform(-20.0, 470.0, 7)])),
+             np.sort(np.concatenate([[30.0, 390.0], rng.uniform(30.0, 390.0, 5)]))]
+    vals = rng.uniform(-300.0, 300.0, (grids[0].size, grids[1].size, grids[2].size))
+    probes = np.vstack([rng.uniform([-100, -100, -100], [700, 600, 500], (40, 3)),
+                        np.stack(np.meshgrid(grids[0][[0, 4, -1]], grids[1][[0, 3, -1]],
+                                             grids[2][[0, 2, -1]], indexing="ij"), -1).reshape(-1, 3)])
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
+        with open(fin, "wb") as fh:
+            np.array([6, 5, 4], dtype=np.int64).tofile(fh)
+            np.array([0.0, 600.0, 0.0, 500.0, 0.0, 400.0], dtype=np.float64).tofile(fh)
+            np.array([pts.shape[0]], dtype=np.int64).tofile(fh)
+            pts.tofile(fh)
+            for g in grids:
+                np.array([g.size], dtype=np.int64).tofile(fh)
+                g.tofile(fh)
+            vals.tofile(fh)
+            np.array([probes.shape[0]], dtype=np.int64).tofile(fh)
+            probes.tofile(fh)
+            np.array([0.25], dtype=np.float64).tofile(fh)
+            np.array([99], dtype=np.uint64).tofile(fh)
+        subprocess.run([str(exe), str(fin), str(fout)], check=True, cwd=td,
+                       stdout=subprocess.DEVNULL)
+        raw = np.fromfile(fout, dtype=np.uint8)
+    off = 0
+
+    def take(cnt, dt):
+        nonlocal off
+        a = raw[off:off + cnt * np.dtype(dt).itemsize].view(dt)
+        off += cnt * np.dtype(dt).itemsize
+        return a
+
+    n0 = int(take(1, np.int64)[0])
+    m0s0 = take(n0, np.float64)
+    probe_vals = take(probes.shape[0], np.float64)
+    n1 = int(take(1, np.int64)[0])
+    leaf1 = take(6 * n1, np.float64).reshape(n1, 6)
+    m0s1 = take(n1, np.float64)
+    assert off == raw.size
+    np.savez_compressed(HERE / "ref_interp.npz", pre_points=pts, grid_x=grids[0], grid_y=grids[1],
+                        grid_z=grids[2], values=vals, probes=probes, probe_values=probe_vals,
+                        m0s0=m0s0, leaf1=leaf1, m0s1=m0s1, fraction=0.25)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -547,7 +604,7 @@ def main() -> None:
     jobs = {"forward_models": lambda: forward_models(ref), "ref_fields": ref_fields,
             "ref_expand": ref_expand, "ref_padded": ref_padded,
             "ref_indicator": ref_indicator, "ref_operators": ref_operators,
-            "ref_output": ref_output, "ref_adapt": ref_adapt}
+            "ref_output": ref_output, "ref_adapt": ref_adapt, "ref_interp": ref_interp}
     try:
         from inversion_cases import inversion_fixtures  # noqa: E402
         jobs["ref_inversion"] = inversion_fixtures

@@ -131,3 +131,44 @@ def test_parent_leaf_maps_children_into_their_parents():
         assert np.all(new[:, 0::2] >= p[:, 0::2]) and np.all(new[:, 1::2] <= p[:, 1::2])
         kept = np.setdiff1d(np.arange(old.shape[0]), split)
         assert np.isin(kept, parent).all()
+
+
+def _lcg_model(n, seed):
+    """The fixture drivers' seeded model: s <- s * 6364136223846793005 +
+    1442695040888963407 (mod 2^64), m = (((s >> 11) % 200001) - 100000) / 137."""
+    out, s, mask = np.empty(n), seed, (1 << 64) - 1
+    for i in range(n):
+        s = (s * 6364136223846793005 + 1442695040888963407) & mask
+        out[i] = (float((s >> 11) % 200001) - 100000.0) / 137.0
+    return out
+
+
+def test_structure_model_interpolation_and_crg_refinement_equal_reference(golden):
+    """mesh.Multilinear is the reference's gridded-model interpolator bitwise
+    (probes inside, on grid points and beyond every side; the cell-centre values
+    invert_with_own_CG gives the leaves), and a refine_mesh(0.25, interpolator,
+    "crg") gives the same leaves and the same structure model, the children
+    interpolated at their centres (ref_interp.npz)."""
+    from graada3d_gb300 import mesh
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.adaptive import carry_over, refinement_marks
+
+    f = golden("ref_interp.npz")
+    interp = mesh.Multilinear(f["grid_x"], f["grid_y"], f["grid_z"], f["values"])
+    np.testing.assert_array_equal(interp(f["probes"]), f["probe_values"])
+    o = mesh.Octree.regular((0.0, 600.0), 6, (0.0, 500.0), 5, (0.0, 400.0), 4)
+    pts, c = f["pre_points"], o.leaves()
+    inside = ((pts[None, :, 0] > c[:, None, 0]) & (pts[None, :, 0] < c[:, None, 1])
+              & (pts[None, :, 1] > c[:, None, 2]) & (pts[None, :, 1] < c[:, None, 3])
+              & (pts[None, :, 2] > c[:, None, 4]) & (pts[None, :, 2] < c[:, None, 5]))
+    o.refine(np.nonzero(inside.any(1))[0])
+    leaf0 = o.leaves()
+    m0s = interp(mesh.cell_centres(leaf0))
+    np.testing.assert_array_equal(m0s, f["m0s0"])
+    m = _lcg_model(leaf0.shape[0], 99)
+    ind = refinement.indicator(m, *reg.indicator_pairs(leaf0))
+    marks = refinement_marks(ind, leaf0, float(f["fraction"]), (1.0, 1.0, 1.0))
+    split = o.refine(marks)
+    assert np.array_equal(o.leaves().view(np.uint64), f["leaf1"].view(np.uint64))
+    parent = o.parent_leaf(split, leaf0.shape[0])
+    np.testing.assert_array_equal(carry_over(m0s, parent, split, o.leaves(), interp), f["m0s1"])
