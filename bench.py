@@ -52,7 +52,7 @@ UNIT = "entries/s"
 # flag, frozen once: the corner-grouped closed form evaluated cell by cell with
 # only the faces of a vertical column shared, counted by ncu (DFMA = 2,
 # DADD/DMUL = 1 from the executed-instruction counters) on a 1,024-point x
-# 4,096-cell case; see profiles/assemble_fp64_9comp.md.  roofline.achieved is
+# 4,096-cell case (bench.py --case profile).  roofline.achieved is
 # this figure x pairs/s.
 FP64_FLOPS_PER_PAIR = 767.4
 
@@ -65,7 +65,7 @@ FP64_FLOPS_EXECUTED_PER_PAIR = 433.0
 
 # DRAM bytes (read + write) of one assembly launch on this workload, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of the full-size
-# launch; see profiles/assemble_fp64_9comp.md.  The algorithmic G write is 96.3 GB.
+# launch.  The algorithmic G write is 96.3 GB.
 ASSEMBLY_DRAM_BYTES_PER_LAUNCH = 4_873_539_072 + 98_284_599_040
 
 

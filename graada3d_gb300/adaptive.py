@@ -23,11 +23,16 @@ def refinement_marks(indicator, prisms, fraction: float, min_size) -> np.ndarray
     """The leaves refine_mesh splits (AdaptiveInversion.cpp:639-683): none when
     fraction < 0 or fraction x Nm < 1; else those whose indicator exceeds the
     int(fraction x Nm)-th largest (0-based) and whose sizes are all above the
-    minimum (a size within 1e-7 of it counts as at the minimum).  Ascending."""
+    minimum (a size within 1e-7 of it counts as at the minimum).  Ascending.
+    fraction x Nm must stay below Nm (fraction < 1): the reference reads past
+    the end of its sorted indicator there, so this raises ValueError instead."""
     ind = np.asarray(indicator, dtype=np.float64)
     nm = ind.size
     if fraction < 0 or abs(fraction * nm) < 1:
         return np.zeros(0, dtype=np.int64)
+    if int(fraction * nm) >= nm:
+        raise ValueError(f"refinement fraction {fraction} selects index {int(fraction * nm)} "
+                         f"of {nm} indicator values; it must satisfy int(fraction * Nm) < Nm")
     tol = np.sort(ind)[::-1][int(fraction * nm)]
     pr = np.asarray(prisms, dtype=np.float64)
     size = np.abs(pr[:, 1::2] - pr[:, 0::2])

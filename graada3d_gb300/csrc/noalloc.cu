@@ -23,7 +23,15 @@
 // stand-in, and a kernel given that stand-in would fault or touch the wrong
 // memory.  The first call on each device (with that device current) looks up
 // the real address with cudaGetSymbolAddress and caches it; make that first
-// call before any stream capture that should contain later calls.
+// call before any stream capture that should contain later calls.  The cached
+// address belongs to the device's current context: after cudaDeviceReset (or
+// any teardown of the primary context) the library's module is loaded again
+// at a new address, so a process that resets a device must not call this
+// entry point on that device again.
+//
+// Errors: the kernels are launched with cudaLaunchKernel and only those
+// launches' own status is checked, so an error left pending by the caller's
+// earlier work is neither reported as this call's nor cleared.
 #include <mutex>
 
 #include "../../include/grada_gpu.h"
@@ -85,18 +93,12 @@ __global__ void noalloc_gx_finish_kernel(const double *__restrict__ partial, int
 // Device address of the scratch array on the current device (looked up once).
 int scratch_address(double **out) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) {
-    cudaGetLastError();
-    return GRADA_ERR_CUDA;
-  }
+  if (cudaGetDevice(&dev) != cudaSuccess) return GRADA_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return GRADA_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (!g_scratch_addr[dev]) {
     void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-      cudaGetLastError();
-      return GRADA_ERR_CUDA;
-    }
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return GRADA_ERR_CUDA;
     g_scratch_addr[dev] = static_cast<double *>(p);
   }
   *out = g_scratch_addr[dev];
@@ -116,10 +118,8 @@ extern "C" int grada_G_vec_mul_noalloc(const double *d_G, int64_t nd, int64_t nm
   if (st != GRADA_OK) return st;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
-    cudaGetLastError();
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return GRADA_ERR_CUDA;
-  }
   const int64_t tiles = grada::ceil_div(ld, (int64_t)NA_THREADS * NA_VEC);
   int64_t splits = grada::ceil_div((int64_t)sms * 8, tiles);
   splits = std::min<int64_t>(splits, grada::ceil_div(nm, 64));
@@ -127,10 +127,18 @@ extern "C" int grada_G_vec_mul_noalloc(const double *d_G, int64_t nd, int64_t nm
   splits = std::max<int64_t>(std::min<int64_t>(splits, 65535), 1);
   const int64_t per = grada::ceil_div(nm, splits);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  dim3 grid((unsigned)tiles, (unsigned)splits);
-  noalloc_gx_partial_kernel<<<grid, NA_THREADS, 0, s>>>(d_G, ld, nm, per, d_x, scratch);
-  noalloc_gx_finish_kernel<<<(unsigned)grada::ceil_div(nd, 256), 256, 0, s>>>(scratch, (int)splits,
-                                                                             ld, nd, d_y);
-  if (cudaGetLastError() != cudaSuccess) return GRADA_ERR_CUDA;
+  const dim3 grid((unsigned)tiles, (unsigned)splits);
+  void *partial_args[] = {(void *)&d_G, (void *)&ld, (void *)&nm, (void *)&per, (void *)&d_x,
+                          (void *)&scratch};
+  if (cudaLaunchKernel(reinterpret_cast<const void *>(&noalloc_gx_partial_kernel), grid,
+                       dim3(NA_THREADS), partial_args, 0, s) != cudaSuccess)
+    return GRADA_ERR_CUDA;
+  int n_split = (int)splits;
+  void *finish_args[] = {(void *)&scratch, (void *)&n_split, (void *)&ld, (void *)&nd,
+                         (void *)&d_y};
+  if (cudaLaunchKernel(reinterpret_cast<const void *>(&noalloc_gx_finish_kernel),
+                       dim3((unsigned)grada::ceil_div(nd, 256)), dim3(256), finish_args, 0,
+                       s) != cudaSuccess)
+    return GRADA_ERR_CUDA;
   return GRADA_OK;
 }

@@ -346,8 +346,10 @@ void Context::compute_G_wavelet(const int64_t *h_order, double rel, int value_st
   const int64_t budget = (int64_t)8 << 30;
   const int64_t per_row = 8 * (nm + 3 * n_dy);
   int64_t pb = std::max<int64_t>(1, budget / (per_row * n_fields));
-  if (const char *e = std::getenv("GRADA_WAVELET_BATCH_POINTS"))  // smaller batches for tests
-    pb = std::max<int64_t>(1, std::atoll(e));
+  // GRADA_WAVELET_BATCH_POINTS makes batches smaller (tests); it never raises
+  // the batch above the ~8 GB budget
+  if (const char *e = std::getenv("GRADA_WAVELET_BATCH_POINTS"))
+    pb = std::min(pb, std::max<int64_t>(1, std::atoll(e)));
   pb = std::min(pb, n_obs);
   pb = std::min<int64_t>(pb, std::max<int64_t>(1, (int64_t)65535 * 32 / n_fields));  // grid rows
   const int64_t rows_max = pb * n_fields, ldb = round_up(rows_max, 32);

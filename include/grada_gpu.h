@@ -6,9 +6,9 @@
  * Fwd (src/Forward_modelling/Fwd.h:14-94), AdaptiveInversion
  * (src/Inversion/AdaptiveInversion.h) and GaussNewtonInversion
  * (src/Inversion/GaussNewtonInversion.h:4-112).  Each entry point below names
- * the reference member it replaces.  A drop-in translation unit that keeps
- * those class headers unchanged and forwards to these calls is shown in
- * INTEGRATION.md.
+ * the reference member it replaces.  Drop-in translation units that keep
+ * those class headers unchanged and forward to these calls are in
+ * graada3d_gb300/dropin/.
  *
  * Conventions
  *  - Every call returns an int status: GRADA_OK (0) or a negative GRADA_ERR_*.
@@ -131,8 +131,11 @@ int grada_GT_vec_mul_dev(grada_ctx *ctx, const double *d_y, double *d_x);
  * library holds it until exit): ld above 1,048,576 returns
  * GRADA_ERR_SCRATCH_LIMIT.  The first call on a device looks up the array's
  * device address (make it before any stream capture that should contain
- * later calls).  All calls on a device share the array: calls that may
- * overlap on the GPU race.
+ * later calls); that address is cached for the process, so after a
+ * cudaDeviceReset of that device the entry point must not be called there
+ * again.  All calls on a device share the array: calls that may overlap on
+ * the GPU race.  Only the status of its own two launches is returned; an
+ * error pending from the caller's earlier work is left for the caller.
  */
 int grada_G_vec_mul_noalloc(const double *d_G, int64_t nd, int64_t nm, int64_t ld,
                             const double *d_x, double *d_y, void *stream);

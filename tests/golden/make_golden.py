@@ -1,9 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the reference.
 
-Run in a checkout that has the reference tree (default /root/reference) after
-``make -C oracle all ref``:
+Run in a checkout that has the reference tree (the one ``make -C oracle -s refdir``
+names, or GRADA_REFERENCE) after ``make -C oracle all ref``:
 
-    python tests/golden/make_golden.py [--ref /root/reference] [--only NAME]
+    python tests/golden/make_golden.py [--ref REFERENCE_TREE] [--only NAME]
 
 Fixtures written (all .npz):
   forward_models.npz  the reference's committed noise-free forward fields
@@ -597,10 +597,18 @@ def ref_interp() -> None:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="reference tree (default: the oracle recipe's)")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
-    ref = Path(a.ref)
+    if a.ref:
+        ref = Path(a.ref)
+    else:
+        sys.path.insert(0, str(HERE.parent.parent))
+        from oracle import reference_dir
+
+        ref = reference_dir()
+        if ref is None:
+            sys.exit("reference tree not found: pass --ref or set GRADA_REFERENCE")
     jobs = {"forward_models": lambda: forward_models(ref), "ref_fields": ref_fields,
             "ref_expand": ref_expand, "ref_padded": ref_padded,
             "ref_indicator": ref_indicator, "ref_operators": ref_operators,

@@ -1,7 +1,6 @@
 """The drop-in translation units (graada3d_gb300/dropin/) compile against the
 reference's unchanged class headers.  Needs the reference tree; skipped
 elsewhere.  No GPU."""
-import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -10,7 +9,9 @@ import pytest
 
 from conftest import REPO
 
-REF = Path(os.environ.get("GRADA_REFERENCE", "/root/reference"))
+from oracle import reference_dir
+
+REF = reference_dir() or Path("missing-reference-tree")
 
 
 @pytest.mark.skipif(not (REF / "src" / "Forward_modelling" / "Fwd.h").exists(),
