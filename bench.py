@@ -85,6 +85,46 @@ def build_problem():
     return prisms, obs, rho
 
 
+# Output rows of the nine-component flag, in G's row order (ascending field bit).
+COMPONENTS = ["gz", "gx", "gy", "Tzz", "Txz", "Tyz", "Txx", "Txy", "Tyy"]
+PARITY_TOL = 1e-10  # FP64 path: |G - oracle| <= 1e-10 x max|component|
+
+
+def parity_points(n_random: int = 39, seed: int = 11) -> np.ndarray:
+    """Observation indices whose rows of the benchmarked G are checked against the
+    oracle: the 25 points on x, y in {0, 5, 10, 15, 20} km, which lie on cell-face
+    planes of the 312.5 m mesh (the coincident case), and n_random seeded others."""
+    plane = [25 * iy * 101 + 25 * ix for iy in range(5) for ix in range(5)]
+    rest = np.setdiff1d(np.arange(101 * 101), plane)
+    pick = np.random.default_rng(seed).choice(rest, n_random, replace=False)
+    return np.concatenate([np.array(plane, dtype=np.int64), np.sort(pick).astype(np.int64)])
+
+
+def bench_parity(f, prisms, obs) -> dict:
+    """Rows of the G that the timed steps assembled, read back from the device
+    (grada_get_G_rows), against the oracle's G for the same points over all cells."""
+    from oracle import prism as oracle_prism
+
+    idx = parity_points()
+    n_obs = obs.shape[0]
+    rows = (idx[None, :] + n_obs * np.arange(len(COMPONENTS))[:, None]).ravel()
+    got = f.get_G_rows(rows)
+    oracle_prism.build()
+    t0 = time.perf_counter()
+    want = oracle_prism.compute_G(prisms, obs[idx], MASK)
+    t_oracle = time.perf_counter() - t0
+    n = idx.size
+    errs = {}
+    for k, name in enumerate(COMPONENTS):
+        blk = slice(k * n, (k + 1) * n)
+        errs[name] = float(np.abs(got[blk] - want[blk]).max() / np.abs(want[blk]).max())
+    worst = max(errs.values())
+    return {"points": int(n), "face_plane_points": 25, "rows": int(rows.size), "cells": int(prisms.shape[0]),
+            "max_rel_err": errs, "worst": worst, "tol": PARITY_TOL, "pass": bool(worst <= PARITY_TOL),
+            "against": "oracle (Fwd::compute_G restated in C) on the same points, all cells",
+            "oracle_s": t_oracle}
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling during the timed region."""
 
@@ -282,6 +322,8 @@ def run_gpu(args):
     e2e_s = max_over_ranks(world, (time.perf_counter() - t0) / e2e_steps)
     assert np.isfinite(d).all()
     e2e_value = world * entries / e2e_s
+    # parity of the benchmarked G itself (after the timed region)
+    parity = bench_parity(f, prisms, obs) if rank == 0 else None
 
     roofline = None
     per_launch = statistics.median(per_launch_ms) * 1e-3
@@ -335,6 +377,7 @@ def run_gpu(args):
             "kernel_ms": {"median": statistics.median(per_launch_ms), "min": min(per_launch_ms),
                           "max": max(per_launch_ms)},
             "roofline": roofline,
+            "parity": parity,
             "hbm_write": hbm,
             "clocks": clk,
         }

@@ -41,6 +41,7 @@ SIGNATURES = {
     "grada_compute_G": (c_int, [c_void_p, c_int]),
     "grada_G_storage": (c_int, [c_void_p]),
     "grada_get_G": (c_int, [c_void_p, _dp, c_int64]),
+    "grada_get_G_rows": (c_int, [c_void_p, POINTER(c_int64), c_int64, _dp]),
     "grada_G_vec_mul": (c_int, [c_void_p, _dp, _dp]),
     "grada_GT_vec_mul": (c_int, [c_void_p, _dp, _dp]),
     "grada_G_vec_mul_dev": (c_int, [c_void_p, c_void_p, c_void_p]),

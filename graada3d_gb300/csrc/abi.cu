@@ -465,6 +465,34 @@ int grada_get_G(grada_ctx *ctx, double *host, int64_t ld_host) {
   });
 }
 
+int grada_get_G_rows(grada_ctx *ctx, const int64_t *rows, int64_t n_rows, double *host) {
+  return guarded(ctx, [&] {
+    ctx->require_G();
+    if (ctx->g_storage == GRADA_G_MATRIX_FREE || ctx->g_storage == GRADA_G_WAVELET)
+      throw Error(GRADA_ERR_STATE, "no stored dense G to read rows from");
+    if (n_rows < 0 || (n_rows > 0 && (!rows || !host)))
+      throw Error(GRADA_ERR_INVALID_ARGUMENT, "bad row list or host buffer");
+    for (int64_t r = 0; r < n_rows; r++)
+      if (rows[r] < 0 || rows[r] >= ctx->nd)
+        throw Error(GRADA_ERR_INVALID_ARGUMENT, "row index " + std::to_string(rows[r]) +
+                                                    " outside G's " + std::to_string(ctx->nd) + " rows");
+    const int64_t nm = ctx->n_cells;
+    // rows in chunks whose FP64 copies take at most ~256 MB of device memory
+    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(65535, ((int64_t)1 << 25) / nm));
+    grada::DevBuf d_rows, stage;
+    d_rows.alloc(ctx, sizeof(int64_t) * (size_t)std::min(chunk, n_rows));
+    stage.alloc(ctx, sizeof(double) * (size_t)(std::min(chunk, n_rows) * nm));
+    for (int64_t r0 = 0; r0 < n_rows; r0 += chunk) {
+      const int64_t nr = std::min(chunk, n_rows - r0);
+      ctx->upload(d_rows.ptr, rows + r0, sizeof(int64_t) * (size_t)nr);
+      grada::launch_gather_rows(ctx->devG(), d_rows.as<int64_t>(), nr, stage.as<double>(),
+                                ctx->stream);
+      ctx->download(host + r0 * nm, stage.ptr, sizeof(double) * (size_t)(nr * nm));
+      ctx->sync();
+    }
+  });
+}
+
 int grada_G_vec_mul(grada_ctx *ctx, const double *x, double *y) {
   return guarded(ctx, [&] {
     ctx->require_G();
@@ -757,10 +785,13 @@ int grada_inject_fault(grada_ctx *ctx, int fault) {
       const int flag = 1;
       ctx->upload(ctx->tc_err.ptr, &flag, sizeof(int));
       ctx->sync();
+    } else if (fault == GRADA_FAULT_CG_WAIT) {
+      ctx->inject_cg_wait = true;
     } else if (fault != GRADA_FAULT_NONE) {
       throw grada::Error(GRADA_ERR_INVALID_ARGUMENT, "unknown fault kind");
     } else {
       ctx->inject_alloc_failure = false;
+      ctx->inject_cg_wait = false;
     }
   });
 }

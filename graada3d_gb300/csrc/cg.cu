@@ -6,6 +6,7 @@
 // partials in order, so repeated runs give bit-identical scalars.  The
 // sparse operators are the host-built regularisation matrices (CSR, <= 9
 // entries per row on the reference's meshes); one thread owns one row.
+#include "cg_body.cuh"
 #include "cg_kernels.h"
 #include "common.cuh"
 
@@ -13,28 +14,8 @@ namespace grada {
 
 namespace {
 
-constexpr int VT = 256;  // threads per block for vector kernels
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-__device__ __forceinline__ double block_sum(double v) {
-  __shared__ double red[VT / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  v = warp_sum(v);
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (warp == 0) {
-    s = (lane < VT / 32) ? red[lane] : 0.0;
-    s = warp_sum(s);
-  }
-  __syncthreads();
-  return s;  // valid in thread 0
-}
+using cgb::block_sum;
+using cgb::VT;
 
 // y = c * wl .* (A (x - xs))    (wl, xs optional)
 __global__ void csr_apply_kernel(DevCSR A, const double *__restrict__ x,
@@ -54,57 +35,33 @@ __global__ void csr_apply_kernel(DevCSR A, const double *__restrict__ x,
 }
 
 // Forward regulariser rows for up to 7 terms in one launch (blockIdx.y = term).
-__global__ void multi_forward_kernel(ForwardTerms T, const double *__restrict__ x,
+__global__ void multi_forward_kernel(ForwardTerms T, const double *x,
                                      const int *__restrict__ skip) {
   if (skip && *skip) return;
-  const ForwardTerm &t = T.t[blockIdx.y];
-  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
-  if (i >= t.A.n) return;
-  double acc = 0.0;
-  for (int k = t.A.rowptr[i]; k < t.A.rowptr[i + 1]; k++) acc = fma(t.A.val[k], x[t.A.col[k]], acc);
-  double v = t.c * acc;
-  if (t.wl) v *= t.wl[i];
-  t.out[i] = v;
+  cgb::forward_term_body(T.t[blockIdx.y], x, blockIdx.x);
 }
 
 // r = P .* (sign_g * gtw + sum_t c_t A_t^T (wl_t .* s_t)), A_t^T given as CSR.
 __global__ void adjoint_kernel(AdjointTerms T, int64_t n, const double *__restrict__ P,
-                               const double *__restrict__ gtw, double sign_g,
-                               double *__restrict__ r, const int *__restrict__ skip) {
+                               const double *gtw, double sign_g, double *r,
+                               const int *__restrict__ skip) {
   if (skip && *skip) return;
   const int64_t j = (int64_t)blockIdx.x * VT + threadIdx.x;
   if (j >= n) return;
-  double acc = gtw ? sign_g * gtw[j] : 0.0;
-  for (int q = 0; q < T.count; q++) {
-    const AdjointTerm &t = T.t[q];
-    double s = 0.0;
-    for (int k = t.AT.rowptr[j]; k < t.AT.rowptr[j + 1]; k++) {
-      const int i = t.AT.col[k];
-      const double w = t.wl ? t.wl[i] : 1.0;
-      s = fma(t.AT.val[k], w * t.s[i], s);
-    }
-    acc = fma(t.c, s, acc);
-  }
-  r[j] = P ? P[j] * acc : acc;
+  r[j] = cgb::adjoint_column(T, j, P, gtw != nullptr, gtw ? __ldcg(gtw + j) : 0.0, sign_g);
 }
 
-__global__ void dot_partial_kernel(const double *__restrict__ a, const double *__restrict__ b,
-                                   int64_t n, double *__restrict__ partial,
+__global__ void dot_partial_kernel(const double *a, const double *b, int64_t n, double *partial,
                                    const int *__restrict__ skip) {
   if (skip && *skip) return;
-  double v = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT)
-    v = fma(a[i], b ? b[i] : a[i], v);
-  v = block_sum(v);
+  const double v = cgb::dot_partial_body(a, b, n, blockIdx.x, gridDim.x);
   if (threadIdx.x == 0) partial[blockIdx.x] = v;
 }
 
-__global__ void sum_partials_kernel(const double *__restrict__ partial, int nblocks,
-                                    double *__restrict__ out, const int *__restrict__ skip) {
+__global__ void sum_partials_kernel(const double *partial, int nblocks, double *out,
+                                    const int *__restrict__ skip) {
   if (skip && *skip) return;
-  double v = 0.0;
-  for (int i = threadIdx.x; i < nblocks; i += VT) v += partial[i];
-  v = block_sum(v);
+  const double v = cgb::sum_partials_body(partial, nblocks);
   if (threadIdx.x == 0) *out = v;
 }
 
@@ -133,28 +90,19 @@ __global__ void negate_kernel(const double *__restrict__ a, int64_t n, double *_
 }
 
 // p = -r + beta p ;  pp = P .* p
-__global__ void p_update_kernel(const double *__restrict__ r, const double *__restrict__ P,
-                                const double *__restrict__ scal, int64_t n, double *__restrict__ p,
-                                double *__restrict__ pp, const int *__restrict__ skip) {
+__global__ void p_update_kernel(const double *r, const double *__restrict__ P,
+                                const double *__restrict__ scal, int64_t n, double *p, double *pp,
+                                const int *__restrict__ skip) {
   if (skip && *skip) return;
-  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
-  if (i >= n) return;
-  const double beta = scal[CG_BETA];
-  const double v = -r[i] + beta * p[i];
-  p[i] = v;
-  pp[i] = P[i] * v;
+  cgb::p_update_body(r, P, scal[CG_BETA], n, p, pp, blockIdx.x);
 }
 
 // s += alpha t (nrow) ;  dx += alpha p (n)
-__global__ void axpy_kernel(const double *__restrict__ t, const double *__restrict__ p,
-                            const double *__restrict__ scal, int64_t nrow, int64_t n,
-                            double *__restrict__ s, double *__restrict__ dx,
+__global__ void axpy_kernel(const double *t, const double *p, const double *__restrict__ scal,
+                            int64_t nrow, int64_t n, double *s, double *dx,
                             const int *__restrict__ skip) {
   if (skip && *skip) return;
-  const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
-  const double alpha = scal[CG_ALPHA];
-  if (i < nrow) s[i] = fma(alpha, t[i], s[i]);
-  if (i < n) dx[i] = fma(alpha, p[i], dx[i]);
+  cgb::axpy_body(t, p, scal[CG_ALPHA], nrow, n, s, dx, blockIdx.x);
 }
 
 // ctl[CTL_DONE] != 0 turns every later kernel of the iteration (and of later

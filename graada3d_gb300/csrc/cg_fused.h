@@ -1,0 +1,47 @@
+// Persistent CG (cg_fused.cu): arguments of one solve's loop and its launch.
+// Internal interface.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cg_kernels.h"
+#include "kernels.h"
+
+namespace grada {
+
+__host__ __device__ inline int64_t ceil_div_d(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Everything the CG loop touches.  The loop starts from the state the setup
+// left on the device (r, p = 0, dx = 0, s, the scalars R2, ATB2, TOL, BETA = 0
+// and the control block) and leaves the same state the graph path leaves.
+struct FusedCgArgs {
+  // stored G and the G x partition (gx_splits)
+  const void *G = nullptr;
+  const float *row_scale = nullptr;
+  int64_t nd = 0, nm = 0, ld = 0;
+  int tiles = 0, splits = 0;
+  int64_t per = 0;
+  double *scratch = nullptr;  // splits * ld doubles: G x partials, then y
+  const double *wd = nullptr;  // Wd: post-scale of G pp, pre-scale of G^T s
+  // CG vectors (GaussNewtonInversion.cpp:1556-1692)
+  double *r = nullptr, *p = nullptr, *pp = nullptr, *dx = nullptr, *t = nullptr, *s = nullptr,
+         *gtw = nullptr;
+  const double *P = nullptr;
+  int64_t nrow = 0;
+  ForwardTerms FT;
+  AdjointTerms AT;
+  double *part = nullptr;
+  int nb_m = 0, nb_row = 0;  // dot-product block counts (dot_blocks)
+  double *scal = nullptr;
+  int *ctl = nullptr;
+  unsigned *barrier = nullptr;  // 2 words: arrivals, error
+  unsigned long long wait_limit_ns = 2000000000ull;
+};
+
+// CTAs of a persistent CG launch for this storage (all co-resident).
+int fused_cg_grid(GKind kind, int sm_count);
+// Clears the barrier words and launches the cooperative kernel.
+void launch_cg_fused(const FusedCgArgs &a, GKind kind, int grid, cudaStream_t s);
+
+}  // namespace grada

@@ -116,7 +116,9 @@ struct Context {
 
   // CG work vectors.
   DevBuf cg_b, cg_s, cg_t, cg_p, cg_pp, cg_r, cg_atb, cg_gtw, cg_gx, cg_tmpd, cg_scal, cg_part;
-  DevBuf cg_wl_ones, cg_ctl;
+  DevBuf cg_wl_ones, cg_ctl, cg_bar;
+  int fused_grid[4] = {0, 0, 0, 0};  // persistent CG grid per G storage kind
+  bool inject_cg_wait = false;       // grada_inject_fault(GRADA_FAULT_CG_WAIT)
   double *h_scal = nullptr;  // pinned
   int *h_flag = nullptr;     // pinned
   int *h_ctl = nullptr;      // pinned
@@ -162,6 +164,10 @@ struct Context {
   void set_data(const double *h_dobs, const double *h_wd);
   void ensure_cg_workspace(int nterms);
   void data_prediction(const double *m, const double *m_start, const double *d64, double *out);
+  bool fused_cg_eligible() const;
+  CgResult solve_cg_fused(double tol, int maxit, const double *P, double *dx,
+                          const ForwardTerms &FT, const AdjointTerms &AT, int64_t nrow, int nb_m,
+                          int nb_row);
   CgResult solve_cg_dev(double lambda, double tol, int maxit, const double *mk, const double *mref,
                         const double *P, const double *const WL[7], double *dx,
                         const double *d64, const double *m_start);

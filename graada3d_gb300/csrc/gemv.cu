@@ -21,211 +21,60 @@
 // in FP64.  bf16 rows carry an FP32 scale applied after the row sum (G x) or
 // folded into y (G^T y).
 #include "common.cuh"
+#include "gemv_body.cuh"
 #include "kernels.h"
 
 namespace grada {
 
 namespace {
 
-constexpr int GV_THREADS = 256;
-
-// ---- element loaders: VEC consecutive entries from a 16-byte load ----------
-
-struct LoadF64 {
-  static constexpr int VEC = 2;
-  using Acc = double;
-  __device__ static void load(const void *base, int64_t idx, double (&v)[2]) {
-    const double2 d = __ldcs(reinterpret_cast<const double2 *>(static_cast<const double *>(base) + idx));
-    v[0] = d.x;
-    v[1] = d.y;
-  }
-};
-struct LoadF32 {
-  static constexpr int VEC = 4;
-  using Acc = float;
-  __device__ static void load(const void *base, int64_t idx, float (&v)[4]) {
-    const float4 d = __ldcs(reinterpret_cast<const float4 *>(static_cast<const float *>(base) + idx));
-    v[0] = d.x;
-    v[1] = d.y;
-    v[2] = d.z;
-    v[3] = d.w;
-  }
-};
-struct LoadBF16 {
-  static constexpr int VEC = 8;
-  using Acc = float;
-  __device__ static void load(const void *base, int64_t idx, float (&v)[8]) {
-    const uint4 d = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(base) + idx));
-    const uint32_t w[4] = {d.x, d.y, d.z, d.w};
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      v[2 * k] = __uint_as_float(w[k] << 16);
-      v[2 * k + 1] = __uint_as_float(w[k] & 0xffff0000u);
-    }
-  }
-};
-
-struct LoadF16 {
-  static constexpr int VEC = 8;
-  using Acc = float;
-  __device__ static void load(const void *base, int64_t idx, float (&v)[8]) {
-    const uint4 d = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(base) + idx));
-    const uint32_t w[4] = {d.x, d.y, d.z, d.w};
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      __half2 h;
-      memcpy(&h, &w[k], 4);
-      const float2 f = __half22float2(h);
-      v[2 * k] = f.x;
-      v[2 * k + 1] = f.y;
-    }
-  }
-};
+using gemv::LoadBF16;
+using gemv::LoadF16;
+using gemv::LoadF32;
+using gemv::LoadF64;
+constexpr int GV_THREADS = gemv::kThreads;
 
 // ---- G x ----------------------------------------------------------------------
 
 template <class L>
 __global__ void __launch_bounds__(GV_THREADS)
     gx_partial_kernel(const void *__restrict__ G, int64_t ld, int64_t nm, int64_t cols_per_split,
-                      const double *__restrict__ x, double *__restrict__ partial,
-                      const int *__restrict__ skip) {
+                      const double *x, double *partial, const int *__restrict__ skip) {
   if (skip && *skip) return;
-  using Acc = typename L::Acc;
-  constexpr int VEC = L::VEC;
-  constexpr int XCH = 256;
-  __shared__ Acc xs[XCH];
-  const int64_t row = ((int64_t)blockIdx.x * GV_THREADS + threadIdx.x) * VEC;
-  const int64_t c_begin = (int64_t)blockIdx.y * cols_per_split;
-  const int64_t c_end = min(nm, c_begin + cols_per_split);
-  Acc acc[VEC];
-#pragma unroll
-  for (int v = 0; v < VEC; v++) acc[v] = Acc(0);
-  for (int64_t c0 = c_begin; c0 < c_end; c0 += XCH) {
-    const int nc = (int)min((int64_t)XCH, c_end - c0);
-    __syncthreads();
-    for (int t = threadIdx.x; t < nc; t += GV_THREADS) xs[t] = (Acc)x[c0 + t];
-    __syncthreads();
-    if (row < ld) {
-      const int64_t base = row + c0 * ld;
-      int c = 0;
-      for (; c + 4 <= nc; c += 4) {
-        Acc g0[VEC], g1[VEC], g2[VEC], g3[VEC];
-        L::load(G, base + (int64_t)c * ld, g0);
-        L::load(G, base + (int64_t)(c + 1) * ld, g1);
-        L::load(G, base + (int64_t)(c + 2) * ld, g2);
-        L::load(G, base + (int64_t)(c + 3) * ld, g3);
-        const Acc x0 = xs[c], x1 = xs[c + 1], x2 = xs[c + 2], x3 = xs[c + 3];
-#pragma unroll
-        for (int v = 0; v < VEC; v++) {
-          acc[v] = fma(g0[v], x0, acc[v]);
-          acc[v] = fma(g1[v], x1, acc[v]);
-          acc[v] = fma(g2[v], x2, acc[v]);
-          acc[v] = fma(g3[v], x3, acc[v]);
-        }
-      }
-      for (; c < nc; c++) {
-        Acc g0[VEC];
-        L::load(G, base + (int64_t)c * ld, g0);
-#pragma unroll
-        for (int v = 0; v < VEC; v++) acc[v] = fma(g0[v], xs[c], acc[v]);
-      }
-    }
-  }
-  if (row < ld) {
-    double *out = partial + (int64_t)blockIdx.y * ld + row;
-#pragma unroll
-    for (int v = 0; v < VEC; v++) out[v] = (double)acc[v];
-  }
+  gemv::gx_partial_body<L>(G, ld, nm, cols_per_split, x, partial, blockIdx.x, blockIdx.y);
 }
 
-__global__ void gx_finish_kernel(const double *__restrict__ partial, int n_split, int64_t ld,
-                                 int64_t nd, const float *__restrict__ row_scale,
-                                 const double *__restrict__ post_scale, double *__restrict__ y,
+__global__ void gx_finish_kernel(const double *partial, int n_split, int64_t ld, int64_t nd,
+                                 const float *__restrict__ row_scale,
+                                 const double *__restrict__ post_scale, double *y,
                                  const int *__restrict__ skip) {
   if (skip && *skip) return;
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nd) return;
-  double s = 0.0;
-  for (int k = 0; k < n_split; k++) s += partial[(int64_t)k * ld + r];
-  if (row_scale) s *= (double)row_scale[r];
-  if (post_scale) s *= post_scale[r];
-  y[r] = s;
+  gemv::gx_finish_body(partial, n_split, ld, nd, row_scale, post_scale, y, blockIdx.x);
 }
 
 // ---- G^T y --------------------------------------------------------------------
 
 template <class L, int COLS>
 __global__ void __launch_bounds__(GV_THREADS)
-    gty_kernel(const void *__restrict__ G, int64_t ld, int64_t nm,
-               const typename L::Acc *__restrict__ y, double *__restrict__ x,
-               const int *__restrict__ skip) {
+    gty_kernel(const void *__restrict__ G, int64_t ld, int64_t nm, const typename L::Acc *y,
+               double *x, const int *__restrict__ skip) {
+  static_assert(COLS == gemv::kGtCols, "G^T y blocks have kGtCols columns");
   if (skip && *skip) return;
-  using Acc = typename L::Acc;
-  constexpr int VEC = L::VEC;
-  const int64_t c0 = (int64_t)blockIdx.x * COLS;
-  const int ncol = (int)min((int64_t)COLS, nm - c0);
-  Acc acc[COLS];
-#pragma unroll
-  for (int c = 0; c < COLS; c++) acc[c] = Acc(0);
-  for (int64_t row = (int64_t)threadIdx.x * VEC; row < ld; row += (int64_t)GV_THREADS * VEC) {
-    Acc yv[VEC];
-#pragma unroll
-    for (int v = 0; v < VEC; v++) yv[v] = y[row + v];
-#pragma unroll
-    for (int c = 0; c < COLS; c++) {
-      if (c < ncol) {
-        Acc g[VEC];
-        L::load(G, row + (c0 + c) * ld, g);
-#pragma unroll
-        for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
-      }
-    }
-  }
-  __shared__ double red[GV_THREADS / 32][COLS];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int c = 0; c < COLS; c++) {
-    double v = (double)acc[c];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[warp][c] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < ncol) {
-    double s = 0.0;
-#pragma unroll
-    for (int w = 0; w < GV_THREADS / 32; w++) s += red[w][threadIdx.x];
-    x[c0 + threadIdx.x] = s;
-  }
+  int ncol = 0;
+  const double s = gemv::gty_body<L>(G, ld, nm, y, blockIdx.x, &ncol);
+  if (threadIdx.x < ncol) x[(int64_t)blockIdx.x * COLS + threadIdx.x] = s;
 }
 
 // y (FP64, nd entries) -> padded vector of the accumulation type, times the
 // row scale for bf16, zero in the padding rows.
 template <typename Acc>
-__global__ void prep_y_kernel(const double *__restrict__ y, int64_t nd, int64_t ld,
+__global__ void prep_y_kernel(const double *y, int64_t nd, int64_t ld,
                               const float *__restrict__ row_scale,
-                              const double *__restrict__ pre_scale, Acc *__restrict__ out,
+                              const double *__restrict__ pre_scale, Acc *out,
                               const int *__restrict__ skip) {
   if (skip && *skip) return;
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= ld) return;
-  double v = (r < nd) ? y[r] : 0.0;
-  if (pre_scale && r < nd) v = pre_scale[r] * v;
-  if (row_scale && r < nd) v *= (double)row_scale[r];
-  out[r] = (Acc)v;
+  gemv::prep_y_body<Acc>(y, nd, ld, row_scale, pre_scale, out, blockIdx.x);
 }
-
-int gx_splits(const DevG &G, int sm_count, int vec) {
-  const int64_t tiles = ceil_div(G.ld, (int64_t)GV_THREADS * vec);
-  int64_t splits = ceil_div((int64_t)sm_count * 8, tiles);
-  const int64_t max_splits = ceil_div(G.nm, 64);
-  if (splits > max_splits) splits = max_splits;
-  if (splits < 1) splits = 1;
-  if (splits > 65535) splits = 65535;
-  return (int)splits;
-}
-
-int vec_of(GKind k) { return k == GKind::FP64 ? 2 : (k == GKind::FP32 ? 4 : 8); }
 
 __global__ void widen_kernel(const void *__restrict__ G, int kind, const float *__restrict__ scale,
                              int64_t nd, int64_t ld, int64_t c0, double *__restrict__ out) {
@@ -263,6 +112,18 @@ void run_gx(const DevG &G, const double *x, double *y, double *scratch, int sm_c
 
 }  // namespace
 
+int gx_splits(const DevG &G, int sm_count, int vec) {
+  const int64_t tiles = ceil_div(G.ld, (int64_t)GV_THREADS * vec);
+  int64_t splits = ceil_div((int64_t)sm_count * 8, tiles);
+  const int64_t max_splits = ceil_div(G.nm, 64);
+  if (splits > max_splits) splits = max_splits;
+  if (splits < 1) splits = 1;
+  if (splits > 65535) splits = 65535;
+  return (int)splits;
+}
+
+int vec_of(GKind k) { return k == GKind::FP64 ? 2 : (k == GKind::FP32 ? 4 : 8); }
+
 int64_t gemv_scratch_doubles(const DevG &G, int sm_count) {
   const int splits = gx_splits(G, sm_count, vec_of(G.kind));
   const int64_t gx = (int64_t)splits * G.ld;
@@ -279,6 +140,42 @@ void launch_G_vec_mul(const DevG &G, const double *x, double *y, double *scratch
     case GKind::BF16: run_gx<LoadBF16>(G, x, y, scratch, sm_count, o, s); break;
     case GKind::FP16: run_gx<LoadF16>(G, x, y, scratch, sm_count, o, s); break;
   }
+}
+
+namespace {
+
+// out[r * nm + j] = G(rows[r], j) widened to FP64 (16-bit entries times their
+// row scale); one thread per (row, column), blockIdx.y = the row.
+__global__ void gather_rows_kernel(const void *__restrict__ G, int kind,
+                                   const float *__restrict__ scale, int64_t nm, int64_t ld,
+                                   const int64_t *__restrict__ rows, double *__restrict__ out) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nm) return;
+  const int64_t r = rows[blockIdx.y];
+  const int64_t src = r + j * ld;
+  double v;
+  if (kind == 0) {
+    v = static_cast<const double *>(G)[src];
+  } else if (kind == 1) {
+    v = (double)static_cast<const float *>(G)[src];
+  } else if (kind == 2) {
+    const uint32_t bits = (uint32_t) static_cast<const uint16_t *>(G)[src] << 16;
+    v = (double)__uint_as_float(bits) * (double)scale[r];
+  } else {
+    const __half h = __ushort_as_half(static_cast<const uint16_t *>(G)[src]);
+    v = (double)__half2float(h) * (double)scale[r];
+  }
+  out[(int64_t)blockIdx.y * nm + j] = v;
+}
+
+}  // namespace
+
+void launch_gather_rows(const DevG &G, const int64_t *rows, int64_t n_rows, double *out,
+                        cudaStream_t s) {
+  if (n_rows <= 0 || G.nm <= 0) return;
+  dim3 grid((unsigned)ceil_div(G.nm, 256), (unsigned)n_rows);
+  gather_rows_kernel<<<grid, 256, 0, s>>>(G.data, (int)G.kind, G.row_scale, G.nm, G.ld, rows, out);
+  GRADA_LAUNCH_CHECK();
 }
 
 void launch_widen_columns(const DevG &G, int64_t c0, int64_t nc, double *out, cudaStream_t s) {

@@ -1,0 +1,211 @@
+// Per-block bodies of the dense products with the stored G (gemv.cu), shared
+// by the one-product kernels and the persistent CG kernel (cg_fused.cu).  A
+// body takes the index of its block as an argument instead of blockIdx, so a
+// persistent kernel can run the blocks of a product in any grid and gets the
+// same sums in the same order: the results are bitwise those of the
+// stand-alone kernels.
+//
+// Vectors that the persistent kernel rewrites between its phases (x, y, the
+// partial sums) are read with ld.global.cg (L2, never a stale L1 or the
+// read-only path); G itself is streamed with evict-first loads.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace grada {
+namespace gemv {
+
+constexpr int kThreads = 256;  // threads of every product block
+constexpr int kXChunk = 256;   // x entries staged in shared memory at a time (G x)
+constexpr int kGtCols = 4;     // columns per G^T y block
+
+// ---- element loaders: VEC consecutive entries from a 16-byte load ----------
+
+struct LoadF64 {
+  static constexpr int VEC = 2;
+  using Acc = double;
+  __device__ static void load(const void *base, int64_t idx, double (&v)[2]) {
+    const double2 d = __ldcs(reinterpret_cast<const double2 *>(static_cast<const double *>(base) + idx));
+    v[0] = d.x;
+    v[1] = d.y;
+  }
+};
+struct LoadF32 {
+  static constexpr int VEC = 4;
+  using Acc = float;
+  __device__ static void load(const void *base, int64_t idx, float (&v)[4]) {
+    const float4 d = __ldcs(reinterpret_cast<const float4 *>(static_cast<const float *>(base) + idx));
+    v[0] = d.x;
+    v[1] = d.y;
+    v[2] = d.z;
+    v[3] = d.w;
+  }
+};
+struct LoadBF16 {
+  static constexpr int VEC = 8;
+  using Acc = float;
+  __device__ static void load(const void *base, int64_t idx, float (&v)[8]) {
+    const uint4 d = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(base) + idx));
+    const uint32_t w[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      v[2 * k] = __uint_as_float(w[k] << 16);
+      v[2 * k + 1] = __uint_as_float(w[k] & 0xffff0000u);
+    }
+  }
+};
+struct LoadF16 {
+  static constexpr int VEC = 8;
+  using Acc = float;
+  __device__ static void load(const void *base, int64_t idx, float (&v)[8]) {
+    const uint4 d = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(base) + idx));
+    const uint32_t w[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      __half2 h;
+      memcpy(&h, &w[k], 4);
+      const float2 f = __half22float2(h);
+      v[2 * k] = f.x;
+      v[2 * k + 1] = f.y;
+    }
+  }
+};
+
+// ---- G x: block (tile, split) accumulates kThreads * VEC rows over one
+// column range; the ranges' partial rows go to partial[split * ld + row].
+template <class L>
+__device__ __forceinline__ void gx_partial_body(const void *__restrict__ G, int64_t ld, int64_t nm,
+                                                int64_t cols_per_split, const double *x,
+                                                double *partial, int64_t tile, int64_t split) {
+  using Acc = typename L::Acc;
+  constexpr int VEC = L::VEC;
+  __shared__ Acc xs[kXChunk];
+  const int64_t row = (tile * kThreads + threadIdx.x) * VEC;
+  const int64_t c_begin = split * cols_per_split;
+  const int64_t c_end = min(nm, c_begin + cols_per_split);
+  Acc acc[VEC];
+#pragma unroll
+  for (int v = 0; v < VEC; v++) acc[v] = Acc(0);
+  for (int64_t c0 = c_begin; c0 < c_end; c0 += kXChunk) {
+    const int nc = (int)min((int64_t)kXChunk, c_end - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc; t += kThreads) xs[t] = (Acc)__ldcg(x + c0 + t);
+    __syncthreads();
+    if (row < ld) {
+      const int64_t base = row + c0 * ld;
+      int c = 0;
+      for (; c + 4 <= nc; c += 4) {
+        Acc g0[VEC], g1[VEC], g2[VEC], g3[VEC];
+        L::load(G, base + (int64_t)c * ld, g0);
+        L::load(G, base + (int64_t)(c + 1) * ld, g1);
+        L::load(G, base + (int64_t)(c + 2) * ld, g2);
+        L::load(G, base + (int64_t)(c + 3) * ld, g3);
+        const Acc x0 = xs[c], x1 = xs[c + 1], x2 = xs[c + 2], x3 = xs[c + 3];
+#pragma unroll
+        for (int v = 0; v < VEC; v++) {
+          acc[v] = fma(g0[v], x0, acc[v]);
+          acc[v] = fma(g1[v], x1, acc[v]);
+          acc[v] = fma(g2[v], x2, acc[v]);
+          acc[v] = fma(g3[v], x3, acc[v]);
+        }
+      }
+      for (; c < nc; c++) {
+        Acc g0[VEC];
+        L::load(G, base + (int64_t)c * ld, g0);
+#pragma unroll
+        for (int v = 0; v < VEC; v++) acc[v] = fma(g0[v], xs[c], acc[v]);
+      }
+    }
+  }
+  if (row < ld) {
+    double *out = partial + split * ld + row;
+#pragma unroll
+    for (int v = 0; v < VEC; v++) out[v] = (double)acc[v];
+  }
+}
+
+// y[r] = (sum over splits of the partial rows) * row_scale[r] * post_scale[r],
+// 256 rows per block b.
+__device__ __forceinline__ void gx_finish_body(const double *partial, int n_split, int64_t ld,
+                                               int64_t nd, const float *__restrict__ row_scale,
+                                               const double *__restrict__ post_scale, double *y,
+                                               int64_t b) {
+  const int64_t r = b * 256 + threadIdx.x;
+  if (r >= nd) return;
+  double s = 0.0;
+  for (int k = 0; k < n_split; k++) s += __ldcg(partial + (int64_t)k * ld + r);
+  if (row_scale) s *= (double)row_scale[r];
+  if (post_scale) s *= post_scale[r];
+  y[r] = s;
+}
+
+// y (FP64, nd entries) -> padded vector of the accumulation type, times the
+// optional pre-scale and the 16-bit row scale, zero in the padding rows;
+// 256 rows per block b.
+template <typename Acc>
+__device__ __forceinline__ void prep_y_body(const double *y, int64_t nd, int64_t ld,
+                                            const float *__restrict__ row_scale,
+                                            const double *__restrict__ pre_scale, Acc *out,
+                                            int64_t b) {
+  const int64_t r = b * 256 + threadIdx.x;
+  if (r >= ld) return;
+  double v = (r < nd) ? __ldcg(y + r) : 0.0;
+  if (pre_scale && r < nd) v = pre_scale[r] * v;
+  if (row_scale && r < nd) v *= (double)row_scale[r];
+  out[r] = (Acc)v;
+}
+
+// G^T y for the kGtCols columns of block b: returns column (b * kGtCols +
+// threadIdx.x)'s sum in threads threadIdx.x < ncol (ncol through *ncol_out),
+// every thread of the block taking part.
+template <class L>
+__device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t ld, int64_t nm,
+                                           const typename L::Acc *y, int64_t b, int *ncol_out) {
+  using Acc = typename L::Acc;
+  constexpr int VEC = L::VEC;
+  constexpr int COLS = kGtCols;
+  const int64_t c0 = b * COLS;
+  const int ncol = (int)min((int64_t)COLS, nm - c0);
+  Acc acc[COLS];
+#pragma unroll
+  for (int c = 0; c < COLS; c++) acc[c] = Acc(0);
+  for (int64_t row = (int64_t)threadIdx.x * VEC; row < ld; row += (int64_t)kThreads * VEC) {
+    Acc yv[VEC];
+#pragma unroll
+    for (int v = 0; v < VEC; v++) yv[v] = __ldcg(y + row + v);
+#pragma unroll
+    for (int c = 0; c < COLS; c++) {
+      if (c < ncol) {
+        Acc g[VEC];
+        L::load(G, row + (c0 + c) * ld, g);
+#pragma unroll
+        for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
+      }
+    }
+  }
+  __shared__ double red[kThreads / 32][COLS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();  // red is reused by the next block the caller runs
+#pragma unroll
+  for (int c = 0; c < COLS; c++) {
+    double v = (double)acc[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][c] = v;
+  }
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x < ncol) {
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; w++) s += red[w][threadIdx.x];
+  }
+  *ncol_out = ncol;
+  return s;
+}
+
+}  // namespace gemv
+}  // namespace grada

@@ -11,9 +11,11 @@
 // (GaussNewtonInversion.cpp:1461-1471): data (Nd), Ws, Wz, Wx, Wy and, with
 // the cross-gradient constraint, Tz, Tx, Ty (Nm each).
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 
+#include "cg_fused.h"
 #include "common.cuh"
 #include "context.h"
 
@@ -61,7 +63,7 @@ void Context::release_all() {
   for (DevBuf *b : {&wv_order, &wv_rowptr, &wv_col, &wv_val, &wv_part, &wv_segptr})
     b->release();
   DevBuf *bufs[] = {&dobs, &wd, &cg_b, &cg_s, &cg_t, &cg_p, &cg_pp, &cg_r, &cg_atb, &cg_gtw,
-                    &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &cg_ctl, &iv_m, &iv_mt, &iv_mt_old,
+                    &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &cg_ctl, &cg_bar, &iv_m, &iv_mt, &iv_mt_old,
                     &iv_mopt, &iv_dx, &iv_P, &iv_mmin, &iv_mmax, &iv_m0, &iv_wl, &iv_tmp, &iv_tmp2,
                     &iv_dpre, &iv_d64, &iv_mstart, &iv_guard, &iv_flag,
                     &bscratch, &tc_err, &bk_b, &bk_s, &bk_t, &bk_p, &bk_pp, &bk_r, &bk_atb,
@@ -341,6 +343,7 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
                                    cudaMemcpyDeviceToHost, stream));
   sync();
   if (h_scal[CG_R2] == 0.0) return res;
+  if (fused_cg_eligible()) return solve_cg_fused(tol, maxit, P, dx, FT, AT_s, nrow, nb_m, nb_row);
   // Device-side stopping: the beta kernel counts iterations and raises
   // ctl[CTL_DONE] on err < tol (or maxit, breakdown, non-finite scalar);
   // every kernel of an iteration returns at once while it is raised, so a
@@ -405,6 +408,84 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
     throw;
   }
   cudaGraphExecDestroy(exec);
+  res.iterations = h_ctl[CTL_ITER];
+  res.err = h_scal[CG_ERR];
+  if (h_ctl[CTL_STATUS] == CG_STATUS_BREAKDOWN)
+    throw Error(GRADA_ERR_BREAKDOWN,
+                "CG breakdown: ||t||^2 = 0 at iteration " + std::to_string(res.iterations));
+  if (h_ctl[CTL_STATUS] == CG_STATUS_NONFINITE)
+    throw Error(GRADA_ERR_NONFINITE,
+                "non-finite CG scalar at iteration " + std::to_string(res.iterations));
+  return res;
+}
+
+bool Context::fused_cg_eligible() const {
+  // stored dense G only (the matrix-free and wavelet products keep the graph
+  // path); GRADA_CG_FUSED=0 selects the graph path for every storage
+  if (g_storage != GRADA_G_FP64 && g_storage != GRADA_G_FP32 && g_storage != GRADA_G_BF16_ROWSCALE &&
+      g_storage != GRADA_G_FP16_ROWSCALE)
+    return false;
+  const char *e = std::getenv("GRADA_CG_FUSED");
+  return !(e && e[0] == '0');
+}
+
+// The CG loop as one persistent cooperative launch (cg_fused.cu), from the
+// state the setup of solve_cg_dev left on the device.
+CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double *dx,
+                                 const ForwardTerms &FT, const AdjointTerms &AT, int64_t nrow,
+                                 int nb_m, int nb_row) {
+  const DevG g = devG();
+  FusedCgArgs a;
+  a.G = g.data;
+  a.row_scale = g.row_scale;
+  a.nd = g.nd;
+  a.nm = g.nm;
+  a.ld = g.ld;
+  a.splits = gx_splits(g, sm_count, vec_of(g.kind));
+  a.tiles = (int)ceil_div(g.ld, (int64_t)256 * vec_of(g.kind));
+  a.per = ceil_div(g.nm, a.splits);
+  a.scratch = scratch_doubles(product_scratch_doubles());
+  a.wd = dptr(wd);
+  a.r = dptr(cg_r);
+  a.p = dptr(cg_p);
+  a.pp = dptr(cg_pp);
+  a.dx = dx;
+  a.t = dptr(cg_t);
+  a.s = dptr(cg_s);
+  a.gtw = dptr(cg_gtw);
+  a.P = P;
+  a.nrow = nrow;
+  a.FT = FT;
+  a.AT = AT;
+  a.part = dptr(cg_part);
+  a.nb_m = nb_m;
+  a.nb_row = nb_row;
+  a.scal = dptr(cg_scal);
+  cg_ctl.alloc(this, sizeof(int) * CTL_NINTS);
+  a.ctl = cg_ctl.as<int>();
+  cg_bar.alloc(this, sizeof(unsigned) * 2);
+  a.barrier = cg_bar.as<unsigned>();
+  if (inject_cg_wait) {  // grada_inject_fault(GRADA_FAULT_CG_WAIT): every barrier wait expires
+    inject_cg_wait = false;
+    a.wait_limit_ns = 0;
+  }
+  h_ctl[CTL_DONE] = 0;
+  h_ctl[CTL_ITER] = 0;
+  h_ctl[CTL_MAXIT] = maxit;
+  h_ctl[CTL_STATUS] = CG_STATUS_RUNNING;
+  upload(a.ctl, h_ctl, sizeof(int) * CTL_NINTS);
+  h_scal[CG_TOL] = tol;
+  upload(a.scal + CG_TOL, h_scal + CG_TOL, sizeof(double));
+  if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
+  launch_cg_fused(a, g.kind, fused_grid[(int)g.kind], stream);
+  unsigned bar_words[2] = {0, 0};
+  download(bar_words, a.barrier, sizeof(bar_words));
+  download(h_ctl, a.ctl, sizeof(int) * CTL_NINTS);
+  download(h_scal, a.scal, sizeof(double) * CG_NSCALARS);
+  sync();
+  if (bar_words[1])
+    throw Error(GRADA_ERR_CUDA, "persistent CG: a grid barrier wait expired; the solve was abandoned");
+  CgResult res;
   res.iterations = h_ctl[CTL_ITER];
   res.err = h_scal[CG_ERR];
   if (h_ctl[CTL_STATUS] == CG_STATUS_BREAKDOWN)

@@ -94,6 +94,10 @@ struct GemvOpts {
   const double *scale = nullptr;
 };
 
+// Partition of G x: column ranges ("splits") per row tile of 256 * vec rows,
+// vec = entries per 16-byte load of the storage (vec_of).
+int gx_splits(const DevG &G, int sm_count, int vec);
+int vec_of(GKind k);
 // Scratch (in doubles) the products need for a given G, and the launches.
 int64_t gemv_scratch_doubles(const DevG &G, int sm_count);
 void launch_G_vec_mul(const DevG &G, const double *x, double *y, double *scratch, int sm_count,
@@ -111,6 +115,9 @@ void launch_round_to_fp32(const double *in, float *out, size_t n, cudaStream_t s
 // Columns [c0, c0+nc) of G widened to FP64 (scale applied for bf16) into
 // out (ld x nc, column-major).
 void launch_widen_columns(const DevG &G, int64_t c0, int64_t nc, double *out, cudaStream_t s);
+// out[r * nm + j] = G(rows[r], j) in FP64 for n_rows (<= 65535) device row indices.
+void launch_gather_rows(const DevG &G, const int64_t *rows, int64_t n_rows, double *out,
+                        cudaStream_t s);
 
 // ---- block products (block_gemm.cu, tc_gemm.cu) -------------------------
 // Y = G X and X = G^T Y for blocks of kBW = 16 right-hand sides, row-

@@ -187,6 +187,14 @@ class Fwd:
         self.ctx.check(self.ctx.lib.grada_get_G(self.ctx.handle, _ptr(out), self.ld))
         return out[: self.Nd, :]
 
+    def get_G_rows(self, rows) -> np.ndarray:
+        """Rows of the stored G, (len(rows), Nm) float64 (grada_get_G_rows)."""
+        idx = np.ascontiguousarray(rows, dtype=np.int64)
+        out = np.empty((idx.size, self.Nm), dtype=np.float64)
+        self.ctx.check(self.ctx.lib.grada_get_G_rows(
+            self.ctx.handle, idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), idx.size, _ptr(out)))
+        return out
+
     def G_column_norms(self) -> np.ndarray:
         """||G(:, j)||_2 for every cell j (grada_G_column_norms), the quantity
         InversionBase::set_depth_weighting(beta, 1) takes from G's columns."""

@@ -109,6 +109,13 @@ int grada_G_storage(const grada_ctx *ctx);
  * dimension ld_host >= Nd, entries widened to double.
  */
 int grada_get_G(grada_ctx *ctx, double *host, int64_t ld_host);
+/*
+ * Rows of the stored G (Fwd::get_G's matrix, Fwd.h:49, read row by row, as
+ * the reference's own callers index G(i, :)): host[r * Nm + j] = G(rows[r], j)
+ * for n_rows row indices in [0, Nd), widened to double.  For checking or
+ * inspecting a G too large to copy whole.
+ */
+int grada_get_G_rows(grada_ctx *ctx, const int64_t *rows, int64_t n_rows, double *host);
 
 /* Replaces Fwd::G_vec_mul, dense branch (Fwd.cpp:114-146): y[Nd] = G x[Nm]. */
 int grada_G_vec_mul(grada_ctx *ctx, const double *x, double *y);
@@ -430,12 +437,16 @@ int grada_refinement_indicator(grada_ctx *ctx, const double *m, const int64_t *r
  * GPU).  GRADA_FAULT_ALLOC: the context's next device allocation fails with
  * GRADA_ERR_OUT_OF_MEMORY.  GRADA_FAULT_TC_TIMEOUT: raises the flag a
  * tensor-core block product sets when one of its bounded waits expires, so
- * the next block product returns GRADA_ERR_CUDA.  GRADA_FAULT_NONE clears a
- * pending allocation fault.  The context stays usable after either.
+ * the next block product returns GRADA_ERR_CUDA.  GRADA_FAULT_CG_WAIT: the
+ * next persistent CG solve (stored dense G) runs with a zero limit on its grid
+ * barriers' waits, so a real device-side wait expires: every CTA returns, the
+ * solve returns GRADA_ERR_CUDA.  GRADA_FAULT_NONE clears pending faults.  The
+ * context stays usable after each.
  */
 #define GRADA_FAULT_NONE 0
 #define GRADA_FAULT_ALLOC 1
 #define GRADA_FAULT_TC_TIMEOUT 2
+#define GRADA_FAULT_CG_WAIT 3
 int grada_inject_fault(grada_ctx *ctx, int fault);
 
 #ifdef __cplusplus
