@@ -18,20 +18,11 @@ using cgb::block_sum;
 using cgb::VT;
 
 // y = c * wl .* (A (x - xs))    (wl, xs optional)
-__global__ void csr_apply_kernel(DevCSR A, const double *__restrict__ x,
-                                 const double *__restrict__ xs, double c,
-                                 const double *__restrict__ wl, double *__restrict__ y) {
+__global__ void csr_apply_kernel(DevCSR A, const double *x, const double *xs, double c,
+                                 const double *wl, double *y) {
   const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
   if (i >= A.n) return;
-  double acc = 0.0;
-  for (int k = A.rowptr[i]; k < A.rowptr[i + 1]; k++) {
-    const int j = A.col[k];
-    const double xv = xs ? (x[j] - xs[j]) : x[j];
-    acc = fma(A.val[k], xv, acc);
-  }
-  double v = c * acc;
-  if (wl) v *= wl[i];
-  y[i] = v;
+  y[i] = cgb::csr_apply_value(A, x, xs, c, wl, i);
 }
 
 // Forward regulariser rows for up to 7 terms in one launch (blockIdx.y = term).
@@ -66,12 +57,12 @@ __global__ void sum_partials_kernel(const double *partial, int nblocks, double *
 }
 
 // b0 = wd .* (dobs - g);  s0 = -b0
-__global__ void data_residual_kernel(const double *__restrict__ dobs, const double *__restrict__ g,
-                                     const double *__restrict__ wd, int64_t n,
-                                     double *__restrict__ b0, double *__restrict__ s0) {
+__global__ void data_residual_kernel(const double *__restrict__ dobs, const double *g,
+                                     const double *__restrict__ wd, int64_t n, double *b0,
+                                     double *s0) {
   const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
   if (i >= n) return;
-  const double v = wd[i] * (dobs[i] - g[i]);
+  const double v = cgb::data_residual_value(dobs, g, wd, i);
   b0[i] = v;
   if (s0) s0[i] = -v;
 }
@@ -146,64 +137,40 @@ __global__ void beta_kernel(double *scal, int *ctl) {
 // Bound transform, GaussNewtonInversion.cpp:877-911.  Cells that hit the
 // infinity / zero-denominator guards are flagged; their values depend on a
 // neighbour updated earlier in the same sweep and are fixed sequentially.
-__global__ void bound_update_kernel(const double *__restrict__ m, const double *__restrict__ dx,
+__global__ void bound_update_kernel(const double *m, const double *dx,
                                     const double *__restrict__ mmin, const double *__restrict__ mmax,
-                                    int64_t n, double *__restrict__ mt, int *__restrict__ guard,
-                                    int *__restrict__ any_guard) {
+                                    int64_t n, double *mt, int *guard, int *any_guard) {
   const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
   if (i >= n) return;
-  const double temp = exp(dx[i]);
-  const double temp2 = mmin[i] * (mmax[i] - m[i]) + mmax[i] * (m[i] - mmin[i]) * temp;
-  const double temp3 = (mmax[i] - m[i]) + (m[i] - mmin[i]) * temp;
-  int g = 0;
-  if (isinf(temp) || isinf(temp2)) g = 1;
-  else if (fabs(temp3) < 1e-10) g = 2;
+  const int g = cgb::bound_update_cell(m, dx, mmin, mmax, mt, i);
   guard[i] = g;
-  if (g) {
-    atomicOr(any_guard, 1);
-  } else {
-    mt[i] = temp2 / temp3;
-  }
+  if (g) atomicOr(any_guard, 1);
 }
 
 // Sequential pass over guarded cells in index order (one thread).  mt_old is
 // m_trial before this sweep (the id == 0 branch reads the not-yet-updated
 // neighbour 1).
-__global__ void bound_fixup_kernel(const int *__restrict__ guard, const double *__restrict__ mmin,
-                                   const double *__restrict__ mmax,
-                                   const double *__restrict__ mt_old, int64_t n,
-                                   double *__restrict__ mt) {
+__global__ void bound_fixup_kernel(const int *guard, const double *__restrict__ mmin,
+                                   const double *__restrict__ mmax, const double *mt_old, int64_t n,
+                                   double *mt) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  for (int64_t id = 0; id < n; id++) {
-    const int g = guard[id];
-    if (!g) continue;
-    double v;
-    if (g == 1) v = (mmax[id] - 1e-6 + mt_old[id]) / 2.0;
-    else v = (mmin[id] + 1e-6 + mt_old[id]) / 2.0;
-    if (id == 0) {
-      v = 0.5 * (v + (n > 1 ? mt_old[1] : v));
-    } else {
-      v = 0.5 * (v + mt[id - 1]);
-    }
-    mt[id] = v;
-  }
+  cgb::bound_fixup_seq(guard, mmin, mmax, mt_old, n, mt);
 }
 
 // P_ii = (mmax - m)(m - mmin)/(mmax - mmin)   (GaussNewtonInversion.cpp:856-861)
-__global__ void p_diag_kernel(const double *__restrict__ m, const double *__restrict__ mmin,
-                              const double *__restrict__ mmax, int64_t n, double *__restrict__ P) {
+__global__ void p_diag_kernel(const double *m, const double *__restrict__ mmin,
+                              const double *__restrict__ mmax, int64_t n, double *P) {
   const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
   if (i >= n) return;
-  const double nn = 1.0;
-  P[i] = nn * (mmax[i] - m[i]) * (m[i] - mmin[i]) / (mmax[i] - mmin[i]);
+  P[i] = cgb::p_diag_value(m, mmin, mmax, i);
 }
 
 // WL_ii = (v_i^2 + eps2)^(-(2-p)/4)   (GaussNewtonInversion.cpp:962-1022)
-__global__ void irls_weight_kernel(const double *__restrict__ v, int64_t n, double eps2, double expo,
-                                   double *__restrict__ wl) {
+__global__ void irls_weight_kernel(const double *v, int64_t n, double eps2, double expo,
+                                   double *wl) {
   const int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x;
   if (i >= n) return;
-  wl[i] = pow(v[i] * v[i] + eps2, expo);
+  wl[i] = cgb::irls_value(__ldcg(v + i), eps2, expo);
 }
 
 __global__ void sub_kernel(const double *__restrict__ a, const double *__restrict__ b, int64_t n,
@@ -219,15 +186,9 @@ __global__ void add_kernel(const double *__restrict__ a, const double *__restric
 }
 
 // misfit partials: sum (wd (g - dobs))^2
-__global__ void misfit_partial_kernel(const double *__restrict__ g, const double *__restrict__ dobs,
-                                      const double *__restrict__ wd, int64_t n,
-                                      double *__restrict__ partial) {
-  double v = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
-    const double e = wd[i] * (g[i] - dobs[i]);
-    v = fma(e, e, v);
-  }
-  v = block_sum(v);
+__global__ void misfit_partial_kernel(const double *g, const double *__restrict__ dobs,
+                                      const double *__restrict__ wd, int64_t n, double *partial) {
+  const double v = cgb::misfit_partial_body(g, dobs, wd, n, blockIdx.x, gridDim.x);
   if (threadIdx.x == 0) partial[blockIdx.x] = v;
 }
 

@@ -112,5 +112,98 @@ __device__ __forceinline__ void axpy_body(const double *t, const double *p, doub
   if (i < n) dx[i] = fma(alpha, __ldcg(p + i), __ldcg(dx + i));
 }
 
+
+// y = c * wl .* (A (x - xs))  (wl, xs optional), block b of rows
+__device__ __forceinline__ double csr_row(const DevCSR &A, const double *x, const double *xs,
+                                          int64_t i) {
+  double acc = 0.0;
+  for (int k = A.rowptr[i]; k < A.rowptr[i + 1]; k++) {
+    const int j = A.col[k];
+    const double xv = xs ? (__ldcg(x + j) - __ldcg(xs + j)) : __ldcg(x + j);
+    acc = fma(A.val[k], xv, acc);
+  }
+  return acc;
+}
+
+__device__ __forceinline__ double csr_apply_value(const DevCSR &A, const double *x,
+                                                  const double *xs, double c,
+                                                  const double *wl, int64_t i) {
+  double v = c * csr_row(A, x, xs, i);
+  if (wl) v *= __ldcg(wl + i);
+  return v;
+}
+
+// b0 = wd .* (dobs - g) ; s0 = -b0 (s0 optional)
+__device__ __forceinline__ double data_residual_value(const double *__restrict__ dobs,
+                                                      const double *g,
+                                                      const double *__restrict__ wd, int64_t i) {
+  return wd[i] * (dobs[i] - __ldcg(g + i));
+}
+
+// misfit partial of block b over nb blocks: sum (wd (g - dobs))^2; valid in thread 0
+__device__ __forceinline__ double misfit_partial_body(const double *g,
+                                                      const double *__restrict__ dobs,
+                                                      const double *__restrict__ wd, int64_t n,
+                                                      int64_t b, int64_t nb) {
+  double v = 0.0;
+  for (int64_t i = b * VT + threadIdx.x; i < n; i += nb * VT) {
+    const double e = wd[i] * (__ldcg(g + i) - dobs[i]);
+    v = fma(e, e, v);
+  }
+  return block_sum(v);
+}
+
+// Bound transform of one cell (GaussNewtonInversion.cpp:877-911): writes mt[i]
+// unless a guard applies; returns the guard (0 none, 1 infinity, 2 zero
+// denominator).
+__device__ __forceinline__ int bound_update_cell(const double *m, const double *dx,
+                                                 const double *__restrict__ mmin,
+                                                 const double *__restrict__ mmax, double *mt,
+                                                 int64_t i) {
+  const double mi = __ldcg(m + i);
+  const double temp = exp(__ldcg(dx + i));
+  const double temp2 = mmin[i] * (mmax[i] - mi) + mmax[i] * (mi - mmin[i]) * temp;
+  const double temp3 = (mmax[i] - mi) + (mi - mmin[i]) * temp;
+  int g = 0;
+  if (isinf(temp) || isinf(temp2)) g = 1;
+  else if (fabs(temp3) < 1e-10) g = 2;
+  if (!g) mt[i] = temp2 / temp3;
+  return g;
+}
+
+// The guarded cells in index order, one thread: their values depend on a
+// neighbour updated earlier in the same sweep.  mt_old is m_trial before the
+// sweep (the id == 0 branch reads the not-yet-updated neighbour 1).
+__device__ __forceinline__ void bound_fixup_seq(const int *guard, const double *__restrict__ mmin,
+                                                const double *__restrict__ mmax,
+                                                const double *mt_old, int64_t n, double *mt) {
+  for (int64_t id = 0; id < n; id++) {
+    const int g = __ldcg(guard + id);
+    if (!g) continue;
+    double v;
+    if (g == 1) v = (mmax[id] - 1e-6 + __ldcg(mt_old + id)) / 2.0;
+    else v = (mmin[id] + 1e-6 + __ldcg(mt_old + id)) / 2.0;
+    if (id == 0) {
+      v = 0.5 * (v + (n > 1 ? __ldcg(mt_old + 1) : v));
+    } else {
+      v = 0.5 * (v + __ldcg(mt + id - 1));
+    }
+    mt[id] = v;
+  }
+}
+
+// P_ii = (mmax - m)(m - mmin)/(mmax - mmin)   (GaussNewtonInversion.cpp:856-861)
+__device__ __forceinline__ double p_diag_value(const double *m, const double *__restrict__ mmin,
+                                               const double *__restrict__ mmax, int64_t i) {
+  const double nn = 1.0;
+  const double mi = __ldcg(m + i);
+  return nn * (mmax[i] - mi) * (mi - mmin[i]) / (mmax[i] - mmin[i]);
+}
+
+// WL_ii = (v_i^2 + eps2)^(-(2-p)/4)   (GaussNewtonInversion.cpp:962-1022)
+__device__ __forceinline__ double irls_value(double v, double eps2, double expo) {
+  return pow(v * v + eps2, expo);
+}
+
 }  // namespace cgb
 }  // namespace grada
