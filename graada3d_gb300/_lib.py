@@ -64,6 +64,11 @@ SIGNATURES = {
     "grada_invert_batch": (c_int, [c_int, POINTER(c_void_p), c_void_p, POINTER(_dp), POINTER(_dp),
                                    POINTER(_dp), POINTER(_dp), POINTER(_dp), c_void_p, c_int,
                                    POINTER(c_int)]),
+    "grada_invert_batch_persistent": (c_int, [c_int, POINTER(c_void_p), c_void_p, POINTER(_dp),
+                                              POINTER(_dp), POINTER(_dp), POINTER(_dp),
+                                              POINTER(_dp), c_void_p, c_int, POINTER(c_int)]),
+    "grada_load_batch_tuning": (c_int, [c_char_p]),
+    "grada_batch_shape": (c_int, [c_void_p, POINTER(c_int), POINTER(c_int)]),
     "grada_G_mat_mul": (c_int, [c_void_p, c_int, _dp, _dp]),
     "grada_GT_mat_mul": (c_int, [c_void_p, c_int, _dp, _dp]),
     "grada_G_block_mul_dev": (c_int, [c_void_p, c_void_p, c_void_p]),

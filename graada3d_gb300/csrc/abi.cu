@@ -697,6 +697,44 @@ int grada_invert_batch(int n, grada_ctx *const *ctxs, const grada_invert_params 
   });
 }
 
+int grada_invert_batch_persistent(int n, grada_ctx *const *ctxs, const grada_invert_params *params,
+                                  const double *const *m_ini, const double *const *m_min,
+                                  const double *const *m_max, const double *const *m0s,
+                                  double *const *m_out, grada_invert_report *reports,
+                                  int team_ctas, int *statuses) {
+  if (n < 0 || (n > 0 && (!ctxs || !params || !m_ini || !m_min || !m_max || !m_out)))
+    return GRADA_ERR_INVALID_ARGUMENT;
+  if (n == 0) return GRADA_OK;
+  for (int k = 0; k < n; k++)
+    if (!ctxs[k] || !m_ini[k] || !m_min[k] || !m_max[k] || !m_out[k])
+      return GRADA_ERR_INVALID_ARGUMENT;
+  std::vector<grada::Context *> cs(ctxs, ctxs + n);
+  std::string err;
+  int st = GRADA_OK;
+  try {
+    if (cudaSetDevice(ctxs[0]->device) != cudaSuccess) return GRADA_ERR_CUDA;
+    st = grada::invert_batch_persistent(n, cs.data(), params, m_ini, m_min, m_max, m0s, m_out,
+                                        reports, team_ctas, statuses, err);
+  } catch (const std::exception &e) {
+    err = e.what();
+    st = GRADA_ERR_CUDA;
+  }
+  ctxs[0]->last_error = (st == GRADA_OK) ? std::string() : err;
+  return st;
+}
+
+int grada_load_batch_tuning(const char *path) {
+  if (!path) return GRADA_ERR_INVALID_ARGUMENT;
+  return grada::load_batch_tuning(path);
+}
+
+int grada_batch_shape(const grada_ctx *ctx, int *teams, int *team_ctas) {
+  if (!ctx) return GRADA_ERR_INVALID_ARGUMENT;
+  if (teams) *teams = ctx->last_batch_teams;
+  if (team_ctas) *team_ctas = ctx->last_batch_team_ctas;
+  return GRADA_OK;
+}
+
 int grada_get_iterations(const grada_ctx *ctx, double *rows, int64_t cap, int64_t *n) {
   if (!ctx) return GRADA_ERR_INVALID_ARGUMENT;
   const int64_t total = (int64_t)ctx->iterations.size();

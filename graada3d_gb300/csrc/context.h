@@ -67,6 +67,17 @@ struct CgResult {
   int iterations = 0;
 };
 
+// The operators of one solve's stacked system (Context::cg_terms).
+struct CgTerms {
+  int nterms = 4;
+  DevCSR seg_A[7];
+  const double *seg_wl[7] = {};
+  ForwardTerms FT;
+  AdjointTerms AT_b, AT_s0, AT_s;
+};
+
+struct BatchProblem;
+
 struct Context {
   int device = 0;
   int sm_count = 0;
@@ -164,6 +175,15 @@ struct Context {
   void set_data(const double *h_dobs, const double *h_wd);
   void ensure_cg_workspace(int nterms);
   void data_prediction(const double *m, const double *m_start, const double *d64, double *out);
+  CgTerms cg_terms(double sl, const double *const WL[7], double *b, double *s, double *t);
+  bool invert_setup(const grada_invert_params &prm, const double *h_m_ini, const double *h_mmin,
+                    const double *h_mmax, const double *h_m0);
+  // invert_batch.cu host side: the device description of this context's
+  // inversion (after invert_setup), and the records read back after the launch
+  DevBuf bt_part2, bt_trials, bt_iters, bt_report;
+  int last_batch_teams = 0, last_batch_team_ctas = 0;  // shape of the last persistent batch
+  void batch_problem(const grada_invert_params &prm, BatchProblem &bp);
+  void batch_results(const grada_invert_params &prm, double *h_m_out, grada_invert_report &rep);
   bool fused_cg_eligible() const;
   CgResult solve_cg_fused(double tol, int maxit, const double *P, double *dx,
                           const ForwardTerms &FT, const AdjointTerms &AT, int64_t nrow, int nb_m,
@@ -225,5 +245,14 @@ struct Context {
                     const double *m_ini, const double *mmin, const double *mmax, const double *m0,
                     double *m_out, grada_invert_report *reps);
 };
+
+// invert_batch.cu: the batched persistent inversion and its tuning table.
+int invert_batch_persistent(int n, Context *const *ctxs, const grada_invert_params *params,
+                            const double *const *m_ini, const double *const *m_min,
+                            const double *const *m_max, const double *const *m0s,
+                            double *const *m_out, grada_invert_report *reports, int team_ctas,
+                            int *statuses, std::string &err);
+int load_batch_tuning(const char *path);
+int tuned_team_ctas(double max_entries);
 
 }  // namespace grada

@@ -63,7 +63,8 @@ void Context::release_all() {
   for (DevBuf *b : {&wv_order, &wv_rowptr, &wv_col, &wv_val, &wv_part, &wv_segptr})
     b->release();
   DevBuf *bufs[] = {&dobs, &wd, &cg_b, &cg_s, &cg_t, &cg_p, &cg_pp, &cg_r, &cg_atb, &cg_gtw,
-                    &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &cg_ctl, &cg_bar, &iv_m, &iv_mt, &iv_mt_old,
+                    &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &cg_ctl, &cg_bar, &bt_part2, &bt_trials,
+                    &bt_iters, &bt_report, &iv_m, &iv_mt, &iv_mt_old,
                     &iv_mopt, &iv_dx, &iv_P, &iv_mmin, &iv_mmax, &iv_m0, &iv_wl, &iv_tmp, &iv_tmp2,
                     &iv_dpre, &iv_d64, &iv_mstart, &iv_guard, &iv_flag,
                     &bscratch, &tc_err, &bk_b, &bk_s, &bk_t, &bk_p, &bk_pp, &bk_r, &bk_atb,
@@ -249,6 +250,47 @@ double Context::misfit_of(const double *m, const double *m_start, const double *
   return std::sqrt(h_scal[CG_MISFIT2] / (double)nd);  // GaussNewtonInversion.cpp:784, :916
 }
 
+// The stacked system's operators for one solve (GaussNewtonInversion.cpp:
+// 1458-1586): row segments s, z, x, y (and tz, tx, ty) with their weights for
+// b, and the forward and adjoint terms of the iteration.  The forward Ws row
+// has no WL_s, the forward crg rows take WL_z / WL_x / WL_y, and the initial
+// adjoint of s0 weights the crg-y rows by WL_y -- the reference's choices.
+CgTerms Context::cg_terms(double sl, const double *const WL[7], double *b, double *s, double *t) {
+  const int nterms = crg_enabled ? 7 : 4;
+  const int64_t Nm = n_cells, Nd = nd;
+  const double *WL_s = WL[0], *WL_x = WL[1], *WL_y = WL[2], *WL_z = WL[3];
+  const double *WL_tx = WL[4], *WL_ty = WL[5], *WL_tz = WL[6];
+  const DevOperator *seg_op[7] = {&ops[GRADA_OP_WS], &ops[GRADA_OP_WZ], &ops[GRADA_OP_WX],
+                                  &ops[GRADA_OP_WY], &crg[2], &crg[0], &crg[1]};
+  auto seg = [&](double *base, int k) { return base + Nd + (int64_t)k * Nm; };
+  CgTerms T;
+  T.nterms = nterms;
+  const double *b_wl[7] = {WL_s, WL_z, WL_x, WL_y, WL_tz, WL_tx, WL_ty};
+  const double adj_c[7] = {sl, sl, sl, sl, 1.0, 1.0, 1.0};
+  const double fwd_c[7] = {sl, sl, sl, sl, 1.0, 1.0, 1.0};
+  const double *fwd_wl[7] = {nullptr, WL_z, WL_x, WL_y, WL_z, WL_x, WL_y};
+  for (int k = 0; k < nterms; k++) {
+    T.seg_A[k] = seg_op[k]->A();
+    T.seg_wl[k] = b_wl[k];
+    AdjointTerm a;
+    a.AT = seg_op[k]->AT();
+    a.c = adj_c[k];
+    a.wl = b_wl[k];
+    a.s = seg(b, k);
+    T.AT_b.t[k] = a;
+    a.s = seg(s, k);
+    T.AT_s.t[k] = a;
+    if (k == 6) a.wl = WL_y;  // the initial adjoint weights the crg-y rows by WL_y (:1508)
+    T.AT_s0.t[k] = a;
+    T.FT.t[k].A = seg_op[k]->A();
+    T.FT.t[k].c = fwd_c[k];
+    T.FT.t[k].wl = fwd_wl[k];
+    T.FT.t[k].out = seg(t, k);
+  }
+  T.AT_b.count = T.AT_s.count = T.AT_s0.count = T.FT.count = nterms;
+  return T;
+}
+
 CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const double *mk,
                                const double *mref, const double *P, const double *const WL[7],
                                double *dx, const double *d64, const double *m_start) {
@@ -261,13 +303,10 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
   ensure_cg_workspace(nterms);
   const int64_t Nm = n_cells, Nd = nd, nrow = Nd + (int64_t)nterms * Nm;
   const double sl = std::sqrt(lambda);
-  // WL in the reference argument order: s, x, y, z, tx, ty, tz
-  const double *WL_s = WL[0], *WL_x = WL[1], *WL_y = WL[2], *WL_z = WL[3];
-  const double *WL_tx = WL[4], *WL_ty = WL[5], *WL_tz = WL[6];
-  // segment operators in row order s, z, x, y, tz, tx, ty
-  const DevOperator *seg_op[7] = {&ops[GRADA_OP_WS], &ops[GRADA_OP_WZ], &ops[GRADA_OP_WX],
-                                  &ops[GRADA_OP_WY], &crg[2], &crg[0], &crg[1]};
   double *b = dptr(cg_b), *s = dptr(cg_s), *t = dptr(cg_t);
+  // WL in the reference argument order s, x, y, z, tx, ty, tz; segments in
+  // row order s, z, x, y, tz, tx, ty
+  const CgTerms T = cg_terms(sl, WL, b, s, t);
   double *p = dptr(cg_p), *pp = dptr(cg_pp), *r = dptr(cg_r), *atb = dptr(cg_atb);
   double *gtw = dptr(cg_gtw), *gx = dptr(cg_gx), *tmpd = dptr(cg_tmpd);
   double *scal = dptr(cg_scal), *part = dptr(cg_part);
@@ -277,37 +316,16 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
   // b and s = -b   (GaussNewtonInversion.cpp:1458-1472)
   data_prediction(mk, m_start, d64, gx);
   launch_data_residual(dptr(dobs), gx, dptr(wd), Nd, b, s, stream);
-  launch_csr_apply(seg_op[0]->A(), mk, mref, -sl, WL_s, seg(b, 0), stream);
-  launch_csr_apply(seg_op[1]->A(), mk, nullptr, -sl, WL_z, seg(b, 1), stream);
-  launch_csr_apply(seg_op[2]->A(), mk, nullptr, -sl, WL_x, seg(b, 2), stream);
-  launch_csr_apply(seg_op[3]->A(), mk, nullptr, -sl, WL_y, seg(b, 3), stream);
-  if (crg_enabled) {
-    launch_csr_apply(seg_op[4]->A(), mk, nullptr, -1.0, WL_tz, seg(b, 4), stream);
-    launch_csr_apply(seg_op[5]->A(), mk, nullptr, -1.0, WL_tx, seg(b, 5), stream);
-    launch_csr_apply(seg_op[6]->A(), mk, nullptr, -1.0, WL_ty, seg(b, 6), stream);
-  }
+  for (int k = 0; k < nterms; k++)
+    launch_csr_apply(T.seg_A[k], mk, k == 0 ? mref : nullptr, k < 4 ? -sl : -1.0, T.seg_wl[k],
+                     seg(b, k), stream);
   launch_negate(b + Nd, nrow - Nd, s + Nd, stream);
 
   // A^T b and the initial r = A^T s (:1485-1551).  G^T(Wd s0) = -G^T(Wd b0)
   // exactly, so one product serves both.
   launch_scale(b, dptr(wd), Nd, 1.0, tmpd, stream);
   GT_vec_mul_dev(tmpd, gtw);
-  const double adj_c[7] = {sl, sl, sl, sl, 1.0, 1.0, 1.0};
-  const double *adj_wl[7] = {WL_s, WL_z, WL_x, WL_y, WL_tz, WL_tx, WL_ty};
-  AdjointTerms AT_b, AT_s0, AT_s;
-  for (int k = 0; k < nterms; k++) {
-    AdjointTerm a;
-    a.AT = seg_op[k]->AT();
-    a.c = adj_c[k];
-    a.wl = adj_wl[k];
-    a.s = seg(b, k);
-    AT_b.t[k] = a;
-    a.s = seg(s, k);
-    AT_s.t[k] = a;
-    if (k == 6) a.wl = WL_y;  // the initial adjoint weights the crg-y rows by WL_y (:1508)
-    AT_s0.t[k] = a;
-  }
-  AT_b.count = AT_s.count = AT_s0.count = nterms;
+  const AdjointTerms &AT_b = T.AT_b, &AT_s0 = T.AT_s0, &AT_s = T.AT_s;
   launch_adjoint(AT_b, Nm, P, gtw, 1.0, atb, stream);
   launch_adjoint(AT_s0, Nm, P, gtw, -1.0, r, stream);
   launch_dot(atb, nullptr, Nm, part, nb_m, scal + CG_ATB2, stream);
@@ -320,16 +338,7 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
 
   // forward rows of t = A p (:1569-1586): Ws row without WL_s, crg rows
   // weighted by WL_z / WL_x / WL_y
-  const double fwd_c[7] = {sl, sl, sl, sl, 1.0, 1.0, 1.0};
-  const double *fwd_wl[7] = {nullptr, WL_z, WL_x, WL_y, WL_z, WL_x, WL_y};
-  ForwardTerms FT;
-  for (int k = 0; k < nterms; k++) {
-    FT.t[k].A = seg_op[k]->A();
-    FT.t[k].c = fwd_c[k];
-    FT.t[k].wl = fwd_wl[k];
-    FT.t[k].out = seg(t, k);
-  }
-  FT.count = nterms;
+  const ForwardTerms &FT = T.FT;
 
   CgResult res;
   if (maxit <= 0) {  // the loop never runs: iterations = maxit (:1693-1696)
@@ -497,18 +506,20 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   return res;
 }
 
-void Context::invert(const grada_invert_params &prm, const double *h_m_ini, const double *h_mmin,
-                     const double *h_mmax, const double *h_m0, double *h_m_out,
-                     grada_invert_report &rep) {
-  NvtxRange nvtx("grada invert");
+// The set-up of invert_with_own_CG (GaussNewtonInversion.cpp:757-786): input
+// checks, the starting model, the device vectors, IRLS weights of one, and
+// the mixed-precision mode (refine: FP64 residual refinement; predict_fp64:
+// every prediction an FP64 product of the kept G).  Shared by invert and the
+// batched persistent inversion.
+bool Context::invert_setup(const grada_invert_params &prm, const double *h_m_ini,
+                           const double *h_mmin, const double *h_mmax, const double *h_m0) {
   require_G();
   if (!data_set) throw Error(GRADA_ERR_STATE, "observed data not set (grada_set_data)");
-  if (!h_m_ini || !h_mmin || !h_mmax || !h_m_out)
+  if (!h_m_ini || !h_mmin || !h_mmax)
     throw Error(GRADA_ERR_INVALID_ARGUMENT, "null model vector");
   if (prm.n_lambda < 1 || prm.gn_iterations < 1)
     throw Error(GRADA_ERR_INVALID_ARGUMENT, "n_lambda and gn_iterations must be >= 1");
   const int64_t Nm = n_cells;
-  std::memset(&rep, 0, sizeof(rep));
   trials.clear();
   iterations.clear();
 
@@ -539,10 +550,6 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
   const bool refine =
       prm.fp64_refinement && g_storage != GRADA_G_FP64 && g_storage != GRADA_G_MATRIX_FREE;
   // with a kept FP64 G every prediction is an FP64 product instead
-  struct PredictGuard {
-    Context *c;
-    ~PredictGuard() { c->predict_fp64 = false; }
-  } predict_guard{this};
   predict_fp64 = refine && fp64_resident();
   fp64_products = 0;
   if (predict_fp64) scratch_doubles(std::max(product_scratch_doubles(),
@@ -558,6 +565,22 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
     upload(iv_wl.ptr, ones.data(), vb * 7);
     sync();
   }
+  return refine;
+}
+
+void Context::invert(const grada_invert_params &prm, const double *h_m_ini, const double *h_mmin,
+                     const double *h_mmax, const double *h_m0, double *h_m_out,
+                     grada_invert_report &rep) {
+  NvtxRange nvtx("grada invert");
+  if (!h_m_out) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null model vector");
+  std::memset(&rep, 0, sizeof(rep));
+  struct PredictGuard {
+    Context *c;
+    ~PredictGuard() { c->predict_fp64 = false; }
+  } predict_guard{this};
+  const bool refine = invert_setup(prm, h_m_ini, h_mmin, h_mmax, h_m0);
+  const int64_t Nm = n_cells;
+  const size_t vb = sizeof(double) * Nm;
   double *dm = dptr(iv_m), *dmt = dptr(iv_mt), *dmt_old = dptr(iv_mt_old), *dmopt = dptr(iv_mopt);
   double *ddx = dptr(iv_dx), *dP = dptr(iv_P), *dmin = dptr(iv_mmin), *dmax = dptr(iv_mmax);
   double *dm0 = dptr(iv_m0), *dtmp = dptr(iv_tmp);

@@ -320,3 +320,52 @@ def invert_batch(invs, prms, m_inis, m_mins, m_maxs, m0s=None, fp64_refinement=F
         invs[bad[0]].ctx.check(st[bad[0]])
     return [(outs[k], {f: getattr(reports[k], f) for f, _ in InvertReport._fields_})
             for k in range(n)]
+
+
+def invert_batch_persistent(invs, prms, m_inis, m_mins, m_maxs, m0s=None, fp64_refinement=False,
+                            team_ctas: int = 0):
+    """grada_invert_batch_persistent: the inversions of several GaussNewtonInversion
+    objects (one device, the same G storage) in one persistent cooperative launch,
+    a team of CTAs per problem.  Returns ([(m, report)] in input order, (teams,
+    CTAs per team))."""
+    lib = invs[0].ctx.lib
+    n = len(invs)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ctxs = (ctypes.c_void_p * n)(*[i.ctx.handle.value for i in invs])
+    params = (InvertParams * n)(*[_params(p, fp64_refinement) for p in prms])
+    keep = []
+
+    def arr(vs):
+        out = (dp * n)()
+        for k, v in enumerate(vs):
+            if v is None:
+                out[k] = dp()
+            else:
+                a = np.ascontiguousarray(v, dtype=np.float64)
+                keep.append(a)
+                out[k] = _ptr(a)
+        return out
+
+    outs = [np.empty(i.Nm) for i in invs]
+    reports = (InvertReport * n)()
+    st = (ctypes.c_int * n)()
+    rc = lib.grada_invert_batch_persistent(n, ctxs, params, arr(m_inis), arr(m_mins), arr(m_maxs),
+                                           arr(m0s if m0s is not None else [None] * n), arr(outs),
+                                           reports, int(team_ctas), st)
+    invs[0].ctx.check(rc)
+    for k in range(n):
+        invs[k].m = outs[k]
+    teams, per = ctypes.c_int(), ctypes.c_int()
+    invs[0].ctx.check(lib.grada_batch_shape(invs[0].ctx.handle, ctypes.byref(teams), ctypes.byref(per)))
+    return ([(outs[k], {f: getattr(reports[k], f) for f, _ in InvertReport._fields_})
+             for k in range(n)], (teams.value, per.value))
+
+
+def load_batch_tuning(path) -> None:
+    """Loads a team-size table for invert_batch_persistent (grada_load_batch_tuning)."""
+    from . import _lib
+
+    lib = _lib.load()
+    rc = lib.grada_load_batch_tuning(str(path).encode())
+    if rc != 0:
+        raise _lib.GradaError(rc, f"cannot load the batch tuning table {path}")

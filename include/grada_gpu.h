@@ -374,6 +374,38 @@ int grada_invert_batch(int n, grada_ctx *const *ctxs, const grada_invert_params 
                        int *statuses);
 
 /*
+ * The same batch as grada_invert_batch in ONE persistent cooperative launch
+ * (captured in a CUDA graph) instead of host threads: the GPU's resident CTAs
+ * are split into teams of team_ctas CTAs (0 = the loaded tuning table's choice
+ * for the batch's largest G, else 8); each team takes the next problem from a
+ * device queue, largest first, and runs its whole invert_with_own_CG
+ * (GaussNewtonInversion.cpp:657-1103: lambda search, CG solves, bound
+ * transform, misfits, IRLS, stopping tests) on the device, then the next.
+ * Each problem's model, report and trial/iteration records are bitwise those
+ * of grada_invert on the same context.  Needs every context on one device,
+ * the same G storage for all, and either an FP64 G or a reduced-precision G
+ * with the FP64 G kept (grada_keep_fp64_G) and params[k].fp64_refinement set;
+ * otherwise GRADA_ERR_STATE (grada_invert_batch covers the rest).  Every
+ * barrier wait of a team is bounded; an expiry returns GRADA_ERR_CUDA.
+ * Messages go to grada_last_error(ctxs[0]).
+ */
+int grada_invert_batch_persistent(int n, grada_ctx *const *ctxs,
+                                  const grada_invert_params *params,
+                                  const double *const *m_ini, const double *const *m_min,
+                                  const double *const *m_max, const double *const *m0s,
+                                  double *const *m_out, grada_invert_report *reports,
+                                  int team_ctas, int *statuses);
+/*
+ * The team-size table of grada_invert_batch_persistent, a text file of rows
+ * "<largest G of the batch, entries> <CTAs per team>" ('#' starts a comment),
+ * written by graada3d_gb300/autotune.py from measured batches.  Process-wide.
+ */
+int grada_load_batch_tuning(const char *path);
+/* Shape of the last persistent batch run on ctx (the first context of the
+ * batch): the number of teams and the CTAs per team. */
+int grada_batch_shape(const grada_ctx *ctx, int *teams, int *team_ctas);
+
+/*
  * Blocks of right-hand sides on one G (no single reference counterpart: each
  * column equals one call of the single entry point named).  Column-major host
  * arrays; n_rhs >= 1 columns are processed sixteen at a time, and each group
