@@ -600,7 +600,8 @@ def run_batched_64(n_problems: int = 64):
 
     from graada3d_gb300 import Context, mesh
     from graada3d_gb300 import regularization as reg
-    from graada3d_gb300.inversion import GaussNewtonInversion, compute_G_batch, invert_batch
+    from graada3d_gb300.inversion import (GaussNewtonInversion, compute_G_batch, invert_batch,
+                                          invert_batch_persistent)
 
     world, rank, local = dist_init()
     if torch.cuda.is_available():
@@ -651,6 +652,15 @@ def run_batched_64(n_problems: int = 64):
     t_bat = time.perf_counter() - t0
     same = all(np.array_equal(a[0], b[0]) for a, b in zip(seq, bat))
     reached = sum(1 for _, r in bat if r["final_misfit"] < 1.0)
+    # the same batch in one persistent launch (a team of CTAs per problem from a
+    # device queue; team size from the tuning table)
+    t0 = time.perf_counter()
+    compute_G_batch(invs, "fp64")
+    per, shape = invert_batch_persistent(invs, [prm] * len(invs), [a[0] for a in args],
+                                         [a[1] for a in args], [a[2] for a in args])
+    torch.cuda.synchronize()
+    t_per = time.perf_counter() - t0
+    per_same = all(np.array_equal(a[0], b[0]) for a, b in zip(seq, per))
     # the same batch with FP32 G (HBM-bound products) and the FP64 G kept for
     # every prediction
     t0 = time.perf_counter()
@@ -662,18 +672,36 @@ def run_batched_64(n_problems: int = 64):
     mix_diff = [float(np.linalg.norm(a[0] - b[0]) / max(np.linalg.norm(b[0]), 1e-30))
                 for a, b in zip(mix, bat)]
     mix_reached = sum(1 for _, r in mix if r["final_misfit"] < 1.0)
+    t0 = time.perf_counter()
+    compute_G_batch(invs, "fp32", keep_fp64=True)
+    mix_per, mix_shape = invert_batch_persistent(invs, [prm] * len(invs), [a[0] for a in args],
+                                                 [a[1] for a in args], [a[2] for a in args],
+                                                 fp64_refinement=True)
+    torch.cuda.synchronize()
+    t_mix_per = time.perf_counter() - t0
+    mix_per_same = all(np.array_equal(a[0], b[0]) for a, b in zip(mix, mix_per))
     for inv in invs:
         inv.ctx.close()
     t_seq, t_bat = max_over_ranks(world, t_seq), max_over_ranks(world, t_bat)
     t_mix = max_over_ranks(world, t_mix)
+    t_per, t_mix_per = max_over_ranks(world, t_per), max_over_ranks(world, t_mix_per)
     return {"case": "batched-64", "problems": n_problems, "ranks": world,
             "problems_per_rank": len(mine),
             "cells_range": [min(s[0] for s in sizes), max(s[0] for s in sizes)],
             "points_range": [min(s[1] for s in sizes), max(s[1] for s in sizes)],
             "sequential_s": t_seq, "batched_s": t_bat, "speedup": t_seq / t_bat,
             "identical_models": same, "chi2_reached_rank0": reached,
+            "persistent": {"launches": 1, "teams": shape[0], "ctas_per_team": shape[1],
+                           "s": t_per, "speedup_vs_sequential": t_seq / t_per,
+                           "speedup_vs_concurrent": t_bat / t_per,
+                           "identical_models_to_single_runs": per_same},
             "cg_iterations_rank0": int(sum(r["cg_iterations"] for _, r in bat)),
             "fp32_kept_fp64": {"batched_s": t_mix, "speedup_vs_fp64_batch": t_bat / t_mix,
+                               "persistent": {"launches": 1, "teams": mix_shape[0],
+                                              "ctas_per_team": mix_shape[1], "s": t_mix_per,
+                                              "speedup_vs_concurrent": t_mix / t_mix_per,
+                                              "speedup_vs_fp64_persistent": t_per / t_mix_per,
+                                              "identical_models_to_single_runs": mix_per_same},
                                "model_rel_diff_vs_fp64": {"median": float(np.median(mix_diff)),
                                                           "max": float(np.max(mix_diff))},
                                "chi2_reached_rank0": mix_reached}}

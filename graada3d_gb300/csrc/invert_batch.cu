@@ -384,7 +384,10 @@ void launch_invert_batch(const BatchProblem *problems, int n, int *queue, unsign
 
 // ---- host side ---------------------------------------------------------------
 
+#include <dlfcn.h>
+
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
@@ -546,16 +549,17 @@ namespace {
 
 // Rows (largest G of the batch in entries, CTAs per team), ascending; the
 // batch takes the first row whose bound holds its largest problem.  Loaded
-// from the file grada_load_batch_tuning names; without one, a team of 8.
+// from the file grada_load_batch_tuning names or, on first use, from
+// tuning/batch_teams.tsv beside the library (graada3d_gb300/autotune.py
+// writes it); without a table, a team of 8.
 std::mutex g_tune_mutex;
 std::vector<std::pair<double, int>> g_tune_rows;
+bool g_tune_tried = false;
 
-}  // namespace
-
-int load_batch_tuning(const char *path) {
-  std::ifstream f(path);
-  if (!f) return GRADA_ERR_INVALID_ARGUMENT;
+std::vector<std::pair<double, int>> read_table(const char *path) {
   std::vector<std::pair<double, int>> rows;
+  std::ifstream f(path);
+  if (!f) return rows;
   std::string line;
   while (std::getline(f, line)) {
     if (line.empty() || line[0] == '#') continue;
@@ -564,19 +568,45 @@ int load_batch_tuning(const char *path) {
     if (std::sscanf(line.c_str(), "%lf %d", &bound, &team) == 2 && team >= 1 && team <= 1024)
       rows.push_back({bound, team});
   }
-  if (rows.empty()) return GRADA_ERR_INVALID_ARGUMENT;
   std::sort(rows.begin(), rows.end());
+  return rows;
+}
+
+// The default table beside this library (once per process).
+void load_default_table_locked() {
+  if (g_tune_tried) return;
+  g_tune_tried = true;
+  Dl_info info;
+  if (!dladdr(reinterpret_cast<void *>(&read_table), &info) || !info.dli_fname) return;
+  std::string dir(info.dli_fname);
+  const size_t slash = dir.find_last_of('/');
+  dir = (slash == std::string::npos) ? std::string(".") : dir.substr(0, slash);
+  auto rows = read_table((dir + "/tuning/batch_teams.tsv").c_str());
+  if (!rows.empty()) g_tune_rows = rows;
+}
+
+}  // namespace
+
+int load_batch_tuning(const char *path) {
+  std::ifstream f(path);
+  if (!f) return GRADA_ERR_INVALID_ARGUMENT;
+  f.close();
+  auto rows = read_table(path);
+  if (rows.empty()) return GRADA_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   g_tune_rows = rows;
+  g_tune_tried = true;
   return GRADA_OK;
 }
 
 int tuned_team_ctas(double max_entries) {
   std::lock_guard<std::mutex> lock(g_tune_mutex);
+  load_default_table_locked();
   for (const auto &r : g_tune_rows)
     if (max_entries <= r.first) return r.second;
   return g_tune_rows.empty() ? 8 : g_tune_rows.back().second;
 }
+
 
 // grada_invert_batch_persistent: see include/grada_gpu.h.
 int invert_batch_persistent(int n, Context *const *ctxs, const grada_invert_params *params,

@@ -10,6 +10,7 @@ namespace gb300 {
 namespace {
 std::mutex g_mutex;
 std::unordered_map<const void *, grada_ctx *> g_contexts;
+std::unordered_map<const grada_ctx *, std::vector<uint64_t>> g_digests;
 
 struct Cleanup {
   ~Cleanup() {
@@ -35,8 +36,14 @@ void release(const void *owner) {
   std::lock_guard<std::mutex> lock(g_mutex);
   auto it = g_contexts.find(owner);
   if (it == g_contexts.end()) return;
+  g_digests.erase(it->second);
   grada_ctx_destroy(it->second);
   g_contexts.erase(it);
+}
+
+std::vector<uint64_t> &upload_digests(grada_ctx *ctx) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  return g_digests[ctx];
 }
 
 void check(grada_ctx *ctx, int status, const char *what) {

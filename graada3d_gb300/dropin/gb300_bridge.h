@@ -22,6 +22,10 @@ void release(const void *owner);
 // Throws std::runtime_error with the library's message on a failing status.
 void check(grada_ctx *ctx, int status, const char *what);
 
+// Digests of the inputs last uploaded to a context (the solve_cg drop-in skips
+// unchanged uploads); dropped with the context by release().
+std::vector<uint64_t> &upload_digests(grada_ctx *ctx);
+
 // grada_build_operators' face table of a mesh (FaceTable_gb300.cpp).
 }  // namespace gb300
 class Mesh;

@@ -42,7 +42,10 @@ def _parse_table(path: Path):
     return np.array(rows)
 
 
-def run_case(c: dict, solve: dict | None, full: bool):
+def run_case(c: dict, solve: dict | None, full: bool, exe: Path = EXE, threads: int = 1):
+    """Runs the fixture driver `exe` (the reference's ref_inversion, or the same
+    driver linked with the drop-ins) on case c; raises CalledProcessError when
+    the driver fails."""
     nx, ny, nz = c["n"]
     nm = nx * ny * nz
     obs = c["obs"]
@@ -83,9 +86,9 @@ def run_case(c: dict, solve: dict | None, full: bool):
             wd.mkdir()
             (wd / "in.bin").write_bytes(bytes(b))
             # one OpenMP thread: the reference's reductions are then reproducible
-            env = dict(os.environ, OMP_NUM_THREADS="1")
-            subprocess.run([str(EXE), "in.bin", "out.bin"], cwd=wd, check=True,
-                           stdout=subprocess.DEVNULL, env=env)
+            env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+            subprocess.run([str(exe), "in.bin", "out.bin"], cwd=wd, check=True,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, env=env)
             buf = (wd / "out.bin").read_bytes()
             off = 0
             rows, cols = struct.unpack_from("<qq", buf, off)

@@ -2,6 +2,8 @@
 reference's unchanged class headers.  Needs the reference tree; skipped
 elsewhere.  No GPU."""
 import shutil
+
+import numpy as np
 import subprocess
 from pathlib import Path
 
@@ -29,3 +31,46 @@ def test_dropin_compiles_against_reference_headers(unit):
            str(REPO / "graada3d_gb300" / "dropin" / f"{unit}.cpp")]
     res = subprocess.run(cmd, capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
+
+
+@pytest.mark.skipif(not (REF / "src" / "Forward_modelling" / "Fwd.h").exists(),
+                    reason="reference sources not available")
+@pytest.mark.skipif(shutil.which("g++") is None or shutil.which("objcopy") is None,
+                    reason="no C++ toolchain")
+def test_dropin_links_into_the_reference_and_takes_over():
+    """The drop-ins linked for real (oracle/Makefile target dropin): the
+    reference's objects with the replaced members weakened, the drop-in units
+    and libgrada_gpu.so link with no duplicate or missing symbol, and the
+    reference's own invert() then calls the drop-in Fwd::compute_G: without a
+    GPU the library's context creation fails inside it (exit status 7 with the
+    library's message), where the reference's own compute_G would have run on
+    the CPU.  With a GPU the run completes and the model and lambda/misfit
+    record equal the reference's (GaussNewtonInversion.cpp:657-1103)."""
+    import subprocess as sp
+    import sys
+
+    sys.path.insert(0, str(REPO / "tests" / "golden"))
+    import inversion_cases as ic
+
+    res = sp.run(["make", "-C", str(REPO / "oracle"), "-j8", "dropin", f"REF={REF}"],
+                 capture_output=True, text=True)
+    assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-2000:]
+    exe = REPO / "oracle" / "_ref" / "dropin_inversion"
+    c, _ = ic.make_case("l2", 11)
+    try:
+        import torch
+
+        has_gpu = torch.cuda.is_available()
+    except ImportError:
+        has_gpu = False
+    if not has_gpu:
+        with pytest.raises(sp.CalledProcessError) as e:
+            ic.run_case(c, None, full=True, exe=exe)
+        assert e.value.returncode == 7
+        assert b"grada_ctx_create failed" in e.value.stderr
+        return
+    got = ic.run_case(c, None, full=True, exe=exe)
+    want = ic.run_case(c, None, full=True)
+    assert np.abs(got["inv_m"] - want["inv_m"]).max() <= 1e-6 * np.abs(want["inv_m"]).max()
+    assert got["inv_trials"].shape == want["inv_trials"].shape
+    assert np.allclose(got["inv_trials"], want["inv_trials"], rtol=1e-6, atol=0)
