@@ -36,7 +36,7 @@ namespace {
 // and control block the host setup left in a.scal / a.ctl and writes them back.
 template <class L>
 __global__ void __launch_bounds__(256) cg_fused_kernel(FusedCgArgs a) {
-  fused::TeamBarrier bar{a.barrier, gridDim.x, 0u, a.wait_limit_ns};
+  fused::TeamBarrier bar(a.barrier, gridDim.x, blockIdx.x, a.wait_limit_ns);
   fused::CgIn in;
   in.R2 = __ldcg(a.scal + CG_R2);
   in.ATB2 = __ldcg(a.scal + CG_ATB2);
@@ -82,8 +82,26 @@ int fused_cg_grid(GKind kind, int sm_count) {
   return std::max(1, per_sm) * sm_count;
 }
 
+void fused_gx_partition(const DevG &G, int resident, int &tiles, int &splits, int64_t &per) {
+  tiles = (int)ceil_div(G.ld, (int64_t)256 * vec_of(G.kind));
+  int64_t sp = (2 * (int64_t)resident) / tiles;  // two rounds of the resident CTAs
+  const int64_t max_splits = ceil_div(G.nm, 64);
+  if (sp > max_splits) sp = max_splits;
+  if (sp < 1) sp = 1;
+  if (sp > 65535) sp = 65535;
+  splits = (int)sp;
+  per = ceil_div(G.nm, splits);
+}
+
+void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t &doubles, int64_t &counters) {
+  const fused::RedLayout rl(nd, nm, nterms);
+  doubles = rl.doubles();
+  counters = rl.counters();
+}
+
 void launch_cg_fused(const FusedCgArgs &a, GKind kind, int grid, cudaStream_t s) {
-  GRADA_CUDA_CHECK(cudaMemsetAsync(a.barrier, 0, 2 * sizeof(unsigned), s));
+  GRADA_CUDA_CHECK(
+      cudaMemsetAsync(a.barrier, 0, fused::kBarrierWords * sizeof(unsigned), s));
   FusedCgArgs copy = a;
   void *args[] = {&copy};
   GRADA_CUDA_CHECK(cudaLaunchCooperativeKernel(fused_kernel_for(kind), dim3((unsigned)grid),

@@ -31,45 +31,6 @@ __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *p) {
   return v;
 }
 
-// Barrier over the n CTAs of a team.  word[0] counts arrivals (it only grows:
-// barrier k of a launch completes at n * k), word[1] is the error word.  Both
-// start at zero (the host clears them before the launch).
-struct TeamBarrier {
-  unsigned *word;
-  unsigned n;
-  unsigned target;
-  unsigned long long limit_ns;
-
-  __device__ bool sync() {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      target += n;
-      int ok = 1;
-      __threadfence();
-      atomicAdd(word, 1u);
-      const unsigned long long t0 = global_timer_ns();
-      while ((int)(ld_acquire_u32(word) - target) < 0) {
-        if (ld_relaxed_u32(word + 1)) {
-          ok = 0;
-          break;
-        }
-        if (global_timer_ns() - t0 > limit_ns) {
-          atomicExch(word + 1, 1u);
-          ok = 0;
-          break;
-        }
-        __nanosleep(32);
-      }
-      __threadfence();
-      if (ld_relaxed_u32(word + 1)) ok = 0;
-      s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-  }
-};
-
 // Broadcast thread 0's value to the block.
 __device__ __forceinline__ double bcast(double v) {
   __shared__ double s_v;
@@ -79,6 +40,119 @@ __device__ __forceinline__ double bcast(double v) {
   __syncthreads();
   return out;
 }
+
+// Block sum (fixed tree) broadcast to every thread.
+__device__ __forceinline__ double bcast_sum(double v) { return bcast(cgb::block_sum(v)); }
+
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Barrier over the n CTAs of a team, a two-level arrival tree: CTA c arrives
+// on counter c % G (G = min(16, n) counters, 32 bytes apart), the last arrival
+// of each counter arrives on the top counter, and the last top arrival
+// publishes the barrier's number on the release word, which every CTA polls.
+// Counters only grow (barrier k completes when counter g reaches size_g * k),
+// so nothing is reset.  The team's words (kBarrierWords, zeroed before the
+// launch): counters at 8 g, top at 160, release at 192, error at 224.  A wait
+// longer than limit_ns raises the error word; every CTA then leaves at its
+// next barrier.
+constexpr int kBarrierWords = 256;
+
+struct TeamBarrier {
+  unsigned *word;
+  unsigned n;
+  unsigned cta;
+  unsigned long long limit_ns;
+  unsigned epoch = 0;
+
+  __device__ TeamBarrier(unsigned *w, unsigned n_ctas, unsigned my_cta, unsigned long long limit)
+      : word(w), n(n_ctas), cta(my_cta), limit_ns(limit) {}
+
+  __device__ bool sync() {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned groups = n < 16u ? n : 16u;
+      const unsigned g = cta % groups;
+      const unsigned gsize = n / groups + (g < n % groups ? 1u : 0u);
+      epoch++;
+      int ok = 1;
+      __threadfence();
+      if (atomicAdd(word + 8 * g, 1u) + 1u == gsize * epoch) {
+        __threadfence();
+        if (atomicAdd(word + 160, 1u) + 1u == groups * epoch) {
+          __threadfence();
+          st_release_u32(word + 192, epoch);
+        }
+      }
+      const unsigned long long t0 = global_timer_ns();
+      while ((int)(ld_acquire_u32(word + 192) - epoch) < 0) {
+        if (ld_relaxed_u32(word + 224)) {
+          ok = 0;
+          break;
+        }
+        if (global_timer_ns() - t0 > limit_ns) {
+          atomicExch(word + 224, 1u);
+          ok = 0;
+          break;
+        }
+        __nanosleep(20);
+      }
+      __threadfence();
+      if (ld_relaxed_u32(word + 224)) ok = 0;
+      s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+  }
+};
+
+// Deterministic two-level sum of per-block partials: block b writes
+// partial[b]; the last block of each group of kGroup blocks to finish (an
+// atomic count) adds its group's partials in index order into group[b /
+// kGroup] and resets the count.  After a barrier every CTA adds the groups in
+// index order.  The result depends only on the partition into blocks, not on
+// which CTA ran which block or when.
+constexpr int kGroup = 32;
+
+__device__ __forceinline__ void publish_partial(double v, int64_t b, int64_t nb, double *partial,
+                                                double *group, unsigned *count) {
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    partial[b] = v;
+    __threadfence();
+    const int64_t gi = b / kGroup;
+    const int64_t g0 = gi * kGroup;
+    const unsigned gsize = (unsigned)((nb - g0) < kGroup ? (nb - g0) : kGroup);
+    s_last = (atomicAdd(count + gi, 1u) + 1u == gsize) ? 1 : 0;
+  }
+  __syncthreads();
+  if (s_last) {
+    const int64_t gi = b / kGroup;
+    const int64_t g0 = gi * kGroup;
+    const int64_t ge = (g0 + kGroup < nb) ? g0 + kGroup : nb;
+    if (threadIdx.x < 32) {
+      __threadfence();
+      double x = (g0 + threadIdx.x < ge) ? __ldcg(partial + g0 + threadIdx.x) : 0.0;
+      x = cgb::warp_sum(x);
+      if (threadIdx.x == 0) {
+        group[gi] = x;
+        count[gi] = 0u;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Sum of the ngroups group sums in index order (fixed tree); every thread
+// gets it.
+__device__ __forceinline__ double sum_groups(const double *group, int64_t ngroups) {
+  double v = 0.0;
+  for (int64_t i = threadIdx.x; i < ngroups; i += cgb::VT) v += __ldcg(group + i);
+  return bcast_sum(v);
+}
+
 
 // Scalars a solve's loop starts from (the setup's) and ends with.
 struct CgIn {
@@ -91,20 +165,48 @@ struct CgOut {
   bool ok = true;  // false: a barrier wait expired (the team abandons its work)
 };
 
+// Layout of a.red for a loop: partials and group sums of ||t||^2 over the
+// G2 blocks, then of ||r||^2 over the G^T blocks.
+struct RedLayout {
+  int64_t nb_t, ng_t, nb_r, ng_r;
+  __host__ __device__ RedLayout(int64_t nd, int64_t nm, int nterms) {
+    nb_t = ceil_div_d(nd, 256) + (int64_t)nterms * ceil_div_d(nm, 256);
+    ng_t = ceil_div_d(nb_t, kGroup);
+    nb_r = ceil_div_d(nm, gemv::kGtCols);
+    ng_r = ceil_div_d(nb_r, kGroup);
+  }
+  __host__ __device__ int64_t doubles() const { return nb_t + ng_t + nb_r + ng_r; }
+  __host__ __device__ int64_t counters() const { return ng_t + ng_r; }
+};
+
 // The loop of one solve, run by CTA `cta` of the nct CTAs of its team, from
 // r (set up), p = dx = 0 and beta = 0.  Every CTA returns the same CgOut.
+// Four team barriers per iteration:
+//   A  p_new = -r + beta p_old and pp = P p_new folded into the partial row
+//      sums of G pp (column ranges x row tiles)
+//   B  t_data = Wd (sum of partials), the forward regulariser rows of t, and
+//      per-block partials of ||t||^2
+//   C  alpha = r2 / t2; s += alpha t, dx += alpha p_new, y = Wd s_data in G's
+//      accumulation type
+//   D  G^T y for 4 columns per block, r for those columns (adjoint of the
+//      regulariser rows, P), per-block partials of ||r||^2; then beta, err
+//      and the stopping test
+// The sums of squares are reduced by blocks and groups in index order, so
+// the result does not depend on the team size.
 template <class L>
 __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, unsigned nct,
                          TeamBarrier &bar) {
   using Acc = typename L::Acc;
   const int64_t Nm = a.nm, nd = a.nd, ld = a.ld, nrow = a.nrow;
-  const int64_t nb_vec = ceil_div_d(Nm, cgb::VT);  // blocks of an Nm-long vector kernel
+  const int64_t nb_vec = ceil_div_d(Nm, cgb::VT);  // blocks of an Nm-long vector
   const int64_t nb_fin = ceil_div_d(nd, 256);
   const int64_t nb_axpy = ceil_div_d(nrow > Nm ? nrow : Nm, cgb::VT);
   const int64_t nb_prep = ceil_div_d(ld, 256);
-  const int64_t nb_gt = ceil_div_d(Nm, gemv::kGtCols);
   const int64_t n_gx = (int64_t)a.tiles * a.splits;
-  const int64_t n_g2 = nb_fin + (int64_t)a.FT.count * nb_vec;
+  const RedLayout rl(nd, Nm, a.FT.count);
+  double *part_t = a.red, *grp_t = part_t + rl.nb_t;
+  double *part_r = grp_t + rl.ng_t, *grp_r = part_r + rl.nb_r;
+  unsigned *cnt_t = a.red_count, *cnt_r = cnt_t + rl.ng_t;
   Acc *y = reinterpret_cast<Acc *>(a.scratch);
 
   CgOut o;
@@ -116,59 +218,64 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
   int status = CG_STATUS_RUNNING;
   bool ok = true;
   while (true) {
-    // P
-    for (int64_t b = cta; b < nb_vec; b += nct) cgb::p_update_body(a.r, a.P, beta, Nm, a.p, a.pp, b);
-    if (!(ok = bar.sync())) break;
-    // G1
+    double *p_old = (it & 1) ? a.p2 : a.p;
+    double *p_new = (it & 1) ? a.p : a.p2;
+    // A
     for (int64_t b = cta; b < n_gx; b += nct)
-      gemv::gx_partial_body<L>(a.G, ld, Nm, a.per, a.pp, a.scratch, b % a.tiles, b / a.tiles);
+      gemv::gx_partial_fold_body<L>(a.G, ld, Nm, a.per, a.r, p_old, a.P, beta, p_new, a.pp,
+                                    a.scratch, b % a.tiles, b / a.tiles);
     if (!(ok = bar.sync())) break;
-    // G2
-    for (int64_t b = cta; b < n_g2; b += nct) {
+    // B
+    for (int64_t b = cta; b < rl.nb_t; b += nct) {
+      double v = 0.0;
       if (b < nb_fin) {
+        const int64_t rr = b * 256 + threadIdx.x;
         gemv::gx_finish_body(a.scratch, a.splits, ld, nd, a.row_scale, a.wd, a.t, b);
+        if (rr < nd) {
+          const double tv = __ldcg(a.t + rr);
+          v = tv * tv;
+        }
       } else {
         const int64_t k = b - nb_fin;
-        cgb::forward_term_body(a.FT.t[k / nb_vec], a.pp, k % nb_vec);
+        const ForwardTerm &ft = a.FT.t[k / nb_vec];
+        cgb::forward_term_body(ft, a.pp, k % nb_vec);
+        const int64_t i = (k % nb_vec) * cgb::VT + threadIdx.x;
+        if (i < Nm) {
+          const double tv = __ldcg(ft.out + i);
+          v = tv * tv;
+        }
       }
+      publish_partial(cgb::block_sum(v), b, rl.nb_t, part_t, grp_t, cnt_t);
     }
     if (!(ok = bar.sync())) break;
-    // D1
-    for (int64_t b = cta; b < a.nb_row; b += nct) {
-      const double v = cgb::dot_partial_body(a.t, nullptr, nrow, b, a.nb_row);
-      if (threadIdx.x == 0) a.part[b] = v;
-    }
-    if (!(ok = bar.sync())) break;
-    T2 = bcast(cgb::sum_partials_body(a.part, a.nb_row));
+    // C
+    T2 = sum_groups(grp_t, rl.ng_t);
     alpha = R2 / T2;  // GaussNewtonInversion.cpp:1601
     if (T2 == 0.0 || !isfinite(alpha)) {
       status = (T2 == 0.0) ? CG_STATUS_BREAKDOWN : CG_STATUS_NONFINITE;
       break;
     }
-    // S
     for (int64_t b = cta; b < nb_axpy; b += nct) {
-      cgb::axpy_body(a.t, a.p, alpha, nrow, Nm, a.s, a.dx, b);
+      cgb::axpy_body(a.t, p_new, alpha, nrow, Nm, a.s, a.dx, b);
       if (b < nb_prep) gemv::prep_y_body<Acc>(a.s, nd, ld, a.row_scale, a.wd, y, b);
     }
     if (!(ok = bar.sync())) break;
-    // GT
-    for (int64_t b = cta; b < nb_gt; b += nct) {
+    // D
+    for (int64_t b = cta; b < rl.nb_r; b += nct) {
       int ncol = 0;
       const double g = gemv::gty_body<L>(a.G, ld, Nm, y, b, &ncol);
+      double v = 0.0;
       if ((int)threadIdx.x < ncol) {
         const int64_t j = b * gemv::kGtCols + threadIdx.x;
         a.gtw[j] = g;
-        a.r[j] = cgb::adjoint_column(a.AT, j, a.P, true, g, 1.0);
+        const double rj = cgb::adjoint_column(a.AT, j, a.P, true, g, 1.0);
+        a.r[j] = rj;
+        v = rj * rj;
       }
+      publish_partial(cgb::block_sum(v), b, rl.nb_r, part_r, grp_r, cnt_r);
     }
     if (!(ok = bar.sync())) break;
-    // D2
-    for (int64_t b = cta; b < a.nb_m; b += nct) {
-      const double v = cgb::dot_partial_body(a.r, nullptr, Nm, b, a.nb_m);
-      if (threadIdx.x == 0) a.part[b] = v;
-    }
-    if (!(ok = bar.sync())) break;
-    const double r2 = bcast(cgb::sum_partials_body(a.part, a.nb_m));
+    const double r2 = sum_groups(grp_r, rl.ng_r);
     // :1674-1691
     rlast2 = R2;
     R2 = r2;

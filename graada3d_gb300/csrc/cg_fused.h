@@ -31,8 +31,11 @@ struct FusedCgArgs {
   int64_t nrow = 0;
   ForwardTerms FT;
   AdjointTerms AT;
-  double *part = nullptr;
-  int nb_m = 0, nb_row = 0;  // dot-product block counts (dot_blocks)
+  double *p2 = nullptr;        // second direction buffer (p and p2 alternate)
+  double *part = nullptr;      // set-up dot products (dot_blocks partition)
+  int nb_m = 0, nb_row = 0;    // dot-product block counts of the set-up
+  double *red = nullptr;       // per-block partials and group sums of ||t||^2, ||r||^2
+  unsigned *red_count = nullptr;  // group counts (zero at the start, reset by their last block)
   double *scal = nullptr;
   int *ctl = nullptr;
   unsigned *barrier = nullptr;  // 2 words: arrivals, error
@@ -41,6 +44,12 @@ struct FusedCgArgs {
 
 // CTAs of a persistent CG launch for this storage (all co-resident).
 int fused_cg_grid(GKind kind, int sm_count);
+// G pp's partition in the persistent loop: row tiles of 256 * vec rows and
+// column ranges so that tiles x splits is two rounds of the resident CTAs.
+void fused_gx_partition(const DevG &G, int resident, int &tiles, int &splits, int64_t &per);
+// Doubles and counters of a.red / a.red_count for a loop over Nm cells, Nd
+// rows and nterms regulariser terms.
+void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t &doubles, int64_t &counters);
 // Clears the barrier words and launches the cooperative kernel.
 void launch_cg_fused(const FusedCgArgs &a, GKind kind, int grid, cudaStream_t s);
 

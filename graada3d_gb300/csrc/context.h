@@ -127,7 +127,7 @@ struct Context {
 
   // CG work vectors.
   DevBuf cg_b, cg_s, cg_t, cg_p, cg_pp, cg_r, cg_atb, cg_gtw, cg_gx, cg_tmpd, cg_scal, cg_part;
-  DevBuf cg_wl_ones, cg_ctl, cg_bar;
+  DevBuf cg_wl_ones, cg_ctl, cg_bar, cg_p2, cg_red, cg_redc;
   int fused_grid[4] = {0, 0, 0, 0};  // persistent CG grid per G storage kind
   bool inject_cg_wait = false;       // grada_inject_fault(GRADA_FAULT_CG_WAIT)
   double *h_scal = nullptr;  // pinned

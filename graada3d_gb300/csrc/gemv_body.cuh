@@ -128,6 +128,71 @@ __device__ __forceinline__ void gx_partial_body(const void *__restrict__ G, int6
   }
 }
 
+// gx_partial_body for x = pp with the CG direction update folded in: the
+// staged entries are pp_j = P_j (-r_j + beta p_old_j); blocks of tile 0 also
+// store p_new_j = -r_j + beta p_old_j and pp_j (GaussNewtonInversion.cpp:
+// 1562-1566), so no separate pass over p is needed before G pp.
+template <class L>
+__device__ __forceinline__ void gx_partial_fold_body(
+    const void *__restrict__ G, int64_t ld, int64_t nm, int64_t cols_per_split, const double *r,
+    const double *p_old, const double *__restrict__ P, double beta, double *p_new, double *pp,
+    double *partial, int64_t tile, int64_t split) {
+  using Acc = typename L::Acc;
+  constexpr int VEC = L::VEC;
+  __shared__ Acc xs[kXChunk];
+  const int64_t row = (tile * kThreads + threadIdx.x) * VEC;
+  const int64_t c_begin = split * cols_per_split;
+  const int64_t c_end = min(nm, c_begin + cols_per_split);
+  Acc acc[VEC];
+#pragma unroll
+  for (int v = 0; v < VEC; v++) acc[v] = Acc(0);
+  for (int64_t c0 = c_begin; c0 < c_end; c0 += kXChunk) {
+    const int nc = (int)min((int64_t)kXChunk, c_end - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc; t += kThreads) {
+      const int64_t j = c0 + t;
+      const double v = -__ldcg(r + j) + beta * __ldcg(p_old + j);
+      const double q = P[j] * v;
+      if (tile == 0) {
+        p_new[j] = v;
+        pp[j] = q;
+      }
+      xs[t] = (Acc)q;
+    }
+    __syncthreads();
+    if (row < ld) {
+      const int64_t base = row + c0 * ld;
+      int c = 0;
+      for (; c + 4 <= nc; c += 4) {
+        Acc g0[VEC], g1[VEC], g2[VEC], g3[VEC];
+        L::load(G, base + (int64_t)c * ld, g0);
+        L::load(G, base + (int64_t)(c + 1) * ld, g1);
+        L::load(G, base + (int64_t)(c + 2) * ld, g2);
+        L::load(G, base + (int64_t)(c + 3) * ld, g3);
+        const Acc x0 = xs[c], x1 = xs[c + 1], x2 = xs[c + 2], x3 = xs[c + 3];
+#pragma unroll
+        for (int v = 0; v < VEC; v++) {
+          acc[v] = fma(g0[v], x0, acc[v]);
+          acc[v] = fma(g1[v], x1, acc[v]);
+          acc[v] = fma(g2[v], x2, acc[v]);
+          acc[v] = fma(g3[v], x3, acc[v]);
+        }
+      }
+      for (; c < nc; c++) {
+        Acc g0[VEC];
+        L::load(G, base + (int64_t)c * ld, g0);
+#pragma unroll
+        for (int v = 0; v < VEC; v++) acc[v] = fma(g0[v], xs[c], acc[v]);
+      }
+    }
+  }
+  if (row < ld) {
+    double *out = partial + split * ld + row;
+#pragma unroll
+    for (int v = 0; v < VEC; v++) out[v] = (double)acc[v];
+  }
+}
+
 // y[r] = (sum over splits of the partial rows) * row_scale[r] * post_scale[r],
 // 256 rows per block b.
 __device__ __forceinline__ void gx_finish_body(const double *partial, int n_split, int64_t ld,

@@ -63,7 +63,8 @@ void Context::release_all() {
   for (DevBuf *b : {&wv_order, &wv_rowptr, &wv_col, &wv_val, &wv_part, &wv_segptr})
     b->release();
   DevBuf *bufs[] = {&dobs, &wd, &cg_b, &cg_s, &cg_t, &cg_p, &cg_pp, &cg_r, &cg_atb, &cg_gtw,
-                    &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &cg_ctl, &cg_bar, &bt_part2, &bt_trials,
+                    &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &cg_ctl, &cg_bar, &cg_p2, &cg_red,
+                    &cg_redc, &bt_part2, &bt_trials,
                     &bt_iters, &bt_report, &iv_m, &iv_mt, &iv_mt_old,
                     &iv_mopt, &iv_dx, &iv_P, &iv_mmin, &iv_mmax, &iv_m0, &iv_wl, &iv_tmp, &iv_tmp2,
                     &iv_dpre, &iv_d64, &iv_mstart, &iv_guard, &iv_flag,
@@ -450,13 +451,15 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   a.nd = g.nd;
   a.nm = g.nm;
   a.ld = g.ld;
-  a.splits = gx_splits(g, sm_count, vec_of(g.kind));
-  a.tiles = (int)ceil_div(g.ld, (int64_t)256 * vec_of(g.kind));
-  a.per = ceil_div(g.nm, a.splits);
-  a.scratch = scratch_doubles(product_scratch_doubles());
+  if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
+  const int grid = fused_grid[(int)g.kind];
+  fused_gx_partition(g, grid, a.tiles, a.splits, a.per);
+  a.scratch = scratch_doubles(std::max(product_scratch_doubles(), (int64_t)a.splits * g.ld));
   a.wd = dptr(wd);
   a.r = dptr(cg_r);
   a.p = dptr(cg_p);
+  cg_p2.alloc(this, sizeof(double) * (size_t)n_cells);
+  a.p2 = dptr(cg_p2);
   a.pp = dptr(cg_pp);
   a.dx = dx;
   a.t = dptr(cg_t);
@@ -472,8 +475,15 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   a.scal = dptr(cg_scal);
   cg_ctl.alloc(this, sizeof(int) * CTL_NINTS);
   a.ctl = cg_ctl.as<int>();
-  cg_bar.alloc(this, sizeof(unsigned) * 2);
+  cg_bar.alloc(this, sizeof(unsigned) * 256);
   a.barrier = cg_bar.as<unsigned>();
+  int64_t red_d = 0, red_c = 0;
+  fused_red_sizes(nd, n_cells, FT.count, red_d, red_c);
+  cg_red.alloc(this, sizeof(double) * (size_t)red_d);
+  cg_redc.alloc(this, sizeof(unsigned) * (size_t)red_c);
+  GRADA_CUDA_CHECK(cudaMemsetAsync(cg_redc.ptr, 0, sizeof(unsigned) * (size_t)red_c, stream));
+  a.red = dptr(cg_red);
+  a.red_count = cg_redc.as<unsigned>();
   if (inject_cg_wait) {  // grada_inject_fault(GRADA_FAULT_CG_WAIT): every barrier wait expires
     inject_cg_wait = false;
     a.wait_limit_ns = 0;
@@ -485,14 +495,13 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   upload(a.ctl, h_ctl, sizeof(int) * CTL_NINTS);
   h_scal[CG_TOL] = tol;
   upload(a.scal + CG_TOL, h_scal + CG_TOL, sizeof(double));
-  if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
-  launch_cg_fused(a, g.kind, fused_grid[(int)g.kind], stream);
-  unsigned bar_words[2] = {0, 0};
+  launch_cg_fused(a, g.kind, grid, stream);
+  unsigned bar_words[256];
   download(bar_words, a.barrier, sizeof(bar_words));
   download(h_ctl, a.ctl, sizeof(int) * CTL_NINTS);
   download(h_scal, a.scal, sizeof(double) * CG_NSCALARS);
   sync();
-  if (bar_words[1])
+  if (bar_words[224])
     throw Error(GRADA_ERR_CUDA, "persistent CG: a grid barrier wait expired; the solve was abandoned");
   CgResult res;
   res.iterations = h_ctl[CTL_ITER];

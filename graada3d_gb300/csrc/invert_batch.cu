@@ -331,7 +331,8 @@ __global__ void __launch_bounds__(256)
   __shared__ __align__(16) unsigned char sp_raw[sizeof(BatchProblem)];
   BatchProblem &sp = *reinterpret_cast<BatchProblem *>(sp_raw);
   const unsigned team = blockIdx.x / team_ctas, cta = blockIdx.x % team_ctas;
-  TeamBarrier bar{bar_words + 32 * team, (unsigned)team_ctas, 0u, wait_ns};
+  TeamBarrier bar(bar_words + (size_t)fused::kBarrierWords * team, (unsigned)team_ctas, cta,
+                  wait_ns);
   while (true) {
     if (cta == 0 && threadIdx.x == 0) {
       team_slot[32 * team] = atomicAdd(queue, 1);
@@ -441,13 +442,16 @@ void Context::batch_problem(const grada_invert_params &prm, BatchProblem &bp) {
   a.nd = g.nd;
   a.nm = g.nm;
   a.ld = g.ld;
-  a.splits = gx_splits(g, sm_count, vec_of(g.kind));
-  a.tiles = (int)ceil_div(g.ld, (int64_t)256 * vec_of(g.kind));
-  a.per = ceil_div(g.nm, a.splits);
+  // the single solve's partition (its grid), so both paths sum alike
+  if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
+  fused_gx_partition(g, fused_grid[(int)g.kind], a.tiles, a.splits, a.per);
+  if ((int64_t)a.splits * g.ld > need) scr = scratch_doubles((int64_t)a.splits * g.ld);
   a.scratch = scr;
   a.wd = dbuf(wd);
   a.r = dbuf(cg_r);
   a.p = dbuf(cg_p);
+  cg_p2.alloc(this, sizeof(double) * (size_t)Nm);
+  a.p2 = dbuf(cg_p2);
   a.pp = dbuf(cg_pp);
   a.dx = dbuf(iv_dx);
   a.t = dbuf(cg_t);
@@ -461,6 +465,13 @@ void Context::batch_problem(const grada_invert_params &prm, BatchProblem &bp) {
   a.nb_m = dot_blocks(Nm, sm_count);
   a.nb_row = dot_blocks(nrow, sm_count);
   a.scal = dbuf(cg_scal);
+  int64_t red_d = 0, red_c = 0;
+  fused_red_sizes(Nd, Nm, nterms, red_d, red_c);
+  cg_red.alloc(this, sizeof(double) * (size_t)red_d);
+  cg_redc.alloc(this, sizeof(unsigned) * (size_t)red_c);
+  GRADA_CUDA_CHECK(cudaMemsetAsync(cg_redc.ptr, 0, sizeof(unsigned) * (size_t)red_c, stream));
+  a.red = dbuf(cg_red);
+  a.red_count = cg_redc.as<unsigned>();
 
   bp.dobs = dbuf(dobs);
   bp.b = dbuf(cg_b);
@@ -662,13 +673,14 @@ int invert_batch_persistent(int n, Context *const *ctxs, const grada_invert_para
     const int n_teams = grid / team;
     DevBuf d_probs, d_words;
     d_probs.alloc(c0, sizeof(BatchProblem) * (size_t)n);
-    // queue (1 int), then per team 32 barrier words and a 32-int problem slot
-    const size_t words = 32 + 64 * (size_t)n_teams;
+    // queue (1 int), then per team its barrier words, then a 32-int problem slot per team
+    const size_t bw = fused::kBarrierWords;
+    const size_t words = 32 + (bw + 32) * (size_t)n_teams;
     d_words.alloc(c0, sizeof(unsigned) * words);
     c0->upload(d_probs.ptr, sorted.data(), sizeof(BatchProblem) * (size_t)n);
     int *queue = d_words.as<int>();
     unsigned *bars = d_words.as<unsigned>() + 32;
-    int *slots = d_words.as<int>() + 32 + 32 * (size_t)n_teams;
+    int *slots = d_words.as<int>() + 32 + bw * (size_t)n_teams;
     unsigned long long wait_ns = 2000000000ull;
     if (c0->inject_cg_wait) {
       c0->inject_cg_wait = false;
@@ -701,7 +713,7 @@ int invert_batch_persistent(int n, Context *const *ctxs, const grada_invert_para
     c0->download(h_words.data(), d_words.ptr, sizeof(unsigned) * words);
     c0->sync();
     for (int t = 0; t < n_teams; t++)
-      if (h_words[32 + 32 * (size_t)t + 1])
+      if (h_words[32 + bw * (size_t)t + 224])
         throw Error(GRADA_ERR_CUDA, "persistent batch: a team barrier wait expired");
     c0->last_batch_teams = n_teams;
     c0->last_batch_team_ctas = team;
