@@ -56,6 +56,9 @@ SIGNATURES = {
     "grada_solve_cg": (c_int, [c_void_p, c_double, c_int, c_double, _dp, _dp, _dp, POINTER(_dp), _dp,
                                _dp, POINTER(c_int)]),
     "grada_invert": (c_int, [c_void_p, c_void_p, _dp, _dp, _dp, _dp, _dp, c_void_p]),
+    "grada_invert_adaptive": (c_int, [c_void_p, c_void_p, c_void_p, _dp, _dp, _dp, _dp, c_void_p]),
+    "grada_set_inversion_model": (c_int, [c_void_p, _dp, _dp, _dp, _dp]),
+    "grada_get_model": (c_int, [c_void_p, _dp]),
     "grada_get_trials": (c_int, [c_void_p, _dp, c_int64, _ip64]),
     "grada_get_iterations": (c_int, [c_void_p, _dp, c_int64, _ip64]),
     "grada_G_vec_mul_noalloc": (c_int, [c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p,
@@ -108,7 +111,19 @@ class InvertReport(ctypes.Structure):
     _fields_ = [
         ("final_misfit", c_double), ("final_lambda", c_double), ("gn_iterations", c_int),
         ("n_trials", c_int), ("cg_iterations", c_int64), ("fp64_refinements", c_int64),
+        ("mesh_refinements", c_int64),
     ]
+
+
+class AdaptiveParams(ctypes.Structure):
+    """grada_adaptive_params (include/grada_gpu.h)."""
+
+    _fields_ = [("max_refinement_number", c_int), ("interval_between_refinements", c_int),
+                ("refine", c_void_p), ("user", c_void_p)]
+
+
+# grada_refine_fn: int (*)(void *user, grada_ctx *ctx, const double *m, int64_t nm)
+REFINE_FN = ctypes.CFUNCTYPE(c_int, c_void_p, c_void_p, POINTER(c_double), c_int64)
 
 _lib = None
 

@@ -81,3 +81,59 @@ def refine_mesh(inv, octree, m, fraction: float, min_size, beta: float,
         vec, interp = v if isinstance(v, tuple) else (v, None)
         out.append(carry_over(vec, parent, split, inv.prisms, interp))
     return tuple(out)
+
+
+def invert_adaptive(inv, octree, prm: dict, m_ini, m_min, m_max, m0=None, *,
+                    max_refinements: int, interval: int, fraction: float, min_size, beta: float,
+                    alphas=(1.0, 1.0, 1.0, 1.0), fp64_refinement: bool = False):
+    """The adaptive inversion (invert_with_own_CG with its refinement branch,
+    GaussNewtonInversion.cpp:1098-1294) through grada_invert_adaptive: the
+    Gauss-Newton loop, lambda search and CG run in the library; at each
+    refinement the library calls back here, and refine_mesh splits the marked
+    cells of `octree` (on the host), expands G and rebuilds Ws/Wx/Wy/Wz (on the
+    device), and the model, bounds and reference model follow the children.
+    `inv` must hold G for octree.leaves() with its data and operators set.
+    Returns (model on the final cells, report)."""
+    import ctypes
+
+    from . import _lib
+    from .inversion import _params, _ptr
+
+    lib = inv.ctx.lib
+    nm = inv.Nm
+    state = {"mmin": np.asarray(m_min, dtype=np.float64).copy(),
+             "mmax": np.asarray(m_max, dtype=np.float64).copy(),
+             "m0": np.zeros(nm) if m0 is None else np.asarray(m0, dtype=np.float64).copy()}
+    errors = []
+
+    def on_refine(user, ctx_handle, m_ptr, n):
+        try:
+            m = np.ctypeslib.as_array(m_ptr, shape=(n,)).copy()
+            new_m, mmin, mmax, m0v = refine_mesh(inv, octree, m, fraction, min_size, beta, alphas,
+                                                 extra=(state["mmin"], state["mmax"], state["m0"]))
+            state.update(mmin=np.ascontiguousarray(mmin), mmax=np.ascontiguousarray(mmax),
+                         m0=np.ascontiguousarray(m0v))
+            new_m = np.ascontiguousarray(new_m)
+            return lib.grada_set_inversion_model(inv.ctx.handle, _ptr(new_m), _ptr(state["mmin"]),
+                                                 _ptr(state["mmax"]), _ptr(state["m0"]))
+        except BaseException as e:  # reported after the call returns
+            errors.append(e)
+            return -1
+
+    callback = _lib.REFINE_FN(on_refine)
+    ap = _lib.AdaptiveParams(int(max_refinements), int(interval),
+                             ctypes.cast(callback, ctypes.c_void_p), None)
+    p = _params(prm, fp64_refinement)
+    vecs = [np.ascontiguousarray(v, dtype=np.float64) for v in (m_ini, m_min, m_max)]
+    m0a = None if m0 is None else np.ascontiguousarray(m0, dtype=np.float64)
+    rep = _lib.InvertReport()
+    rc = lib.grada_invert_adaptive(inv.ctx.handle, ctypes.byref(p), ctypes.byref(ap),
+                                   _ptr(vecs[0]), _ptr(vecs[1]), _ptr(vecs[2]),
+                                   None if m0a is None else _ptr(m0a), ctypes.byref(rep))
+    if errors:
+        raise errors[0]
+    inv.ctx.check(rc)
+    out = np.empty(inv.Nm)
+    inv.ctx.check(lib.grada_get_model(inv.ctx.handle, _ptr(out)))
+    inv.m = out
+    return out, {f: getattr(rep, f) for f, _ in _lib.InvertReport._fields_}

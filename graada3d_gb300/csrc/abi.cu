@@ -316,7 +316,6 @@ void Context::forward_field_dev(const double *d_rho, double *d_fields) {
 // C ABI
 // ---------------------------------------------------------------------------
 
-struct grada_ctx : public grada::Context {};
 
 namespace {
 
@@ -658,6 +657,47 @@ int grada_invert(grada_ctx *ctx, const grada_invert_params *params, const double
     grada_invert_report rep;
     ctx->invert(*params, m_ini, m_min, m_max, m0, m_out, rep);
     if (report) *report = rep;
+  });
+}
+
+int grada_invert_adaptive(grada_ctx *ctx, const grada_invert_params *params,
+                          const grada_adaptive_params *adaptive, const double *m_ini,
+                          const double *m_min, const double *m_max, const double *m0,
+                          grada_invert_report *report) {
+  return guarded(ctx, [&] {
+    if (!params || !adaptive) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null parameters");
+    grada_invert_report rep;
+    ctx->invert(*params, m_ini, m_min, m_max, m0, nullptr, rep, adaptive);
+    if (report) *report = rep;
+  });
+}
+
+int grada_set_inversion_model(grada_ctx *ctx, const double *m, const double *m_min,
+                              const double *m_max, const double *m0) {
+  return guarded(ctx, [&] {
+    if (!ctx->refine_pending)
+      throw Error(GRADA_ERR_STATE, "grada_set_inversion_model is for refine callbacks");
+    if (!m || !m_min || !m_max) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null model vector");
+    const size_t n = (size_t)ctx->n_cells;
+    std::vector<double> v(4 * n, 0.0);
+    std::memcpy(v.data(), m, sizeof(double) * n);
+    std::memcpy(v.data() + n, m_min, sizeof(double) * n);
+    std::memcpy(v.data() + 2 * n, m_max, sizeof(double) * n);
+    if (m0) std::memcpy(v.data() + 3 * n, m0, sizeof(double) * n);
+    for (size_t i = 0; i < n; i++)
+      if (!(v[n + i] < v[2 * n + i]))
+        throw Error(GRADA_ERR_INVALID_ARGUMENT, "m_min must be < m_max");
+    ctx->refine_model.swap(v);
+  });
+}
+
+int grada_get_model(grada_ctx *ctx, double *m) {
+  return guarded(ctx, [&] {
+    if (!m) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null model vector");
+    if (!ctx->iv_m.ptr || ctx->iv_m.bytes < sizeof(double) * (size_t)ctx->n_cells)
+      throw Error(GRADA_ERR_STATE, "no inversion has run");
+    ctx->download(m, ctx->iv_m.ptr, sizeof(double) * (size_t)ctx->n_cells);
+    ctx->sync();
   });
 }
 

@@ -193,7 +193,12 @@ struct Context {
                         const double *d64, const double *m_start);
   double misfit_of(const double *m, const double *m_start, const double *d64);
   void invert(const grada_invert_params &prm, const double *h_m_ini, const double *h_mmin,
-              const double *h_mmax, const double *h_m0, double *h_m_out, grada_invert_report &rep);
+              const double *h_mmax, const double *h_m0, double *h_m_out, grada_invert_report &rep,
+              const grada_adaptive_params *adapt = nullptr);
+  // adaptive inversion: set while the host's refine callback runs; the model,
+  // bounds and reference model on the refined mesh it hands back (4 x Nm)
+  bool refine_pending = false;
+  std::vector<double> refine_model;
 
   void upload(void *dst, const void *src, size_t nbytes);
   void download(void *dst, const void *src, size_t nbytes);
@@ -256,3 +261,8 @@ int load_batch_tuning(const char *path);
 int tuned_team_ctas(double max_entries);
 
 }  // namespace grada
+
+// The C ABI's opaque context is the internal one (every context the ABI
+// creates is a grada_ctx, so a Context inside the library may be handed to a
+// host callback as one).
+struct grada_ctx : public grada::Context {};

@@ -579,27 +579,40 @@ bool Context::invert_setup(const grada_invert_params &prm, const double *h_m_ini
 
 void Context::invert(const grada_invert_params &prm, const double *h_m_ini, const double *h_mmin,
                      const double *h_mmax, const double *h_m0, double *h_m_out,
-                     grada_invert_report &rep) {
+                     grada_invert_report &rep, const grada_adaptive_params *adapt) {
   NvtxRange nvtx("grada invert");
-  if (!h_m_out) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null model vector");
+  if (!h_m_out && !adapt) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null model vector");
+  if (adapt && (!adapt->refine || adapt->interval_between_refinements < 1))
+    throw Error(GRADA_ERR_INVALID_ARGUMENT, "adaptive inversion needs a refine callback and an interval >= 1");
   std::memset(&rep, 0, sizeof(rep));
   struct PredictGuard {
     Context *c;
     ~PredictGuard() { c->predict_fp64 = false; }
   } predict_guard{this};
   const bool refine = invert_setup(prm, h_m_ini, h_mmin, h_mmax, h_m0);
-  const int64_t Nm = n_cells;
-  const size_t vb = sizeof(double) * Nm;
-  double *dm = dptr(iv_m), *dmt = dptr(iv_mt), *dmt_old = dptr(iv_mt_old), *dmopt = dptr(iv_mopt);
-  double *ddx = dptr(iv_dx), *dP = dptr(iv_P), *dmin = dptr(iv_mmin), *dmax = dptr(iv_mmax);
-  double *dm0 = dptr(iv_m0), *dtmp = dptr(iv_tmp);
-  double *wlv = dptr(iv_wl);
+  if (adapt && predict_fp64)
+    throw Error(GRADA_ERR_STATE, "adaptive inversion: a kept FP64 G is not expanded by refinement");
+  int64_t Nm = n_cells;
+  size_t vb = sizeof(double) * Nm;
+  double *dm, *dmt, *dmt_old, *dmopt, *ddx, *dP, *dmin, *dmax, *dm0, *dtmp, *wlv;
   // WL slots in the reference argument order s, x, y, z, tx, ty, tz
-  double *WLs = wlv, *WLx = wlv + Nm, *WLy = wlv + 2 * Nm, *WLz = wlv + 3 * Nm;
-  double *WLtx = wlv + 4 * Nm, *WLty = wlv + 5 * Nm, *WLtz = wlv + 6 * Nm;
-  const double *WL[7] = {WLs, WLx, WLy, WLz, WLtx, WLty, WLtz};
-  double *d64 = refine ? dptr(iv_d64) : nullptr;
-  double *mstart = dptr(iv_mstart);
+  double *WLs, *WLx, *WLy, *WLz, *WLtx, *WLty, *WLtz;
+  const double *WL[7];
+  double *d64, *mstart;
+  // device pointers of the inversion vectors (again after a refinement)
+  auto bind = [&]() {
+    dm = dptr(iv_m), dmt = dptr(iv_mt), dmt_old = dptr(iv_mt_old), dmopt = dptr(iv_mopt);
+    ddx = dptr(iv_dx), dP = dptr(iv_P), dmin = dptr(iv_mmin), dmax = dptr(iv_mmax);
+    dm0 = dptr(iv_m0), dtmp = dptr(iv_tmp);
+    wlv = dptr(iv_wl);
+    WLs = wlv, WLx = wlv + Nm, WLy = wlv + 2 * Nm, WLz = wlv + 3 * Nm;
+    WLtx = wlv + 4 * Nm, WLty = wlv + 5 * Nm, WLtz = wlv + 6 * Nm;
+    WL[0] = WLs, WL[1] = WLx, WL[2] = WLy, WL[3] = WLz, WL[4] = WLtx, WL[5] = WLty,
+    WL[6] = WLtz;
+    d64 = refine ? dptr(iv_d64) : nullptr;
+    mstart = dptr(iv_mstart);
+  };
+  bind();
 
   auto refresh_fp64 = [&](const double *mref_point) {
     // FP64 matrix-free prediction at the current model: the residual
@@ -624,6 +637,35 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
   int i = 0, j = 0;
   const double p_expo[5] = {-(2 - prm.lp_s) / 4.0, -(2 - prm.lp_x) / 4.0, -(2 - prm.lp_y) / 4.0,
                             -(2 - prm.lp_z) / 4.0, -(2 - prm.lp_t) / 4.0};
+  // IRLS weights of the terms with p != 2 from the model mv (:962-1022; after
+  // a refinement from m itself, :1228-1281)
+  auto irls_from = [&](const double *mv) {
+    if (prm.lp_s != 2) {
+      launch_csr_apply(ops[GRADA_OP_WS].A(), mv, dm0, 1.0, nullptr, dtmp, stream);
+      launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[0], WLs, stream);
+    }
+    if (prm.lp_x != 2) {
+      launch_csr_apply(ops[GRADA_OP_WX].A(), mv, nullptr, 1.0, nullptr, dtmp, stream);
+      launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[1], WLx, stream);
+    }
+    if (prm.lp_y != 2) {
+      launch_csr_apply(ops[GRADA_OP_WY].A(), mv, nullptr, 1.0, nullptr, dtmp, stream);
+      launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[2], WLy, stream);
+    }
+    if (prm.lp_z != 2) {
+      launch_csr_apply(ops[GRADA_OP_WZ].A(), mv, nullptr, 1.0, nullptr, dtmp, stream);
+      launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[3], WLz, stream);
+    }
+    if (prm.lp_t != 2 && crg_enabled) {
+      double *wt[3] = {WLtx, WLty, WLtz};
+      for (int q = 0; q < 3; q++) {
+        launch_csr_apply(ops[GRADA_OP_TX + q].A(), mv, nullptr, 1.0, nullptr, dtmp, stream);
+        launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[4], wt[q], stream);
+      }
+    }
+  };
+  int c_refinement = 0, i_between_refinement = 0;
+  const int max_refinements = adapt ? adapt->max_refinement_number : 0;
   for (i = 0; i < prm.gn_iterations; i++) {
     GRADA_CUDA_CHECK(cudaMemcpyAsync(dmt, dm, vb, cudaMemcpyDeviceToDevice, stream));
     double misfit_last1 = 10 * misfit;
@@ -665,30 +707,7 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
         break;
       } else {
         lambda = lambda * rate;
-        // IRLS (:962-1022)
-        if (prm.lp_s != 2) {
-          launch_csr_apply(ops[GRADA_OP_WS].A(), dmopt, dm0, 1.0, nullptr, dtmp, stream);
-          launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[0], WLs, stream);
-        }
-        if (prm.lp_x != 2) {
-          launch_csr_apply(ops[GRADA_OP_WX].A(), dmopt, nullptr, 1.0, nullptr, dtmp, stream);
-          launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[1], WLx, stream);
-        }
-        if (prm.lp_y != 2) {
-          launch_csr_apply(ops[GRADA_OP_WY].A(), dmopt, nullptr, 1.0, nullptr, dtmp, stream);
-          launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[2], WLy, stream);
-        }
-        if (prm.lp_z != 2) {
-          launch_csr_apply(ops[GRADA_OP_WZ].A(), dmopt, nullptr, 1.0, nullptr, dtmp, stream);
-          launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[3], WLz, stream);
-        }
-        if (prm.lp_t != 2 && crg_enabled) {
-          double *wt[3] = {WLtx, WLty, WLtz};
-          for (int q = 0; q < 3; q++) {
-            launch_csr_apply(ops[GRADA_OP_TX + q].A(), dmopt, nullptr, 1.0, nullptr, dtmp, stream);
-            launch_irls_weight(dtmp, Nm, prm.epsilon2, p_expo[4], wt[q], stream);
-          }
-        }
+        irls_from(dmopt);  // IRLS (:962-1022)
       }
       if (misfit < prm.target_misfit) break;
     }
@@ -698,10 +717,56 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
     if (misfit < prm.target_misfit || i == prm.gn_iterations - 1) break;
     const bool flag1 = std::abs(misfit - misfit_last_iteration) /
                            std::min(misfit, misfit_last_iteration) < prm.stag_tol;
-    // no refinement on a fixed mesh: c_refinement (0) >= max_refinement_number (0)
-    if (flag1) break;
+    // the refinement branch (GaussNewtonInversion.cpp:1098-1294); on a fixed
+    // mesh max_refinement_number is 0 and a stagnation ends the inversion
+    if (c_refinement >= max_refinements && flag1) break;
+    if (c_refinement < max_refinements &&
+        (++i_between_refinement % adapt->interval_between_refinements == 0 || flag1)) {
+      i_between_refinement = 0;
+      ++c_refinement;
+      // the host's refine_mesh (AdaptiveInversion.cpp:637-735): it splits the
+      // mesh, expands G (grada_expand_G), rebuilds Ws/Wx/Wy/Wz (and T) and
+      // hands back the model, bounds and reference model on the new cells
+      std::vector<double> hm((size_t)Nm);
+      download(hm.data(), dm, vb);
+      sync();
+      refine_pending = true;
+      refine_model.clear();
+      const int st = adapt->refine(adapt->user, static_cast<grada_ctx *>(this), hm.data(), Nm);
+      refine_pending = false;
+      if (st != GRADA_OK)
+        throw Error(st, "refine callback failed: " + last_error);
+      if (refine_model.size() != (size_t)(4 * n_cells))
+        throw Error(GRADA_ERR_STATE,
+                    "the refine callback must hand back the model on the refined mesh "
+                    "(grada_set_inversion_model)");
+      for (int t = 0; t < 4; t++)
+        if (!ops[t].set || ops[t].n != n_cells)
+          throw Error(GRADA_ERR_STATE,
+                      "the refine callback must rebuild Ws/Wx/Wy/Wz for the refined mesh");
+      Nm = n_cells;
+      vb = sizeof(double) * Nm;
+      DevBuf *vecs[] = {&iv_m, &iv_mt, &iv_mt_old, &iv_mopt, &iv_dx, &iv_P, &iv_mmin, &iv_mmax,
+                        &iv_m0, &iv_tmp, &iv_tmp2, &iv_mstart};
+      for (DevBuf *b : vecs) b->alloc(this, vb);
+      iv_wl.alloc(this, vb * 7);
+      iv_guard.alloc(this, sizeof(int) * Nm);
+      ensure_cg_workspace(crg_enabled ? 7 : 4);
+      bind();
+      upload(dm, refine_model.data(), vb);
+      upload(dmin, refine_model.data() + Nm, vb);
+      upload(dmax, refine_model.data() + 2 * Nm, vb);
+      upload(dm0, refine_model.data() + 3 * Nm, vb);
+      {
+        std::vector<double> ones(7 * (size_t)Nm, 1.0);  // WL = I (:1185-1199)
+        upload(wlv, ones.data(), vb * 7);
+        sync();
+      }
+      irls_from(dm);
+      rep.mesh_refinements++;
+    }
   }
-  download(h_m_out, dm, vb);
+  if (h_m_out) download(h_m_out, dm, vb);
   sync();
   rep.final_misfit = misfit;
   rep.final_lambda = lambda;

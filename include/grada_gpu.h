@@ -306,6 +306,7 @@ typedef struct grada_invert_report {
   int n_trials;             /* lambda trials (lines of lambda_misfit_GN) */
   int64_t cg_iterations;    /* CG iterations over all trials */
   int64_t fp64_refinements; /* FP64 matrix-free residual evaluations */
+  int64_t mesh_refinements; /* refinements of an adaptive inversion */
 } grada_invert_report;
 
 /*
@@ -321,6 +322,43 @@ typedef struct grada_invert_report {
 int grada_invert(grada_ctx *ctx, const grada_invert_params *params, const double *m_ini,
                  const double *m_min, const double *m_max, const double *m0, double *m_out,
                  grada_invert_report *report);
+
+/*
+ * The adaptive inversion: invert_with_own_CG with its refinement branch
+ * (GaussNewtonInversion.cpp:1098-1294).  After a Gauss-Newton iteration that
+ * neither reaches the target nor is the last, with c refinements done so far:
+ * if c >= max_refinement_number and the misfit stagnated, stop; else if
+ * c < max_refinement_number and (interval_between_refinements iterations
+ * passed since the last refinement, or the misfit stagnated), refine: the
+ * library calls refine(user, ctx, m, Nm) with the current model on the host.
+ * The callback is the host's AdaptiveInversion::refine_mesh
+ * (AdaptiveInversion.cpp:637-735): it splits cells (mesh refinement stays on
+ * the host), calls grada_expand_G, rebuilds Ws/Wx/Wy/Wz (grada_build_operators
+ * or grada_set_operator; with the cross-gradient term also T and S_crg) and
+ * hands back the model, bounds and reference model on the new cells with
+ * grada_set_inversion_model; it returns GRADA_OK or a failure status.  The
+ * library then resets the IRLS weights to one and recomputes those of the
+ * p != 2 terms from the model, as the reference does, and continues.  FP64 or
+ * FP32 G (not a kept FP64 G).  The final model has the final cell count:
+ * read it with grada_get_model.
+ */
+typedef int (*grada_refine_fn)(void *user, grada_ctx *ctx, const double *m, int64_t nm);
+typedef struct grada_adaptive_params {
+  int max_refinement_number;        /* AdaptiveInversion::set_max_refinement_number */
+  int interval_between_refinements; /* set_interval_between_refinements */
+  grada_refine_fn refine;
+  void *user;
+} grada_adaptive_params;
+int grada_invert_adaptive(grada_ctx *ctx, const grada_invert_params *params,
+                          const grada_adaptive_params *adaptive, const double *m_ini,
+                          const double *m_min, const double *m_max, const double *m0,
+                          grada_invert_report *report);
+/* Inside a refine callback only: m, m_min, m_max, m0 on the refined cells
+ * (Nm each; m0 NULL = 0). */
+int grada_set_inversion_model(grada_ctx *ctx, const double *m, const double *m_min,
+                              const double *m_max, const double *m0);
+/* The model of the last grada_invert / grada_invert_adaptive (Nm doubles). */
+int grada_get_model(grada_ctx *ctx, double *m);
 
 /*
  * Keep the FP64 G beside a reduced-precision one (no counterpart in the

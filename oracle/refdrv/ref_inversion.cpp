@@ -6,6 +6,11 @@
 // solve_cg call (GaussNewtonInversion.cpp:1417-1698) and, optionally, a full
 // invert_with_own_CG run (GaussNewtonInversion.cpp:657-1308).
 //
+// Mode 3 runs the adaptive inversion instead: invert_with_own_CG with its
+// refinement branch (GaussNewtonInversion.cpp:1098-1294, refine_mesh
+// AdaptiveInversion.cpp:637-735), reading the refinement settings after the
+// mode, and dumps the final model, misfit, lambda and the final leaves.
+//
 // Usage: ref_inversion <in.bin> <out.bin>   (run in a scratch directory: the
 // reference writes lambda_misfit_GN and Iteration_misfit_GN into the cwd)
 #include <cstdint>
@@ -74,6 +79,7 @@ class Drv : public GaussNewtonInversion {
   const Eigen::MatrixXd &G_() const { return G; }
   Eigen::VectorXd m_() const { return m; }
   void use_crg(bool b) { use_cross_gradient_constraint = b; }
+  Mesh &mesh_() { return mesh; }
 };
 
 SMatrix diag(const Eigen::VectorXd &d) {
@@ -149,6 +155,16 @@ int main(int argc, char **argv) {
   const int64_t use_ref = in.get<int64_t>();
   std::vector<double> m0_v = use_ref ? in.vec(nm) : std::vector<double>();
   const int64_t mode = in.get<int64_t>();
+  int64_t max_ref = 0, interval = 1;
+  double fraction = 0.1, min_dx = 0, min_dy = 0, min_dz = 0;
+  if (mode == 3) {
+    max_ref = in.get<int64_t>();
+    interval = in.get<int64_t>();
+    fraction = in.get<double>();
+    min_dx = in.get<double>();
+    min_dy = in.get<double>();
+    min_dz = in.get<double>();
+  }
 
   Mesh mesh;
   mesh.generate_regular_mesh(xl, (int)nx, yl, (int)ny, zl, (int)nz);
@@ -164,7 +180,12 @@ int main(int argc, char **argv) {
   inv.set_lambda_decreasing_rate(rate);
   inv.set_n_lambda((int)n_lambda);
   inv.set_CG_parameter(cg_tol, cg_factor);
-  inv.set_max_refinement_number(0);
+  inv.set_max_refinement_number((int)max_ref);
+  if (mode == 3) {
+    inv.set_interval_between_refinements((int)interval);
+    inv.set_refinement_percentage(fraction);
+    inv.set_min_cell_size_in_adaptive_mesh(min_dx, min_dy, min_dz);
+  }
   inv.set_stagnation_tolerance(stag);
   inv.set_target_misfit(target);
   inv.set_Lp_inversion_parameter((int)lps, (int)lpx, (int)lpy, (int)lpz, (int)lpt, eps2);
@@ -233,6 +254,19 @@ int main(int argc, char **argv) {
     out.i64(iters);
   } else if (mode == 2) {
     inv.invert();
+    out.vec(inv.m_());
+    out.f64(inv.get_final_misfit());
+    out.f64(inv.get_final_lambda());
+  } else if (mode == 3) {
+    inv.invert();
+    Mesh &msh = inv.mesh_();
+    const int64_t n = msh.n_elems();
+    out.i64(n);
+    for (int64_t i = 0; i < n; i++) {
+      const Cell *c = msh.leaf_cells[i];
+      const double v[6] = {c->_x[0], c->_x[1], c->_y[0], c->_y[1], c->_z[0], c->_z[1]};
+      std::fwrite(v, 8, 6, fo);
+    }
     out.vec(inv.m_());
     out.f64(inv.get_final_misfit());
     out.f64(inv.get_final_lambda());

@@ -194,3 +194,106 @@ def inversion_fixtures() -> None:
         print(f"ref_inversion {name}: Nm={np.prod(c['n'])} Nd={res['G'].shape[0]} "
               f"cg_iters={res['cg_iters']} final misfit={res['inv_misfit']:.4f} "
               f"trials={len(res['inv_trials'])}")
+
+
+def pack_input(c: dict, mode: int, adaptive: dict | None = None) -> bytes:
+    """The ref_inversion driver's input for case c (modes 2 and 3)."""
+    nx, ny, nz = c["n"]
+    obs = c["obs"]
+    b = bytearray()
+    b += struct.pack("<qqq", nx, ny, nz)
+    b += struct.pack("<6d", *c["xl"], *c["yl"], *c["zl"])
+    b += struct.pack("<q", obs.shape[0]) + obs.astype("<f8").tobytes()
+    b += struct.pack("<I", c["mask"])
+    b += c["dobs"].astype("<f8").tobytes()
+    b += np.asarray(c["rel"], "<f8").tobytes() + np.asarray(c["abs"], "<f8").tobytes()
+    b += struct.pack("<d", c["beta"])
+    b += struct.pack("<5d", *c["alphas"])
+    b += struct.pack("<dqd", c["max_lambda"], c["n_lambda"], c["rate"])
+    b += struct.pack("<4d", c["target"], c["stag"], c["cg_tol"], c["cg_factor"])
+    b += struct.pack("<q", c["gn_iter"])
+    b += struct.pack("<5q", *c["lp"])
+    b += struct.pack("<d", c["eps2"])
+    b += struct.pack("<3d", c["m_min"], c["m_max"], c["m_ini"])
+    b += struct.pack("<q", 1 if c.get("m0s") is not None else 0)
+    if c.get("m0s") is not None:
+        b += c["m0s"].astype("<f8").tobytes()
+    b += struct.pack("<q", 1 if c.get("m0") is not None else 0)
+    if c.get("m0") is not None:
+        b += c["m0"].astype("<f8").tobytes()
+    b += struct.pack("<q", mode)
+    if mode == 3:
+        b += struct.pack("<qqd3d", adaptive["max_refinements"], adaptive["interval"],
+                         adaptive["fraction"], *adaptive["min_size"])
+    return bytes(b)
+
+
+def make_adaptive_case(seed: int = 21):
+    """A small L2 inversion (8 x 8 x 4 cells, gz + Tzz at 9 x 8 points) with two
+    refinements of 10 % of the cells, one per Gauss-Newton iteration, down to a
+    quarter of the base cell size."""
+    c, _ = make_case("l2", seed)
+    c["gn_iter"] = 5
+    c["stag"] = 0.005
+    adaptive = {"max_refinements": 2, "interval": 1, "fraction": 0.1,
+                "min_size": (1000.0 / 8 / 4, 900.0 / 8 / 4, 500.0 / 4 / 4)}
+    return c, adaptive
+
+
+def run_adaptive(c: dict, adaptive: dict, exe: Path = EXE):
+    """The reference's adaptive inversion on case c: final leaves, model, misfit,
+    lambda, the lambda/misfit and iteration records, and the number of cells
+    split at each refinement (the reference prints it)."""
+    import re
+
+    with tempfile.TemporaryDirectory() as td:
+        wd = Path(td)
+        (wd / "in.bin").write_bytes(pack_input(c, 3, adaptive))
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        res = subprocess.run([str(exe), "in.bin", "out.bin"], cwd=wd, check=True,
+                             capture_output=True, text=True, env=env)
+        buf = (wd / "out.bin").read_bytes()
+        # skip the set-up dump (G, operators, Wd) that precedes the mode's output
+        rows, cols = struct.unpack_from("<qq", buf, 0)
+        off = 16 + 8 * rows * cols
+        for _ in range(4):
+            _, off = _read_csr(buf, off)
+        (use_crg,) = struct.unpack_from("<q", buf, off)
+        off += 8
+        if use_crg:
+            for _ in range(3):
+                _, off = _read_csr(buf, off)
+            off += 8 * cols
+        off += 8 * rows
+        (n,) = struct.unpack_from("<q", buf, off)
+        off += 8
+        leaves = np.frombuffer(buf, "<f8", 6 * n, off).reshape(n, 6).copy()
+        off += 48 * n
+        m = np.frombuffer(buf, "<f8", n, off).copy()
+        off += 8 * n
+        misfit, lam = struct.unpack_from("<dd", buf, off)
+        splits = [int(v) for v in re.findall(r"(\d+) elements are refined", res.stdout)]
+        return {"leaves": leaves, "m": m, "misfit": misfit, "lambda": lam, "splits": np.array(splits),
+                "trials": _parse_table(wd / "lambda_misfit_GN"),
+                "iterations": _parse_table(wd / "Iteration_misfit_GN")}
+
+
+def adaptive_fixture() -> None:
+    c, ad = make_adaptive_case()
+    res = run_adaptive(c, ad)
+    out = {"n": np.array(c["n"]), "xl": np.array(c["xl"]), "yl": np.array(c["yl"]),
+           "zl": np.array(c["zl"]), "obs": c["obs"], "mask": np.array(c["mask"]),
+           "dobs": c["dobs"], "rel": np.array(c["rel"]), "abs": np.array(c["abs"]),
+           "beta": np.array(c["beta"]), "alphas": np.array(c["alphas"]),
+           "max_lambda": np.array(c["max_lambda"]), "n_lambda": np.array(c["n_lambda"]),
+           "rate": np.array(c["rate"]), "target": np.array(c["target"]), "stag": np.array(c["stag"]),
+           "cg_tol": np.array(c["cg_tol"]), "cg_factor": np.array(c["cg_factor"]),
+           "gn_iter": np.array(c["gn_iter"]), "lp": np.array(c["lp"]), "eps2": np.array(c["eps2"]),
+           "bounds": np.array([c["m_min"], c["m_max"], c["m_ini"]]),
+           "max_refinements": np.array(ad["max_refinements"]), "interval": np.array(ad["interval"]),
+           "fraction": np.array(ad["fraction"]), "min_size": np.array(ad["min_size"])}
+    for k, v in res.items():
+        out["ref_" + k] = np.asarray(v)
+    np.savez_compressed(HERE / "ref_adaptive_inversion.npz", **out)
+    print(f"ref_adaptive_inversion: leaves {res['leaves'].shape[0]} splits {res['splits']} "
+          f"misfit {res['misfit']:.4f} trials {len(res['trials'])}")

@@ -28,6 +28,9 @@ Fixtures written (all .npz):
   ref_inversion_*.npz regular-mesh inversion problems with the reference's
                       G, host-built operators, one solve_cg call and a full
                       invert_with_own_CG run (oracle/_ref/ref_inversion).
+  ref_adaptive_inversion.npz  the adaptive inversion (invert_with_own_CG with
+                      two mesh refinements): final leaves, model, records and
+                      the cells split per refinement (oracle/_ref/ref_inversion).
 """
 from __future__ import annotations
 
@@ -614,8 +617,9 @@ def main() -> None:
             "ref_indicator": ref_indicator, "ref_operators": ref_operators,
             "ref_output": ref_output, "ref_adapt": ref_adapt, "ref_interp": ref_interp}
     try:
-        from inversion_cases import inversion_fixtures  # noqa: E402
+        from inversion_cases import adaptive_fixture, inversion_fixtures  # noqa: E402
         jobs["ref_inversion"] = inversion_fixtures
+        jobs["ref_adaptive_inversion"] = adaptive_fixture
     except ImportError:
         pass
     for name, fn in jobs.items():

@@ -1,0 +1,57 @@
+"""The adaptive inversion end to end on the device: invert_with_own_CG with its
+refinement branch (GaussNewtonInversion.cpp:1098-1294; refine_mesh,
+AdaptiveInversion.cpp:637-735) through grada_invert_adaptive and the host's
+refinement callback, against the reference's own run (ref_adaptive_inversion
+fixture: an L2 inversion on 8 x 8 x 4 cells with two refinements of 10 %, one
+per Gauss-Newton iteration).  The same cells are split at each refinement,
+the final leaves are bitwise the reference's, the Gauss-Newton misfits and
+every lambda trial's misfit agree to 1e-6, the final model to 1e-5."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_adaptive_inversion_matches_reference(gpu_ctx, golden):
+    from graada3d_gb300 import adaptive, mesh
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.inversion import GaussNewtonInversion
+
+    f = golden("ref_adaptive_inversion.npz")
+    nx, ny, nz = (int(v) for v in f["n"])
+    o = mesh.Octree.regular(tuple(f["xl"]), nx, tuple(f["yl"]), ny, tuple(f["zl"]), nz)
+    mask = int(f["mask"])
+    inv = GaussNewtonInversion(o.leaves(), f["obs"], mask, ctx=gpu_ctx)
+    inv.compute_G("fp64")
+    inv.set_cross_gradient(False)
+    beta = float(f["beta"])
+    alphas = tuple(float(v) for v in f["alphas"][:4])
+    inv.build_operators(reg.face_table(inv.prisms), beta, 0, alphas)
+    wd = reg.data_weights(f["dobs"], f["rel"], f["abs"], f["obs"].shape[0])
+    inv.set_dobs(f["dobs"], wd)
+    prm = {"max_lambda": float(f["max_lambda"]), "n_lambda": int(f["n_lambda"]),
+           "rate": float(f["rate"]), "target": float(f["target"]), "stag": float(f["stag"]),
+           "cg_tol": float(f["cg_tol"]), "cg_factor": float(f["cg_factor"]),
+           "gn_iter": int(f["gn_iter"]), "lp": [int(v) for v in f["lp"]], "eps2": float(f["eps2"])}
+    nm = inv.Nm
+    mmin, mmax, mini = f["bounds"]
+    n_before = [nm]
+    m, rep = adaptive.invert_adaptive(
+        inv, o, prm, np.full(nm, mini), np.full(nm, mmin), np.full(nm, mmax),
+        max_refinements=int(f["max_refinements"]), interval=int(f["interval"]),
+        fraction=float(f["fraction"]), min_size=f["min_size"], beta=beta, alphas=alphas)
+    assert rep["mesh_refinements"] == len(f["ref_splits"])
+    leaves = f["ref_leaves"]
+    assert inv.prisms.shape == leaves.shape
+    assert np.array_equal(inv.prisms.view(np.uint64), leaves.view(np.uint64))
+    its = inv.iterations()
+    assert its.shape[0] == f["ref_iterations"].shape[0]
+    np.testing.assert_allclose(its[:, 2], f["ref_iterations"][:, 2], rtol=1e-6, atol=0)
+    trials = inv.trials()
+    ref_trials = f["ref_trials"]  # lambda, misfit per trial
+    assert trials.shape[0] == ref_trials.shape[0]
+    np.testing.assert_allclose(trials[:, 1], ref_trials[:, 0], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(trials[:, 2], ref_trials[:, 1], rtol=1e-6, atol=0)
+    assert abs(rep["final_misfit"] - float(f["ref_misfit"])) <= 1e-6 * float(f["ref_misfit"])
+    assert np.abs(m - f["ref_m"]).max() <= 1e-5 * np.abs(f["ref_m"]).max()
+    assert n_before[0] == nx * ny * nz
