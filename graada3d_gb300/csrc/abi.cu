@@ -865,11 +865,22 @@ int grada_inject_fault(grada_ctx *ctx, int fault) {
       ctx->sync();
     } else if (fault == GRADA_FAULT_CG_WAIT) {
       ctx->inject_cg_wait = true;
+    } else if (fault == GRADA_FAULT_TC_WAIT) {
+      // arms the tensor-core kernels' expiry test (word 1 of their flag
+      // block); the host check that reports the expiry disarms it
+      ctx->tc_err.alloc(ctx, sizeof(int) * 4);
+      const int arm[2] = {0, 1};
+      ctx->upload(ctx->tc_err.ptr, arm, sizeof(arm));
+      ctx->sync();
     } else if (fault != GRADA_FAULT_NONE) {
       throw grada::Error(GRADA_ERR_INVALID_ARGUMENT, "unknown fault kind");
     } else {
       ctx->inject_alloc_failure = false;
       ctx->inject_cg_wait = false;
+      if (ctx->tc_err.ptr) {
+        GRADA_CUDA_CHECK(cudaMemsetAsync(ctx->tc_err.ptr, 0, sizeof(int) * 4, ctx->stream));
+        ctx->sync();
+      }
     }
   });
 }

@@ -67,7 +67,7 @@ void Context::check_tc_error() {
   sync();
   const int e = h_bflag[kBW];
   if (e) {
-    GRADA_CUDA_CHECK(cudaMemsetAsync(tc_err.ptr, 0, sizeof(int), stream));
+    GRADA_CUDA_CHECK(cudaMemsetAsync(tc_err.ptr, 0, sizeof(int) * 2, stream));  // flags, test arm
     sync();
     throw Error(GRADA_ERR_CUDA, "tensor-core block product: a bounded wait expired (flags " +
                                     std::to_string(e) + ")");

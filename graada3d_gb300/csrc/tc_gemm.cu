@@ -179,18 +179,40 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
+// Non-blocking test of the phase of parity `parity` of `bar`.
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 // Bounded wait for the phase of parity `parity` of `bar`.  Returns false when
 // the CTA is aborting (watch_abort) or the time limit ran out; the latter
-// raises the abort flag and `code` in err.
+// raises the abort flag and `code` in err.  limit_ns = 0 (the expiry test of
+// grada_inject_fault) does not wait at all: a phase not complete at the first
+// test expires.
 __device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *err,
-                          int code, bool watch_abort = true) {
+                          int code, uint64_t limit_ns, bool watch_abort = true) {
+  if (limit_ns == 0) {
+    if (mbar_test(bar, parity)) return true;
+    if (watch_abort && *abort_flag) return false;
+    *abort_flag = 1;
+    atomicOr(err, code);
+    return false;
+  }
   if (mbar_try(bar, parity)) return true;
   const uint64_t t0 = gtimer();
   for (uint32_t n = 1;; n++) {
     if (mbar_try(bar, parity)) return true;
     if ((n & 15) == 0) {
       if (watch_abort && *abort_flag) return false;
-      if (gtimer() - t0 > kWaitLimitNs) {
+      if (gtimer() - t0 > limit_ns) {
         *abort_flag = 1;
         atomicOr(err, code);
         return false;
@@ -342,6 +364,9 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
 
+  // main-loop waits: the usual limit, or none at all while the expiry test of
+  // grada_inject_fault (err[1]) is armed; drains always keep the usual limit
+  const uint64_t wait_ns = (p.err && p.err[1]) ? 0ull : kWaitLimitNs;
   const int n_units = p.n_mtiles * p.n_splits;
   auto unit_mtile = [&](int u) { return u % p.n_mtiles; };
   auto unit_split = [&](int u) { return u / p.n_mtiles; };
@@ -362,7 +387,7 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
         for (int ks = k0; ks < k1; ks++, it++) {
           const int s = (int)(it % C::STAGES);
           const uint32_t ph = (it / C::STAGES) & 1u;
-          if (!mbar_wait(smem_u32(&bar_empty[s]), ph ^ 1u, &abort_flag, p.err, TCERR_PRODUCER)) {
+          if (!mbar_wait(smem_u32(&bar_empty[s]), ph ^ 1u, &abort_flag, p.err, TCERR_PRODUCER, wait_ns)) {
             ok = false;
             break;
           }
@@ -389,7 +414,7 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
       for (uint32_t q = 0; q < n_out; q++) {
         const uint32_t j = it - 1 - q;
         mbar_wait(smem_u32(&bar_full[j % C::STAGES]), (j / C::STAGES) & 1u, &abort_flag, p.err,
-                  TCERR_DRAIN, false);
+                  TCERR_DRAIN, kWaitLimitNs, false);
       }
     }
   } else if (warp == 1) {
@@ -410,7 +435,7 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
         const int acc = (int)(uc & 1u);
         const uint32_t aph = (uc >> 1) & 1u;
         if (!mbar_wait(smem_u32(&bar_acc_empty[acc]), aph ^ 1u, &abort_flag, p.err,
-                       TCERR_MMA_ACC)) {
+                       TCERR_MMA_ACC, wait_ns)) {
           ok = false;
           break;
         }
@@ -434,14 +459,14 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
             wb = smem_u32(&bar_full[s]);
             a_s = stage_a(s);
           }
-          if (!mbar_wait(wb, ph, &abort_flag, p.err, TCERR_MMA_FULL)) {
+          if (!mbar_wait(wb, ph, &abort_flag, p.err, TCERR_MMA_FULL, wait_ns)) {
             ok = false;
             break;
           }
           if constexpr (C::split_a) {
             // the right-hand-side tile comes straight from the TMA stage
             if (!mbar_wait(smem_u32(&bar_full[s]), (it / C::STAGES) & 1u, &abort_flag, p.err,
-                           TCERR_MMA_FULL)) {
+                           TCERR_MMA_FULL, wait_ns)) {
               ok = false;
               break;
             }
@@ -468,7 +493,7 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
       }
       // all MMAs of this thread complete before the CTA releases TMEM
       mma_commit(smem_u32(&bar_drain));
-      mbar_wait(smem_u32(&bar_drain), 0, &abort_flag, p.err, TCERR_DRAIN, false);
+      mbar_wait(smem_u32(&bar_drain), 0, &abort_flag, p.err, TCERR_DRAIN, kWaitLimitNs, false);
     }
   } else if (C::split_a && warp < C::W_EPI0) {
     // ---------------- TF32 split (and K-major transpose) of the G tile ----------
@@ -490,8 +515,8 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
         const uint32_t ph = (it / C::STAGES) & 1u;
         const int c = (int)(it % NCS);
         const uint32_t cph = (it / NCS) & 1u;
-        if (!mbar_wait(smem_u32(&bar_full[s]), ph, &abort_flag, p.err, TCERR_CONVERT) ||
-            !mbar_wait(smem_u32(&bar_cempty[c]), cph ^ 1u, &abort_flag, p.err, TCERR_CONVERT)) {
+        if (!mbar_wait(smem_u32(&bar_full[s]), ph, &abort_flag, p.err, TCERR_CONVERT, wait_ns) ||
+            !mbar_wait(smem_u32(&bar_cempty[c]), cph ^ 1u, &abort_flag, p.err, TCERR_CONVERT, wait_ns)) {
           ok = false;
           break;
         }
@@ -558,7 +583,7 @@ __global__ void __launch_bounds__(EltCfg<ELT>::THREADS, 1)
     for (int u = blockIdx.x; u < n_units; u += gridDim.x, uc++) {
       const int acc = (int)(uc & 1u);
       const uint32_t aph = (uc >> 1) & 1u;
-      if (!mbar_wait(smem_u32(&bar_acc_full[acc]), aph, &abort_flag, p.err, TCERR_EPILOGUE))
+      if (!mbar_wait(smem_u32(&bar_acc_full[acc]), aph, &abort_flag, p.err, TCERR_EPILOGUE, wait_ns))
         break;
       tc_fence_after();
       __syncwarp();

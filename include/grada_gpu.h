@@ -510,13 +510,18 @@ int grada_refinement_indicator(grada_ctx *ctx, const double *m, const int64_t *r
  * the next block product returns GRADA_ERR_CUDA.  GRADA_FAULT_CG_WAIT: the
  * next persistent CG solve (stored dense G) runs with a zero limit on its grid
  * barriers' waits, so a real device-side wait expires: every CTA returns, the
- * solve returns GRADA_ERR_CUDA.  GRADA_FAULT_NONE clears pending faults.  The
- * context stays usable after each.
+ * solve returns GRADA_ERR_CUDA.  GRADA_FAULT_TC_WAIT: the next tensor-core
+ * block products run their main-loop mbarrier waits with no time at all, so a
+ * real wait expires on the device: the CTA stops issuing, drains its own TMA
+ * loads and MMAs (with the usual limit), frees its tensor memory and exits,
+ * and the product returns GRADA_ERR_CUDA.  GRADA_FAULT_NONE clears pending
+ * faults.  The context stays usable after each.
  */
 #define GRADA_FAULT_NONE 0
 #define GRADA_FAULT_ALLOC 1
 #define GRADA_FAULT_TC_TIMEOUT 2
 #define GRADA_FAULT_CG_WAIT 3
+#define GRADA_FAULT_TC_WAIT 4
 int grada_inject_fault(grada_ctx *ctx, int fault);
 
 #ifdef __cplusplus

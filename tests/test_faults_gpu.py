@@ -1,7 +1,9 @@
 """Failure handling without a GPU fault: faults are injected on the host
 (grada_inject_fault) and every call reports a status and leaves the context
-usable -- a failed device allocation, the expiry flag of a tensor-core wait,
-non-finite input, empty or malformed geometry."""
+usable -- a failed device allocation, the expiry flag of a tensor-core wait, a
+real expiry of the tensor-core kernels' bounded mbarrier waits (their main-loop
+limit set to nothing, the drains kept), non-finite input, empty or malformed
+geometry."""
 import numpy as np
 import pytest
 
@@ -10,7 +12,7 @@ from graada3d_gb300.inversion import GaussNewtonInversion
 
 pytestmark = pytest.mark.gpu
 
-FAULT_ALLOC, FAULT_TC_TIMEOUT = 1, 2
+FAULT_ALLOC, FAULT_TC_TIMEOUT, FAULT_TC_WAIT = 1, 2, 4
 ERR_CUDA, ERR_OOM, ERR_NONFINITE, ERR_INVALID = -2, -3, -5, -1
 
 
@@ -50,6 +52,22 @@ def test_tensor_core_wait_expiry_is_reported_and_cleared(gpu_ctx):
         inv.G_mat_mul(X)
     assert _status(e) == ERR_CUDA and "bounded wait" in str(e.value)
     np.testing.assert_array_equal(inv.G_mat_mul(X), good)  # context usable, same result
+
+
+@pytest.mark.parametrize("storage", ["bf16", "fp32"])
+def test_tensor_core_real_wait_expiry_then_same_product(gpu_ctx, storage):
+    inv = _inv(gpu_ctx)
+    inv.compute_G(storage)
+    X = np.random.default_rng(2).standard_normal((inv.Nm, 16))
+    Y = np.random.default_rng(3).standard_normal((inv.Nd, 16))
+    good = inv.G_mat_mul(X)
+    good_t = inv.GT_mat_mul(Y)
+    gpu_ctx.check(gpu_ctx.lib.grada_inject_fault(gpu_ctx.handle, FAULT_TC_WAIT))
+    with pytest.raises(GradaError) as e:
+        inv.G_mat_mul(X)
+    assert _status(e) == ERR_CUDA and "bounded wait" in str(e.value)
+    np.testing.assert_array_equal(inv.G_mat_mul(X), good)  # TMEM freed, context usable
+    np.testing.assert_array_equal(inv.GT_mat_mul(Y), good_t)
 
 
 def test_nonfinite_and_malformed_inputs(gpu_ctx):
