@@ -412,6 +412,15 @@ INVERSION_CASES = {
     "l1_refined": dict(cells="dyke_refined", domain=(10000.0, 10000.0, 5000.0), obs=(101, 101),
                        height=100.0, mask=0x072, lp=[1, 1, 1, 1, 2], eps2=1e-10, boxes="dykes",
                        gn_iter=10),
+    # the same refined problem with a schedule under which the runs reach chi^2 = N:
+    # lambda_0 = 1e-4 halved per trial, up to 200 CG iterations per solve and a
+    # 0.5 % stagnation test (with at most 50 CG iterations every format stops on
+    # stagnation at a misfit near 1.5; schedules with lambda_0 = 0.1, 1e-3 and
+    # rates 0.3-0.6 reach it with 5,200-7,600 CG iterations, this one with the fewest)
+    "l1_refined_chi2": dict(cells="dyke_refined", domain=(10000.0, 10000.0, 5000.0),
+                            obs=(101, 101), height=100.0, mask=0x072, lp=[1, 1, 1, 1, 2],
+                            eps2=1e-10, boxes="dykes", gn_iter=10,
+                            prm=dict(max_lambda=1e-4, rate=0.5, cg_factor=200, stag=0.005)),
 }
 
 
@@ -469,8 +478,11 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16", "fp32+fp6
     nm = inv.Nm
     prm = dict(max_lambda=1e-1, n_lambda=30, rate=0.6, target=1.0, stag=0.02, cg_tol=1e-6,
                cg_factor=50, gn_iter=c["gn_iter"], lp=c["lp"], eps2=c["eps2"])
+    prm.update(c.get("prm", {}))
     args = (np.zeros(nm), np.full(nm, -1000.0), np.full(nm, 1000.0))
-    out = {"case": name, "cells": nm, "data": inv.Nd, "lp": c["lp"][0]}
+    out = {"case": name, "cells": nm, "data": inv.Nd, "lp": c["lp"][0],
+           "schedule": {k: prm[k] for k in ("max_lambda", "n_lambda", "rate", "stag", "cg_tol",
+                                             "cg_factor", "gn_iter", "target")}}
     m64 = None
     for st in storages:
         torch.cuda.synchronize()
@@ -1279,6 +1291,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="bench", choices=["bench", "profile", "inversion-l2-16k",
                                                          "inversion-l1-196k", "inversion-l1-refined",
+                                                         "inversion-l1-refined-chi2",
                                                          "matrix-free-1m",
                                                          "gemv", "batched-64", "block-gemm",
                                                          "lambda-sweep-16", "block-gemm-profile",
@@ -1295,6 +1308,8 @@ def main():
     ap.add_argument("--no-block", action="store_true")
     ap.add_argument("--sweep-storages", default="fp64,fp32,bf16,fp32+fp64,bf16+fp64")
     ap.add_argument("--no-sequential", action="store_true")
+    ap.add_argument("--storages", default=None,
+                    help="G storages of an --case inversion-* run, e.g. fp64,fp32+fp64")
     args = ap.parse_args()
     if args.case == "profile":
         run_profile_case(args)
@@ -1326,7 +1341,9 @@ def main():
     elif args.case == "matrix-free-1m":
         print(json.dumps(run_matrix_free_1m()))
     elif args.case.startswith("inversion-"):
-        print(json.dumps(run_inversion(args.case.split("-", 1)[1].replace("-", "_"))))
+        name = args.case.split("-", 1)[1].replace("-", "_")
+        st = tuple(args.storages.split(",")) if args.storages else None
+        print(json.dumps(run_inversion(name, st) if st else run_inversion(name)))
     elif args.impl == "reference":
         run_reference(args)
     else:

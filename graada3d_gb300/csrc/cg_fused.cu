@@ -2,28 +2,17 @@
 //
 // Reference: GaussNewtonInversion::solve_cg, the iteration loop
 // (src/Inversion/GaussNewtonInversion.cpp:1556-1692).  The graph-replayed
-// iteration (inversion.cu) launches 13 kernels per iteration; at the sizes of
-// small inversions those launches, not the two reads of G, set the time.
-// Here every CTA of a cooperative grid (all co-resident) runs the iteration's
-// phases in turn, separated by grid barriers, and decides the stopping test
-// itself from the same reduced scalars, so no host round trip or launch
-// happens until the solve ends.  Each phase runs the blocks of the
-// corresponding stand-alone kernel (gemv_body.cuh, cg_body.cuh) with the same
-// arithmetic and summation orders, so the iterates are bitwise those of the
-// graph path.  Phases per iteration:
-//   P    p = -r + beta p, pp = P p
-//   G1   partial row sums of G pp over column ranges
-//   G2   t_data = Wd (sum of partials) and the forward regulariser rows of t
-//   D1   block partials of ||t||^2
-//   S    alpha = r2 / t2; s += alpha t, dx += alpha p, and y = Wd s_data in
-//        G's accumulation type (each thread converts the entries it updated)
-//   GT   G^T y for 4 columns per block, then r for those columns (the adjoint
-//        of the regulariser rows and P) in the same block
-//   D2   block partials of ||r||^2; beta, err and the stopping test
-// Seven grid barriers per iteration.  Every barrier wait is bounded (a
-// globaltimer limit): a CTA whose wait expires raises the barrier's error word
-// and returns, every other CTA returns at its next barrier, and the host turns
-// the word into GRADA_ERR_CUDA with the context still usable.
+// iteration (inversion.cu) launches 13 kernels per iteration.  Here every CTA
+// of a cooperative grid (all co-resident) runs the iteration's phases in turn
+// (cg_fused.cuh: four team barriers per iteration) and decides the stopping
+// test itself from the same reduced scalars, so no host round trip or launch
+// happens until the solve ends.  The sums are fixed-order and independent of
+// the grid, so a solve is deterministic and gives what the batched kernel
+// (invert_batch.cu) gives for the same problem; against the graph path it
+// agrees to rounding (different summation orders).  Every barrier wait is
+// bounded (a globaltimer limit): a CTA whose wait expires raises the barrier's
+// error word and returns, every other CTA returns at its next barrier, and the
+// host turns the word into GRADA_ERR_CUDA with the context still usable.
 #include <algorithm>
 
 #include "cg_fused.cuh"
@@ -35,7 +24,7 @@ namespace {
 // One solve on the whole cooperative grid: the loop starts from the scalars
 // and control block the host setup left in a.scal / a.ctl and writes them back.
 template <class L>
-__global__ void __launch_bounds__(256) cg_fused_kernel(FusedCgArgs a) {
+__global__ void __launch_bounds__(256, 3) cg_fused_kernel(FusedCgArgs a) {
   fused::TeamBarrier bar(a.barrier, gridDim.x, blockIdx.x, a.wait_limit_ns);
   fused::CgIn in;
   in.R2 = __ldcg(a.scal + CG_R2);

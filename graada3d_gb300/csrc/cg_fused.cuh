@@ -108,51 +108,106 @@ struct TeamBarrier {
   }
 };
 
-// Deterministic two-level sum of per-block partials: block b writes
-// partial[b]; the last block of each group of kGroup blocks to finish (an
-// atomic count) adds its group's partials in index order into group[b /
-// kGroup] and resets the count.  After a barrier every CTA adds the groups in
-// index order.  The result depends only on the partition into blocks, not on
-// which CTA ran which block or when.
-constexpr int kGroup = 32;
-
-__device__ __forceinline__ void publish_partial(double v, int64_t b, int64_t nb, double *partial,
-                                                double *group, unsigned *count) {
-  __shared__ int s_last;
-  if (threadIdx.x == 0) {
-    partial[b] = v;
-    __threadfence();
-    const int64_t gi = b / kGroup;
-    const int64_t g0 = gi * kGroup;
-    const unsigned gsize = (unsigned)((nb - g0) < kGroup ? (nb - g0) : kGroup);
-    s_last = (atomicAdd(count + gi, 1u) + 1u == gsize) ? 1 : 0;
-  }
-  __syncthreads();
-  if (s_last) {
-    const int64_t gi = b / kGroup;
-    const int64_t g0 = gi * kGroup;
-    const int64_t ge = (g0 + kGroup < nb) ? g0 + kGroup : nb;
-    if (threadIdx.x < 32) {
-      __threadfence();
-      double x = (g0 + threadIdx.x < ge) ? __ldcg(partial + g0 + threadIdx.x) : 0.0;
-      x = cgb::warp_sum(x);
-      if (threadIdx.x == 0) {
-        group[gi] = x;
-        count[gi] = 0u;
-      }
-    }
-  }
-  __syncthreads();
-}
-
-// Sum of the ngroups group sums in index order (fixed tree); every thread
-// gets it.
-__device__ __forceinline__ double sum_groups(const double *group, int64_t ngroups) {
+// Sum of the n per-block partials in index order (each thread a fixed stride,
+// then the block's fixed tree); every thread of every CTA gets the same value.
+__device__ __forceinline__ double sum_partials_all(const double *partial, int64_t n) {
   double v = 0.0;
-  for (int64_t i = threadIdx.x; i < ngroups; i += cgb::VT) v += __ldcg(group + i);
+  for (int64_t i = threadIdx.x; i < n; i += cgb::VT) v += __ldcg(partial + i);
   return bcast_sum(v);
 }
 
+// Rows per finish block and columns per G^T block of the persistent loop.
+constexpr int kFinRows = 32;
+constexpr int kGtWarpCols = 4;                        // columns per warp
+constexpr int kGtBlockCols = kGtWarpCols * (cgb::VT / 32);  // 32 per block
+
+// G pp's rows r0 .. r0 + 31 (block b): the split partial sums added by 8 warps
+// (warp w takes splits w, w + 8, ...) and the 8 sums in warp order; times the
+// row scale and Wd.  Returns t_r^2 for the block's rows, summed (valid in
+// every thread).
+__device__ __forceinline__ double finish_rows(const double *partial, int n_split, int64_t ld,
+                                             int64_t nd, const float *__restrict__ row_scale,
+                                             const double *__restrict__ wd, double *t,
+                                             int64_t b) {
+  __shared__ double part[cgb::VT / 32][kFinRows];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t r = b * kFinRows + lane;
+  double s = 0.0;
+  if (r < nd)
+    for (int k = warp; k < n_split; k += cgb::VT / 32) s += __ldcg(partial + (int64_t)k * ld + r);
+  __syncthreads();
+  part[warp][lane] = s;
+  __syncthreads();
+  double sq = 0.0;
+  if (warp == 0) {
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < cgb::VT / 32; w++) v += part[w][lane];
+    if (r < nd) {
+      if (row_scale) v *= (double)row_scale[r];
+      v *= wd[r];
+      t[r] = v;
+      sq = v * v;
+    }
+  }
+  return bcast_sum(sq);
+}
+
+// G^T y for the 32 columns of block b (warp w: columns 4w .. 4w + 3, lanes
+// striding the rows), then r_j for those columns (the adjoint of the
+// regulariser rows and P) by lanes 0-3 of each warp.  Writes gtw and r;
+// returns the block's sum of r_j^2 (valid in every thread).
+template <class L>
+__device__ __forceinline__ double gty_adjoint_block(const FusedCgArgs &a, const typename L::Acc *y,
+                                                    int64_t b) {
+  using Acc = typename L::Acc;
+  constexpr int VEC = L::VEC;
+  __shared__ double wsum[cgb::VT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t c0 = b * kGtBlockCols + (int64_t)warp * kGtWarpCols;
+  const int ncol = (int)max((int64_t)0, min((int64_t)kGtWarpCols, a.nm - c0));
+  Acc acc[kGtWarpCols];
+#pragma unroll
+  for (int c = 0; c < kGtWarpCols; c++) acc[c] = Acc(0);
+  if (ncol > 0) {
+    for (int64_t row = (int64_t)lane * VEC; row < a.ld; row += 32 * VEC) {
+      Acc yv[VEC];
+#pragma unroll
+      for (int v = 0; v < VEC; v++) yv[v] = __ldcg(y + row + v);
+#pragma unroll
+      for (int c = 0; c < kGtWarpCols; c++) {
+        if (c < ncol) {
+          Acc g[VEC];
+          L::load(a.G, row + (c0 + c) * a.ld, g);
+#pragma unroll
+          for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
+        }
+      }
+    }
+  }
+  double mine = 0.0;
+#pragma unroll
+  for (int c = 0; c < kGtWarpCols; c++) {
+    const double v = cgb::warp_sum((double)acc[c]);
+    if (lane == c) mine = v;
+  }
+  double sq = 0.0;
+  if (lane < ncol) {
+    const int64_t j = c0 + lane;
+    a.gtw[j] = mine;
+    const double rj = cgb::adjoint_column(a.AT, j, a.P, true, mine, 1.0);
+    a.r[j] = rj;
+    sq = rj * rj;
+  }
+  sq = cgb::warp_sum(sq);
+  __syncthreads();
+  if (lane == 0) wsum[warp] = sq;
+  __syncthreads();
+  double tot = 0.0;
+#pragma unroll
+  for (int w = 0; w < cgb::VT / 32; w++) tot += wsum[w];
+  return tot;
+}
 
 // Scalars a solve's loop starts from (the setup's) and ends with.
 struct CgIn {
@@ -165,18 +220,17 @@ struct CgOut {
   bool ok = true;  // false: a barrier wait expired (the team abandons its work)
 };
 
-// Layout of a.red for a loop: partials and group sums of ||t||^2 over the
-// G2 blocks, then of ||r||^2 over the G^T blocks.
+// Layout of a.red for a loop: per-block partials of ||t||^2 over the finish
+// and forward-row blocks, then of ||r||^2 over the G^T blocks.
 struct RedLayout {
-  int64_t nb_t, ng_t, nb_r, ng_r;
+  int64_t nb_fin, nb_t, nb_r;
   __host__ __device__ RedLayout(int64_t nd, int64_t nm, int nterms) {
-    nb_t = ceil_div_d(nd, 256) + (int64_t)nterms * ceil_div_d(nm, 256);
-    ng_t = ceil_div_d(nb_t, kGroup);
-    nb_r = ceil_div_d(nm, gemv::kGtCols);
-    ng_r = ceil_div_d(nb_r, kGroup);
+    nb_fin = ceil_div_d(nd, kFinRows);
+    nb_t = nb_fin + (int64_t)nterms * ceil_div_d(nm, 256);
+    nb_r = ceil_div_d(nm, kGtBlockCols);
   }
-  __host__ __device__ int64_t doubles() const { return nb_t + ng_t + nb_r + ng_r; }
-  __host__ __device__ int64_t counters() const { return ng_t + ng_r; }
+  __host__ __device__ int64_t doubles() const { return nb_t + nb_r; }
+  __host__ __device__ int64_t counters() const { return 1; }
 };
 
 // The loop of one solve, run by CTA `cta` of the nct CTAs of its team, from
@@ -184,29 +238,26 @@ struct RedLayout {
 // Four team barriers per iteration:
 //   A  p_new = -r + beta p_old and pp = P p_new folded into the partial row
 //      sums of G pp (column ranges x row tiles)
-//   B  t_data = Wd (sum of partials), the forward regulariser rows of t, and
-//      per-block partials of ||t||^2
+//   B  t_data = Wd (sum of the partials, 32 rows per block, the splits shared
+//      by 8 warps), the forward regulariser rows of t, per-block ||t||^2
 //   C  alpha = r2 / t2; s += alpha t, dx += alpha p_new, y = Wd s_data in G's
 //      accumulation type
-//   D  G^T y for 4 columns per block, r for those columns (adjoint of the
-//      regulariser rows, P), per-block partials of ||r||^2; then beta, err
+//   D  G^T y for 32 columns per block (4 per warp), r for those columns (the
+//      adjoint of the regulariser rows, P), per-block ||r||^2; then beta, err
 //      and the stopping test
-// The sums of squares are reduced by blocks and groups in index order, so
-// the result does not depend on the team size.
+// Every CTA adds the per-block partials in index order, so the sums do not
+// depend on the team size or on which CTA ran which block.
 template <class L>
 __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, unsigned nct,
                          TeamBarrier &bar) {
   using Acc = typename L::Acc;
   const int64_t Nm = a.nm, nd = a.nd, ld = a.ld, nrow = a.nrow;
   const int64_t nb_vec = ceil_div_d(Nm, cgb::VT);  // blocks of an Nm-long vector
-  const int64_t nb_fin = ceil_div_d(nd, 256);
   const int64_t nb_axpy = ceil_div_d(nrow > Nm ? nrow : Nm, cgb::VT);
   const int64_t nb_prep = ceil_div_d(ld, 256);
   const int64_t n_gx = (int64_t)a.tiles * a.splits;
   const RedLayout rl(nd, Nm, a.FT.count);
-  double *part_t = a.red, *grp_t = part_t + rl.nb_t;
-  double *part_r = grp_t + rl.ng_t, *grp_r = part_r + rl.nb_r;
-  unsigned *cnt_t = a.red_count, *cnt_r = cnt_t + rl.ng_t;
+  double *part_t = a.red, *part_r = a.red + rl.nb_t;
   Acc *y = reinterpret_cast<Acc *>(a.scratch);
 
   CgOut o;
@@ -227,29 +278,26 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
     if (!(ok = bar.sync())) break;
     // B
     for (int64_t b = cta; b < rl.nb_t; b += nct) {
-      double v = 0.0;
-      if (b < nb_fin) {
-        const int64_t rr = b * 256 + threadIdx.x;
-        gemv::gx_finish_body(a.scratch, a.splits, ld, nd, a.row_scale, a.wd, a.t, b);
-        if (rr < nd) {
-          const double tv = __ldcg(a.t + rr);
-          v = tv * tv;
-        }
+      double v;
+      if (b < rl.nb_fin) {
+        v = finish_rows(a.scratch, a.splits, ld, nd, a.row_scale, a.wd, a.t, b);
       } else {
-        const int64_t k = b - nb_fin;
+        const int64_t k = b - rl.nb_fin;
         const ForwardTerm &ft = a.FT.t[k / nb_vec];
         cgb::forward_term_body(ft, a.pp, k % nb_vec);
         const int64_t i = (k % nb_vec) * cgb::VT + threadIdx.x;
+        double q = 0.0;
         if (i < Nm) {
           const double tv = __ldcg(ft.out + i);
-          v = tv * tv;
+          q = tv * tv;
         }
+        v = bcast_sum(q);
       }
-      publish_partial(cgb::block_sum(v), b, rl.nb_t, part_t, grp_t, cnt_t);
+      if (threadIdx.x == 0) part_t[b] = v;
     }
     if (!(ok = bar.sync())) break;
     // C
-    T2 = sum_groups(grp_t, rl.ng_t);
+    T2 = sum_partials_all(part_t, rl.nb_t);
     alpha = R2 / T2;  // GaussNewtonInversion.cpp:1601
     if (T2 == 0.0 || !isfinite(alpha)) {
       status = (T2 == 0.0) ? CG_STATUS_BREAKDOWN : CG_STATUS_NONFINITE;
@@ -262,20 +310,11 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
     if (!(ok = bar.sync())) break;
     // D
     for (int64_t b = cta; b < rl.nb_r; b += nct) {
-      int ncol = 0;
-      const double g = gemv::gty_body<L>(a.G, ld, Nm, y, b, &ncol);
-      double v = 0.0;
-      if ((int)threadIdx.x < ncol) {
-        const int64_t j = b * gemv::kGtCols + threadIdx.x;
-        a.gtw[j] = g;
-        const double rj = cgb::adjoint_column(a.AT, j, a.P, true, g, 1.0);
-        a.r[j] = rj;
-        v = rj * rj;
-      }
-      publish_partial(cgb::block_sum(v), b, rl.nb_r, part_r, grp_r, cnt_r);
+      const double v = gty_adjoint_block<L>(a, y, b);
+      if (threadIdx.x == 0) part_r[b] = v;
     }
     if (!(ok = bar.sync())) break;
-    const double r2 = sum_groups(grp_r, rl.ng_r);
+    const double r2 = sum_partials_all(part_r, rl.nb_r);
     // :1674-1691
     rlast2 = R2;
     R2 = r2;
