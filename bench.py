@@ -502,7 +502,8 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16", "fp32+fp6
         if st == "fp64":
             m64 = m
         else:
-            r["model_rel_diff_vs_fp64"] = float(np.linalg.norm(m - m64) / np.linalg.norm(m64))
+            if m64 is not None:
+                r["model_rel_diff_vs_fp64"] = float(np.linalg.norm(m - m64) / np.linalg.norm(m64))
             r["fp64_refinements"] = int(rep["fp64_refinements"])
         out[st] = r
     if "fp64" in out:
