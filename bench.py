@@ -385,8 +385,12 @@ def run_gpu(args):
             line["block_products"] = block_products_summary()
         if world == 1 and not args.no_inversion:
             # second half of the metric: inversion time to chi^2 = N, mixed precision vs
-            # all-FP64 (16,384 cells; the 196,608-cell L1 run is --case inversion-l1-196k)
+            # all-FP64 -- the 16,384-cell L2 problem and the L1 problem on the
+            # 236,226-leaf refined dyke mesh (gz, Tzz, Txz, Tyz at 101 x 101 points)
             line["inversion"] = run_inversion("l2_16k")
+            if not args.no_refined_inversion:
+                line["inversion_refined"] = run_inversion(
+                    "l1_refined_chi2", ("fp64", "fp32+fp64", "bf16+fp64", "fp16+fp64"))
         if world == 1 and not args.no_cpu_baseline:
             cb = cpu_sample(prisms, obs, target_s=args.ref_seconds)
             cb.pop("seconds", None)
@@ -1306,6 +1310,8 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-inversion", action="store_true")
+    ap.add_argument("--no-refined-inversion", action="store_true",
+                    help="skip the refined-mesh L1 inversion (about five minutes)")
     ap.add_argument("--no-block", action="store_true")
     ap.add_argument("--sweep-storages", default="fp64,fp32,bf16,fp32+fp64,bf16+fp64")
     ap.add_argument("--no-sequential", action="store_true")
