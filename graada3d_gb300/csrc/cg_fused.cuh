@@ -116,10 +116,8 @@ __device__ __forceinline__ double sum_partials_all(const double *partial, int64_
   return bcast_sum(v);
 }
 
-// Rows per finish block and columns per G^T block of the persistent loop.
+// Rows per finish block of the persistent loop.
 constexpr int kFinRows = 32;
-constexpr int kGtWarpCols = 4;                        // columns per warp
-constexpr int kGtBlockCols = kGtWarpCols * (cgb::VT / 32);  // 32 per block
 
 // G pp's rows r0 .. r0 + 31 (block b): the split partial sums added by 8 warps
 // (warp w takes splits w, w + 8, ...) and the 8 sums in warp order; times the
@@ -153,49 +151,21 @@ __device__ __forceinline__ double finish_rows(const double *partial, int n_split
   return bcast_sum(sq);
 }
 
-// G^T y for the 32 columns of block b (warp w: columns 4w .. 4w + 3, lanes
-// striding the rows), then r_j for those columns (the adjoint of the
-// regulariser rows and P) by lanes 0-3 of each warp.  Writes gtw and r;
-// returns the block's sum of r_j^2 (valid in every thread).
+// G^T y for the 32 columns of block b (gemv::gty_body: warp w takes columns
+// 4w .. 4w + 3, lanes striding the rows), then r_j for those columns (the
+// adjoint of the regulariser rows and P) on the lanes holding a column.
+// Writes gtw and r; returns the block's sum of r_j^2 (valid in every thread).
 template <class L>
 __device__ __forceinline__ double gty_adjoint_block(const FusedCgArgs &a, const typename L::Acc *y,
                                                     int64_t b) {
-  using Acc = typename L::Acc;
-  constexpr int VEC = L::VEC;
   __shared__ double wsum[cgb::VT / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t c0 = b * kGtBlockCols + (int64_t)warp * kGtWarpCols;
-  const int ncol = (int)max((int64_t)0, min((int64_t)kGtWarpCols, a.nm - c0));
-  Acc acc[kGtWarpCols];
-#pragma unroll
-  for (int c = 0; c < kGtWarpCols; c++) acc[c] = Acc(0);
-  if (ncol > 0) {
-    for (int64_t row = (int64_t)lane * VEC; row < a.ld; row += 32 * VEC) {
-      Acc yv[VEC];
-#pragma unroll
-      for (int v = 0; v < VEC; v++) yv[v] = __ldcg(y + row + v);
-#pragma unroll
-      for (int c = 0; c < kGtWarpCols; c++) {
-        if (c < ncol) {
-          Acc g[VEC];
-          L::load(a.G, row + (c0 + c) * a.ld, g);
-#pragma unroll
-          for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
-        }
-      }
-    }
-  }
-  double mine = 0.0;
-#pragma unroll
-  for (int c = 0; c < kGtWarpCols; c++) {
-    const double v = cgb::warp_sum((double)acc[c]);
-    if (lane == c) mine = v;
-  }
+  int64_t j = -1;
+  const double g = gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j);
   double sq = 0.0;
-  if (lane < ncol) {
-    const int64_t j = c0 + lane;
-    a.gtw[j] = mine;
-    const double rj = cgb::adjoint_column(a.AT, j, a.P, true, mine, 1.0);
+  if (j >= 0) {
+    a.gtw[j] = g;
+    const double rj = cgb::adjoint_column(a.AT, j, a.P, true, g, 1.0);
     a.r[j] = rj;
     sq = rj * rj;
   }
@@ -227,7 +197,7 @@ struct RedLayout {
   __host__ __device__ RedLayout(int64_t nd, int64_t nm, int nterms) {
     nb_fin = ceil_div_d(nd, kFinRows);
     nb_t = nb_fin + (int64_t)nterms * ceil_div_d(nm, 256);
-    nb_r = ceil_div_d(nm, kGtBlockCols);
+    nb_r = ceil_div_d(nm, gemv::kGtBlockCols);
   }
   __host__ __device__ int64_t doubles() const { return nb_t + nb_r; }
   __host__ __device__ int64_t counters() const { return 1; }

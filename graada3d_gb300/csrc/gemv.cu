@@ -8,13 +8,14 @@
 // Both products stream G once from HBM with 16-byte vector loads and are
 // bound by HBM bandwidth.  G is column-major with leading dimension ld (a
 // multiple of 64, padding rows zero), so:
-//  * G^T y: a block owns COLS consecutive columns; each thread walks the rows
-//    with 16-byte loads, multiplies by y (loaded once per row chunk and reused
-//    for the block's COLS columns) and the block reduces COLS sums with warp
-//    shuffles.  Deterministic: fixed per-thread row order and reduction tree.
+//  * G^T y: a block owns 32 consecutive columns, 4 per warp; the lanes walk
+//    the rows with 16-byte loads, multiply by y (loaded once per row chunk
+//    and reused for the warp's 4 columns) and each column is summed with a
+//    warp butterfly.  Deterministic: fixed per-lane row order and tree.
 //  * G x: a block owns a tile of 256*VEC rows and a range of columns; threads
 //    accumulate VEC rows each over that range; the column ranges' partial rows
-//    go to scratch and a second pass sums them in split order (deterministic,
+//    go to scratch and a second pass sums them (32 rows per block, the ranges
+//    shared by the block's 8 warps, then added in warp order; deterministic,
 //    no atomics).
 // FP64 G accumulates in FP64.  FP32 / bf16 G multiply and accumulate in FP32
 // (the vector is rounded to FP32 once); partial sums across blocks are added
@@ -54,15 +55,14 @@ __global__ void gx_finish_kernel(const double *partial, int n_split, int64_t ld,
 
 // ---- G^T y --------------------------------------------------------------------
 
-template <class L, int COLS>
+template <class L>
 __global__ void __launch_bounds__(GV_THREADS)
     gty_kernel(const void *__restrict__ G, int64_t ld, int64_t nm, const typename L::Acc *y,
                double *x, const int *__restrict__ skip) {
-  static_assert(COLS == gemv::kGtCols, "G^T y blocks have kGtCols columns");
   if (skip && *skip) return;
-  int ncol = 0;
-  const double s = gemv::gty_body<L>(G, ld, nm, y, blockIdx.x, &ncol);
-  if (threadIdx.x < ncol) x[(int64_t)blockIdx.x * COLS + threadIdx.x] = s;
+  int64_t col = -1;
+  const double s = gemv::gty_body<L>(G, ld, nm, y, blockIdx.x, &col);
+  if (col >= 0) x[col] = s;
 }
 
 // y (FP64, nd entries) -> padded vector of the accumulation type, times the
@@ -105,8 +105,8 @@ void run_gx(const DevG &G, const double *x, double *y, double *scratch, int sm_c
   dim3 grid((unsigned)ceil_div(G.ld, (int64_t)GV_THREADS * L::VEC), (unsigned)splits);
   gx_partial_kernel<L><<<grid, GV_THREADS, 0, s>>>(G.data, G.ld, G.nm, per, x, scratch, o.skip);
   GRADA_LAUNCH_CHECK();
-  gx_finish_kernel<<<(unsigned)ceil_div(G.nd, 256), 256, 0, s>>>(scratch, splits, G.ld, G.nd,
-                                                                 G.row_scale, o.scale, y, o.skip);
+  gx_finish_kernel<<<(unsigned)ceil_div(G.nd, gemv::kFinishRows), GV_THREADS, 0, s>>>(
+      scratch, splits, G.ld, G.nd, G.row_scale, o.scale, y, o.skip);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -195,8 +195,7 @@ void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratc
       prep_y_kernel<double><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, nullptr, o.scale, scratch,
                                                         o.skip);
       GRADA_LAUNCH_CHECK();
-      constexpr int COLS = 4;
-      gty_kernel<LoadF64, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
+      gty_kernel<LoadF64><<<(unsigned)ceil_div(G.nm, gemv::kGtBlockCols), GV_THREADS, 0, s>>>(
           G.data, G.ld, G.nm, scratch, x, o.skip);
       break;
     }
@@ -205,8 +204,7 @@ void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratc
       prep_y_kernel<float><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, nullptr, o.scale, y32,
                                                        o.skip);
       GRADA_LAUNCH_CHECK();
-      constexpr int COLS = 4;
-      gty_kernel<LoadF32, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
+      gty_kernel<LoadF32><<<(unsigned)ceil_div(G.nm, gemv::kGtBlockCols), GV_THREADS, 0, s>>>(
           G.data, G.ld, G.nm, y32, x, o.skip);
       break;
     }
@@ -215,8 +213,7 @@ void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratc
       prep_y_kernel<float><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, G.row_scale, o.scale, y32,
                                                        o.skip);
       GRADA_LAUNCH_CHECK();
-      constexpr int COLS = 4;
-      gty_kernel<LoadBF16, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
+      gty_kernel<LoadBF16><<<(unsigned)ceil_div(G.nm, gemv::kGtBlockCols), GV_THREADS, 0, s>>>(
           G.data, G.ld, G.nm, y32, x, o.skip);
       break;
     }
@@ -225,8 +222,7 @@ void launch_GT_vec_mul(const DevG &G, const double *y, double *x, double *scratc
       prep_y_kernel<float><<<prep_blocks, 256, 0, s>>>(y, G.nd, G.ld, G.row_scale, o.scale, y32,
                                                        o.skip);
       GRADA_LAUNCH_CHECK();
-      constexpr int COLS = 4;
-      gty_kernel<LoadF16, COLS><<<(unsigned)ceil_div(G.nm, COLS), GV_THREADS, 0, s>>>(
+      gty_kernel<LoadF16><<<(unsigned)ceil_div(G.nm, gemv::kGtBlockCols), GV_THREADS, 0, s>>>(
           G.data, G.ld, G.nm, y32, x, o.skip);
       break;
     }

@@ -21,7 +21,6 @@ namespace gemv {
 
 constexpr int kThreads = 256;  // threads of every product block
 constexpr int kXChunk = 256;   // x entries staged in shared memory at a time (G x)
-constexpr int kGtCols = 4;     // columns per G^T y block
 
 // ---- element loaders: VEC consecutive entries from a 16-byte load ----------
 
@@ -98,19 +97,16 @@ __device__ __forceinline__ void gx_partial_body(const void *__restrict__ G, int6
     if (row < ld) {
       const int64_t base = row + c0 * ld;
       int c = 0;
-      for (; c + 4 <= nc; c += 4) {
-        Acc g0[VEC], g1[VEC], g2[VEC], g3[VEC];
-        L::load(G, base + (int64_t)c * ld, g0);
-        L::load(G, base + (int64_t)(c + 1) * ld, g1);
-        L::load(G, base + (int64_t)(c + 2) * ld, g2);
-        L::load(G, base + (int64_t)(c + 3) * ld, g3);
-        const Acc x0 = xs[c], x1 = xs[c + 1], x2 = xs[c + 2], x3 = xs[c + 3];
+      // eight columns' loads in flight before their FMAs
+      for (; c + 8 <= nc; c += 8) {
+        Acc g[8][VEC];
 #pragma unroll
-        for (int v = 0; v < VEC; v++) {
-          acc[v] = fma(g0[v], x0, acc[v]);
-          acc[v] = fma(g1[v], x1, acc[v]);
-          acc[v] = fma(g2[v], x2, acc[v]);
-          acc[v] = fma(g3[v], x3, acc[v]);
+        for (int q = 0; q < 8; q++) L::load(G, base + (int64_t)(c + q) * ld, g[q]);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const Acc xq = xs[c + q];
+#pragma unroll
+          for (int v = 0; v < VEC; v++) acc[v] = fma(g[q][v], xq, acc[v]);
         }
       }
       for (; c < nc; c++) {
@@ -163,19 +159,16 @@ __device__ __forceinline__ void gx_partial_fold_body(
     if (row < ld) {
       const int64_t base = row + c0 * ld;
       int c = 0;
-      for (; c + 4 <= nc; c += 4) {
-        Acc g0[VEC], g1[VEC], g2[VEC], g3[VEC];
-        L::load(G, base + (int64_t)c * ld, g0);
-        L::load(G, base + (int64_t)(c + 1) * ld, g1);
-        L::load(G, base + (int64_t)(c + 2) * ld, g2);
-        L::load(G, base + (int64_t)(c + 3) * ld, g3);
-        const Acc x0 = xs[c], x1 = xs[c + 1], x2 = xs[c + 2], x3 = xs[c + 3];
+      // eight columns' loads in flight before their FMAs
+      for (; c + 8 <= nc; c += 8) {
+        Acc g[8][VEC];
 #pragma unroll
-        for (int v = 0; v < VEC; v++) {
-          acc[v] = fma(g0[v], x0, acc[v]);
-          acc[v] = fma(g1[v], x1, acc[v]);
-          acc[v] = fma(g2[v], x2, acc[v]);
-          acc[v] = fma(g3[v], x3, acc[v]);
+        for (int q = 0; q < 8; q++) L::load(G, base + (int64_t)(c + q) * ld, g[q]);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const Acc xq = xs[c + q];
+#pragma unroll
+          for (int v = 0; v < VEC; v++) acc[v] = fma(g[q][v], xq, acc[v]);
         }
       }
       for (; c < nc; c++) {
@@ -193,19 +186,34 @@ __device__ __forceinline__ void gx_partial_fold_body(
   }
 }
 
-// y[r] = (sum over splits of the partial rows) * row_scale[r] * post_scale[r],
-// 256 rows per block b.
+// y[r] = (sum over splits of the partial rows) * row_scale[r] * post_scale[r]
+// for the kFinishRows rows of block b: warp w adds splits w, w + 8, ... of
+// its lane's row, then warp 0 adds the 8 warp sums in warp order.  Sharing a
+// row's splits among the warps keeps the many column ranges of a tall-thin G
+// from turning the sum into one long dependent chain per thread.
+constexpr int kFinishRows = 32;
+
 __device__ __forceinline__ void gx_finish_body(const double *partial, int n_split, int64_t ld,
                                                int64_t nd, const float *__restrict__ row_scale,
                                                const double *__restrict__ post_scale, double *y,
                                                int64_t b) {
-  const int64_t r = b * 256 + threadIdx.x;
-  if (r >= nd) return;
+  __shared__ double part[kThreads / 32][kFinishRows];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t r = b * kFinishRows + lane;
   double s = 0.0;
-  for (int k = 0; k < n_split; k++) s += __ldcg(partial + (int64_t)k * ld + r);
-  if (row_scale) s *= (double)row_scale[r];
-  if (post_scale) s *= post_scale[r];
-  y[r] = s;
+  if (r < nd)
+    for (int k = warp; k < n_split; k += kThreads / 32) s += __ldcg(partial + (int64_t)k * ld + r);
+  __syncthreads();  // part is reused by the next block the caller runs
+  part[warp][lane] = s;
+  __syncthreads();
+  if (warp == 0 && r < nd) {
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; w++) v += part[w][lane];
+    if (row_scale) v *= (double)row_scale[r];
+    if (post_scale) v *= post_scale[r];
+    y[r] = v;
+  }
 }
 
 // y (FP64, nd entries) -> padded vector of the accumulation type, times the
@@ -224,52 +232,53 @@ __device__ __forceinline__ void prep_y_body(const double *y, int64_t nd, int64_t
   out[r] = (Acc)v;
 }
 
-// G^T y for the kGtCols columns of block b: returns column (b * kGtCols +
-// threadIdx.x)'s sum in threads threadIdx.x < ncol (ncol through *ncol_out),
-// every thread of the block taking part.
+// G^T y for the kGtBlockCols columns of block b: warp w takes columns
+// 4w .. 4w + 3 of the block, its lanes striding the rows with 16-byte loads,
+// and sums each column with a butterfly.  Lane c < 4 of warp w returns column
+// b * kGtBlockCols + 4w + c's sum and sets *col to that column; every other
+// thread gets *col = -1.
+constexpr int kGtWarpCols = 4;
+constexpr int kGtBlockCols = kGtWarpCols * (kThreads / 32);
+
 template <class L>
 __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t ld, int64_t nm,
-                                           const typename L::Acc *y, int64_t b, int *ncol_out) {
+                                           const typename L::Acc *y, int64_t b, int64_t *col) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
-  constexpr int COLS = kGtCols;
-  const int64_t c0 = b * COLS;
-  const int ncol = (int)min((int64_t)COLS, nm - c0);
-  Acc acc[COLS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t c0 = b * kGtBlockCols + (int64_t)warp * kGtWarpCols;
+  const int64_t left = nm - c0;
+  const int ncol = left <= 0 ? 0 : (left < kGtWarpCols ? (int)left : kGtWarpCols);
+  Acc acc[kGtWarpCols];
 #pragma unroll
-  for (int c = 0; c < COLS; c++) acc[c] = Acc(0);
-  for (int64_t row = (int64_t)threadIdx.x * VEC; row < ld; row += (int64_t)kThreads * VEC) {
-    Acc yv[VEC];
+  for (int c = 0; c < kGtWarpCols; c++) acc[c] = Acc(0);
+  if (ncol > 0) {
+#pragma unroll 2
+    for (int64_t row = (int64_t)lane * VEC; row < ld; row += 32 * VEC) {
+      Acc yv[VEC];
 #pragma unroll
-    for (int v = 0; v < VEC; v++) yv[v] = __ldcg(y + row + v);
+      for (int v = 0; v < VEC; v++) yv[v] = __ldcg(y + row + v);
 #pragma unroll
-    for (int c = 0; c < COLS; c++) {
-      if (c < ncol) {
-        Acc g[VEC];
-        L::load(G, row + (c0 + c) * ld, g);
+      for (int c = 0; c < kGtWarpCols; c++) {
+        if (c < ncol) {
+          Acc g[VEC];
+          L::load(G, row + (c0 + c) * ld, g);
 #pragma unroll
-        for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
+          for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
+        }
       }
     }
   }
-  __shared__ double red[kThreads / 32][COLS];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  __syncthreads();  // red is reused by the next block the caller runs
+  double mine = 0.0;
 #pragma unroll
-  for (int c = 0; c < COLS; c++) {
+  for (int c = 0; c < kGtWarpCols; c++) {
     double v = (double)acc[c];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[warp][c] = v;
+    if (lane == c) mine = v;
   }
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x < ncol) {
-#pragma unroll
-    for (int w = 0; w < kThreads / 32; w++) s += red[w][threadIdx.x];
-  }
-  *ncol_out = ncol;
-  return s;
+  *col = (lane < ncol) ? c0 + lane : -1;
+  return mine;
 }
 
 }  // namespace gemv

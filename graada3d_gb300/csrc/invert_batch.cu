@@ -53,7 +53,7 @@ struct TeamInversion {
       gemv::gx_partial_body<gemv::LoadF64>(P.Gp, ld, Nm, P.p_per, mv, P.cg.scratch,
                                            b % P.p_tiles, b / P.p_tiles);
     if (!bar.sync()) return false;
-    const int64_t nb = ceil_div_d(Nd, 256);
+    const int64_t nb = ceil_div_d(Nd, gemv::kFinishRows);
     for (int64_t b = cta; b < nb; b += nct)
       gemv::gx_finish_body(P.cg.scratch, P.p_splits, ld, Nd, nullptr, nullptr, out, b);
     if (!bar.sync()) return false;
@@ -147,12 +147,11 @@ struct TeamInversion {
     for (int64_t b = cta; b < nb_prep; b += nct)
       gemv::prep_y_body<Acc>(P.tmpd, Nd, ld, a.row_scale, nullptr, y, b);
     if (!bar.sync()) return false;
-    const int64_t nb_gt = ceil_div_d(Nm, gemv::kGtCols);
+    const int64_t nb_gt = ceil_div_d(Nm, gemv::kGtBlockCols);
     for (int64_t b = cta; b < nb_gt; b += nct) {
-      int ncol = 0;
-      const double g = gemv::gty_body<L>(a.G, ld, Nm, y, b, &ncol);
-      if ((int)threadIdx.x < ncol) {
-        const int64_t j = b * gemv::kGtCols + threadIdx.x;
+      int64_t j = -1;
+      const double g = gemv::gty_body<L>(a.G, ld, Nm, y, b, &j);
+      if (j >= 0) {
         a.gtw[j] = g;
         P.atb[j] = cgb::adjoint_column(P.AT_b, j, a.P, true, g, 1.0);
         a.r[j] = cgb::adjoint_column(P.AT_s0, j, a.P, true, g, -1.0);

@@ -3,7 +3,8 @@ against the reference's solve_cg (GaussNewtonInversion.cpp:1417-1698, the
 compiled reference's fixtures) and against the graph-replayed iteration it
 replaces.  The two device paths sum the dot products and G p's column ranges
 in different (each fixed) orders, so they agree to rounding: FP64 to 1e-9 of
-max|dx|, reduced-precision G to 1e-4, iteration counts within one.  The
+max|dx|, reduced-precision G to 1e-4, iteration counts within one (whole L2
+inversions: FP64 trial misfits to 1e-6, FP32 to 1e-3).  The
 persistent solve is deterministic: repeated solves are bitwise equal.  Also: a
 real device-side wait expiry of a grid barrier, and the context afterwards."""
 import os
@@ -82,9 +83,12 @@ def test_fused_l2_invert_matches_graph_path(gpu_ctx, storage):
     trials = inv.trials()
     with graph_path():
         m_g, rep_g = inv.invert(*args, fp64_refinement=storage != "fp64")
+    # FP32 products summed in other orders differ at FP32 rounding, which the
+    # lambda search carries on; FP64 ones at FP64 rounding
+    rt, mt = (1e-6, 1e-5) if storage == "fp64" else (1e-3, 1e-2)
     assert rep["n_trials"] == rep_g["n_trials"]
-    assert np.allclose(trials[:, 2], inv.trials()[:, 2], rtol=1e-6, atol=0)
-    assert np.abs(m - m_g).max() <= 1e-5 * np.abs(m_g).max()
+    assert np.allclose(trials[:, 2], inv.trials()[:, 2], rtol=rt, atol=0)
+    assert np.abs(m - m_g).max() <= mt * np.abs(m_g).max()
 
 
 def test_fused_barrier_wait_expiry_is_reported_and_context_recovers(gpu_ctx):
