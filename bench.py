@@ -677,7 +677,10 @@ def run_batched_64(n_problems: int = 64):
                                          [a[1] for a in args], [a[2] for a in args])
     torch.cuda.synchronize()
     t_per = time.perf_counter() - t0
-    per_same = all(np.array_equal(a[0], b[0]) for a, b in zip(seq, per))
+    # the single FP64 runs take the graph-replayed CG (the faster one for FP64 G);
+    # the batch runs the persistent loop, which sums in other orders
+    per_diff = max(float(np.linalg.norm(a[0] - b[0]) / max(np.linalg.norm(a[0]), 1e-30))
+                   for a, b in zip(seq, per))
     # the same batch with FP32 G (HBM-bound products) and the FP64 G kept for
     # every prediction
     t0 = time.perf_counter()
@@ -711,7 +714,7 @@ def run_batched_64(n_problems: int = 64):
             "persistent": {"launches": 1, "teams": shape[0], "ctas_per_team": shape[1],
                            "s": t_per, "speedup_vs_sequential": t_seq / t_per,
                            "speedup_vs_concurrent": t_bat / t_per,
-                           "identical_models_to_single_runs": per_same},
+                           "max_model_rel_diff_vs_single_runs": per_diff},
             "cg_iterations_rank0": int(sum(r["cg_iterations"] for _, r in bat)),
             "fp32_kept_fp64": {"batched_s": t_mix, "speedup_vs_fp64_batch": t_bat / t_mix,
                                "persistent": {"launches": 1, "teams": mix_shape[0],

@@ -430,13 +430,20 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
 }
 
 bool Context::fused_cg_eligible() const {
-  // stored dense G only (the matrix-free and wavelet products keep the graph
-  // path); GRADA_CG_FUSED=0 selects the graph path for every storage
+  // Stored dense G only (the matrix-free and wavelet products keep the graph
+  // path).  FP32 and 16-bit G: the persistent loop (HBM-bound products, where
+  // removing launches and host round trips pays).  FP64 G: the graph path,
+  // whose full-occupancy products keep the FP64 pipe (2 DFMA per clock per
+  // SM) busier than the persistent loop's three CTAs per SM.
+  // GRADA_CG_FUSED=1 takes the persistent loop for every stored G (FP64
+  // included, as the batched kernel runs it), =0 the graph path for all.
   if (g_storage != GRADA_G_FP64 && g_storage != GRADA_G_FP32 && g_storage != GRADA_G_BF16_ROWSCALE &&
       g_storage != GRADA_G_FP16_ROWSCALE)
     return false;
   const char *e = std::getenv("GRADA_CG_FUSED");
-  return !(e && e[0] == '0');
+  if (e && e[0] == '0') return false;
+  if (e && e[0] == '1') return true;
+  return g_storage != GRADA_G_FP64;
 }
 
 // The CG loop as one persistent cooperative launch (cg_fused.cu), from the
@@ -454,6 +461,15 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
   const int grid = fused_grid[(int)g.kind];
   fused_gx_partition(g, grid, a.tiles, a.splits, a.per);
+  // G is read twice per iteration: the columns that fit in about 100 MB of L2
+  // (GRADA_L2_KEEP_MB overrides) are loaded to stay there between the reads
+  {
+    const char *e = std::getenv("GRADA_L2_KEEP_MB");
+    const double keep_mb = e ? std::atof(e) : 100.0;
+    const int64_t col_bytes = g.ld * (int64_t)(g.kind == GKind::FP64 ? 8 : g.kind == GKind::FP32 ? 4 : 2);
+    const int64_t cols = (int64_t)(keep_mb * 1048576.0) / std::max<int64_t>(col_bytes, 1);
+    a.keep_cols = std::max<int64_t>(0, std::min<int64_t>(g.nm, cols));
+  }
   a.scratch = scratch_doubles(std::max(product_scratch_doubles(), (int64_t)a.splits * g.ld));
   a.wd = dptr(wd);
   a.r = dptr(cg_r);

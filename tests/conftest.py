@@ -1,3 +1,5 @@
+import contextlib
+import os
 import sys
 from pathlib import Path
 
@@ -28,3 +30,18 @@ def gpu_ctx():
     ctx = Context(0)
     yield ctx
     ctx.close()
+
+
+@contextlib.contextmanager
+def cg_path(mode: str):
+    """Selects the CG loop inside the block: "1" the persistent launch for every
+    stored G, "0" the graph-replayed iteration (GRADA_CG_FUSED)."""
+    old = os.environ.get("GRADA_CG_FUSED")
+    os.environ["GRADA_CG_FUSED"] = mode
+    try:
+        yield
+    finally:
+        if old is None:
+            os.environ.pop("GRADA_CG_FUSED", None)
+        else:
+            os.environ["GRADA_CG_FUSED"] = old

@@ -3,11 +3,13 @@ each problem's whole invert_with_own_CG (GaussNewtonInversion.cpp:657-1103)
 runs on a team of CTAs from a device queue, and its model, report and
 lambda/misfit record are bitwise those of grada_invert on its own -- for L2,
 L1 with the cross-gradient and reference-model terms, and L0 problems, FP64 G
-or FP32 G with the FP64 G kept, and any team size."""
+or FP32 G with the FP64 G kept, and any team size (the single runs take the
+persistent CG loop too, GRADA_CG_FUSED=1)."""
 import numpy as np
 import pytest
 
 import inversion_fixtures as fx
+from conftest import cg_path
 from graada3d_gb300 import Context, GradaError, mesh
 from graada3d_gb300 import regularization as reg
 from graada3d_gb300.inversion import GaussNewtonInversion, invert_batch_persistent
@@ -71,10 +73,12 @@ def _problems(storage):
 
 
 def _singles(probs, mixed):
+    # the batch runs the persistent CG loop for every storage, FP64 included
     out = []
-    for inv, prm, (mi, lo, hi, m0) in probs:
-        m, rep = inv.invert(prm, mi, lo, hi, m0, fp64_refinement=mixed)
-        out.append((m, rep, inv.trials(), inv.iterations()))
+    with cg_path("1"):
+        for inv, prm, (mi, lo, hi, m0) in probs:
+            m, rep = inv.invert(prm, mi, lo, hi, m0, fp64_refinement=mixed)
+            out.append((m, rep, inv.trials(), inv.iterations()))
     return out
 
 

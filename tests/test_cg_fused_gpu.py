@@ -7,30 +7,23 @@ max|dx|, reduced-precision G to 1e-4, iteration counts within one (whole L2
 inversions: FP64 trial misfits to 1e-6, FP32 to 1e-3).  The
 persistent solve is deterministic: repeated solves are bitwise equal.  Also: a
 real device-side wait expiry of a grid barrier, and the context afterwards."""
-import os
-
 import numpy as np
 import pytest
 
 import inversion_fixtures as fx
+from conftest import cg_path
 from graada3d_gb300 import GradaError
 from graada3d_gb300.inversion import GaussNewtonInversion
 
 pytestmark = pytest.mark.gpu
 
 
-class graph_path:
-    """Selects the graph-replayed CG path (GRADA_CG_FUSED=0) inside the block."""
+def graph_path():
+    return cg_path("0")
 
-    def __enter__(self):
-        self.old = os.environ.get("GRADA_CG_FUSED")
-        os.environ["GRADA_CG_FUSED"] = "0"
 
-    def __exit__(self, *exc):
-        if self.old is None:
-            os.environ.pop("GRADA_CG_FUSED", None)
-        else:
-            os.environ["GRADA_CG_FUSED"] = self.old
+def fused_path():
+    return cg_path("1")
 
 
 def _setup(f, ctx, storage):
@@ -57,8 +50,9 @@ def _solve(inv, f):
 def test_fused_solve_cg_matches_graph_path_and_reference(gpu_ctx, name, storage):
     f = fx.load(name)
     inv = _setup(f, gpu_ctx, storage)
-    dx, err, it = _solve(inv, f)
-    dx2, err2, it2 = _solve(inv, f)
+    with fused_path():
+        dx, err, it = _solve(inv, f)
+        dx2, err2, it2 = _solve(inv, f)
     assert it2 == it and err2 == err and np.array_equal(dx2, dx)  # deterministic
     with graph_path():
         dx_g, err_g, it_g = _solve(inv, f)
@@ -79,7 +73,8 @@ def test_fused_l2_invert_matches_graph_path(gpu_ctx, storage):
     nm = inv.Nm
     mmin, mmax, mini = f["bounds"]
     args = (fx.prm(f), np.full(nm, mini), np.full(nm, mmin), np.full(nm, mmax), None)
-    m, rep = inv.invert(*args, fp64_refinement=storage != "fp64")
+    with fused_path():
+        m, rep = inv.invert(*args, fp64_refinement=storage != "fp64")
     trials = inv.trials()
     with graph_path():
         m_g, rep_g = inv.invert(*args, fp64_refinement=storage != "fp64")
@@ -93,7 +88,7 @@ def test_fused_l2_invert_matches_graph_path(gpu_ctx, storage):
 
 def test_fused_barrier_wait_expiry_is_reported_and_context_recovers(gpu_ctx):
     f = fx.load("l2")
-    inv = _setup(f, gpu_ctx, "fp32")
+    inv = _setup(f, gpu_ctx, "fp32")  # FP32 G: the persistent loop
     dx, err, it = _solve(inv, f)
     FAULT_CG_WAIT = 3  # the next solve's barrier waits have a zero limit
     inv.ctx.check(inv.ctx.lib.grada_inject_fault(inv.ctx.handle, FAULT_CG_WAIT))
