@@ -146,9 +146,11 @@ __device__ __forceinline__ void gx_partial_fold_body(
   const int64_t row = (tile * kThreads + threadIdx.x) * VEC;
   const int64_t c_begin = split * cols_per_split;
   const int64_t c_end = min(nm, c_begin + cols_per_split);
-  Acc acc[VEC];
+  // two accumulators per row (even and odd columns of a group of eight): twice
+  // the independent FMA chains, which the FP64 pipe needs at three CTAs per SM
+  Acc acc[VEC], acc2[VEC];
 #pragma unroll
-  for (int v = 0; v < VEC; v++) acc[v] = Acc(0);
+  for (int v = 0; v < VEC; v++) acc[v] = acc2[v] = Acc(0);
   for (int64_t c0 = c_begin; c0 < c_end; c0 += kXChunk) {
     const int nc = (int)min((int64_t)kXChunk, c_end - c0);
     __syncthreads();
@@ -172,10 +174,13 @@ __device__ __forceinline__ void gx_partial_fold_body(
 #pragma unroll
         for (int q = 0; q < 8; q++) L::load(G, base + (int64_t)(c + q) * ld, g[q], c0 + c + q < keep_cols);
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-          const Acc xq = xs[c + q];
+        for (int q = 0; q < 8; q += 2) {
+          const Acc xq = xs[c + q], xr = xs[c + q + 1];
 #pragma unroll
-          for (int v = 0; v < VEC; v++) acc[v] = fma(g[q][v], xq, acc[v]);
+          for (int v = 0; v < VEC; v++) {
+            acc[v] = fma(g[q][v], xq, acc[v]);
+            acc2[v] = fma(g[q + 1][v], xr, acc2[v]);
+          }
         }
       }
       for (; c < nc; c++) {
@@ -189,7 +194,7 @@ __device__ __forceinline__ void gx_partial_fold_body(
   if (row < ld) {
     double *out = partial + split * ld + row;
 #pragma unroll
-    for (int v = 0; v < VEC; v++) out[v] = (double)acc[v];
+    for (int v = 0; v < VEC; v++) out[v] = (double)acc[v] + (double)acc2[v];
   }
 }
 
