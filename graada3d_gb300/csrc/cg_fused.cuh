@@ -161,7 +161,7 @@ __device__ __forceinline__ double gty_adjoint_block(const FusedCgArgs &a, const 
   __shared__ double wsum[cgb::VT / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int64_t j = -1;
-  const double g = gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j, a.keep_cols);
+  const double g = gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j);
   double sq = 0.0;
   if (j >= 0) {
     a.gtw[j] = g;
@@ -244,7 +244,7 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
     // A
     for (int64_t b = cta; b < n_gx; b += nct)
       gemv::gx_partial_fold_body<L>(a.G, ld, Nm, a.per, a.r, p_old, a.P, beta, p_new, a.pp,
-                                    a.scratch, b % a.tiles, b / a.tiles, a.keep_cols);
+                                    a.scratch, b % a.tiles, b / a.tiles);
     if (!(ok = bar.sync())) break;
     // B
     for (int64_t b = cta; b < rl.nb_t; b += nct) {

@@ -22,7 +22,6 @@ struct FusedCgArgs {
   int64_t nd = 0, nm = 0, ld = 0;
   int tiles = 0, splits = 0;
   int64_t per = 0;
-  int64_t keep_cols = 0;      // columns [0, keep_cols) of G loaded to stay in L2
   double *scratch = nullptr;  // splits * ld doubles: G x partials, then y
   const double *wd = nullptr;  // Wd: post-scale of G pp, pre-scale of G^T s
   // CG vectors (GaussNewtonInversion.cpp:1556-1692)

@@ -23,16 +23,14 @@ constexpr int kThreads = 256;  // threads of every product block
 constexpr int kXChunk = 256;   // x entries staged in shared memory at a time (G x)
 
 // ---- element loaders: VEC consecutive entries from a 16-byte load ----------
-// keep = false streams the entries (evict-first: a G larger than L2 would only
-// push other data out); keep = true loads them normally, so a part of G that
-// fits in L2 stays there from one product to the next.
+// (streamed, evict-first: G is read once per product and would only push the
+// vectors out of L2)
 
 struct LoadF64 {
   static constexpr int VEC = 2;
   using Acc = double;
-  __device__ static void load(const void *base, int64_t idx, double (&v)[2], bool keep = false) {
-    const double2 *p = reinterpret_cast<const double2 *>(static_cast<const double *>(base) + idx);
-    const double2 d = keep ? __ldg(p) : __ldcs(p);
+  __device__ static void load(const void *base, int64_t idx, double (&v)[2]) {
+    const double2 d = __ldcs(reinterpret_cast<const double2 *>(static_cast<const double *>(base) + idx));
     v[0] = d.x;
     v[1] = d.y;
   }
@@ -40,9 +38,8 @@ struct LoadF64 {
 struct LoadF32 {
   static constexpr int VEC = 4;
   using Acc = float;
-  __device__ static void load(const void *base, int64_t idx, float (&v)[4], bool keep = false) {
-    const float4 *p = reinterpret_cast<const float4 *>(static_cast<const float *>(base) + idx);
-    const float4 d = keep ? __ldg(p) : __ldcs(p);
+  __device__ static void load(const void *base, int64_t idx, float (&v)[4]) {
+    const float4 d = __ldcs(reinterpret_cast<const float4 *>(static_cast<const float *>(base) + idx));
     v[0] = d.x;
     v[1] = d.y;
     v[2] = d.z;
@@ -52,9 +49,8 @@ struct LoadF32 {
 struct LoadBF16 {
   static constexpr int VEC = 8;
   using Acc = float;
-  __device__ static void load(const void *base, int64_t idx, float (&v)[8], bool keep = false) {
-    const uint4 *p = reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(base) + idx);
-    const uint4 d = keep ? __ldg(p) : __ldcs(p);
+  __device__ static void load(const void *base, int64_t idx, float (&v)[8]) {
+    const uint4 d = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(base) + idx));
     const uint32_t w[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -66,9 +62,8 @@ struct LoadBF16 {
 struct LoadF16 {
   static constexpr int VEC = 8;
   using Acc = float;
-  __device__ static void load(const void *base, int64_t idx, float (&v)[8], bool keep = false) {
-    const uint4 *p = reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(base) + idx);
-    const uint4 d = keep ? __ldg(p) : __ldcs(p);
+  __device__ static void load(const void *base, int64_t idx, float (&v)[8]) {
+    const uint4 d = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(base) + idx));
     const uint32_t w[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -139,7 +134,7 @@ template <class L>
 __device__ __forceinline__ void gx_partial_fold_body(
     const void *__restrict__ G, int64_t ld, int64_t nm, int64_t cols_per_split, const double *r,
     const double *p_old, const double *__restrict__ P, double beta, double *p_new, double *pp,
-    double *partial, int64_t tile, int64_t split, int64_t keep_cols = 0) {
+    double *partial, int64_t tile, int64_t split) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
   __shared__ Acc xs[kXChunk];
@@ -172,7 +167,7 @@ __device__ __forceinline__ void gx_partial_fold_body(
       for (; c + 8 <= nc; c += 8) {
         Acc g[8][VEC];
 #pragma unroll
-        for (int q = 0; q < 8; q++) L::load(G, base + (int64_t)(c + q) * ld, g[q], c0 + c + q < keep_cols);
+        for (int q = 0; q < 8; q++) L::load(G, base + (int64_t)(c + q) * ld, g[q]);
 #pragma unroll
         for (int q = 0; q < 8; q += 2) {
           const Acc xq = xs[c + q], xr = xs[c + q + 1];
@@ -185,7 +180,7 @@ __device__ __forceinline__ void gx_partial_fold_body(
       }
       for (; c < nc; c++) {
         Acc g0[VEC];
-        L::load(G, base + (int64_t)c * ld, g0, c0 + c < keep_cols);
+        L::load(G, base + (int64_t)c * ld, g0);
 #pragma unroll
         for (int v = 0; v < VEC; v++) acc[v] = fma(g0[v], xs[c], acc[v]);
       }
@@ -254,8 +249,7 @@ constexpr int kGtBlockCols = kGtWarpCols * (kThreads / 32);
 
 template <class L>
 __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t ld, int64_t nm,
-                                           const typename L::Acc *y, int64_t b, int64_t *col,
-                                           int64_t keep_cols = 0) {
+                                           const typename L::Acc *y, int64_t b, int64_t *col) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -275,7 +269,7 @@ __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t l
       for (int c = 0; c < kGtWarpCols; c++) {
         if (c < ncol) {
           Acc g[VEC];
-          L::load(G, row + (c0 + c) * ld, g, c0 + c < keep_cols);
+          L::load(G, row + (c0 + c) * ld, g);
 #pragma unroll
           for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
         }

@@ -461,15 +461,6 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
   const int grid = fused_grid[(int)g.kind];
   fused_gx_partition(g, grid, a.tiles, a.splits, a.per);
-  // G is read twice per iteration: the columns that fit in about 100 MB of L2
-  // (GRADA_L2_KEEP_MB overrides) are loaded to stay there between the reads
-  {
-    const char *e = std::getenv("GRADA_L2_KEEP_MB");
-    const double keep_mb = e ? std::atof(e) : 100.0;
-    const int64_t col_bytes = g.ld * (int64_t)(g.kind == GKind::FP64 ? 8 : g.kind == GKind::FP32 ? 4 : 2);
-    const int64_t cols = (int64_t)(keep_mb * 1048576.0) / std::max<int64_t>(col_bytes, 1);
-    a.keep_cols = std::max<int64_t>(0, std::min<int64_t>(g.nm, cols));
-  }
   a.scratch = scratch_doubles(std::max(product_scratch_doubles(), (int64_t)a.splits * g.ld));
   a.wd = dptr(wd);
   a.r = dptr(cg_r);
