@@ -4,12 +4,15 @@ grada_invert_batch_persistent splits the GPU's resident CTAs into teams; a team
 takes one problem at a time from a device queue.  Small teams keep many
 problems in flight but give each one little bandwidth; large teams finish a
 problem sooner but leave CTAs idle on small problems and lengthen the tail.
-The best size depends on the problem sizes, so it is measured: for each class
+A third layout gives each problem its own team, sized in proportion to its G, and
+starts them all at once (-1).  The best choice depends on the problem sizes, so it is
+measured: for each class
 of synthetic batches (uniform meshes, gz + Tzz, the batch's spread of cell and
 point counts) the batch is run with every candidate team size under shortened
 inversion settings (the team-size effect is per CG iteration), and the fastest
 wins.  The table row is "<largest G of the class, entries> <CTAs per team>";
-the library reads tuning/batch_teams.tsv beside itself on first use.
+the library reads tuning/batch_teams.tsv beside itself on first use.  A row's team size
+may be -1, the proportional layout.
 
     python -m graada3d_gb300.autotune [--out PATH] [--storage fp32+fp64|fp64]
 
@@ -37,7 +40,8 @@ CLASSES = [
     ("uneven-64", 64, (4000, 60000), (400, 5000)),
     ("large", 8, (60000, 100000), (3000, 6000)),
 ]
-CANDIDATES = (1, 2, 4, 8, 16, 32, 64)
+# team sizes tried; -1 is one team per problem sized by its G, all problems at once
+CANDIDATES = (-1, 2, 4, 8, 16, 32, 64)
 SHORT = dict(max_lambda=1e-1, n_lambda=3, rate=0.6, target=1e-9, stag=0.0, cg_tol=1e-30,
              cg_factor=20, gn_iter=1, lp=[2, 2, 2, 2, 2], eps2=1e-9)
 

@@ -323,22 +323,36 @@ struct TeamInversion {
   }
 };
 
+// Team layout of a launch: CTA c belongs to team team_of[c] as its
+// rank_of[c]-th CTA; team t has size_of[t] CTAs and starts with problem
+// first_of[t] (-1: it takes its first problem from the queue too).
+struct TeamMap {
+  const int *team_of, *rank_of, *size_of, *first_of;
+};
+
 template <class L>
 __global__ void __launch_bounds__(256)
-    invert_batch_kernel(const BatchProblem *problems, int n, int *queue, unsigned *bar_words,
-                        int *team_slot, int team_ctas, unsigned long long wait_ns) {
+    invert_batch_kernel(const BatchProblem *problems, int n, int *queue, int queue_base,
+                        unsigned *bar_words, int *team_slot, TeamMap map,
+                        unsigned long long wait_ns) {
   __shared__ __align__(16) unsigned char sp_raw[sizeof(BatchProblem)];
   BatchProblem &sp = *reinterpret_cast<BatchProblem *>(sp_raw);
-  const unsigned team = blockIdx.x / team_ctas, cta = blockIdx.x % team_ctas;
-  TeamBarrier bar(bar_words + (size_t)fused::kBarrierWords * team, (unsigned)team_ctas, cta,
-                  wait_ns);
+  const unsigned team = (unsigned)map.team_of[blockIdx.x];
+  const unsigned cta = (unsigned)map.rank_of[blockIdx.x];
+  const unsigned team_ctas = (unsigned)map.size_of[team];
+  TeamBarrier bar(bar_words + (size_t)fused::kBarrierWords * team, team_ctas, cta, wait_ns);
+  int next = map.first_of[team];
   while (true) {
-    if (cta == 0 && threadIdx.x == 0) {
-      team_slot[32 * team] = atomicAdd(queue, 1);
-      __threadfence();
+    int k = next;
+    next = -1;
+    if (k < 0) {
+      if (cta == 0 && threadIdx.x == 0) {
+        team_slot[32 * team] = queue_base + atomicAdd(queue, 1);
+        __threadfence();
+      }
+      if (!bar.sync()) return;
+      k = __ldcg(team_slot + 32 * team);
     }
-    if (!bar.sync()) return;
-    const int k = __ldcg(team_slot + 32 * team);
     if (k >= n) return;
     // this CTA's copy of the problem (its lambda-dependent coefficients change)
     const uint4 *src = reinterpret_cast<const uint4 *>(problems + k);
@@ -363,19 +377,19 @@ const void *batch_kernel_for(GKind k) {
 
 }  // namespace
 
-int invert_batch_grid(GKind kind, int sm_count, int team_ctas) {
+int invert_batch_resident(GKind kind, int sm_count) {
   int per_sm = 0;
   GRADA_CUDA_CHECK(
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel_for(kind), 256, 0));
-  const int resident = std::max(1, per_sm) * sm_count;
-  return std::max(1, resident / team_ctas) * team_ctas;
+  return std::max(1, per_sm) * sm_count;
 }
 
-void launch_invert_batch(const BatchProblem *problems, int n, int *queue, unsigned *bar_words,
-                         int *team_slot, int team_ctas, int grid, GKind kind,
-                         unsigned long long wait_ns, cudaStream_t s) {
-  void *args[] = {(void *)&problems, (void *)&n, (void *)&queue, (void *)&bar_words,
-                  (void *)&team_slot, (void *)&team_ctas, (void *)&wait_ns};
+void launch_invert_batch(const BatchProblem *problems, int n, int *queue, int queue_base,
+                         unsigned *bar_words, int *team_slot, const int *map, int n_teams,
+                         int grid, GKind kind, unsigned long long wait_ns, cudaStream_t s) {
+  TeamMap tm{map, map + grid, map + 2 * grid, map + 2 * grid + n_teams};
+  void *args[] = {(void *)&problems,  (void *)&n,  (void *)&queue,  (void *)&queue_base,
+                  (void *)&bar_words, (void *)&team_slot, (void *)&tm, (void *)&wait_ns};
   GRADA_CUDA_CHECK(cudaLaunchCooperativeKernel(batch_kernel_for(kind), dim3((unsigned)grid),
                                                dim3(256), args, 0, s));
 }
@@ -557,8 +571,9 @@ void Context::batch_results(const grada_invert_params &prm, double *h_m_out,
 
 namespace {
 
-// Rows (largest G of the batch in entries, CTAs per team), ascending; the
-// batch takes the first row whose bound holds its largest problem.  Loaded
+// Rows (largest G of the batch in entries, CTAs per team, -1 for one team per
+// problem sized by its G), ascending; the batch takes the first row whose
+// bound holds its largest problem.  Loaded
 // from the file grada_load_batch_tuning names or, on first use, from
 // tuning/batch_teams.tsv beside the library (graada3d_gb300/autotune.py
 // writes it); without a table, a team of 8.
@@ -575,7 +590,8 @@ std::vector<std::pair<double, int>> read_table(const char *path) {
     if (line.empty() || line[0] == '#') continue;
     double bound = 0;
     int team = 0;
-    if (std::sscanf(line.c_str(), "%lf %d", &bound, &team) == 2 && team >= 1 && team <= 1024)
+    if (std::sscanf(line.c_str(), "%lf %d", &bound, &team) == 2 && team >= -1 && team != 0 &&
+        team <= 1024)
       rows.push_back({bound, team});
   }
   std::sort(rows.begin(), rows.end());
@@ -666,20 +682,72 @@ int invert_batch_persistent(int n, Context *const *ctxs, const grada_invert_para
   for (int k = 0; k < n; k++) sorted[k] = probs[order[k]];
   try {
     const GKind kind = (GKind)c0->g_storage;
-    const int team = team_ctas > 0 ? team_ctas : tuned_team_ctas(max_entries);
-    const int grid = invert_batch_grid(kind, c0->sm_count, team);
-    if (grid < team) throw Error(GRADA_ERR_INVALID_ARGUMENT, "team larger than the resident grid");
-    const int n_teams = grid / team;
-    DevBuf d_probs, d_words;
+    const int resident = invert_batch_resident(kind, c0->sm_count);
+    // team_ctas > 0: teams of that size take problems from the queue; 0: the
+    // tuning table's choice; a table value (or team_ctas) of -1: one team per
+    // problem, sized in proportion to its G, all problems at once
+    int team = team_ctas != 0 ? team_ctas : tuned_team_ctas(max_entries);
+    if (team < 0 && n > resident) team = 8;  // more problems than CTAs: queue
+    std::vector<int> team_of, rank_of, size_of, first_of;
+    int grid = 0;
+    if (team > 0) {
+      if (team > resident) throw Error(GRADA_ERR_INVALID_ARGUMENT, "team larger than the resident grid");
+      const int nt = resident / team;
+      grid = nt * team;
+      for (int c = 0; c < grid; c++) {
+        team_of.push_back(c / team);
+        rank_of.push_back(c % team);
+      }
+      size_of.assign(nt, team);
+      first_of.assign(nt, -1);
+    } else {
+      // sizes in proportion to each problem's G entries, at least one CTA each,
+      // the resident CTAs left over by the rounding given to the largest
+      std::vector<double> w(n);
+      double W = 0;
+      for (int k = 0; k < n; k++) {
+        w[k] = (double)ctxs[order[k]]->nd * (double)ctxs[order[k]]->n_cells;
+        W += w[k];
+      }
+      size_of.assign(n, 1);
+      int used = n;
+      for (int k = 0; k < n; k++) {
+        const int extra = std::max(0, (int)std::floor(resident * w[k] / W) - 1);
+        const int take = std::min(extra, resident - used);
+        size_of[k] += take;
+        used += take;
+      }
+      for (int k = 0; used < resident; k = (k + 1) % n, used++) size_of[k]++;
+      for (int t = 0; t < n; t++) {
+        for (int r = 0; r < size_of[t]; r++) {
+          team_of.push_back(t);
+          rank_of.push_back(r);
+        }
+        first_of.push_back(t);
+      }
+      grid = (int)team_of.size();
+    }
+    const int n_teams = (int)size_of.size();
+    DevBuf d_probs, d_words, d_map;
     d_probs.alloc(c0, sizeof(BatchProblem) * (size_t)n);
     // queue (1 int), then per team its barrier words, then a 32-int problem slot per team
     const size_t bw = fused::kBarrierWords;
     const size_t words = 32 + (bw + 32) * (size_t)n_teams;
     d_words.alloc(c0, sizeof(unsigned) * words);
+    std::vector<int> map;
+    map.insert(map.end(), team_of.begin(), team_of.end());
+    map.insert(map.end(), rank_of.begin(), rank_of.end());
+    map.insert(map.end(), size_of.begin(), size_of.end());
+    map.insert(map.end(), first_of.begin(), first_of.end());
+    d_map.alloc(c0, sizeof(int) * map.size());
+    c0->upload(d_map.ptr, map.data(), sizeof(int) * map.size());
     c0->upload(d_probs.ptr, sorted.data(), sizeof(BatchProblem) * (size_t)n);
     int *queue = d_words.as<int>();
     unsigned *bars = d_words.as<unsigned>() + 32;
     int *slots = d_words.as<int>() + 32 + bw * (size_t)n_teams;
+    // problems handed out in advance (one per team in the proportional layout)
+    int handed = 0;
+    for (int f : first_of) handed += (f >= 0) ? 1 : 0;
     unsigned long long wait_ns = 2000000000ull;
     if (c0->inject_cg_wait) {
       c0->inject_cg_wait = false;
@@ -691,8 +759,8 @@ int invert_batch_persistent(int n, Context *const *ctxs, const grada_invert_para
     GRADA_CUDA_CHECK(cudaStreamBeginCapture(c0->stream, cudaStreamCaptureModeThreadLocal));
     try {
       GRADA_CUDA_CHECK(cudaMemsetAsync(d_words.ptr, 0, sizeof(unsigned) * words, c0->stream));
-      launch_invert_batch(d_probs.as<BatchProblem>(), n, queue, bars, slots, team, grid, kind,
-                          wait_ns, c0->stream);
+      launch_invert_batch(d_probs.as<BatchProblem>(), n, queue, handed, bars, slots,
+                          d_map.as<int>(), n_teams, grid, kind, wait_ns, c0->stream);
     } catch (...) {
       cudaGraph_t gph = nullptr;
       cudaStreamEndCapture(c0->stream, &gph);
@@ -715,7 +783,7 @@ int invert_batch_persistent(int n, Context *const *ctxs, const grada_invert_para
       if (h_words[32 + bw * (size_t)t + 224])
         throw Error(GRADA_ERR_CUDA, "persistent batch: a team barrier wait expired");
     c0->last_batch_teams = n_teams;
-    c0->last_batch_team_ctas = team;
+    c0->last_batch_team_ctas = team > 0 ? team : -1;
   } catch (const Error &e) {
     err = e.what();
     return e.status;

@@ -52,13 +52,16 @@ struct alignas(16) BatchProblem {
 // The kernel copies a problem to shared memory in 16-byte words.
 static_assert(sizeof(BatchProblem) % 16 == 0, "BatchProblem is copied in 16-byte words");
 
-// Runs problems[0..n) (device array) on teams of team_ctas CTAs of one
-// cooperative launch; queue[0] (zeroed) hands out problems in index order,
-// bar_words holds 32 words per team (zeroed).  kind: storage of the CG G
-// (the same for every problem).
-int invert_batch_grid(GKind kind, int sm_count, int team_ctas);
-void launch_invert_batch(const BatchProblem *problems, int n, int *queue, unsigned *bar_words,
-                         int *team_slot, int team_ctas, int grid, GKind kind,
-                         unsigned long long wait_ns, cudaStream_t s);
+// Runs problems[0..n) (device array) on the teams of one cooperative launch.
+// map (device ints): team of each CTA [grid], its rank in the team [grid], the
+// size of each team [n_teams], each team's first problem [n_teams] (-1: take
+// it from the queue); queue[0] (zeroed) counts the problems the queue has
+// handed out after the first queue_base (those handed out in advance), in
+// index order; bar_words holds the teams' barrier words (zeroed); team_slot
+// 32 ints per team.  kind: storage of the CG G (the same for every problem).
+int invert_batch_resident(GKind kind, int sm_count);
+void launch_invert_batch(const BatchProblem *problems, int n, int *queue, int queue_base,
+                         unsigned *bar_words, int *team_slot, const int *map, int n_teams,
+                         int grid, GKind kind, unsigned long long wait_ns, cudaStream_t s);
 
 }  // namespace grada

@@ -326,8 +326,10 @@ def invert_batch_persistent(invs, prms, m_inis, m_mins, m_maxs, m0s=None, fp64_r
                             team_ctas: int = 0):
     """grada_invert_batch_persistent: the inversions of several GaussNewtonInversion
     objects (one device, the same G storage) in one persistent cooperative launch,
-    a team of CTAs per problem.  Returns ([(m, report)] in input order, (teams,
-    CTAs per team))."""
+    a team of CTAs per problem.  team_ctas: > 0 teams of that size taking problems
+    from a device queue, -1 one team per problem sized by its G, 0 the tuning
+    table's choice.  Returns ([(m, report)] in input order, (teams, CTAs per team
+    or -1))."""
     lib = invs[0].ctx.lib
     n = len(invs)
     dp = ctypes.POINTER(ctypes.c_double)

@@ -414,9 +414,12 @@ int grada_invert_batch(int n, grada_ctx *const *ctxs, const grada_invert_params 
 /*
  * The same batch as grada_invert_batch in ONE persistent cooperative launch
  * (captured in a CUDA graph) instead of host threads: the GPU's resident CTAs
- * are split into teams of team_ctas CTAs (0 = the loaded tuning table's choice
- * for the batch's largest G, else 8); each team takes the next problem from a
- * device queue, largest first, and runs its whole invert_with_own_CG
+ * are split into teams.  team_ctas > 0: teams of that many CTAs, each taking
+ * the next problem from a device queue, largest first; -1: one team per
+ * problem, its CTAs in proportion to the problem's G, all problems at once
+ * (with more problems than resident CTAs, teams of 8 and the queue); 0: the
+ * loaded tuning table's choice for the batch's largest G (8 without a table).
+ * A team runs its problem's whole invert_with_own_CG
  * (GaussNewtonInversion.cpp:657-1103: lambda search, CG solves, bound
  * transform, misfits, IRLS, stopping tests) on the device, then the next.
  * Each problem's model, report and trial/iteration records are bitwise those
@@ -435,7 +438,7 @@ int grada_invert_batch_persistent(int n, grada_ctx *const *ctxs,
                                   int team_ctas, int *statuses);
 /*
  * The team-size table of grada_invert_batch_persistent, a text file of rows
- * "<largest G of the batch, entries> <CTAs per team>" ('#' starts a comment),
+ * "<largest G of the batch, entries> <CTAs per team, or -1>" ('#' starts a comment),
  * written by graada3d_gb300/autotune.py from measured batches.  Process-wide.
  */
 int grada_load_batch_tuning(const char *path);

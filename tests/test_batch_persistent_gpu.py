@@ -3,7 +3,8 @@ each problem's whole invert_with_own_CG (GaussNewtonInversion.cpp:657-1103)
 runs on a team of CTAs from a device queue, and its model, report and
 lambda/misfit record are bitwise those of grada_invert on its own -- for L2,
 L1 with the cross-gradient and reference-model terms, and L0 problems, FP64 G
-or FP32 G with the FP64 G kept, and any team size (the single runs take the
+or FP32 G with the FP64 G kept, any team size and the one-team-per-problem
+layout (the single runs take the
 persistent CG loop too, GRADA_CG_FUSED=1)."""
 import numpy as np
 import pytest
@@ -96,9 +97,11 @@ def test_persistent_batch_equals_single_inversions(storage):
     mixed = storage != "fp64"
     probs = _problems(storage)
     single = _singles(probs, mixed)
-    for team in (1, 3, 16):
+    for team in (1, 3, 16, -1):  # -1: one team per problem, sized by its G
         res, (teams, per) = _batch(probs, mixed, team)
         assert per == team and teams >= 1
+        if team < 0:
+            assert teams == len(probs)
         for k, ((m, rep), (m1, rep1, tr1, it1)) in enumerate(zip(res, single)):
             assert np.array_equal(m, m1), (storage, team, k)
             assert rep == rep1, (storage, team, k)
