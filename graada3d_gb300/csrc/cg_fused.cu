@@ -74,7 +74,7 @@ int fused_cg_grid(GKind kind, int sm_count) {
 void fused_gx_partition(const DevG &G, int resident, int &tiles, int &splits, int64_t &per) {
   tiles = (int)ceil_div(G.ld, (int64_t)256 * vec_of(G.kind));
   int64_t sp = (2 * (int64_t)resident) / tiles;  // two rounds of the resident CTAs
-  const int64_t max_splits = ceil_div(G.nm, 64);
+  const int64_t max_splits = ceil_div(G.nm, 16);  // at least 16 columns per range
   if (sp > max_splits) sp = max_splits;
   if (sp < 1) sp = 1;
   if (sp > 65535) sp = 65535;
