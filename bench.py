@@ -503,6 +503,10 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16", "fp32+fp6
              "cg_iterations": int(rep["cg_iterations"]),
              "ms_per_cg_iteration": 1e3 * t_inv / max(1, rep["cg_iterations"]),
              "gn_misfits": [float(v) for v in inv.iterations()[:, 2]]}
+        ph, n_ph = inv.cg_phase_times()
+        if n_ph:  # the persistent CG loop ran: its phases' mean time per iteration
+            r["cg_phase_us"] = {"gp": ph[0] / 1e3, "finish_rows": ph[1] / 1e3, "step": ph[2] / 1e3,
+                                "gts_adjoint": ph[3] / 1e3}
         if st == "fp64":
             m64 = m
         else:

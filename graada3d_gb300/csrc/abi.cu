@@ -691,6 +691,15 @@ int grada_set_inversion_model(grada_ctx *ctx, const double *m, const double *m_m
   });
 }
 
+int grada_cg_phase_times(grada_ctx *ctx, double *mean_ns, int64_t *iterations) {
+  return guarded(ctx, [&] {
+    const unsigned long long it = ctx->trace_sum[4];
+    if (iterations) *iterations = (int64_t)it;
+    if (mean_ns)
+      for (int q = 0; q < 4; q++) mean_ns[q] = it ? (double)ctx->trace_sum[q] / (double)it : 0.0;
+  });
+}
+
 int grada_get_model(grada_ctx *ctx, double *m) {
   return guarded(ctx, [&] {
     if (!m) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null model vector");

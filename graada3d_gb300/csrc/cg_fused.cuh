@@ -238,6 +238,15 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
   const int maxit = in.maxit;
   int status = CG_STATUS_RUNNING;
   bool ok = true;
+  const bool tracing = a.trace && cta == 0 && threadIdx.x == 0;
+  unsigned long long span[4] = {0, 0, 0, 0}, t_last = tracing ? global_timer_ns() : 0;
+  auto stamp = [&](int phase) {
+    if (tracing) {
+      const unsigned long long t = global_timer_ns();
+      span[phase] += t - t_last;
+      t_last = t;
+    }
+  };
   while (true) {
     double *p_old = (it & 1) ? a.p2 : a.p;
     double *p_new = (it & 1) ? a.p : a.p2;
@@ -246,6 +255,7 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
       gemv::gx_partial_fold_body<L>(a.G, ld, Nm, a.per, a.r, p_old, a.P, beta, p_new, a.pp,
                                     a.scratch, b % a.tiles, b / a.tiles);
     if (!(ok = bar.sync())) break;
+    stamp(0);
     // B
     for (int64_t b = cta; b < rl.nb_t; b += nct) {
       double v;
@@ -266,6 +276,7 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
       if (threadIdx.x == 0) part_t[b] = v;
     }
     if (!(ok = bar.sync())) break;
+    stamp(1);
     // C
     T2 = sum_partials_all(part_t, rl.nb_t);
     alpha = R2 / T2;  // GaussNewtonInversion.cpp:1601
@@ -278,12 +289,14 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
       if (b < nb_prep) gemv::prep_y_body<Acc>(a.s, nd, ld, a.row_scale, a.wd, y, b);
     }
     if (!(ok = bar.sync())) break;
+    stamp(2);
     // D
     for (int64_t b = cta; b < rl.nb_r; b += nct) {
       const double v = gty_adjoint_block<L>(a, y, b);
       if (threadIdx.x == 0) part_r[b] = v;
     }
     if (!(ok = bar.sync())) break;
+    stamp(3);
     const double r2 = sum_partials_all(part_r, rl.nb_r);
     // :1674-1691
     rlast2 = R2;
@@ -300,6 +313,10 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
       break;
     }
     if (it >= maxit) break;
+  }
+  if (tracing) {
+    for (int q = 0; q < 4; q++) a.trace[q] += span[q];
+    a.trace[4] += (unsigned long long)it;
   }
   o.R2 = R2;
   o.T2 = T2;

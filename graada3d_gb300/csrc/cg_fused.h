@@ -38,7 +38,10 @@ struct FusedCgArgs {
   unsigned *red_count = nullptr;  // group counts (zero at the start, reset by their last block)
   double *scal = nullptr;
   int *ctl = nullptr;
-  unsigned *barrier = nullptr;  // 2 words: arrivals, error
+  unsigned *barrier = nullptr;  // the team barrier's words
+  // phase trace (CTA 0 of the team): summed globaltimer spans of phases A-D,
+  // each up to the end of its barrier, and the iteration count; null: none
+  unsigned long long *trace = nullptr;
   unsigned long long wait_limit_ns = 2000000000ull;
 };
 

@@ -129,6 +129,8 @@ struct Context {
   DevBuf cg_b, cg_s, cg_t, cg_p, cg_pp, cg_r, cg_atb, cg_gtw, cg_gx, cg_tmpd, cg_scal, cg_part;
   DevBuf cg_wl_ones, cg_ctl, cg_bar, cg_p2, cg_red, cg_redc;
   int fused_grid[4] = {0, 0, 0, 0};  // persistent CG grid per G storage kind
+  DevBuf cg_trace;                    // phase trace of a persistent solve (5 u64)
+  unsigned long long trace_sum[5] = {0, 0, 0, 0, 0};  // since the last invert / reset
   bool inject_cg_wait = false;       // grada_inject_fault(GRADA_FAULT_CG_WAIT)
   double *h_scal = nullptr;  // pinned
   int *h_flag = nullptr;     // pinned

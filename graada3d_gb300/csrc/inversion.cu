@@ -64,6 +64,7 @@ void Context::release_all() {
     b->release();
   DevBuf *bufs[] = {&dobs, &wd, &cg_b, &cg_s, &cg_t, &cg_p, &cg_pp, &cg_r, &cg_atb, &cg_gtw,
                     &cg_gx, &cg_tmpd, &cg_scal, &cg_part, &cg_wl_ones, &cg_ctl, &cg_bar, &cg_p2, &cg_red,
+                    &cg_trace,
                     &cg_redc, &bt_part2, &bt_trials,
                     &bt_iters, &bt_report, &iv_m, &iv_mt, &iv_mt_old,
                     &iv_mopt, &iv_dx, &iv_P, &iv_mmin, &iv_mmax, &iv_m0, &iv_wl, &iv_tmp, &iv_tmp2,
@@ -502,14 +503,20 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   upload(a.ctl, h_ctl, sizeof(int) * CTL_NINTS);
   h_scal[CG_TOL] = tol;
   upload(a.scal + CG_TOL, h_scal + CG_TOL, sizeof(double));
+  cg_trace.alloc(this, sizeof(unsigned long long) * 5);
+  a.trace = cg_trace.as<unsigned long long>();
+  GRADA_CUDA_CHECK(cudaMemsetAsync(a.trace, 0, sizeof(unsigned long long) * 5, stream));
   launch_cg_fused(a, g.kind, grid, stream);
   unsigned bar_words[256];
+  unsigned long long trace[5];
+  download(trace, a.trace, sizeof(trace));
   download(bar_words, a.barrier, sizeof(bar_words));
   download(h_ctl, a.ctl, sizeof(int) * CTL_NINTS);
   download(h_scal, a.scal, sizeof(double) * CG_NSCALARS);
   sync();
   if (bar_words[224])
     throw Error(GRADA_ERR_CUDA, "persistent CG: a grid barrier wait expired; the solve was abandoned");
+  for (int q = 0; q < 5; q++) trace_sum[q] += trace[q];
   CgResult res;
   res.iterations = h_ctl[CTL_ITER];
   res.err = h_scal[CG_ERR];
@@ -597,6 +604,7 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
     ~PredictGuard() { c->predict_fp64 = false; }
   } predict_guard{this};
   const bool refine = invert_setup(prm, h_m_ini, h_mmin, h_mmax, h_m0);
+  for (auto &t : trace_sum) t = 0;
   if (adapt && predict_fp64)
     throw Error(GRADA_ERR_STATE, "adaptive inversion: a kept FP64 G is not expanded by refinement");
   int64_t Nm = n_cells;

@@ -107,6 +107,15 @@ class GaussNewtonInversion(Fwd):
             _ptr(vec[2]), arr, _ptr(dx), ctypes.byref(err), ctypes.byref(it)))
         return dx, err.value, it.value
 
+    def cg_phase_times(self):
+        """Mean ns per CG iteration of the persistent loop's four phases (G p,
+        finish and regulariser rows, step, G^T s and adjoint) over the persistent
+        solves since the last invert, and their iteration count."""
+        out = np.zeros(4)
+        n = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.grada_cg_phase_times(self.ctx.handle, _ptr(out), ctypes.byref(n)))
+        return out, n.value
+
     def invert(self, prm: dict, m_ini, m_min, m_max, m0=None, fp64_refinement: bool = False):
         """invert_with_own_CG on the current G.  prm keys as oracle.inversion.invert
         (max_lambda, n_lambda, rate, target, stag, cg_tol, cg_factor, gn_iter,
