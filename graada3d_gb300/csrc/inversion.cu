@@ -506,7 +506,14 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   cg_trace.alloc(this, sizeof(unsigned long long) * 5);
   a.trace = cg_trace.as<unsigned long long>();
   GRADA_CUDA_CHECK(cudaMemsetAsync(a.trace, 0, sizeof(unsigned long long) * 5, stream));
-  launch_cg_fused(a, g.kind, grid, stream);
+  // CTAs of the launch: all resident ones, or fewer with GRADA_CG_CTAS (the
+  // partition above stays that of the full grid, so the sums do not change)
+  int launch_grid = grid;
+  if (const char *e = std::getenv("GRADA_CG_CTAS")) {
+    const int c = std::atoi(e);
+    if (c >= 1 && c < grid) launch_grid = c;
+  }
+  launch_cg_fused(a, g.kind, launch_grid, stream);
   unsigned bar_words[256];
   unsigned long long trace[5];
   download(trace, a.trace, sizeof(trace));
