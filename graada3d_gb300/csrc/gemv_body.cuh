@@ -241,17 +241,20 @@ __device__ __forceinline__ void prep_y_body(const double *y, int64_t nd, int64_t
 
 // G^T y for the kGtBlockCols columns of block b: warp w takes columns
 // 4w .. 4w + 3 of the block, its lanes striding the rows with 16-byte loads,
-// and sums each column with a butterfly.  Lane c < 4 of warp w returns column
-// b * kGtBlockCols + 4w + c's sum and sets *col to that column; every other
-// thread gets *col = -1.
+// and sums each column with a butterfly.  y goes through shared memory in
+// chunks of kYChunk rows, read once per block with 16-byte loads (not once
+// per warp).  Lane c < 4 of warp w returns column b * kGtBlockCols + 4w + c's
+// sum and sets *col to that column; every other thread gets *col = -1.
 constexpr int kGtWarpCols = 4;
 constexpr int kGtBlockCols = kGtWarpCols * (kThreads / 32);
+constexpr int kYChunk = 1024;
 
 template <class L>
 __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t ld, int64_t nm,
                                            const typename L::Acc *y, int64_t b, int64_t *col) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
+  __shared__ __align__(16) Acc ys[kYChunk];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t c0 = b * kGtBlockCols + (int64_t)warp * kGtWarpCols;
   const int64_t left = nm - c0;
@@ -259,19 +262,34 @@ __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t l
   Acc acc[kGtWarpCols];
 #pragma unroll
   for (int c = 0; c < kGtWarpCols; c++) acc[c] = Acc(0);
-  if (ncol > 0) {
+  // 16 bytes of y per load: 4 floats or 2 doubles
+  constexpr int YV = 16 / (int)sizeof(Acc);
+  for (int64_t r0 = 0; r0 < ld; r0 += kYChunk) {
+    const int n = (int)min((int64_t)kYChunk, ld - r0);  // a multiple of 64 (ld is)
+    __syncthreads();
+    for (int t = threadIdx.x * YV; t < n; t += kThreads * YV) {
+      if constexpr (YV == 4) {
+        *reinterpret_cast<float4 *>(&ys[t]) = __ldcg(reinterpret_cast<const float4 *>(y + r0 + t));
+      } else {
+        *reinterpret_cast<double2 *>(&ys[t]) =
+            __ldcg(reinterpret_cast<const double2 *>(y + r0 + t));
+      }
+    }
+    __syncthreads();
+    if (ncol > 0) {
 #pragma unroll 2
-    for (int64_t row = (int64_t)lane * VEC; row < ld; row += 32 * VEC) {
-      Acc yv[VEC];
+      for (int row = lane * VEC; row < n; row += 32 * VEC) {
+        Acc yv[VEC];
 #pragma unroll
-      for (int v = 0; v < VEC; v++) yv[v] = __ldcg(y + row + v);
+        for (int v = 0; v < VEC; v++) yv[v] = ys[row + v];
 #pragma unroll
-      for (int c = 0; c < kGtWarpCols; c++) {
-        if (c < ncol) {
-          Acc g[VEC];
-          L::load(G, row + (c0 + c) * ld, g);
+        for (int c = 0; c < kGtWarpCols; c++) {
+          if (c < ncol) {
+            Acc g[VEC];
+            L::load(G, r0 + row + (c0 + c) * ld, g);
 #pragma unroll
-          for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
+            for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
+          }
         }
       }
     }
