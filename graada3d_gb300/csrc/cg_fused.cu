@@ -82,8 +82,9 @@ void fused_gx_partition(const DevG &G, int resident, int &tiles, int &splits, in
   per = ceil_div(G.nm, splits);
 }
 
-void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t &doubles, int64_t &counters) {
-  const fused::RedLayout rl(nd, nm, nterms);
+void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t vranges, int64_t &doubles,
+                     int64_t &counters) {
+  const fused::RedLayout rl(nd, nm, nterms, vranges);
   doubles = rl.doubles();
   counters = rl.counters();
 }

@@ -22,6 +22,7 @@ struct FusedCgArgs {
   int64_t nd = 0, nm = 0, ld = 0;
   int tiles = 0, splits = 0;
   int64_t per = 0;
+  int64_t vranges = 1;        // column ranges of G^T s (the full grid's CTA count)
   double *scratch = nullptr;  // splits * ld doubles: G x partials, then y
   const double *wd = nullptr;  // Wd: post-scale of G pp, pre-scale of G^T s
   // CG vectors (GaussNewtonInversion.cpp:1556-1692)
@@ -52,7 +53,8 @@ int fused_cg_grid(GKind kind, int sm_count);
 void fused_gx_partition(const DevG &G, int resident, int &tiles, int &splits, int64_t &per);
 // Doubles and counters of a.red / a.red_count for a loop over Nm cells, Nd
 // rows and nterms regulariser terms.
-void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t &doubles, int64_t &counters);
+void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t vranges, int64_t &doubles,
+                     int64_t &counters);
 // Clears the barrier words and launches the cooperative kernel.
 void launch_cg_fused(const FusedCgArgs &a, GKind kind, int grid, cudaStream_t s);
 

@@ -462,6 +462,7 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
   const int grid = fused_grid[(int)g.kind];
   fused_gx_partition(g, grid, a.tiles, a.splits, a.per);
+  a.vranges = std::min<int64_t>(grid, g.nm);
   a.scratch = scratch_doubles(std::max(product_scratch_doubles(), (int64_t)a.splits * g.ld));
   a.wd = dptr(wd);
   a.r = dptr(cg_r);
@@ -486,7 +487,7 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   cg_bar.alloc(this, sizeof(unsigned) * 256);
   a.barrier = cg_bar.as<unsigned>();
   int64_t red_d = 0, red_c = 0;
-  fused_red_sizes(nd, n_cells, FT.count, red_d, red_c);
+  fused_red_sizes(nd, n_cells, FT.count, a.vranges, red_d, red_c);
   cg_red.alloc(this, sizeof(double) * (size_t)red_d);
   cg_redc.alloc(this, sizeof(unsigned) * (size_t)red_c);
   GRADA_CUDA_CHECK(cudaMemsetAsync(cg_redc.ptr, 0, sizeof(unsigned) * (size_t)red_c, stream));
