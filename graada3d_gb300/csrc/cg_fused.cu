@@ -8,12 +8,14 @@
 // test itself from the same reduced scalars, so no host round trip or launch
 // happens until the solve ends.  The sums are fixed-order and independent of
 // the grid, so a solve is deterministic and gives what the batched kernel
-// (invert_batch.cu) gives for the same problem; against the graph path it
-// agrees to rounding (different summation orders).  Every barrier wait is
+// (invert_batch.cu) and the phase kernels (cg_phases.cu) give for the same
+// problem; against the generic graph path it agrees to rounding (different
+// summation orders).  Every barrier wait is
 // bounded (a globaltimer limit): a CTA whose wait expires raises the barrier's
 // error word and returns, every other CTA returns at its next barrier, and the
 // host turns the word into GRADA_ERR_CUDA with the context still usable.
 #include <algorithm>
+#include <cstdlib>
 
 #include "cg_fused.cuh"
 
@@ -71,9 +73,18 @@ int fused_cg_grid(GKind kind, int sm_count) {
   return std::max(1, per_sm) * sm_count;
 }
 
-void fused_gx_partition(const DevG &G, int resident, int &tiles, int &splits, int64_t &per) {
+int fused_gx_units(int sm_count) {
+  int per_sm = 12;  // divisible by 1, 2, 3, 4 and 6 resident blocks per SM
+  if (const char *e = std::getenv("GRADA_GX_UNITS_PER_SM")) {
+    const int v = std::atoi(e);
+    if (v >= 1 && v <= 64) per_sm = v;
+  }
+  return per_sm * sm_count;
+}
+
+void fused_gx_partition(const DevG &G, int units, int &tiles, int &splits, int64_t &per) {
   tiles = (int)ceil_div(G.ld, (int64_t)256 * vec_of(G.kind));
-  int64_t sp = (2 * (int64_t)resident) / tiles;  // two rounds of the resident CTAs
+  int64_t sp = (int64_t)units / tiles;
   const int64_t max_splits = ceil_div(G.nm, 16);  // at least 16 columns per range
   if (sp > max_splits) sp = max_splits;
   if (sp < 1) sp = 1;
@@ -82,9 +93,8 @@ void fused_gx_partition(const DevG &G, int resident, int &tiles, int &splits, in
   per = ceil_div(G.nm, splits);
 }
 
-void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t vranges, int64_t &doubles,
-                     int64_t &counters) {
-  const fused::RedLayout rl(nd, nm, nterms, vranges);
+void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t &doubles, int64_t &counters) {
+  const fused::RedLayout rl(nd, nm, nterms);
   doubles = rl.doubles();
   counters = rl.counters();
 }

@@ -151,80 +151,27 @@ __device__ __forceinline__ double finish_rows(const double *partial, int n_split
   return bcast_sum(sq);
 }
 
-// G^T y and r for the columns [c_lo, c_hi) of one range: warp w takes columns
-// c_lo + w, c_lo + w + 8, ... in passes of up to kPassCols, its lanes striding
-// the rows with 16-byte loads; y goes through shared memory in chunks of
-// gemv::kYChunk rows.  Lane c of a pass holds its c-th column's sum and
-// computes r_j there (the adjoint of the regulariser rows and P).  Writes gtw
-// and r; returns the range's sum of r_j^2, added lane by lane in pass order,
-// then over lanes and warps in fixed trees (valid in every thread) -- the same
-// whichever CTA runs the range.
-constexpr int kPassCols = 8;
-
-template <class L>
-__device__ __forceinline__ double gty_adjoint_range(const FusedCgArgs &a, const typename L::Acc *y,
-                                                    int64_t c_lo, int64_t c_hi) {
-  using Acc = typename L::Acc;
-  constexpr int VEC = L::VEC;
-  constexpr int NW = cgb::VT / 32;
-  constexpr int YV = 16 / (int)sizeof(Acc);
-  __shared__ __align__(16) Acc ys[gemv::kYChunk];
-  __shared__ double wsum[NW];
+// G^T y for the 32 columns of block b (warp w takes columns 4w .. 4w + 3,
+// lanes striding the rows), then r_j for those columns (the adjoint of the
+// regulariser rows and P) on the lanes holding a column.  StageY: y through
+// shared memory (gemv::gty_body, for a kernel of its own at full occupancy),
+// else read from L2 by each warp (gemv::gty_body_l2, the persistent loop's);
+// both sum each column in the same order.  Writes gtw and r; returns the
+// block's sum of r_j^2 (valid in every thread).
+template <class L, bool StageY = false>
+__device__ __forceinline__ double gty_adjoint_block(const FusedCgArgs &a, const typename L::Acc *y,
+                                                    int64_t b) {
+  __shared__ double wsum[cgb::VT / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t width = c_hi > c_lo ? c_hi - c_lo : 0;
-  const int64_t per_warp_max = (width + NW - 1) / NW;  // columns of warp 0
-  const int64_t passes = (per_warp_max + kPassCols - 1) / kPassCols;
-  const int64_t mine_cols = width > warp ? (width - warp + NW - 1) / NW : 0;
+  int64_t j = -1;
+  const double g = StageY ? gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j)
+                          : gemv::gty_body_l2<L>(a.G, a.ld, a.nm, y, b, &j);
   double sq = 0.0;
-  for (int64_t ps = 0; ps < passes; ps++) {
-    const int64_t k0 = ps * kPassCols;  // this pass: the warp's columns k0 .. k0 + 7
-    const int ncol = (int)max((int64_t)0, min((int64_t)kPassCols, mine_cols - k0));
-    Acc acc[kPassCols];
-#pragma unroll
-    for (int c = 0; c < kPassCols; c++) acc[c] = Acc(0);
-    for (int64_t r0 = 0; r0 < a.ld; r0 += gemv::kYChunk) {
-      const int n = (int)min((int64_t)gemv::kYChunk, a.ld - r0);
-      __syncthreads();
-      for (int t = threadIdx.x * YV; t < n; t += cgb::VT * YV) {
-        if constexpr (YV == 4) {
-          *reinterpret_cast<float4 *>(&ys[t]) = __ldcg(reinterpret_cast<const float4 *>(y + r0 + t));
-        } else {
-          *reinterpret_cast<double2 *>(&ys[t]) =
-              __ldcg(reinterpret_cast<const double2 *>(y + r0 + t));
-        }
-      }
-      __syncthreads();
-      if (ncol > 0) {
-        for (int row = lane * VEC; row < n; row += 32 * VEC) {
-          Acc yv[VEC];
-#pragma unroll
-          for (int v = 0; v < VEC; v++) yv[v] = ys[row + v];
-#pragma unroll
-          for (int c = 0; c < kPassCols; c++) {
-            if (c < ncol) {
-              const int64_t j = c_lo + warp + (k0 + c) * NW;
-              Acc g[VEC];
-              L::load(a.G, r0 + row + j * a.ld, g);
-#pragma unroll
-              for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
-            }
-          }
-        }
-      }
-    }
-    double colsum = 0.0;
-#pragma unroll
-    for (int c = 0; c < kPassCols; c++) {
-      const double v = cgb::warp_sum((double)acc[c]);
-      if (lane == c) colsum = v;
-    }
-    if (lane < ncol) {
-      const int64_t j = c_lo + warp + (k0 + lane) * NW;
-      a.gtw[j] = colsum;
-      const double rj = cgb::adjoint_column(a.AT, j, a.P, true, colsum, 1.0);
-      a.r[j] = rj;
-      sq += rj * rj;
-    }
+  if (j >= 0) {
+    a.gtw[j] = g;
+    const double rj = cgb::adjoint_column(a.AT, j, a.P, true, g, 1.0);
+    a.r[j] = rj;
+    sq = rj * rj;
   }
   sq = cgb::warp_sum(sq);
   __syncthreads();
@@ -232,7 +179,7 @@ __device__ __forceinline__ double gty_adjoint_range(const FusedCgArgs &a, const 
   __syncthreads();
   double tot = 0.0;
 #pragma unroll
-  for (int w = 0; w < NW; w++) tot += wsum[w];
+  for (int w = 0; w < cgb::VT / 32; w++) tot += wsum[w];
   return tot;
 }
 
@@ -251,10 +198,10 @@ struct CgOut {
 // and forward-row blocks, then of ||r||^2 over the G^T blocks.
 struct RedLayout {
   int64_t nb_fin, nb_t, nb_r;
-  __host__ __device__ RedLayout(int64_t nd, int64_t nm, int nterms, int64_t vranges) {
+  __host__ __device__ RedLayout(int64_t nd, int64_t nm, int nterms) {
     nb_fin = ceil_div_d(nd, kFinRows);
     nb_t = nb_fin + (int64_t)nterms * ceil_div_d(nm, 256);
-    nb_r = vranges;
+    nb_r = ceil_div_d(nm, gemv::kGtBlockCols);
   }
   __host__ __device__ int64_t doubles() const { return nb_t + nb_r; }
   __host__ __device__ int64_t counters() const { return 1; }
@@ -269,10 +216,9 @@ struct RedLayout {
 //      by 8 warps), the forward regulariser rows of t, per-block ||t||^2
 //   C  alpha = r2 / t2; s += alpha t, dx += alpha p_new, y = Wd s_data in G's
 //      accumulation type
-//   D  G^T y and r (the adjoint of the regulariser rows, P) over column
-//      ranges, one per CTA of the full grid (vranges of them, the same for a
-//      team of any size), per-range ||r||^2; then beta, err and the stopping
-//      test
+//   D  G^T y for 32 columns per block (4 per warp), r for those columns (the
+//      adjoint of the regulariser rows, P), per-block ||r||^2; then beta, err
+//      and the stopping test
 // Every CTA adds the per-block partials in index order, so the sums do not
 // depend on the team size or on which CTA ran which block.
 template <class L>
@@ -284,8 +230,7 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
   const int64_t nb_axpy = ceil_div_d(nrow > Nm ? nrow : Nm, cgb::VT);
   const int64_t nb_prep = ceil_div_d(ld, 256);
   const int64_t n_gx = (int64_t)a.tiles * a.splits;
-  const RedLayout rl(nd, Nm, a.FT.count, a.vranges);
-  const int64_t vwidth = ceil_div_d(Nm, a.vranges);  // columns per range
+  const RedLayout rl(nd, Nm, a.FT.count);
   double *part_t = a.red, *part_r = a.red + rl.nb_t;
   Acc *y = reinterpret_cast<Acc *>(a.scratch);
 
@@ -358,8 +303,7 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
     stamp(2);
     // D
     for (int64_t b = cta; b < rl.nb_r; b += nct) {
-      const int64_t lo = b * vwidth, hi = min(Nm, lo + vwidth);
-      const double v = gty_adjoint_range<L>(a, y, lo, hi);
+      const double v = gty_adjoint_block<L>(a, y, b);
       if (threadIdx.x == 0) part_r[b] = v;
     }
     if (!(ok = bar.sync())) break;

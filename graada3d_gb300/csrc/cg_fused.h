@@ -22,7 +22,6 @@ struct FusedCgArgs {
   int64_t nd = 0, nm = 0, ld = 0;
   int tiles = 0, splits = 0;
   int64_t per = 0;
-  int64_t vranges = 1;        // column ranges of G^T s (the full grid's CTA count)
   double *scratch = nullptr;  // splits * ld doubles: G x partials, then y
   const double *wd = nullptr;  // Wd: post-scale of G pp, pre-scale of G^T s
   // CG vectors (GaussNewtonInversion.cpp:1556-1692)
@@ -48,14 +47,20 @@ struct FusedCgArgs {
 
 // CTAs of a persistent CG launch for this storage (all co-resident).
 int fused_cg_grid(GKind kind, int sm_count);
-// G pp's partition in the persistent loop: row tiles of 256 * vec rows and
-// column ranges so that tiles x splits is two rounds of the resident CTAs.
-void fused_gx_partition(const DevG &G, int resident, int &tiles, int &splits, int64_t &per);
+// Work units of G pp in the persistent loop and its phase kernels: 12 per SM
+// (GRADA_GX_UNITS_PER_SM overrides), a whole number of rounds at 1, 2, 3, 4
+// or 6 resident blocks per SM.
+int fused_gx_units(int sm_count);
+// G pp's partition: row tiles of 256 * vec rows and column ranges, about
+// `units` of them.  The sums of a solve depend on it, not on the launch.
+void fused_gx_partition(const DevG &G, int units, int &tiles, int &splits, int64_t &per);
 // Doubles and counters of a.red / a.red_count for a loop over Nm cells, Nd
 // rows and nterms regulariser terms.
-void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t vranges, int64_t &doubles,
-                     int64_t &counters);
+void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t &doubles, int64_t &counters);
 // Clears the barrier words and launches the cooperative kernel.
 void launch_cg_fused(const FusedCgArgs &a, GKind kind, int grid, cudaStream_t s);
+// One iteration of the same loop as four kernels (cg_phases.cu); parity
+// alternates p and p2 as the persistent loop's iteration count does.
+void launch_cg_phase_iteration(const FusedCgArgs &a, GKind kind, int parity, cudaStream_t s);
 
 }  // namespace grada

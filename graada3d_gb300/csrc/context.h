@@ -77,6 +77,7 @@ struct CgTerms {
 };
 
 struct BatchProblem;
+struct FusedCgArgs;
 
 struct Context {
   int device = 0;
@@ -186,10 +187,14 @@ struct Context {
   int last_batch_teams = 0, last_batch_team_ctas = 0;  // shape of the last persistent batch
   void batch_problem(const grada_invert_params &prm, BatchProblem &bp);
   void batch_results(const grada_invert_params &prm, double *h_m_out, grada_invert_report &rep);
-  bool fused_cg_eligible() const;
+  // CG loop of a single solve: kCgGeneric (graph of the generic product
+  // kernels), kCgPhases (graph of the persistent loop's four phases), kCgPersistent
+  enum CgLoop { kCgGeneric = 0, kCgPersistent = 1, kCgPhases = 2 };
+  CgLoop cg_loop_kind() const;
   CgResult solve_cg_fused(double tol, int maxit, const double *P, double *dx,
                           const ForwardTerms &FT, const AdjointTerms &AT, int64_t nrow, int nb_m,
-                          int nb_row);
+                          int nb_row, bool persistent);
+  CgResult solve_cg_phases(const FusedCgArgs &a, GKind kind, int maxit);
   CgResult solve_cg_dev(double lambda, double tol, int maxit, const double *mk, const double *mref,
                         const double *P, const double *const WL[7], double *dx,
                         const double *d64, const double *m_start);

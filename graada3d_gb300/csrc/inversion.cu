@@ -354,7 +354,9 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
                                    cudaMemcpyDeviceToHost, stream));
   sync();
   if (h_scal[CG_R2] == 0.0) return res;
-  if (fused_cg_eligible()) return solve_cg_fused(tol, maxit, P, dx, FT, AT_s, nrow, nb_m, nb_row);
+  const CgLoop loop = cg_loop_kind();
+  if (loop != kCgGeneric)
+    return solve_cg_fused(tol, maxit, P, dx, FT, AT_s, nrow, nb_m, nb_row, loop == kCgPersistent);
   // Device-side stopping: the beta kernel counts iterations and raises
   // ctl[CTL_DONE] on err < tol (or maxit, breakdown, non-finite scalar);
   // every kernel of an iteration returns at once while it is raised, so a
@@ -430,28 +432,27 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
   return res;
 }
 
-bool Context::fused_cg_eligible() const {
-  // Stored dense G only (the matrix-free and wavelet products keep the graph
-  // path).  FP32 and 16-bit G: the persistent loop (HBM-bound products, where
-  // removing launches and host round trips pays).  FP64 G: the graph path,
-  // whose full-occupancy products keep the FP64 pipe (2 DFMA per clock per
-  // SM) busier than the persistent loop's three CTAs per SM.
-  // GRADA_CG_FUSED=1 takes the persistent loop for every stored G (FP64
-  // included, as the batched kernel runs it), =0 the graph path for all.
+Context::CgLoop Context::cg_loop_kind() const {
+  // Stored dense G runs the persistent loop's phase bodies: by default as a
+  // graph of four kernels per iteration (cg_phases.cu), each at its own
+  // occupancy; GRADA_CG_FUSED=1 takes the one-launch persistent loop (the
+  // batched inversion's engine, bitwise the same solve).  The matrix-free and
+  // wavelet products, and GRADA_CG_FUSED=0, take the graph of the generic
+  // product kernels (13 per iteration, other summation orders).
   if (g_storage != GRADA_G_FP64 && g_storage != GRADA_G_FP32 && g_storage != GRADA_G_BF16_ROWSCALE &&
       g_storage != GRADA_G_FP16_ROWSCALE)
-    return false;
+    return kCgGeneric;
   const char *e = std::getenv("GRADA_CG_FUSED");
-  if (e && e[0] == '0') return false;
-  if (e && e[0] == '1') return true;
-  return g_storage != GRADA_G_FP64;
+  if (e && e[0] == '0') return kCgGeneric;
+  if (e && e[0] == '1') return kCgPersistent;
+  return kCgPhases;
 }
 
 // The CG loop as one persistent cooperative launch (cg_fused.cu), from the
 // state the setup of solve_cg_dev left on the device.
 CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double *dx,
                                  const ForwardTerms &FT, const AdjointTerms &AT, int64_t nrow,
-                                 int nb_m, int nb_row) {
+                                 int nb_m, int nb_row, bool persistent) {
   const DevG g = devG();
   FusedCgArgs a;
   a.G = g.data;
@@ -461,8 +462,7 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   a.ld = g.ld;
   if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
   const int grid = fused_grid[(int)g.kind];
-  fused_gx_partition(g, grid, a.tiles, a.splits, a.per);
-  a.vranges = std::min<int64_t>(grid, g.nm);
+  fused_gx_partition(g, fused_gx_units(sm_count), a.tiles, a.splits, a.per);
   a.scratch = scratch_doubles(std::max(product_scratch_doubles(), (int64_t)a.splits * g.ld));
   a.wd = dptr(wd);
   a.r = dptr(cg_r);
@@ -487,7 +487,7 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   cg_bar.alloc(this, sizeof(unsigned) * 256);
   a.barrier = cg_bar.as<unsigned>();
   int64_t red_d = 0, red_c = 0;
-  fused_red_sizes(nd, n_cells, FT.count, a.vranges, red_d, red_c);
+  fused_red_sizes(nd, n_cells, FT.count, red_d, red_c);
   cg_red.alloc(this, sizeof(double) * (size_t)red_d);
   cg_redc.alloc(this, sizeof(unsigned) * (size_t)red_c);
   GRADA_CUDA_CHECK(cudaMemsetAsync(cg_redc.ptr, 0, sizeof(unsigned) * (size_t)red_c, stream));
@@ -504,11 +504,12 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   upload(a.ctl, h_ctl, sizeof(int) * CTL_NINTS);
   h_scal[CG_TOL] = tol;
   upload(a.scal + CG_TOL, h_scal + CG_TOL, sizeof(double));
+  if (!persistent) return solve_cg_phases(a, g.kind, maxit);
   cg_trace.alloc(this, sizeof(unsigned long long) * 5);
   a.trace = cg_trace.as<unsigned long long>();
   GRADA_CUDA_CHECK(cudaMemsetAsync(a.trace, 0, sizeof(unsigned long long) * 5, stream));
   // CTAs of the launch: all resident ones, or fewer with GRADA_CG_CTAS (the
-  // partition above stays that of the full grid, so the sums do not change)
+  // partition above does not depend on the launch, so the sums do not change)
   int launch_grid = grid;
   if (const char *e = std::getenv("GRADA_CG_CTAS")) {
     const int c = std::atoi(e);
@@ -525,6 +526,56 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   if (bar_words[224])
     throw Error(GRADA_ERR_CUDA, "persistent CG: a grid barrier wait expired; the solve was abandoned");
   for (int q = 0; q < 5; q++) trace_sum[q] += trace[q];
+  CgResult res;
+  res.iterations = h_ctl[CTL_ITER];
+  res.err = h_scal[CG_ERR];
+  if (h_ctl[CTL_STATUS] == CG_STATUS_BREAKDOWN)
+    throw Error(GRADA_ERR_BREAKDOWN,
+                "CG breakdown: ||t||^2 = 0 at iteration " + std::to_string(res.iterations));
+  if (h_ctl[CTL_STATUS] == CG_STATUS_NONFINITE)
+    throw Error(GRADA_ERR_NONFINITE,
+                "non-finite CG scalar at iteration " + std::to_string(res.iterations));
+  return res;
+}
+
+// The persistent loop's phases as a graph of four kernels per iteration
+// (cg_phases.cu), replayed until the device raises ctl[CTL_DONE]; a holds the
+// state solve_cg_fused set up.  K iterations per graph, K even (or maxit), so
+// the p / p2 parity of a captured iteration is that of the solve's count.
+CgResult Context::solve_cg_phases(const FusedCgArgs &a, GKind kind, int maxit) {
+  const int K = std::min(maxit, kCgGraphIters);
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  GRADA_CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    for (int k = 0; k < K; k++) launch_cg_phase_iteration(a, kind, k & 1, stream);
+  } catch (...) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(stream, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  GRADA_CUDA_CHECK(cudaStreamEndCapture(stream, &graph));
+  cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  GRADA_CUDA_CHECK(ie);
+  int launched = 0;
+  try {
+    while (true) {
+      GRADA_CUDA_CHECK(cudaGraphLaunch(exec, stream));
+      launched += K;
+      GRADA_CUDA_CHECK(cudaMemcpyAsync(h_ctl, a.ctl, sizeof(int) * CTL_NINTS,
+                                       cudaMemcpyDeviceToHost, stream));
+      GRADA_CUDA_CHECK(cudaMemcpyAsync(h_scal, a.scal, sizeof(double) * CG_NSCALARS,
+                                       cudaMemcpyDeviceToHost, stream));
+      sync();
+      if (h_ctl[CTL_DONE] || launched >= maxit) break;
+    }
+  } catch (...) {
+    cudaGraphExecDestroy(exec);
+    throw;
+  }
+  cudaGraphExecDestroy(exec);
   CgResult res;
   res.iterations = h_ctl[CTL_ITER];
   res.err = h_scal[CG_ERR];

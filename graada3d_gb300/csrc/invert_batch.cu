@@ -455,10 +455,9 @@ void Context::batch_problem(const grada_invert_params &prm, BatchProblem &bp) {
   a.nd = g.nd;
   a.nm = g.nm;
   a.ld = g.ld;
-  // the single solve's partition (its grid), so both paths sum alike
+  // the single solve's partition, so both paths sum alike
   if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
-  fused_gx_partition(g, fused_grid[(int)g.kind], a.tiles, a.splits, a.per);
-  a.vranges = std::min<int64_t>(fused_grid[(int)g.kind], g.nm);
+  fused_gx_partition(g, fused_gx_units(sm_count), a.tiles, a.splits, a.per);
   if ((int64_t)a.splits * g.ld > need) scr = scratch_doubles((int64_t)a.splits * g.ld);
   a.scratch = scr;
   a.wd = dbuf(wd);
@@ -480,7 +479,7 @@ void Context::batch_problem(const grada_invert_params &prm, BatchProblem &bp) {
   a.nb_row = dot_blocks(nrow, sm_count);
   a.scal = dbuf(cg_scal);
   int64_t red_d = 0, red_c = 0;
-  fused_red_sizes(Nd, Nm, nterms, a.vranges, red_d, red_c);
+  fused_red_sizes(Nd, Nm, nterms, red_d, red_c);
   cg_red.alloc(this, sizeof(double) * (size_t)red_d);
   cg_redc.alloc(this, sizeof(unsigned) * (size_t)red_c);
   GRADA_CUDA_CHECK(cudaMemsetAsync(cg_redc.ptr, 0, sizeof(unsigned) * (size_t)red_c, stream));

@@ -1,7 +1,8 @@
 """The persistent CG solve (one cooperative launch per solve_cg, cg_fused.cu)
 against the reference's solve_cg (GaussNewtonInversion.cpp:1417-1698, the
-compiled reference's fixtures) and against the graph-replayed iteration it
-replaces.  The two device paths sum the dot products and G p's column ranges
+compiled reference's fixtures), against its phases run as a graph of four
+kernels per iteration (cg_phases.cu, the default for stored G: bitwise the same
+solve) and against the generic graph-replayed iteration.  The two device paths sum the dot products and G p's column ranges
 in different (each fixed) orders, so they agree to rounding: FP64 to 1e-9 of
 max|dx|, reduced-precision G to 1e-4, iteration counts within one (whole L2
 inversions: FP64 trial misfits to 1e-6, FP32 to 1e-3).  The
@@ -26,6 +27,10 @@ def fused_path():
     return cg_path("1")
 
 
+def phase_path():
+    return cg_path("2")
+
+
 def _setup(f, ctx, storage):
     inv = GaussNewtonInversion(fx.prisms(f), f["obs"], int(f["mask"]), ctx=ctx)
     inv.compute_G(storage)
@@ -40,9 +45,25 @@ def _setup(f, ctx, storage):
     return inv
 
 
-def _solve(inv, f):
-    return inv.solve_cg(float(f["solve_tol"]), int(f["solve_maxit"]), float(f["solve_lambda"]),
+def _solve(inv, f, maxit=None):
+    maxit = int(f["solve_maxit"]) if maxit is None else maxit
+    return inv.solve_cg(float(f["solve_tol"]), maxit, float(f["solve_lambda"]),
                         f["solve_mk"], f["solve_mref"], f["solve_P"], fx.wl_dict(f))
+
+
+@pytest.mark.parametrize("storage", ["fp64", "fp32", "bf16", "fp16"])
+@pytest.mark.parametrize("name", fx.CASES)
+def test_phase_kernels_give_the_persistent_solve_bitwise(gpu_ctx, name, storage):
+    f = fx.load(name)
+    inv = _setup(f, gpu_ctx, storage)
+    # the fixture's limit, one that ends inside the first graph replay (odd:
+    # the graph then holds maxit iterations) and one past a replay boundary
+    for maxit in (None, 5, 17):
+        with fused_path():
+            dx, err, it = _solve(inv, f, maxit)
+        with phase_path():
+            dx2, err2, it2 = _solve(inv, f, maxit)
+        assert it2 == it and err2 == err and np.array_equal(dx2, dx), maxit
 
 
 @pytest.mark.parametrize("storage", ["fp64", "fp32", "bf16", "fp16"])
@@ -88,12 +109,13 @@ def test_fused_l2_invert_matches_graph_path(gpu_ctx, storage):
 
 def test_fused_barrier_wait_expiry_is_reported_and_context_recovers(gpu_ctx):
     f = fx.load("l2")
-    inv = _setup(f, gpu_ctx, "fp32")  # FP32 G: the persistent loop
-    dx, err, it = _solve(inv, f)
-    FAULT_CG_WAIT = 3  # the next solve's barrier waits have a zero limit
-    inv.ctx.check(inv.ctx.lib.grada_inject_fault(inv.ctx.handle, FAULT_CG_WAIT))
-    with pytest.raises(GradaError) as e:
-        _solve(inv, f)
-    assert e.value.status == -2 and "barrier" in str(e.value)
-    dx2, err2, it2 = _solve(inv, f)  # same context, normal limits
+    inv = _setup(f, gpu_ctx, "fp32")
+    with fused_path():
+        dx, err, it = _solve(inv, f)
+        FAULT_CG_WAIT = 3  # the next persistent solve's barrier waits have a zero limit
+        inv.ctx.check(inv.ctx.lib.grada_inject_fault(inv.ctx.handle, FAULT_CG_WAIT))
+        with pytest.raises(GradaError) as e:
+            _solve(inv, f)
+        assert e.value.status == -2 and "barrier" in str(e.value)
+        dx2, err2, it2 = _solve(inv, f)  # same context, normal limits
     assert it2 == it and err2 == err and np.array_equal(dx2, dx)
