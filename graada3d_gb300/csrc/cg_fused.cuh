@@ -117,41 +117,46 @@ __device__ __forceinline__ double sum_partials_all(const double *partial, int64_
 }
 
 // Rows per finish block of the persistent loop.
-constexpr int kFinRows = 32;
+constexpr int kFinRows = 16;
 
-// G pp's rows r0 .. r0 + 31 (block b): the split partial sums added by 8 warps
-// (warp w takes splits w, w + 8, ...) and the 8 sums in warp order; times the
-// row scale and Wd.  Returns t_r^2 for the block's rows, summed (valid in
-// every thread).
+// G pp's rows r0 .. r0 + 15 (block b): the 16 half-warps each add the split
+// partials k = g, g + 16, ... (g = 2 warp + half) of the 16 rows, loads eight
+// deep, and the 16 sums are added in g order; times the row scale and Wd.
+// Returns t_r^2 for the block's rows, summed (valid in every thread).
 __device__ __forceinline__ double finish_rows(const double *partial, int n_split, int64_t ld,
                                              int64_t nd, const float *__restrict__ row_scale,
                                              const double *__restrict__ wd, double *t,
                                              int64_t b) {
-  __shared__ double part[cgb::VT / 32][kFinRows];
+  constexpr int kGroups = 2 * (cgb::VT / 32);
+  __shared__ double part[kGroups][kFinRows];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t r = b * kFinRows + lane;
+  const int row_in = lane & (kFinRows - 1), g = 2 * warp + (lane >> 4);
+  const int64_t r = b * kFinRows + row_in;
   double s = 0.0;
-  if (r < nd)
-    for (int k = warp; k < n_split; k += cgb::VT / 32) s += __ldcg(partial + (int64_t)k * ld + r);
+  if (r < nd) {
+#pragma unroll 8
+    for (int k = g; k < n_split; k += kGroups) s += __ldcg(partial + (int64_t)k * ld + r);
+  }
   __syncthreads();
-  part[warp][lane] = s;
+  part[g][row_in] = s;
   __syncthreads();
   double sq = 0.0;
-  if (warp == 0) {
+  if (threadIdx.x < kFinRows) {
+    const int64_t rr = b * kFinRows + threadIdx.x;
     double v = 0.0;
 #pragma unroll
-    for (int w = 0; w < cgb::VT / 32; w++) v += part[w][lane];
-    if (r < nd) {
-      if (row_scale) v *= (double)row_scale[r];
-      v *= wd[r];
-      t[r] = v;
+    for (int w = 0; w < kGroups; w++) v += part[w][threadIdx.x];
+    if (rr < nd) {
+      if (row_scale) v *= (double)row_scale[rr];
+      v *= wd[rr];
+      t[rr] = v;
       sq = v * v;
     }
   }
   return bcast_sum(sq);
 }
 
-// G^T y for the 32 columns of block b (warp w takes columns 4w .. 4w + 3,
+// G^T y for the 16 columns of block b (warp w takes columns 2w and 2w + 1,
 // lanes striding the rows), then r_j for those columns (the adjoint of the
 // regulariser rows and P) on the lanes holding a column.  StageY: y through
 // shared memory (gemv::gty_body, for a kernel of its own at full occupancy),
@@ -212,11 +217,11 @@ struct RedLayout {
 // Four team barriers per iteration:
 //   A  p_new = -r + beta p_old and pp = P p_new folded into the partial row
 //      sums of G pp (column ranges x row tiles)
-//   B  t_data = Wd (sum of the partials, 32 rows per block, the splits shared
-//      by 8 warps), the forward regulariser rows of t, per-block ||t||^2
+//   B  t_data = Wd (sum of the partials, 16 rows per block, the splits shared
+//      by 16 half-warps), the forward regulariser rows of t, per-block ||t||^2
 //   C  alpha = r2 / t2; s += alpha t, dx += alpha p_new, y = Wd s_data in G's
 //      accumulation type
-//   D  G^T y for 32 columns per block (4 per warp), r for those columns (the
+//   D  G^T y for 16 columns per block (2 per warp), r for those columns (the
 //      adjoint of the regulariser rows, P), per-block ||r||^2; then beta, err
 //      and the stopping test
 // Every CTA adds the per-block partials in index order, so the sums do not

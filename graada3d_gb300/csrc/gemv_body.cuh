@@ -240,12 +240,14 @@ __device__ __forceinline__ void prep_y_body(const double *y, int64_t nd, int64_t
 }
 
 // G^T y for the kGtBlockCols columns of block b: warp w takes columns
-// 4w .. 4w + 3 of the block, its lanes striding the rows with 16-byte loads,
+// 2w and 2w + 1 of the block, its lanes striding the rows with 16-byte loads,
 // and sums each column with a butterfly.  y goes through shared memory in
 // chunks of kYChunk rows, read once per block with 16-byte loads (not once
-// per warp).  Lane c < 4 of warp w returns column b * kGtBlockCols + 4w + c's
+// per warp).  Lane c < 2 of warp w returns column b * kGtBlockCols + 2w + c's
 // sum and sets *col to that column; every other thread gets *col = -1.
-constexpr int kGtWarpCols = 4;
+// Sixteen columns per block: 1,024 blocks for 16,384 cells, an even spread
+// over 152 SMs (32-column blocks left some SMs a fourth block against 3.4).
+constexpr int kGtWarpCols = 2;
 constexpr int kGtBlockCols = kGtWarpCols * (kThreads / 32);
 constexpr int kYChunk = 1024;
 
