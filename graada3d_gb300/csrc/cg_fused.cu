@@ -73,24 +73,32 @@ int fused_cg_grid(GKind kind, int sm_count) {
   return std::max(1, per_sm) * sm_count;
 }
 
-int fused_gx_units(int sm_count) {
-  int per_sm = 12;  // divisible by 1, 2, 3, 4 and 6 resident blocks per SM
-  if (const char *e = std::getenv("GRADA_GX_UNITS_PER_SM")) {
-    const int v = std::atoi(e);
-    if (v >= 1 && v <= 64) per_sm = v;
+void fused_gx_partition(const DevG &G, int sm_count, int &tiles, int &splits, int64_t &per) {
+  const int vec = vec_of(G.kind);
+  const int64_t rows = 32 * (int64_t)vec;  // gemv::fold_tile_rows
+  const int64_t esize = G.kind == GKind::FP64 ? 8 : (G.kind == GKind::FP32 ? 4 : 2);
+  const int64_t t = ceil_div(G.ld, rows);
+  const int64_t slots = (int64_t)cg_phase_a_blocks_per_sm(G.kind) * sm_count;
+  const int64_t max_s = std::max<int64_t>(1, std::min<int64_t>(ceil_div(G.nm, 64), 65535));
+  // at least one full round of the phase kernel's resident blocks where the
+  // columns allow; among those, the split count with the fewest bytes per
+  // round times whole rounds (a last, partly filled round streams at the rate
+  // of its few blocks), plus the partial rows' write and read
+  const int64_t min_s = std::min<int64_t>(max_s, std::max<int64_t>(1, ceil_div(slots, t)));
+  int64_t best_s = min_s;
+  double best = -1.0;
+  for (int64_t sp = min_s; sp <= max_s; sp++) {
+    const double unit_bytes = (double)(rows * esize) * (double)ceil_div(G.nm, sp);
+    const double cost = (double)ceil_div(t * sp, slots) * (double)slots * unit_bytes +
+                        (double)sp * (double)G.ld * 16.0;
+    if (best < 0.0 || cost < best) {
+      best = cost;
+      best_s = sp;
+    }
   }
-  return per_sm * sm_count;
-}
-
-void fused_gx_partition(const DevG &G, int units, int &tiles, int &splits, int64_t &per) {
-  tiles = (int)ceil_div(G.ld, (int64_t)256 * vec_of(G.kind));
-  int64_t sp = (int64_t)units / tiles;
-  const int64_t max_splits = ceil_div(G.nm, 16);  // at least 16 columns per range
-  if (sp > max_splits) sp = max_splits;
-  if (sp < 1) sp = 1;
-  if (sp > 65535) sp = 65535;
-  splits = (int)sp;
-  per = ceil_div(G.nm, splits);
+  tiles = (int)t;
+  splits = (int)best_s;
+  per = ceil_div(G.nm, best_s);
 }
 
 void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t &doubles, int64_t &counters) {

@@ -169,8 +169,11 @@ __device__ __forceinline__ double gty_adjoint_block(const FusedCgArgs &a, const 
   __shared__ double wsum[cgb::VT / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int64_t j = -1;
-  const double g = StageY ? gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j)
-                          : gemv::gty_body_l2<L>(a.G, a.ld, a.nm, y, b, &j);
+  double g;
+  if constexpr (StageY)
+    g = gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j);
+  else
+    g = gemv::gty_body_l2<L>(a.G, a.ld, a.nm, y, b, &j);
   double sq = 0.0;
   if (j >= 0) {
     a.gtw[j] = g;
@@ -216,7 +219,8 @@ struct RedLayout {
 // r (set up), p = dx = 0 and beta = 0.  Every CTA returns the same CgOut.
 // Four team barriers per iteration:
 //   A  p_new = -r + beta p_old and pp = P p_new folded into the partial row
-//      sums of G pp (column ranges x row tiles)
+//      sums of G pp (row tiles of 32 VEC rows x column ranges, the block's 8
+//      warps splitting a range)
 //   B  t_data = Wd (sum of the partials, 16 rows per block, the splits shared
 //      by 16 half-warps), the forward regulariser rows of t, per-block ||t||^2
 //   C  alpha = r2 / t2; s += alpha t, dx += alpha p_new, y = Wd s_data in G's

@@ -47,18 +47,19 @@ struct FusedCgArgs {
 
 // CTAs of a persistent CG launch for this storage (all co-resident).
 int fused_cg_grid(GKind kind, int sm_count);
-// Work units of G pp in the persistent loop and its phase kernels: 12 per SM
-// (GRADA_GX_UNITS_PER_SM overrides), a whole number of rounds at 1, 2, 3, 4
-// or 6 resident blocks per SM.
-int fused_gx_units(int sm_count);
-// G pp's partition: row tiles of 256 * vec rows and column ranges, about
-// `units` of them.  The sums of a solve depend on it, not on the launch.
-void fused_gx_partition(const DevG &G, int units, int &tiles, int &splits, int64_t &per);
+// G pp's partition in the persistent loop and its phase kernels: row tiles of
+// 32 * vec rows x column ranges, the split count chosen for whole rounds of
+// the phase-A kernel's resident blocks and few partial rows.  It depends on
+// G's shape, the SM count and that kernel's occupancy only, so the sums of a
+// solve do not depend on the launch.
+void fused_gx_partition(const DevG &G, int sm_count, int &tiles, int &splits, int64_t &per);
 // Doubles and counters of a.red / a.red_count for a loop over Nm cells, Nd
 // rows and nterms regulariser terms.
 void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t &doubles, int64_t &counters);
 // Clears the barrier words and launches the cooperative kernel.
 void launch_cg_fused(const FusedCgArgs &a, GKind kind, int grid, cudaStream_t s);
+// Resident blocks per SM of the phase-A kernel (G pp) for this storage.
+int cg_phase_a_blocks_per_sm(GKind kind);
 // One iteration of the same loop as four kernels (cg_phases.cu); parity
 // alternates p and p2 as the persistent loop's iteration count does.
 void launch_cg_phase_iteration(const FusedCgArgs &a, GKind kind, int parity, cudaStream_t s);

@@ -2,9 +2,9 @@
 //
 // Reference: GaussNewtonInversion::solve_cg, the iteration loop
 // (src/Inversion/GaussNewtonInversion.cpp:1556-1692).  The phase bodies are
-// the persistent loop's (cg_fused.cuh), on its partition of G pp (row tiles x
-// column ranges, 12 units per SM), so both paths compute the same sums in the
-// same order and give bitwise the same solve.  What the
+// the persistent loop's (cg_fused.cuh), on its partition of G pp
+// (fused_gx_partition), so both paths compute the same sums in the same order
+// and give bitwise the same solve.  What the
 // persistent loop does at a team barrier happens here at a kernel boundary,
 // and the two reductions that end a phase (||t||^2 -> alpha, ||r||^2 -> beta
 // and the stopping test) run in the phase's last block: every block stores
@@ -13,15 +13,9 @@
 // returns at once while ctl[CTL_DONE] is raised, so a graph of K iterations
 // can be replayed until the solve ends, one host synchronisation per replay.
 // Each phase kernel runs at its own occupancy, which the products need: the
-// persistent launch holds three CTAs per SM throughout.  Consecutive phases
-// are launched as programmatic dependents (GRADA_CG_PDL=0: plain launches):
-// every block of a phase signals griddepcontrol.launch_dependents when it
-// starts, so the next phase's blocks are placed on the SMs its tail frees and
-// wait in griddepcontrol.wait, which returns once the previous grid has
-// completed and its writes are visible; nothing is read before that.
-#include <cstdlib>
-#include <utility>
-
+// persistent launch holds three CTAs per SM throughout.  (Launching the
+// phases as programmatic dependents, each block waiting in griddepcontrol.wait,
+// measured slower at 3,392 x 16,384: 0.165 against 0.158 ms per FP32 iteration.)
 #include "cg_fused.cuh"
 
 namespace grada {
@@ -48,18 +42,14 @@ __device__ __forceinline__ bool last_block(unsigned *count, unsigned nblocks) {
   return s_last != 0;
 }
 
-// Waits for the previous grid of the stream (a no-op for a plain launch),
-// lets the next one launch, and reads the stop flag.
-__device__ __forceinline__ bool enter_done(const FusedCgArgs &a) {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+__device__ __forceinline__ bool done(const FusedCgArgs &a) {
   return *reinterpret_cast<volatile const int *>(a.ctl + CTL_DONE) != 0;
 }
 
 // A: p_new = -r + beta p_old, pp = P p_new, folded into G pp's partial sums.
 template <class L>
 __global__ void __launch_bounds__(256) phase_a_kernel(FusedCgArgs a, int parity) {
-  if (enter_done(a)) return;
+  if (done(a)) return;
   const double *p_old = parity ? a.p2 : a.p;
   double *p_new = parity ? a.p : a.p2;
   const double beta = __ldcg(a.scal + CG_BETA);
@@ -72,7 +62,7 @@ __global__ void __launch_bounds__(256) phase_a_kernel(FusedCgArgs a, int parity)
 // per-block ||t||^2; the last block: t2, alpha = r2 / t2 (:1601) and the
 // breakdown / non-finite checks.
 __global__ void __launch_bounds__(256) phase_b_kernel(FusedCgArgs a) {
-  if (enter_done(a)) return;
+  if (done(a)) return;
   const RedLayout rl(a.nd, a.nm, a.FT.count);
   const int64_t nb_vec = ceil_div_d(a.nm, cgb::VT);
   const int64_t b = blockIdx.x;
@@ -108,7 +98,7 @@ __global__ void __launch_bounds__(256) phase_b_kernel(FusedCgArgs a) {
 // C: s += alpha t, dx += alpha p_new, y = Wd s_data in G's accumulation type.
 template <class L>
 __global__ void __launch_bounds__(256) phase_c_kernel(FusedCgArgs a, int parity) {
-  if (enter_done(a)) return;
+  if (done(a)) return;
   using Acc = typename L::Acc;
   const double *p_new = parity ? a.p : a.p2;
   const double alpha = __ldcg(a.scal + CG_ALPHA);
@@ -124,7 +114,7 @@ __global__ void __launch_bounds__(256) phase_c_kernel(FusedCgArgs a, int parity)
 // and the stopping tests (:1674-1691).
 template <class L>
 __global__ void __launch_bounds__(256) phase_d_kernel(FusedCgArgs a) {
-  if (enter_done(a)) return;
+  if (done(a)) return;
   using Acc = typename L::Acc;
   const RedLayout rl(a.nd, a.nm, a.FT.count);
   double *part_r = a.red + rl.nb_t;
@@ -154,39 +144,34 @@ __global__ void __launch_bounds__(256) phase_d_kernel(FusedCgArgs a) {
   }
 }
 
-bool use_pdl() {
-  const char *e = std::getenv("GRADA_CG_PDL");
-  return !(e && e[0] == '0');
-}
-
-template <typename... Params, typename... Args>
-void launch_phase(void (*kernel)(Params...), int64_t blocks, bool pdl, cudaStream_t s,
-                  Args &&...args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)blocks);
-  cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = pdl ? 1 : 0;
-  GRADA_CUDA_CHECK(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
-}
-
 template <class L>
 void launch_iteration(const FusedCgArgs &a, int parity, cudaStream_t s) {
   const RedLayout rl(a.nd, a.nm, a.FT.count);
   const int64_t nb_axpy = ceil_div_d(a.nrow > a.nm ? a.nrow : a.nm, cgb::VT);
-  const bool pdl = use_pdl();
-  launch_phase(phase_a_kernel<L>, (int64_t)a.tiles * a.splits, pdl, s, a, parity);
-  launch_phase(phase_b_kernel, rl.nb_t, pdl, s, a);
-  launch_phase(phase_c_kernel<L>, nb_axpy, pdl, s, a, parity);
-  launch_phase(phase_d_kernel<L>, rl.nb_r, pdl, s, a);
+  phase_a_kernel<L><<<(unsigned)((int64_t)a.tiles * a.splits), 256, 0, s>>>(a, parity);
+  GRADA_LAUNCH_CHECK();
+  phase_b_kernel<<<(unsigned)rl.nb_t, 256, 0, s>>>(a);
+  GRADA_LAUNCH_CHECK();
+  phase_c_kernel<L><<<(unsigned)nb_axpy, 256, 0, s>>>(a, parity);
+  GRADA_LAUNCH_CHECK();
+  phase_d_kernel<L><<<(unsigned)rl.nb_r, 256, 0, s>>>(a);
+  GRADA_LAUNCH_CHECK();
 }
 
 }  // namespace
+
+int cg_phase_a_blocks_per_sm(GKind kind) {
+  const void *k = nullptr;
+  switch (kind) {
+    case GKind::FP64: k = reinterpret_cast<const void *>(&phase_a_kernel<gemv::LoadF64>); break;
+    case GKind::FP32: k = reinterpret_cast<const void *>(&phase_a_kernel<gemv::LoadF32>); break;
+    case GKind::BF16: k = reinterpret_cast<const void *>(&phase_a_kernel<gemv::LoadBF16>); break;
+    case GKind::FP16: k = reinterpret_cast<const void *>(&phase_a_kernel<gemv::LoadF16>); break;
+  }
+  int n = 0;
+  GRADA_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256, 0));
+  return n > 0 ? n : 1;
+}
 
 void launch_cg_phase_iteration(const FusedCgArgs &a, GKind kind, int parity, cudaStream_t s) {
   switch (kind) {

@@ -126,10 +126,23 @@ __device__ __forceinline__ void gx_partial_body(const void *__restrict__ G, int6
   }
 }
 
-// gx_partial_body for x = pp with the CG direction update folded in: the
-// staged entries are pp_j = P_j (-r_j + beta p_old_j); blocks of tile 0 also
-// store p_new_j = -r_j + beta p_old_j and pp_j (GaussNewtonInversion.cpp:
-// 1562-1566), so no separate pass over p is needed before G pp.
+// Rows of a fold-body tile: one warp's lanes x VEC rows (512 bytes of a
+// column per warp load for every storage).
+template <class L>
+__host__ __device__ constexpr int fold_tile_rows() {
+  return 32 * L::VEC;
+}
+
+// G pp's partial row sums for the CG with the direction update folded in:
+// the staged entries are pp_j = P_j (-r_j + beta p_old_j); blocks of tile 0
+// also store p_new_j = -r_j + beta p_old_j and pp_j (GaussNewtonInversion.cpp:
+// 1562-1566), so no separate pass over p is needed before G pp.  Unit (tile,
+// split): the tile's fold_tile_rows rows over the split's columns.  Within a
+// staged chunk of columns warp w takes the w-th of 8 consecutive column
+// sub-ranges (eight columns' loads in flight, two accumulator chains per row);
+// the 8 warp sums of each row are added in warp order through shared memory
+// and stored to partial[split * ld + row].  Short, wide G thus gets many row
+// tiles and few column splits (few partial rows for the finish to add).
 template <class L>
 __device__ __forceinline__ void gx_partial_fold_body(
     const void *__restrict__ G, int64_t ld, int64_t nm, int64_t cols_per_split, const double *r,
@@ -137,12 +150,14 @@ __device__ __forceinline__ void gx_partial_fold_body(
     double *partial, int64_t tile, int64_t split) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
+  constexpr int kWarps = kThreads / 32;
+  constexpr int kRows = fold_tile_rows<L>();
   __shared__ Acc xs[kXChunk];
-  const int64_t row = (tile * kThreads + threadIdx.x) * VEC;
+  __shared__ double wsum[kWarps][kRows];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t row = tile * kRows + lane * VEC;
   const int64_t c_begin = split * cols_per_split;
   const int64_t c_end = min(nm, c_begin + cols_per_split);
-  // two accumulators per row (even and odd columns of a group of eight): twice
-  // the independent FMA chains, which the FP64 pipe needs at three CTAs per SM
   Acc acc[VEC], acc2[VEC];
 #pragma unroll
   for (int v = 0; v < VEC; v++) acc[v] = acc2[v] = Acc(0);
@@ -160,11 +175,11 @@ __device__ __forceinline__ void gx_partial_fold_body(
       xs[t] = (Acc)q;
     }
     __syncthreads();
+    const int lo = (nc * warp) / kWarps, hi = (nc * (warp + 1)) / kWarps;
     if (row < ld) {
       const int64_t base = row + c0 * ld;
-      int c = 0;
-      // eight columns' loads in flight before their FMAs
-      for (; c + 8 <= nc; c += 8) {
+      int c = lo;
+      for (; c + 8 <= hi; c += 8) {
         Acc g[8][VEC];
 #pragma unroll
         for (int q = 0; q < 8; q++) L::load(G, base + (int64_t)(c + q) * ld, g[q]);
@@ -178,7 +193,7 @@ __device__ __forceinline__ void gx_partial_fold_body(
           }
         }
       }
-      for (; c < nc; c++) {
+      for (; c < hi; c++) {
         Acc g0[VEC];
         L::load(G, base + (int64_t)c * ld, g0);
 #pragma unroll
@@ -186,10 +201,18 @@ __device__ __forceinline__ void gx_partial_fold_body(
       }
     }
   }
-  if (row < ld) {
-    double *out = partial + split * ld + row;
+  __syncthreads();  // wsum may still be read for the caller's previous unit
 #pragma unroll
-    for (int v = 0; v < VEC; v++) out[v] = (double)acc[v] + (double)acc2[v];
+  for (int v = 0; v < VEC; v++) wsum[warp][lane * VEC + v] = (double)acc[v] + (double)acc2[v];
+  __syncthreads();
+  if (threadIdx.x < kRows) {
+    const int64_t rr = tile * kRows + threadIdx.x;
+    if (rr < ld) {
+      double sum = 0.0;
+#pragma unroll
+      for (int w = 0; w < kWarps; w++) sum += wsum[w][threadIdx.x];
+      partial[split * ld + rr] = sum;
+    }
   }
 }
 
@@ -242,20 +265,21 @@ __device__ __forceinline__ void prep_y_body(const double *y, int64_t nd, int64_t
 // G^T y for the kGtBlockCols columns of block b: warp w takes columns
 // 2w and 2w + 1 of the block, its lanes striding the rows with 16-byte loads,
 // and sums each column with a butterfly.  y goes through shared memory in
-// chunks of kYChunk rows, read once per block with 16-byte loads (not once
-// per warp).  Lane c < 2 of warp w returns column b * kGtBlockCols + 2w + c's
+// chunks of 32 KB, read once per block with 16-byte loads (not once per warp);
+// one chunk, two block barriers, for the heights of most problems.  Lane c < 2 of warp w returns column b * kGtBlockCols + 2w + c's
 // sum and sets *col to that column; every other thread gets *col = -1.
 // Sixteen columns per block: 1,024 blocks for 16,384 cells, an even spread
 // over 152 SMs (32-column blocks left some SMs a fourth block against 3.4).
 constexpr int kGtWarpCols = 2;
 constexpr int kGtBlockCols = kGtWarpCols * (kThreads / 32);
-constexpr int kYChunk = 1024;
+constexpr int kYChunkBytes = 32768;  // y staged 32 KB at a time: one chunk for ld <= 8,192 (FP32)
 
 template <class L>
 __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t ld, int64_t nm,
                                            const typename L::Acc *y, int64_t b, int64_t *col) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
+  constexpr int kYChunk = kYChunkBytes / (int)sizeof(Acc);
   __shared__ __align__(16) Acc ys[kYChunk];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t c0 = b * kGtBlockCols + (int64_t)warp * kGtWarpCols;

@@ -462,7 +462,7 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   a.ld = g.ld;
   if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
   const int grid = fused_grid[(int)g.kind];
-  fused_gx_partition(g, fused_gx_units(sm_count), a.tiles, a.splits, a.per);
+  fused_gx_partition(g, sm_count, a.tiles, a.splits, a.per);
   a.scratch = scratch_doubles(std::max(product_scratch_doubles(), (int64_t)a.splits * g.ld));
   a.wd = dptr(wd);
   a.r = dptr(cg_r);

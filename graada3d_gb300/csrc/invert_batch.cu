@@ -331,7 +331,7 @@ struct TeamMap {
 };
 
 template <class L>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
     invert_batch_kernel(const BatchProblem *problems, int n, int *queue, int queue_base,
                         unsigned *bar_words, int *team_slot, TeamMap map,
                         unsigned long long wait_ns) {
@@ -457,7 +457,7 @@ void Context::batch_problem(const grada_invert_params &prm, BatchProblem &bp) {
   a.ld = g.ld;
   // the single solve's partition, so both paths sum alike
   if (fused_grid[(int)g.kind] <= 0) fused_grid[(int)g.kind] = fused_cg_grid(g.kind, sm_count);
-  fused_gx_partition(g, fused_gx_units(sm_count), a.tiles, a.splits, a.per);
+  fused_gx_partition(g, sm_count, a.tiles, a.splits, a.per);
   if ((int64_t)a.splits * g.ld > need) scr = scratch_doubles((int64_t)a.splits * g.ld);
   a.scratch = scr;
   a.wd = dbuf(wd);
