@@ -142,7 +142,10 @@ def test_mixed_precision_inversion_close_to_fp64(gpu_ctx, storage, p, tol):
     the 50-step cap, and near the target misfit the discrete lambda search
     makes even the all-FP64 run move by ~1 % (model) and ~3 % (final misfit)
     when the data are perturbed at the rounding level (4e-16 relative), so the
-    bounds are at least 3 times that measured spread."""
+    bounds are at least 3 times that measured spread.  A 16-bit G perturbs the
+    iterates far more than rounding (bf16 entries carry 2^-9 relative error), and
+    the discrete lambda steps (rate 0.6) can then end the search one trial over,
+    so the L2 final-misfit bound is also at least the storage's model bound."""
     prisms, obs, rho, n, mask, rng = _l2_problem(mask=0x072)
     inv = GaussNewtonInversion(prisms, obs, mask, ctx=gpu_ctx)
     inv.compute_G("fp64")
@@ -174,7 +177,7 @@ def test_mixed_precision_inversion_close_to_fp64(gpu_ctx, storage, p, tol):
     assert rel < max(tol, 3 * f_model), (rel, f_model)
     if p == 2:
         assert abs(replp["final_misfit"] - rep64["final_misfit"]) <= \
-            max(0.02, 3 * f_misfit) * rep64["final_misfit"], f_misfit
+            max(0.02, tol, 3 * f_misfit) * rep64["final_misfit"], f_misfit
     else:  # the perturbed L1 run may well end lower; it must not end higher
         assert replp["final_misfit"] <= max(1.05, 1 + 3 * f_misfit) * rep64["final_misfit"]
 
