@@ -503,6 +503,10 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16", "fp32+fp6
              "cg_iterations": int(rep["cg_iterations"]),
              "ms_per_cg_iteration": 1e3 * t_inv / max(1, rep["cg_iterations"]),
              "gn_misfits": [float(v) for v in inv.iterations()[:, 2]]}
+        loop_s, graph_s, n_loop = inv.cg_loop_time()
+        if n_loop:  # the CG loops alone (set-up, predictions and lambda control excluded)
+            r["cg_loop_ms_per_iteration"] = 1e3 * loop_s / n_loop
+            r["cg_graph_build_s"] = graph_s
         ph, n_ph = inv.cg_phase_times()
         if n_ph:  # the persistent CG loop ran: its phases' mean time per iteration
             r["cg_phase_us"] = {"gp": ph[0] / 1e3, "finish_rows": ph[1] / 1e3, "step": ph[2] / 1e3,
@@ -681,10 +685,11 @@ def run_batched_64(n_problems: int = 64):
                                          [a[1] for a in args], [a[2] for a in args])
     torch.cuda.synchronize()
     t_per = time.perf_counter() - t0
-    # the single FP64 runs take the graph-replayed CG (the faster one for FP64 G);
-    # the batch runs the persistent loop, which sums in other orders
+    # the single runs take the CG loop's phase kernels, the batch the same
+    # phases in one persistent launch: the same sums in the same order
     per_diff = max(float(np.linalg.norm(a[0] - b[0]) / max(np.linalg.norm(a[0]), 1e-30))
                    for a, b in zip(seq, per))
+    per_same = all(np.array_equal(a[0], b[0]) for a, b in zip(seq, per))
     # the same batch with FP32 G (HBM-bound products) and the FP64 G kept for
     # every prediction
     t0 = time.perf_counter()
@@ -704,6 +709,16 @@ def run_batched_64(n_problems: int = 64):
     torch.cuda.synchronize()
     t_mix_per = time.perf_counter() - t0
     mix_per_same = all(np.array_equal(a[0], b[0]) for a, b in zip(mix, mix_per))
+    # G bytes the CG products stream (two reads of G per CG iteration), the
+    # bulk of the batch's HBM traffic; over the whole wall time (assembly,
+    # predictions and set-up included) a lower bound on the products' rate
+    entries = [inv.ld * inv.Nm for inv in invs]
+
+    def cg_bytes(results, esize):
+        return float(sum(2 * r["cg_iterations"] * e * esize for (_, r), e in zip(results, entries)))
+
+    b64, b64_per = cg_bytes(bat, 8), cg_bytes(per, 8)
+    b32, b32_per = cg_bytes(mix, 4), cg_bytes(mix_per, 4)
     for inv in invs:
         inv.ctx.close()
     t_seq, t_bat = max_over_ranks(world, t_seq), max_over_ranks(world, t_bat)
@@ -718,8 +733,14 @@ def run_batched_64(n_problems: int = 64):
             "persistent": {"launches": 1, "teams": shape[0], "ctas_per_team": shape[1],
                            "s": t_per, "speedup_vs_sequential": t_seq / t_per,
                            "speedup_vs_concurrent": t_bat / t_per,
+                           "identical_models_to_single_runs": per_same,
                            "max_model_rel_diff_vs_single_runs": per_diff},
             "cg_iterations_rank0": int(sum(r["cg_iterations"] for _, r in bat)),
+            "cg_G_bytes_rank0": {"fp64": b64, "fp32": b32},
+            "cg_G_TB_per_s_rank0": {"fp64_concurrent": b64 / t_bat / 1e12,
+                                    "fp64_persistent": b64_per / t_per / 1e12,
+                                    "fp32_concurrent": b32 / t_mix / 1e12,
+                                    "fp32_persistent": b32_per / t_mix_per / 1e12},
             "fp32_kept_fp64": {"batched_s": t_mix, "speedup_vs_fp64_batch": t_bat / t_mix,
                                "persistent": {"launches": 1, "teams": mix_shape[0],
                                               "ctas_per_team": mix_shape[1], "s": t_mix_per,

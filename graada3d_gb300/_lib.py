@@ -60,6 +60,7 @@ SIGNATURES = {
     "grada_set_inversion_model": (c_int, [c_void_p, _dp, _dp, _dp, _dp]),
     "grada_get_model": (c_int, [c_void_p, _dp]),
     "grada_cg_phase_times": (c_int, [c_void_p, _dp, _ip64]),
+    "grada_cg_loop_time": (c_int, [c_void_p, _dp, _ip64]),
     "grada_get_trials": (c_int, [c_void_p, _dp, c_int64, _ip64]),
     "grada_get_iterations": (c_int, [c_void_p, _dp, c_int64, _ip64]),
     "grada_G_vec_mul_noalloc": (c_int, [c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p,

@@ -700,6 +700,16 @@ int grada_cg_phase_times(grada_ctx *ctx, double *mean_ns, int64_t *iterations) {
   });
 }
 
+int grada_cg_loop_time(grada_ctx *ctx, double *seconds, int64_t *iterations) {
+  return guarded(ctx, [&] {
+    if (iterations) *iterations = ctx->cg_loop_iters;
+    if (seconds) {
+      seconds[0] = ctx->cg_loop_ns * 1e-9;
+      seconds[1] = ctx->cg_graph_ns * 1e-9;
+    }
+  });
+}
+
 int grada_get_model(grada_ctx *ctx, double *m) {
   return guarded(ctx, [&] {
     if (!m) throw Error(GRADA_ERR_INVALID_ARGUMENT, "null model vector");

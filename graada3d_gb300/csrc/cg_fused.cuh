@@ -156,16 +156,20 @@ __device__ __forceinline__ double finish_rows(const double *partial, int n_split
   return bcast_sum(sq);
 }
 
-// G^T y for the 16 columns of block b (warp w takes columns 2w and 2w + 1,
+// G^T y for the 32 columns of block b (warp w takes columns 4w .. 4w + 3,
 // lanes striding the rows), then r_j for those columns (the adjoint of the
-// regulariser rows and P) on the lanes holding a column.  StageY: y through
-// shared memory (gemv::gty_body, for a kernel of its own at full occupancy),
-// else read from L2 by each warp (gemv::gty_body_l2, the persistent loop's);
-// both sum each column in the same order.  Writes gtw and r; returns the
-// block's sum of r_j^2 (valid in every thread).
+// regulariser rows and P).  StageY: y through shared memory (gemv::gty_body,
+// for a kernel of its own at full occupancy), else read from L2 by each warp
+// (gemv::gty_body_l2, the persistent loop's); both sum each column in the same
+// order.  The regulariser terms of the warp's 4 columns run on one lane per
+// (column, term), their dependent CSR loads in parallel; the lane holding a
+// column adds them to its G^T sum in term order (cgb::adjoint_column's
+// arithmetic).  Writes gtw and r; returns the block's sum of r_j^2 (valid in
+// every thread).
 template <class L, bool StageY = false>
 __device__ __forceinline__ double gty_adjoint_block(const FusedCgArgs &a, const typename L::Acc *y,
                                                     int64_t b) {
+  static_assert(gemv::kGtWarpCols * 8 <= 32, "one lane per (column, term)");
   __shared__ double wsum[cgb::VT / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int64_t j = -1;
@@ -174,10 +178,27 @@ __device__ __forceinline__ double gty_adjoint_block(const FusedCgArgs &a, const 
     g = gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j);
   else
     g = gemv::gty_body_l2<L>(a.G, a.ld, a.nm, y, b, &j);
+  // lane 8c + q: term q of the warp's column c
+  const int tc = lane >> 3, tq = lane & 7;
+  const int64_t tj = b * gemv::kGtBlockCols + (int64_t)warp * gemv::kGtWarpCols + tc;
+  double ts = 0.0;
+  if (tc < gemv::kGtWarpCols && tq < a.AT.count && tj < a.nm) {
+    const AdjointTerm &t = a.AT.t[tq];
+    for (int k = t.AT.rowptr[tj]; k < t.AT.rowptr[tj + 1]; k++) {
+      const int i = t.AT.col[k];
+      const double w = t.wl ? t.wl[i] : 1.0;
+      ts = fma(t.AT.val[k], w * __ldcg(t.s + i), ts);
+    }
+  }
+  double acc = g;  // lanes c < 4: P_j (gtw_j + sum_q c_q s_q), terms in order
+  for (int q = 0; q < a.AT.count; q++) {
+    const double sq_term = __shfl_sync(0xffffffffu, ts, (lane & 3) * 8 + q);
+    acc = fma(a.AT.t[q].c, sq_term, acc);
+  }
   double sq = 0.0;
   if (j >= 0) {
     a.gtw[j] = g;
-    const double rj = cgb::adjoint_column(a.AT, j, a.P, true, g, 1.0);
+    const double rj = a.P ? a.P[j] * acc : acc;
     a.r[j] = rj;
     sq = rj * rj;
   }
@@ -225,7 +246,7 @@ struct RedLayout {
 //      by 16 half-warps), the forward regulariser rows of t, per-block ||t||^2
 //   C  alpha = r2 / t2; s += alpha t, dx += alpha p_new, y = Wd s_data in G's
 //      accumulation type
-//   D  G^T y for 16 columns per block (2 per warp), r for those columns (the
+//   D  G^T y for 32 columns per block (4 per warp), r for those columns (the
 //      adjoint of the regulariser rows, P), per-block ||r||^2; then beta, err
 //      and the stopping test
 // Every CTA adds the per-block partials in index order, so the sums do not

@@ -48,7 +48,9 @@ __device__ __forceinline__ bool done(const FusedCgArgs &a) {
 
 // A: p_new = -r + beta p_old, pp = P p_new, folded into G pp's partial sums.
 template <class L>
-__global__ void __launch_bounds__(256) phase_a_kernel(FusedCgArgs a, int parity) {
+__global__ void __launch_bounds__(256)
+    phase_a_kernel(const FusedCgArgs *__restrict__ ap, int parity) {
+  const FusedCgArgs &a = *ap;
   if (done(a)) return;
   const double *p_old = parity ? a.p2 : a.p;
   double *p_new = parity ? a.p : a.p2;
@@ -61,7 +63,8 @@ __global__ void __launch_bounds__(256) phase_a_kernel(FusedCgArgs a, int parity)
 // B: t_data = Wd (sum of the partials), the forward regulariser rows, the
 // per-block ||t||^2; the last block: t2, alpha = r2 / t2 (:1601) and the
 // breakdown / non-finite checks.
-__global__ void __launch_bounds__(256) phase_b_kernel(FusedCgArgs a) {
+__global__ void __launch_bounds__(256) phase_b_kernel(const FusedCgArgs *__restrict__ ap) {
+  const FusedCgArgs &a = *ap;
   if (done(a)) return;
   const RedLayout rl(a.nd, a.nm, a.FT.count);
   const int64_t nb_vec = ceil_div_d(a.nm, cgb::VT);
@@ -97,7 +100,9 @@ __global__ void __launch_bounds__(256) phase_b_kernel(FusedCgArgs a) {
 
 // C: s += alpha t, dx += alpha p_new, y = Wd s_data in G's accumulation type.
 template <class L>
-__global__ void __launch_bounds__(256) phase_c_kernel(FusedCgArgs a, int parity) {
+__global__ void __launch_bounds__(256)
+    phase_c_kernel(const FusedCgArgs *__restrict__ ap, int parity) {
+  const FusedCgArgs &a = *ap;
   if (done(a)) return;
   using Acc = typename L::Acc;
   const double *p_new = parity ? a.p : a.p2;
@@ -109,11 +114,12 @@ __global__ void __launch_bounds__(256) phase_c_kernel(FusedCgArgs a, int parity)
                            b);
 }
 
-// D: G^T y and r for 16 columns per block, the per-block ||r||^2; the last
+// D: G^T y and r for 32 columns per block, the per-block ||r||^2; the last
 // block: r2, beta = r2 / rlast2, err = r2 / ||A^T b||^2, the iteration count
 // and the stopping tests (:1674-1691).
 template <class L>
-__global__ void __launch_bounds__(256) phase_d_kernel(FusedCgArgs a) {
+__global__ void __launch_bounds__(256) phase_d_kernel(const FusedCgArgs *__restrict__ ap) {
+  const FusedCgArgs &a = *ap;
   if (done(a)) return;
   using Acc = typename L::Acc;
   const RedLayout rl(a.nd, a.nm, a.FT.count);
@@ -145,16 +151,16 @@ __global__ void __launch_bounds__(256) phase_d_kernel(FusedCgArgs a) {
 }
 
 template <class L>
-void launch_iteration(const FusedCgArgs &a, int parity, cudaStream_t s) {
-  const RedLayout rl(a.nd, a.nm, a.FT.count);
-  const int64_t nb_axpy = ceil_div_d(a.nrow > a.nm ? a.nrow : a.nm, cgb::VT);
-  phase_a_kernel<L><<<(unsigned)((int64_t)a.tiles * a.splits), 256, 0, s>>>(a, parity);
+void launch_iteration(const FusedCgArgs &a, const FusedCgArgs *ap, int parity, cudaStream_t s) {
+  int64_t g[4];
+  cg_phase_grids(a, g);
+  phase_a_kernel<L><<<(unsigned)g[0], 256, 0, s>>>(ap, parity);
   GRADA_LAUNCH_CHECK();
-  phase_b_kernel<<<(unsigned)rl.nb_t, 256, 0, s>>>(a);
+  phase_b_kernel<<<(unsigned)g[1], 256, 0, s>>>(ap);
   GRADA_LAUNCH_CHECK();
-  phase_c_kernel<L><<<(unsigned)nb_axpy, 256, 0, s>>>(a, parity);
+  phase_c_kernel<L><<<(unsigned)g[2], 256, 0, s>>>(ap, parity);
   GRADA_LAUNCH_CHECK();
-  phase_d_kernel<L><<<(unsigned)rl.nb_r, 256, 0, s>>>(a);
+  phase_d_kernel<L><<<(unsigned)g[3], 256, 0, s>>>(ap);
   GRADA_LAUNCH_CHECK();
 }
 
@@ -173,12 +179,21 @@ int cg_phase_a_blocks_per_sm(GKind kind) {
   return n > 0 ? n : 1;
 }
 
-void launch_cg_phase_iteration(const FusedCgArgs &a, GKind kind, int parity, cudaStream_t s) {
+void cg_phase_grids(const FusedCgArgs &a, int64_t grids[4]) {
+  const RedLayout rl(a.nd, a.nm, a.FT.count);
+  grids[0] = (int64_t)a.tiles * a.splits;
+  grids[1] = rl.nb_t;
+  grids[2] = ceil_div_d(a.nrow > a.nm ? a.nrow : a.nm, cgb::VT);
+  grids[3] = rl.nb_r;
+}
+
+void launch_cg_phase_iteration(const FusedCgArgs &a, const FusedCgArgs *dev_args, GKind kind,
+                               int parity, cudaStream_t s) {
   switch (kind) {
-    case GKind::FP64: launch_iteration<gemv::LoadF64>(a, parity, s); break;
-    case GKind::FP32: launch_iteration<gemv::LoadF32>(a, parity, s); break;
-    case GKind::BF16: launch_iteration<gemv::LoadBF16>(a, parity, s); break;
-    case GKind::FP16: launch_iteration<gemv::LoadF16>(a, parity, s); break;
+    case GKind::FP64: launch_iteration<gemv::LoadF64>(a, dev_args, parity, s); break;
+    case GKind::FP32: launch_iteration<gemv::LoadF32>(a, dev_args, parity, s); break;
+    case GKind::BF16: launch_iteration<gemv::LoadBF16>(a, dev_args, parity, s); break;
+    case GKind::FP16: launch_iteration<gemv::LoadF16>(a, dev_args, parity, s); break;
   }
 }
 

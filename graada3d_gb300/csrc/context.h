@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <chrono>
 #include <string>
 #include <vector>
 
@@ -132,6 +133,19 @@ struct Context {
   int fused_grid[4] = {0, 0, 0, 0};  // persistent CG grid per G storage kind
   DevBuf cg_trace;                    // phase trace of a persistent solve (5 u64)
   unsigned long long trace_sum[5] = {0, 0, 0, 0, 0};  // since the last invert / reset
+  // The graph of the CG loop's phase kernels (cg_phases.cu), kept across the
+  // solves of one shape: its kernels read their arguments from cg_args, which
+  // each solve rewrites from the pinned h_cg_args.  phase_key: what the graph
+  // bakes in (storage, iterations, grids, the argument buffer).
+  DevBuf cg_args;
+  FusedCgArgs *h_cg_args = nullptr;
+  cudaGraphExec_t phase_exec = nullptr;
+  int64_t phase_key[7] = {-1, -1, -1, -1, -1, -1, -1};
+  // CG loops since the last invert / reset: host wall ns from the first launch
+  // of a solve's loop to its last synchronisation, ns building their graphs,
+  // their iterations
+  double cg_loop_ns = 0.0, cg_graph_ns = 0.0;
+  int64_t cg_loop_iters = 0;
   bool inject_cg_wait = false;       // grada_inject_fault(GRADA_FAULT_CG_WAIT)
   double *h_scal = nullptr;  // pinned
   int *h_flag = nullptr;     // pinned
@@ -195,6 +209,8 @@ struct Context {
                           const ForwardTerms &FT, const AdjointTerms &AT, int64_t nrow, int nb_m,
                           int nb_row, bool persistent);
   CgResult solve_cg_phases(const FusedCgArgs &a, GKind kind, int maxit);
+  void count_cg_loop(std::chrono::steady_clock::time_point t_build,
+                     std::chrono::steady_clock::time_point t_loop, int iterations);
   CgResult solve_cg_dev(double lambda, double tol, int maxit, const double *mk, const double *mref,
                         const double *P, const double *const WL[7], double *dx,
                         const double *d64, const double *m_start);

@@ -8,9 +8,9 @@
 // Both products stream G once from HBM with 16-byte vector loads and are
 // bound by HBM bandwidth.  G is column-major with leading dimension ld (a
 // multiple of 64, padding rows zero), so:
-//  * G^T y: a block owns 16 consecutive columns, 2 per warp; the lanes walk
+//  * G^T y: a block owns 32 consecutive columns, 4 per warp; the lanes walk
 //    the rows with 16-byte loads, multiply by y (staged per row chunk in
-//    shared memory and reused for the warp's 2 columns) and each column is
+//    shared memory and reused for the warp's 4 columns) and each column is
 //    summed with a warp butterfly.  Deterministic: fixed per-lane row order
 //    and tree.
 //  * G x: a block owns a tile of 256*VEC rows and a range of columns; threads

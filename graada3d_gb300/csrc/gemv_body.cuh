@@ -263,14 +263,13 @@ __device__ __forceinline__ void prep_y_body(const double *y, int64_t nd, int64_t
 }
 
 // G^T y for the kGtBlockCols columns of block b: warp w takes columns
-// 2w and 2w + 1 of the block, its lanes striding the rows with 16-byte loads,
+// 4w .. 4w + 3 of the block, its lanes striding the rows with 16-byte loads,
 // and sums each column with a butterfly.  y goes through shared memory in
 // chunks of 32 KB, read once per block with 16-byte loads (not once per warp);
-// one chunk, two block barriers, for the heights of most problems.  Lane c < 2 of warp w returns column b * kGtBlockCols + 2w + c's
-// sum and sets *col to that column; every other thread gets *col = -1.
-// Sixteen columns per block: 1,024 blocks for 16,384 cells, an even spread
-// over 152 SMs (32-column blocks left some SMs a fourth block against 3.4).
-constexpr int kGtWarpCols = 2;
+// one chunk, two block barriers, for the heights of most problems.  Lane
+// c < 4 of warp w returns column b * kGtBlockCols + 4w + c's sum and sets
+// *col to that column; every other thread gets *col = -1.
+constexpr int kGtWarpCols = 4;
 constexpr int kGtBlockCols = kGtWarpCols * (kThreads / 32);
 constexpr int kYChunkBytes = 32768;  // y staged 32 KB at a time: one chunk for ld <= 8,192 (FP32)
 

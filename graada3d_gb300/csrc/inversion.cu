@@ -10,6 +10,8 @@
 // Row segments of the stacked CG system, in the reference's order
 // (GaussNewtonInversion.cpp:1461-1471): data (Nd), Ws, Wz, Wx, Wy and, with
 // the cross-gradient constraint, Tz, Tx, Ty (Nm each).
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -73,8 +75,13 @@ void Context::release_all() {
                     &bk_gtw, &bk_gx, &bk_tmpd, &bk_scal, &bk_part, &bk_ctl, &bk_coef, &sw_m, &sw_mt,
                     &sw_mt_old, &sw_mopt, &sw_dx, &sw_P, &sw_mmin, &sw_mmax, &sw_m0, &sw_wl,
                     &sw_tmp, &sw_tmp2, &sw_dpre, &sw_d64, &sw_mstart, &sw_guard, &sw_flag, &sw_in,
-                    &sw_out};
+                    &sw_out, &cg_args};
   for (DevBuf *b : bufs) b->release();
+  if (phase_exec) cudaGraphExecDestroy(phase_exec);
+  phase_exec = nullptr;
+  for (auto &k : phase_key) k = -1;
+  if (h_cg_args) cudaFreeHost(h_cg_args);
+  h_cg_args = nullptr;
   if (h_scal) cudaFreeHost(h_scal);
   if (h_flag) cudaFreeHost(h_flag);
   if (h_ctl) cudaFreeHost(h_ctl);
@@ -389,6 +396,7 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
     launch_beta(scal, ctl, stream);
   };
   const int K = std::min(maxit, kCgGraphIters);
+  const auto t_build = std::chrono::steady_clock::now();
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   GRADA_CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -404,6 +412,7 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
   cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
   cudaGraphDestroy(graph);
   GRADA_CUDA_CHECK(ie);
+  const auto t_loop = std::chrono::steady_clock::now();
   int launched = 0;
   try {
     while (true) {
@@ -421,6 +430,7 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
     throw;
   }
   cudaGraphExecDestroy(exec);
+  count_cg_loop(t_build, t_loop, h_ctl[CTL_ITER]);
   res.iterations = h_ctl[CTL_ITER];
   res.err = h_scal[CG_ERR];
   if (h_ctl[CTL_STATUS] == CG_STATUS_BREAKDOWN)
@@ -430,6 +440,14 @@ CgResult Context::solve_cg_dev(double lambda, double tol, int maxit, const doubl
     throw Error(GRADA_ERR_NONFINITE,
                 "non-finite CG scalar at iteration " + std::to_string(res.iterations));
   return res;
+}
+
+void Context::count_cg_loop(std::chrono::steady_clock::time_point t_build,
+                            std::chrono::steady_clock::time_point t_loop, int iterations) {
+  const auto t_end = std::chrono::steady_clock::now();
+  cg_graph_ns += (double)std::chrono::duration_cast<std::chrono::nanoseconds>(t_loop - t_build).count();
+  cg_loop_ns += (double)std::chrono::duration_cast<std::chrono::nanoseconds>(t_end - t_loop).count();
+  cg_loop_iters += iterations;
 }
 
 Context::CgLoop Context::cg_loop_kind() const {
@@ -515,6 +533,7 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
     const int c = std::atoi(e);
     if (c >= 1 && c < grid) launch_grid = c;
   }
+  const auto t_loop = std::chrono::steady_clock::now();
   launch_cg_fused(a, g.kind, launch_grid, stream);
   unsigned bar_words[256];
   unsigned long long trace[5];
@@ -526,6 +545,7 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   if (bar_words[224])
     throw Error(GRADA_ERR_CUDA, "persistent CG: a grid barrier wait expired; the solve was abandoned");
   for (int q = 0; q < 5; q++) trace_sum[q] += trace[q];
+  count_cg_loop(t_loop, t_loop, h_ctl[CTL_ITER]);
   CgResult res;
   res.iterations = h_ctl[CTL_ITER];
   res.err = h_scal[CG_ERR];
@@ -541,41 +561,62 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
 // The persistent loop's phases as a graph of four kernels per iteration
 // (cg_phases.cu), replayed until the device raises ctl[CTL_DONE]; a holds the
 // state solve_cg_fused set up.  K iterations per graph, K even (or maxit), so
-// the p / p2 parity of a captured iteration is that of the solve's count.
+// the p / p2 parity of a captured iteration is that of the solve's count.  The
+// kernels take their arguments from cg_args, so a graph built for one solve
+// serves every later solve of the same shape (the arguments are rewritten,
+// nothing is captured or instantiated again).
 CgResult Context::solve_cg_phases(const FusedCgArgs &a, GKind kind, int maxit) {
   const int K = std::min(maxit, kCgGraphIters);
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  GRADA_CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-  try {
-    for (int k = 0; k < K; k++) launch_cg_phase_iteration(a, kind, k & 1, stream);
-  } catch (...) {
-    cudaGraph_t g = nullptr;
-    cudaStreamEndCapture(stream, &g);
-    if (g) cudaGraphDestroy(g);
-    throw;
+  const auto t_build = std::chrono::steady_clock::now();
+  cg_args.alloc(this, sizeof(FusedCgArgs));
+  if (!h_cg_args) {
+    void *hp = nullptr;
+    GRADA_CUDA_CHECK(cudaMallocHost(&hp, sizeof(FusedCgArgs)));
+    h_cg_args = static_cast<FusedCgArgs *>(hp);
   }
-  GRADA_CUDA_CHECK(cudaStreamEndCapture(stream, &graph));
-  cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);
-  GRADA_CUDA_CHECK(ie);
-  int launched = 0;
-  try {
-    while (true) {
-      GRADA_CUDA_CHECK(cudaGraphLaunch(exec, stream));
-      launched += K;
-      GRADA_CUDA_CHECK(cudaMemcpyAsync(h_ctl, a.ctl, sizeof(int) * CTL_NINTS,
-                                       cudaMemcpyDeviceToHost, stream));
-      GRADA_CUDA_CHECK(cudaMemcpyAsync(h_scal, a.scal, sizeof(double) * CG_NSCALARS,
-                                       cudaMemcpyDeviceToHost, stream));
-      sync();
-      if (h_ctl[CTL_DONE] || launched >= maxit) break;
+  // the previous solve's upload has completed (every solve ends synchronised)
+  *h_cg_args = a;
+  const FusedCgArgs *dev_args = cg_args.as<FusedCgArgs>();
+  GRADA_CUDA_CHECK(cudaMemcpyAsync(cg_args.ptr, h_cg_args, sizeof(FusedCgArgs),
+                                   cudaMemcpyHostToDevice, stream));
+  int64_t key[7];
+  cg_phase_grids(a, key);
+  key[4] = (int64_t)kind;
+  key[5] = K;
+  key[6] = (int64_t)(uintptr_t)dev_args;
+  if (!phase_exec || !std::equal(key, key + 7, phase_key)) {
+    if (phase_exec) cudaGraphExecDestroy(phase_exec);
+    phase_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    GRADA_CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (int k = 0; k < K; k++) launch_cg_phase_iteration(a, dev_args, kind, k & 1, stream);
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(stream, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
     }
-  } catch (...) {
-    cudaGraphExecDestroy(exec);
-    throw;
+    GRADA_CUDA_CHECK(cudaStreamEndCapture(stream, &graph));
+    cudaError_t ie = cudaGraphInstantiate(&phase_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) phase_exec = nullptr;
+    GRADA_CUDA_CHECK(ie);
+    std::copy(key, key + 7, phase_key);
   }
-  cudaGraphExecDestroy(exec);
+  const auto t_loop = std::chrono::steady_clock::now();
+  int launched = 0;
+  while (true) {
+    GRADA_CUDA_CHECK(cudaGraphLaunch(phase_exec, stream));
+    launched += K;
+    GRADA_CUDA_CHECK(cudaMemcpyAsync(h_ctl, a.ctl, sizeof(int) * CTL_NINTS,
+                                     cudaMemcpyDeviceToHost, stream));
+    GRADA_CUDA_CHECK(cudaMemcpyAsync(h_scal, a.scal, sizeof(double) * CG_NSCALARS,
+                                     cudaMemcpyDeviceToHost, stream));
+    sync();
+    if (h_ctl[CTL_DONE] || launched >= maxit) break;
+  }
+  count_cg_loop(t_build, t_loop, h_ctl[CTL_ITER]);
   CgResult res;
   res.iterations = h_ctl[CTL_ITER];
   res.err = h_scal[CG_ERR];
@@ -664,6 +705,8 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
   } predict_guard{this};
   const bool refine = invert_setup(prm, h_m_ini, h_mmin, h_mmax, h_m0);
   for (auto &t : trace_sum) t = 0;
+  cg_loop_ns = cg_graph_ns = 0.0;
+  cg_loop_iters = 0;
   if (adapt && predict_fp64)
     throw Error(GRADA_ERR_STATE, "adaptive inversion: a kept FP64 G is not expanded by refinement");
   int64_t Nm = n_cells;

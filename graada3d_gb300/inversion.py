@@ -116,6 +116,15 @@ class GaussNewtonInversion(Fwd):
         self.ctx.check(self.ctx.lib.grada_cg_phase_times(self.ctx.handle, _ptr(out), ctypes.byref(n)))
         return out, n.value
 
+    def cg_loop_time(self):
+        """(loop seconds, graph-building seconds, CG iterations) of the CG loops
+        since the last invert: the loops alone, without the set-up, predictions
+        and lambda control around them (grada_cg_loop_time)."""
+        out = np.zeros(2)
+        n = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.grada_cg_loop_time(self.ctx.handle, _ptr(out), ctypes.byref(n)))
+        return float(out[0]), float(out[1]), n.value
+
     def invert(self, prm: dict, m_ini, m_min, m_max, m0=None, fp64_refinement: bool = False):
         """invert_with_own_CG on the current G.  prm keys as oracle.inversion.invert
         (max_lambda, n_lambda, rate, target, stag, cg_tol, cg_factor, gn_iter,

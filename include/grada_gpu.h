@@ -366,6 +366,16 @@ int grada_set_inversion_model(grada_ctx *ctx, const double *m, const double *m_m
  * since the context was made); *iterations gets their iteration count.
  */
 int grada_cg_phase_times(grada_ctx *ctx, double *mean_ns, int64_t *iterations);
+/*
+ * Host time in the CG loops of the solves since the last grada_invert (or since
+ * the context was made), any G storage and loop (no reference counterpart):
+ * seconds[0] from the first launch of each solve's loop to its last host
+ * synchronisation, seconds[1] building the loops' CUDA graphs (capture and
+ * instantiation; nothing for a solve that reuses a graph); *iterations gets
+ * their CG iteration count.  Separates the loop's cost per iteration from the
+ * set-up, predictions and lambda control around it.
+ */
+int grada_cg_loop_time(grada_ctx *ctx, double *seconds, int64_t *iterations);
 
 /* The model of the last grada_invert / grada_invert_adaptive (Nm doubles). */
 int grada_get_model(grada_ctx *ctx, double *m);
