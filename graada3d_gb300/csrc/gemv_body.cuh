@@ -273,6 +273,44 @@ constexpr int kGtWarpCols = 4;
 constexpr int kGtBlockCols = kGtWarpCols * (kThreads / 32);
 constexpr int kYChunkBytes = 32768;  // y staged 32 KB at a time: one chunk for ld <= 8,192 (FP32)
 
+// Rows row_begin, row_begin + 32 VEC, ... < row_end of the warp's columns
+// c0 .. c0 + ncol - 1 (G rows offset by g_row0), y's VEC values of a row from
+// y_at.  Full (ncol = kGtWarpCols, every warp but the last): no per-column
+// tests, so every column's loads of a row step issue before its FMAs.  Each
+// column adds its rows in the same order either way.
+template <class L, bool Full, class YAt>
+__device__ __forceinline__ void gty_rows(const void *__restrict__ G, int64_t ld, int64_t c0,
+                                         int ncol, int64_t g_row0, int64_t row_begin,
+                                         int64_t row_end, YAt y_at,
+                                         typename L::Acc (&acc)[kGtWarpCols]) {
+  using Acc = typename L::Acc;
+  constexpr int VEC = L::VEC;
+#pragma unroll 2
+  for (int64_t row = row_begin; row < row_end; row += 32 * VEC) {
+    Acc yv[VEC];
+    y_at(row, yv);
+    if constexpr (Full) {
+      Acc g[kGtWarpCols][VEC];
+#pragma unroll
+      for (int c = 0; c < kGtWarpCols; c++) L::load(G, g_row0 + row + (c0 + c) * ld, g[c]);
+#pragma unroll
+      for (int c = 0; c < kGtWarpCols; c++)
+#pragma unroll
+        for (int v = 0; v < VEC; v++) acc[c] = fma(g[c][v], yv[v], acc[c]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < kGtWarpCols; c++) {
+        if (c < ncol) {
+          Acc g[VEC];
+          L::load(G, g_row0 + row + (c0 + c) * ld, g);
+#pragma unroll
+          for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
+        }
+      }
+    }
+  }
+}
+
 template <class L>
 __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t ld, int64_t nm,
                                            const typename L::Acc *y, int64_t b, int64_t *col) {
@@ -289,6 +327,10 @@ __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t l
   for (int c = 0; c < kGtWarpCols; c++) acc[c] = Acc(0);
   // 16 bytes of y per load: 4 floats or 2 doubles
   constexpr int YV = 16 / (int)sizeof(Acc);
+  auto y_at = [&](int64_t row, Acc (&yv)[VEC]) {
+#pragma unroll
+    for (int v = 0; v < VEC; v++) yv[v] = ys[row + v];
+  };
   for (int64_t r0 = 0; r0 < ld; r0 += kYChunk) {
     const int n = (int)min((int64_t)kYChunk, ld - r0);  // a multiple of 64 (ld is)
     __syncthreads();
@@ -301,23 +343,10 @@ __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t l
       }
     }
     __syncthreads();
-    if (ncol > 0) {
-#pragma unroll 2
-      for (int row = lane * VEC; row < n; row += 32 * VEC) {
-        Acc yv[VEC];
-#pragma unroll
-        for (int v = 0; v < VEC; v++) yv[v] = ys[row + v];
-#pragma unroll
-        for (int c = 0; c < kGtWarpCols; c++) {
-          if (c < ncol) {
-            Acc g[VEC];
-            L::load(G, r0 + row + (c0 + c) * ld, g);
-#pragma unroll
-            for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
-          }
-        }
-      }
-    }
+    if (ncol == kGtWarpCols)
+      gty_rows<L, true>(G, ld, c0, ncol, r0, lane * VEC, n, y_at, acc);
+    else if (ncol > 0)
+      gty_rows<L, false>(G, ld, c0, ncol, r0, lane * VEC, n, y_at, acc);
   }
   double mine = 0.0;
 #pragma unroll
@@ -347,23 +376,14 @@ __device__ __forceinline__ double gty_body_l2(const void *__restrict__ G, int64_
   Acc acc[kGtWarpCols];
 #pragma unroll
   for (int c = 0; c < kGtWarpCols; c++) acc[c] = Acc(0);
-  if (ncol > 0) {
-#pragma unroll 2
-    for (int64_t row = (int64_t)lane * VEC; row < ld; row += 32 * VEC) {
-      Acc yv[VEC];
+  auto y_at = [&](int64_t row, Acc (&yv)[VEC]) {
 #pragma unroll
-      for (int v = 0; v < VEC; v++) yv[v] = __ldcg(y + row + v);
-#pragma unroll
-      for (int c = 0; c < kGtWarpCols; c++) {
-        if (c < ncol) {
-          Acc g[VEC];
-          L::load(G, row + (c0 + c) * ld, g);
-#pragma unroll
-          for (int v = 0; v < VEC; v++) acc[c] = fma(g[v], yv[v], acc[c]);
-        }
-      }
-    }
-  }
+    for (int v = 0; v < VEC; v++) yv[v] = __ldcg(y + row + v);
+  };
+  if (ncol == kGtWarpCols)
+    gty_rows<L, true>(G, ld, c0, ncol, 0, (int64_t)lane * VEC, ld, y_at, acc);
+  else if (ncol > 0)
+    gty_rows<L, false>(G, ld, c0, ncol, 0, (int64_t)lane * VEC, ld, y_at, acc);
   double mine = 0.0;
 #pragma unroll
   for (int c = 0; c < kGtWarpCols; c++) {
