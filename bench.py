@@ -509,8 +509,8 @@ def run_inversion(name: str, storages=("fp64", "fp32", "fp16", "bf16", "fp32+fp6
             r["cg_graph_build_s"] = graph_s
         ph, n_ph = inv.cg_phase_times()
         if n_ph:  # the persistent CG loop ran: its phases' mean time per iteration
-            r["cg_phase_us"] = {"gp_forward_rows": ph[0] / 1e3, "finish": ph[1] / 1e3,
-                                "step_gts_adjoint": ph[2] / 1e3}
+            r["cg_phase_us"] = {"gp": ph[0] / 1e3, "finish_rows": ph[1] / 1e3, "step": ph[2] / 1e3,
+                                "gts_adjoint": ph[3] / 1e3}
         if st == "fp64":
             m64 = m
         else:

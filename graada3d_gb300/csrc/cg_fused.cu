@@ -4,7 +4,7 @@
 // (src/Inversion/GaussNewtonInversion.cpp:1556-1692).  The graph-replayed
 // iteration (inversion.cu) launches 13 kernels per iteration.  Here every CTA
 // of a cooperative grid (all co-resident) runs the iteration's phases in turn
-// (cg_fused.cuh: three team barriers per iteration) and decides the stopping
+// (cg_fused.cuh: four team barriers per iteration) and decides the stopping
 // test itself from the same reduced scalars, so no host round trip or launch
 // happens until the solve ends.  The sums are fixed-order and independent of
 // the grid, so a solve is deterministic and gives what the batched kernel

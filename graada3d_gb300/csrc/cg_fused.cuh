@@ -156,89 +156,38 @@ __device__ __forceinline__ double finish_rows(const double *partial, int n_split
   return bcast_sum(sq);
 }
 
-// Forward regulariser row block k of phase A: term k / nb_vec, rows
-// (k % nb_vec) * VT + thread: t_out = c (A pp) (x wl), with pp_j computed from
-// r, p_old and beta by gemv::cg_direction (the bits G pp's staging uses), so
-// the rows need no stored pp.  Returns the block's sum of t^2 (every thread).
-__device__ __forceinline__ double forward_rows_block(const FusedCgArgs &a, const double *p_old,
-                                                     double beta, int64_t k, int64_t nb_vec) {
-  const ForwardTerm &t = a.FT.t[k / nb_vec];
-  const int64_t i = (k % nb_vec) * cgb::VT + threadIdx.x;
-  double q = 0.0;
-  if (i < t.A.n) {
-    double acc = 0.0;
-    for (int e = t.A.rowptr[i]; e < t.A.rowptr[i + 1]; e++)
-      acc = fma(t.A.val[e], gemv::cg_direction(a.r, p_old, a.P, beta, t.A.col[e], nullptr), acc);
-    double v = t.c * acc;
-    if (t.wl) v *= t.wl[i];
-    t.out[i] = v;
-    q = v * v;
-  }
-  return bcast_sum(q);
-}
-
-// y of phase C for rows r0 .. r0 + n - 1: Wd (s_old + alpha t) on the data
-// rows (times the 16-bit row scale), zero in the padding, in G's
-// accumulation type -- the bits of the step s += alpha t followed by the
-// scaling of y.
-template <typename Acc>
-struct StepY {
-  const double *s_old, *t, *wd;
-  const float *row_scale;
-  double alpha;
-  int64_t nd;
-  __device__ __forceinline__ void operator()(int64_t r0, int n, Acc *ys) const {
-    for (int k = threadIdx.x; k < n; k += cgb::VT) {
-      const int64_t r = r0 + k;
-      double v = 0.0;
-      if (r < nd) {
-        v = fma(alpha, __ldcg(t + r), __ldcg(s_old + r));
-        v = wd[r] * v;
-        if (row_scale) v *= (double)row_scale[r];
-      }
-      ys[k] = (Acc)v;
-    }
-  }
-};
-
-// Phase C block b of nb: the step s_new = s_old + alpha t and dx += alpha
-// p_new over the indices b * VT + thread + m nb VT; then G^T y for the 32
-// columns of block b (warp w takes columns 4w .. 4w + 3, lanes striding the
-// rows, y = StepY staged in shared memory) and r_j for those columns: the
-// regulariser adjoint terms on one lane per (column, term), their dependent
-// CSR loads in parallel and s_new formed on the fly from s_old and t, added
-// by the lane holding the column to its G^T sum in term order
-// (cgb::adjoint_column's arithmetic), then P.  Writes s_new, dx, gtw and r;
-// returns the block's sum of r_j^2 (valid in every thread).
-template <class L>
-__device__ __forceinline__ double step_gty_adjoint_block(const FusedCgArgs &a, double alpha,
-                                                         const double *s_old, double *s_new,
-                                                         const double *p_new, int64_t b,
-                                                         int64_t nb) {
+// G^T y for the 32 columns of block b (warp w takes columns 4w .. 4w + 3,
+// lanes striding the rows), then r_j for those columns (the adjoint of the
+// regulariser rows and P).  StageY: y through shared memory (gemv::gty_body,
+// for a kernel of its own at full occupancy), else read from L2 by each warp
+// (gemv::gty_body_l2, the persistent loop's); both sum each column in the same
+// order.  The regulariser terms of the warp's 4 columns run on one lane per
+// (column, term), their dependent CSR loads in parallel; the lane holding a
+// column adds them to its G^T sum in term order (cgb::adjoint_column's
+// arithmetic).  Writes gtw and r; returns the block's sum of r_j^2 (valid in
+// every thread).
+template <class L, bool StageY = false>
+__device__ __forceinline__ double gty_adjoint_block(const FusedCgArgs &a, const typename L::Acc *y,
+                                                    int64_t b) {
   static_assert(gemv::kGtWarpCols * 8 <= 32, "one lane per (column, term)");
-  using Acc = typename L::Acc;
   __shared__ double wsum[cgb::VT / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t top = a.nrow > a.nm ? a.nrow : a.nm;
-  for (int64_t i = b * cgb::VT + threadIdx.x; i < top; i += nb * cgb::VT) {
-    if (i < a.nrow) s_new[i] = fma(alpha, __ldcg(a.t + i), __ldcg(s_old + i));
-    if (i < a.nm) a.dx[i] = fma(alpha, __ldcg(p_new + i), __ldcg(a.dx + i));
-  }
   int64_t j = -1;
-  const StepY<Acc> fill{s_old, a.t, a.wd, a.row_scale, alpha, a.nd};
-  const double g = gemv::gty_body_f<L>(a.G, a.ld, a.nm, fill, b, &j);
+  double g;
+  if constexpr (StageY)
+    g = gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j);
+  else
+    g = gemv::gty_body_l2<L>(a.G, a.ld, a.nm, y, b, &j);
   // lane 8c + q: term q of the warp's column c
   const int tc = lane >> 3, tq = lane & 7;
   const int64_t tj = b * gemv::kGtBlockCols + (int64_t)warp * gemv::kGtWarpCols + tc;
   double ts = 0.0;
   if (tc < gemv::kGtWarpCols && tq < a.AT.count && tj < a.nm) {
     const AdjointTerm &t = a.AT.t[tq];
-    const int64_t off = t.s - a.s;  // the term's segment of s (and of t)
     for (int k = t.AT.rowptr[tj]; k < t.AT.rowptr[tj + 1]; k++) {
-      const int64_t i = off + t.AT.col[k];
-      const double w = t.wl ? t.wl[t.AT.col[k]] : 1.0;
-      const double sv = fma(alpha, __ldcg(a.t + i), __ldcg(s_old + i));
-      ts = fma(t.AT.val[k], w * sv, ts);
+      const int i = t.AT.col[k];
+      const double w = t.wl ? t.wl[i] : 1.0;
+      ts = fma(t.AT.val[k], w * __ldcg(t.s + i), ts);
     }
   }
   double acc = g;  // lanes c < 4: P_j (gtw_j + sum_q c_q s_q), terms in order
@@ -275,8 +224,7 @@ struct CgOut {
 };
 
 // Layout of a.red for a loop: per-block partials of ||t||^2 over the finish
-// blocks (phase B) and the forward-row blocks (phase A), then of ||r||^2 over
-// the G^T blocks.
+// and forward-row blocks, then of ||r||^2 over the G^T blocks.
 struct RedLayout {
   int64_t nb_fin, nb_t, nb_r;
   __host__ __device__ RedLayout(int64_t nd, int64_t nm, int nterms) {
@@ -290,28 +238,31 @@ struct RedLayout {
 
 // The loop of one solve, run by CTA `cta` of the nct CTAs of its team, from
 // r (set up), p = dx = 0 and beta = 0.  Every CTA returns the same CgOut.
-// Three team barriers per iteration:
-//   A  p_new = -r + beta p_old folded into the partial row sums of G pp (row
-//      tiles of 32 VEC rows x column ranges, the block's 8 warps splitting a
-//      range), and the forward regulariser rows of t from pp formed on the
-//      fly, with their per-block ||t||^2
+// Four team barriers per iteration:
+//   A  p_new = -r + beta p_old and pp = P p_new folded into the partial row
+//      sums of G pp (row tiles of 32 VEC rows x column ranges, the block's 8
+//      warps splitting a range)
 //   B  t_data = Wd (sum of the partials, 16 rows per block, the splits shared
-//      by 16 half-warps), per-block ||t||^2; then alpha = r2 / t2
-//   C  s += alpha t (s and s2 alternate), dx += alpha p_new, and G^T y with
-//      y = Wd s_data staged per block, for 32 columns per block (4 per warp),
-//      r for those columns (the adjoint of the regulariser rows, P), per-block
-//      ||r||^2; then beta, err and the stopping test
+//      by 16 half-warps), the forward regulariser rows of t, per-block ||t||^2
+//   C  alpha = r2 / t2; s += alpha t, dx += alpha p_new, y = Wd s_data in G's
+//      accumulation type
+//   D  G^T y for 32 columns per block (4 per warp), r for those columns (the
+//      adjoint of the regulariser rows, P), per-block ||r||^2; then beta, err
+//      and the stopping test
 // Every CTA adds the per-block partials in index order, so the sums do not
 // depend on the team size or on which CTA ran which block.
 template <class L>
 __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, unsigned nct,
                          TeamBarrier &bar) {
-  const int64_t Nm = a.nm, nd = a.nd;
+  using Acc = typename L::Acc;
+  const int64_t Nm = a.nm, nd = a.nd, ld = a.ld, nrow = a.nrow;
   const int64_t nb_vec = ceil_div_d(Nm, cgb::VT);  // blocks of an Nm-long vector
+  const int64_t nb_axpy = ceil_div_d(nrow > Nm ? nrow : Nm, cgb::VT);
+  const int64_t nb_prep = ceil_div_d(ld, 256);
   const int64_t n_gx = (int64_t)a.tiles * a.splits;
   const RedLayout rl(nd, Nm, a.FT.count);
-  const int64_t n_a = n_gx + (rl.nb_t - rl.nb_fin);  // G pp units, then forward-row blocks
   double *part_t = a.red, *part_r = a.red + rl.nb_t;
+  Acc *y = reinterpret_cast<Acc *>(a.scratch);
 
   CgOut o;
   double R2 = in.R2, beta = 0.0, rlast2 = in.rlast2, err = in.err;
@@ -338,42 +289,55 @@ __device__ CgOut cg_loop(const FusedCgArgs &a, const CgIn &in, unsigned cta, uns
     }
   };
   while (true) {
-    const double *p_old = (it & 1) ? a.p2 : a.p;
+    double *p_old = (it & 1) ? a.p2 : a.p;
     double *p_new = (it & 1) ? a.p : a.p2;
-    const double *s_old = (it & 1) ? a.s2 : a.s;
-    double *s_new = (it & 1) ? a.s : a.s2;
     // A
-    for (int64_t b = cta; b < n_a; b += nct) {
-      if (b < n_gx) {
-        gemv::gx_partial_fold_body<L>(a.G, a.ld, Nm, a.per, a.r, p_old, a.P, beta, p_new, nullptr,
-                                      a.scratch, b % a.tiles, b / a.tiles);
-      } else {
-        const double v = forward_rows_block(a, p_old, beta, b - n_gx, nb_vec);
-        if (threadIdx.x == 0) part_t[rl.nb_fin + (b - n_gx)] = v;
-      }
-    }
+    for (int64_t b = cta; b < n_gx; b += nct)
+      gemv::gx_partial_fold_body<L>(a.G, ld, Nm, a.per, a.r, p_old, a.P, beta, p_new, a.pp,
+                                    a.scratch, b % a.tiles, b / a.tiles);
     if (!(ok = bar.sync())) break;
     stamp(0);
     // B
-    for (int64_t b = cta; b < rl.nb_fin; b += nct) {
-      const double v = finish_rows(a.scratch, a.splits, a.ld, nd, a.row_scale, a.wd, a.t, b);
+    for (int64_t b = cta; b < rl.nb_t; b += nct) {
+      double v;
+      if (b < rl.nb_fin) {
+        v = finish_rows(a.scratch, a.splits, ld, nd, a.row_scale, a.wd, a.t, b);
+      } else {
+        const int64_t k = b - rl.nb_fin;
+        const ForwardTerm &ft = a.FT.t[k / nb_vec];
+        cgb::forward_term_body(ft, a.pp, k % nb_vec);
+        const int64_t i = (k % nb_vec) * cgb::VT + threadIdx.x;
+        double q = 0.0;
+        if (i < Nm) {
+          const double tv = __ldcg(ft.out + i);
+          q = tv * tv;
+        }
+        v = bcast_sum(q);
+      }
       if (threadIdx.x == 0) part_t[b] = v;
     }
     if (!(ok = bar.sync())) break;
     stamp(1);
+    // C
     T2 = sum_partials_all(part_t, rl.nb_t);
     alpha = R2 / T2;  // GaussNewtonInversion.cpp:1601
     if (T2 == 0.0 || !isfinite(alpha)) {
       status = (T2 == 0.0) ? CG_STATUS_BREAKDOWN : CG_STATUS_NONFINITE;
       break;
     }
-    // C
-    for (int64_t b = cta; b < rl.nb_r; b += nct) {
-      const double v = step_gty_adjoint_block<L>(a, alpha, s_old, s_new, p_new, b, rl.nb_r);
-      if (threadIdx.x == 0) part_r[b] = v;
+    for (int64_t b = cta; b < nb_axpy; b += nct) {
+      cgb::axpy_body(a.t, p_new, alpha, nrow, Nm, a.s, a.dx, b);
+      if (b < nb_prep) gemv::prep_y_body<Acc>(a.s, nd, ld, a.row_scale, a.wd, y, b);
     }
     if (!(ok = bar.sync())) break;
     stamp(2);
+    // D
+    for (int64_t b = cta; b < rl.nb_r; b += nct) {
+      const double v = gty_adjoint_block<L>(a, y, b);
+      if (threadIdx.x == 0) part_r[b] = v;
+    }
+    if (!(ok = bar.sync())) break;
+    stamp(3);
     const double r2 = sum_partials_all(part_r, rl.nb_r);
     // :1674-1691
     rlast2 = R2;

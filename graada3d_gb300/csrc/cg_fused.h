@@ -32,7 +32,6 @@ struct FusedCgArgs {
   ForwardTerms FT;
   AdjointTerms AT;
   double *p2 = nullptr;        // second direction buffer (p and p2 alternate)
-  double *s2 = nullptr;        // second s buffer (s and s2 alternate; nrow doubles)
   double *part = nullptr;      // set-up dot products (dot_blocks partition)
   int nb_m = 0, nb_row = 0;    // dot-product block counts of the set-up
   double *red = nullptr;       // per-block partials and group sums of ||t||^2, ||r||^2
@@ -61,13 +60,13 @@ void fused_red_sizes(int64_t nd, int64_t nm, int nterms, int64_t &doubles, int64
 void launch_cg_fused(const FusedCgArgs &a, GKind kind, int grid, cudaStream_t s);
 // Resident blocks per SM of the phase-A kernel (G pp) for this storage.
 int cg_phase_a_blocks_per_sm(GKind kind);
-// One iteration of the same loop as three kernels (cg_phases.cu) reading their
+// One iteration of the same loop as four kernels (cg_phases.cu) reading their
 // arguments from dev_args (a device copy of a, which sizes the grids); parity
-// alternates p / p2 and s / s2 as the persistent loop's iteration count does.
+// alternates p and p2 as the persistent loop's iteration count does.
 void launch_cg_phase_iteration(const FusedCgArgs &a, const FusedCgArgs *dev_args, GKind kind,
                                int parity, cudaStream_t s);
-// The three phase kernels' grid sizes for a, and 0 (what a captured iteration
-// bakes in besides the storage and the argument pointer).
+// The four phase kernels' grid sizes for a (what a captured iteration bakes in
+// besides the storage and the argument pointer).
 void cg_phase_grids(const FusedCgArgs &a, int64_t grids[4]);
 
 }  // namespace grada

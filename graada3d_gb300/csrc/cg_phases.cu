@@ -1,4 +1,4 @@
-// The CG loop's three phases as separate kernels, replayed from a CUDA graph.
+// The CG loop's four phases as separate kernels, replayed from a CUDA graph.
 //
 // Reference: GaussNewtonInversion::solve_cg, the iteration loop
 // (src/Inversion/GaussNewtonInversion.cpp:1556-1692).  The phase bodies are
@@ -6,8 +6,8 @@
 // (fused_gx_partition), so both paths compute the same sums in the same order
 // and give bitwise the same solve.  What the
 // persistent loop does at a team barrier happens here at a kernel boundary,
-// and the two reductions that end a phase (||t||^2 -> alpha in B, ||r||^2 ->
-// beta and the stopping test in C) run in the phase's last block: every block stores
+// and the two reductions that end a phase (||t||^2 -> alpha, ||r||^2 -> beta
+// and the stopping test) run in the phase's last block: every block stores
 // its partial, fences and counts itself in; the block that counts last adds
 // the partials in index order (nothing waits on another block).  Each kernel
 // returns at once while ctl[CTL_DONE] is raised, so a graph of K iterations
@@ -46,9 +46,7 @@ __device__ __forceinline__ bool done(const FusedCgArgs &a) {
   return *reinterpret_cast<volatile const int *>(a.ctl + CTL_DONE) != 0;
 }
 
-// A: p_new = -r + beta p_old folded into G pp's partial sums (blocks below
-// tiles x splits), then the forward regulariser rows of t with their per-block
-// ||t||^2 (the remaining blocks).
+// A: p_new = -r + beta p_old, pp = P p_new, folded into G pp's partial sums.
 template <class L>
 __global__ void __launch_bounds__(256)
     phase_a_kernel(const FusedCgArgs *__restrict__ ap, int parity) {
@@ -57,29 +55,37 @@ __global__ void __launch_bounds__(256)
   const double *p_old = parity ? a.p2 : a.p;
   double *p_new = parity ? a.p : a.p2;
   const double beta = __ldcg(a.scal + CG_BETA);
-  const int64_t b = blockIdx.x, n_gx = (int64_t)a.tiles * a.splits;
-  if (b < n_gx) {
-    gemv::gx_partial_fold_body<L>(a.G, a.ld, a.nm, a.per, a.r, p_old, a.P, beta, p_new, nullptr,
-                                  a.scratch, b % a.tiles, b / a.tiles);
-  } else {
-    const RedLayout rl(a.nd, a.nm, a.FT.count);
-    const double v =
-        fused::forward_rows_block(a, p_old, beta, b - n_gx, ceil_div_d(a.nm, cgb::VT));
-    if (threadIdx.x == 0) a.red[rl.nb_fin + (b - n_gx)] = v;
-  }
+  const int64_t b = blockIdx.x;
+  gemv::gx_partial_fold_body<L>(a.G, a.ld, a.nm, a.per, a.r, p_old, a.P, beta, p_new, a.pp,
+                                a.scratch, b % a.tiles, b / a.tiles);
 }
 
-// B: t_data = Wd (sum of the partials) with the per-block ||t||^2; the last
-// block: t2 over the finish and forward-row partials, alpha = r2 / t2 (:1601)
-// and the breakdown / non-finite checks.
+// B: t_data = Wd (sum of the partials), the forward regulariser rows, the
+// per-block ||t||^2; the last block: t2, alpha = r2 / t2 (:1601) and the
+// breakdown / non-finite checks.
 __global__ void __launch_bounds__(256) phase_b_kernel(const FusedCgArgs *__restrict__ ap) {
   const FusedCgArgs &a = *ap;
   if (done(a)) return;
   const RedLayout rl(a.nd, a.nm, a.FT.count);
+  const int64_t nb_vec = ceil_div_d(a.nm, cgb::VT);
   const int64_t b = blockIdx.x;
-  const double v = fused::finish_rows(a.scratch, a.splits, a.ld, a.nd, a.row_scale, a.wd, a.t, b);
+  double v;
+  if (b < rl.nb_fin) {
+    v = fused::finish_rows(a.scratch, a.splits, a.ld, a.nd, a.row_scale, a.wd, a.t, b);
+  } else {
+    const int64_t k = b - rl.nb_fin;
+    const ForwardTerm &ft = a.FT.t[k / nb_vec];
+    cgb::forward_term_body(ft, a.pp, k % nb_vec);
+    const int64_t i = (k % nb_vec) * cgb::VT + threadIdx.x;
+    double q = 0.0;
+    if (i < a.nm) {
+      const double tv = __ldcg(ft.out + i);
+      q = tv * tv;
+    }
+    v = fused::bcast_sum(q);
+  }
   if (threadIdx.x == 0) a.red[b] = v;
-  if (!last_block(a.red_count, (unsigned)rl.nb_fin)) return;
+  if (!last_block(a.red_count, (unsigned)rl.nb_t)) return;
   const double T2 = fused::sum_partials_all(a.red, rl.nb_t);
   if (threadIdx.x == 0) {
     const double alpha = __ldcg(a.scal + CG_R2) / T2;
@@ -92,23 +98,34 @@ __global__ void __launch_bounds__(256) phase_b_kernel(const FusedCgArgs *__restr
   }
 }
 
-// C: s += alpha t, dx += alpha p_new, G^T y (y = Wd s_data) and r for 32
-// columns per block, the per-block ||r||^2; the last block: r2, beta = r2 /
-// rlast2, err = r2 / ||A^T b||^2, the iteration count and the stopping tests
-// (:1674-1691).
+// C: s += alpha t, dx += alpha p_new, y = Wd s_data in G's accumulation type.
 template <class L>
 __global__ void __launch_bounds__(256)
     phase_c_kernel(const FusedCgArgs *__restrict__ ap, int parity) {
   const FusedCgArgs &a = *ap;
   if (done(a)) return;
-  const RedLayout rl(a.nd, a.nm, a.FT.count);
+  using Acc = typename L::Acc;
   const double *p_new = parity ? a.p : a.p2;
-  const double *s_old = parity ? a.s2 : a.s;
-  double *s_new = parity ? a.s : a.s2;
   const double alpha = __ldcg(a.scal + CG_ALPHA);
+  const int64_t b = blockIdx.x;
+  cgb::axpy_body(a.t, p_new, alpha, a.nrow, a.nm, a.s, a.dx, b);
+  if (b < ceil_div_d(a.ld, 256))
+    gemv::prep_y_body<Acc>(a.s, a.nd, a.ld, a.row_scale, a.wd, reinterpret_cast<Acc *>(a.scratch),
+                           b);
+}
+
+// D: G^T y and r for 32 columns per block, the per-block ||r||^2; the last
+// block: r2, beta = r2 / rlast2, err = r2 / ||A^T b||^2, the iteration count
+// and the stopping tests (:1674-1691).
+template <class L>
+__global__ void __launch_bounds__(256) phase_d_kernel(const FusedCgArgs *__restrict__ ap) {
+  const FusedCgArgs &a = *ap;
+  if (done(a)) return;
+  using Acc = typename L::Acc;
+  const RedLayout rl(a.nd, a.nm, a.FT.count);
   double *part_r = a.red + rl.nb_t;
   const double v =
-      fused::step_gty_adjoint_block<L>(a, alpha, s_old, s_new, p_new, blockIdx.x, rl.nb_r);
+      fused::gty_adjoint_block<L, true>(a, reinterpret_cast<const Acc *>(a.scratch), blockIdx.x);
   if (threadIdx.x == 0) part_r[blockIdx.x] = v;
   if (!last_block(a.red_count, (unsigned)rl.nb_r)) return;
   const double r2 = fused::sum_partials_all(part_r, rl.nb_r);
@@ -143,6 +160,8 @@ void launch_iteration(const FusedCgArgs &a, const FusedCgArgs *ap, int parity, c
   GRADA_LAUNCH_CHECK();
   phase_c_kernel<L><<<(unsigned)g[2], 256, 0, s>>>(ap, parity);
   GRADA_LAUNCH_CHECK();
+  phase_d_kernel<L><<<(unsigned)g[3], 256, 0, s>>>(ap);
+  GRADA_LAUNCH_CHECK();
 }
 
 }  // namespace
@@ -162,10 +181,10 @@ int cg_phase_a_blocks_per_sm(GKind kind) {
 
 void cg_phase_grids(const FusedCgArgs &a, int64_t grids[4]) {
   const RedLayout rl(a.nd, a.nm, a.FT.count);
-  grids[0] = (int64_t)a.tiles * a.splits + (rl.nb_t - rl.nb_fin);
-  grids[1] = rl.nb_fin;
-  grids[2] = rl.nb_r;
-  grids[3] = 0;
+  grids[0] = (int64_t)a.tiles * a.splits;
+  grids[1] = rl.nb_t;
+  grids[2] = ceil_div_d(a.nrow > a.nm ? a.nrow : a.nm, cgb::VT);
+  grids[3] = rl.nb_r;
 }
 
 void launch_cg_phase_iteration(const FusedCgArgs &a, const FusedCgArgs *dev_args, GKind kind,

@@ -129,7 +129,7 @@ struct Context {
 
   // CG work vectors.
   DevBuf cg_b, cg_s, cg_t, cg_p, cg_pp, cg_r, cg_atb, cg_gtw, cg_gx, cg_tmpd, cg_scal, cg_part;
-  DevBuf cg_wl_ones, cg_ctl, cg_bar, cg_p2, cg_s2, cg_red, cg_redc;
+  DevBuf cg_wl_ones, cg_ctl, cg_bar, cg_p2, cg_red, cg_redc;
   int fused_grid[4] = {0, 0, 0, 0};  // persistent CG grid per G storage kind
   DevBuf cg_trace;                    // phase trace of a persistent solve (5 u64)
   unsigned long long trace_sum[5] = {0, 0, 0, 0, 0};  // since the last invert / reset

@@ -126,18 +126,6 @@ __device__ __forceinline__ void gx_partial_body(const void *__restrict__ G, int6
   }
 }
 
-// The CG direction at column j: v = -r_j + beta p_old_j and pp_j = P_j v
-// (GaussNewtonInversion.cpp:1562-1566), with explicit rounding steps so that
-// every caller (the staging of G pp, the forward regulariser rows) gets the
-// same bits.
-__device__ __forceinline__ double cg_direction(const double *r, const double *p_old,
-                                               const double *__restrict__ P, double beta,
-                                               int64_t j, double *v_out) {
-  const double v = fma(beta, __ldcg(p_old + j), -__ldcg(r + j));
-  if (v_out) *v_out = v;
-  return P[j] * v;
-}
-
 // Rows of a fold-body tile: one warp's lanes x VEC rows (512 bytes of a
 // column per warp load for every storage).
 template <class L>
@@ -178,11 +166,11 @@ __device__ __forceinline__ void gx_partial_fold_body(
     __syncthreads();
     for (int t = threadIdx.x; t < nc; t += kThreads) {
       const int64_t j = c0 + t;
-      double v;
-      const double q = cg_direction(r, p_old, P, beta, j, &v);
+      const double v = -__ldcg(r + j) + beta * __ldcg(p_old + j);
+      const double q = P[j] * v;
       if (tile == 0) {
         p_new[j] = v;
-        if (pp) pp[j] = q;
+        pp[j] = q;
       }
       xs[t] = (Acc)q;
     }
@@ -297,10 +285,7 @@ __device__ __forceinline__ void gty_rows(const void *__restrict__ G, int64_t ld,
                                          typename L::Acc (&acc)[kGtWarpCols]) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
-  // two row steps per trip, one for 16-bit G (measured at 3,392 x 16,384:
-  // bf16 27.7 us with one, 28.6 with two; FP32 the same either way)
-  constexpr int kUnroll = VEC == 8 ? 1 : 2;
-#pragma unroll kUnroll
+#pragma unroll 2
   for (int64_t row = row_begin; row < row_end; row += 32 * VEC) {
     Acc yv[VEC];
     y_at(row, yv);
@@ -326,28 +311,9 @@ __device__ __forceinline__ void gty_rows(const void *__restrict__ G, int64_t ld,
   }
 }
 
-// y copied into shared memory 16 bytes at a time (4 floats or 2 doubles).
-template <typename Acc>
-struct CopyY {
-  const Acc *y;
-  __device__ __forceinline__ void operator()(int64_t r0, int n, Acc *ys) const {
-    constexpr int YV = 16 / (int)sizeof(Acc);
-    for (int t = threadIdx.x * YV; t < n; t += kThreads * YV) {
-      if constexpr (YV == 4) {
-        *reinterpret_cast<float4 *>(&ys[t]) = __ldcg(reinterpret_cast<const float4 *>(y + r0 + t));
-      } else {
-        *reinterpret_cast<double2 *>(&ys[t]) =
-            __ldcg(reinterpret_cast<const double2 *>(y + r0 + t));
-      }
-    }
-  }
-};
-
-// G^T y for block b with y staged in shared memory 32 KB at a time by
-// fill(r0, n, ys) (rows r0 .. r0 + n - 1; n a multiple of 64, as ld is).
-template <class L, class Fill>
-__device__ __forceinline__ double gty_body_f(const void *__restrict__ G, int64_t ld, int64_t nm,
-                                             const Fill &fill, int64_t b, int64_t *col) {
+template <class L>
+__device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t ld, int64_t nm,
+                                           const typename L::Acc *y, int64_t b, int64_t *col) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
   constexpr int kYChunk = kYChunkBytes / (int)sizeof(Acc);
@@ -359,14 +325,23 @@ __device__ __forceinline__ double gty_body_f(const void *__restrict__ G, int64_t
   Acc acc[kGtWarpCols];
 #pragma unroll
   for (int c = 0; c < kGtWarpCols; c++) acc[c] = Acc(0);
+  // 16 bytes of y per load: 4 floats or 2 doubles
+  constexpr int YV = 16 / (int)sizeof(Acc);
   auto y_at = [&](int64_t row, Acc (&yv)[VEC]) {
 #pragma unroll
     for (int v = 0; v < VEC; v++) yv[v] = ys[row + v];
   };
   for (int64_t r0 = 0; r0 < ld; r0 += kYChunk) {
-    const int n = (int)min((int64_t)kYChunk, ld - r0);
+    const int n = (int)min((int64_t)kYChunk, ld - r0);  // a multiple of 64 (ld is)
     __syncthreads();
-    fill(r0, n, ys);
+    for (int t = threadIdx.x * YV; t < n; t += kThreads * YV) {
+      if constexpr (YV == 4) {
+        *reinterpret_cast<float4 *>(&ys[t]) = __ldcg(reinterpret_cast<const float4 *>(y + r0 + t));
+      } else {
+        *reinterpret_cast<double2 *>(&ys[t]) =
+            __ldcg(reinterpret_cast<const double2 *>(y + r0 + t));
+      }
+    }
     __syncthreads();
     if (ncol == kGtWarpCols)
       gty_rows<L, true>(G, ld, c0, ncol, r0, lane * VEC, n, y_at, acc);
@@ -385,10 +360,40 @@ __device__ __forceinline__ double gty_body_f(const void *__restrict__ G, int64_t
   return mine;
 }
 
+// The same sums with y read straight from L2 by each warp (no shared-memory
+// staging): the persistent loop's variant, which runs with few CTAs per SM and
+// many problems at once, where the staging's block barriers cost more than the
+// repeated reads of y.
 template <class L>
-__device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t ld, int64_t nm,
-                                           const typename L::Acc *y, int64_t b, int64_t *col) {
-  return gty_body_f<L>(G, ld, nm, CopyY<typename L::Acc>{y}, b, col);
+__device__ __forceinline__ double gty_body_l2(const void *__restrict__ G, int64_t ld, int64_t nm,
+                                              const typename L::Acc *y, int64_t b, int64_t *col) {
+  using Acc = typename L::Acc;
+  constexpr int VEC = L::VEC;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t c0 = b * kGtBlockCols + (int64_t)warp * kGtWarpCols;
+  const int64_t left = nm - c0;
+  const int ncol = left <= 0 ? 0 : (left < kGtWarpCols ? (int)left : kGtWarpCols);
+  Acc acc[kGtWarpCols];
+#pragma unroll
+  for (int c = 0; c < kGtWarpCols; c++) acc[c] = Acc(0);
+  auto y_at = [&](int64_t row, Acc (&yv)[VEC]) {
+#pragma unroll
+    for (int v = 0; v < VEC; v++) yv[v] = __ldcg(y + row + v);
+  };
+  if (ncol == kGtWarpCols)
+    gty_rows<L, true>(G, ld, c0, ncol, 0, (int64_t)lane * VEC, ld, y_at, acc);
+  else if (ncol > 0)
+    gty_rows<L, false>(G, ld, c0, ncol, 0, (int64_t)lane * VEC, ld, y_at, acc);
+  double mine = 0.0;
+#pragma unroll
+  for (int c = 0; c < kGtWarpCols; c++) {
+    double v = (double)acc[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == c) mine = v;
+  }
+  *col = (lane < ncol) ? c0 + lane : -1;
+  return mine;
 }
 
 }  // namespace gemv

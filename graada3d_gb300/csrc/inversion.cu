@@ -75,7 +75,7 @@ void Context::release_all() {
                     &bk_gtw, &bk_gx, &bk_tmpd, &bk_scal, &bk_part, &bk_ctl, &bk_coef, &sw_m, &sw_mt,
                     &sw_mt_old, &sw_mopt, &sw_dx, &sw_P, &sw_mmin, &sw_mmax, &sw_m0, &sw_wl,
                     &sw_tmp, &sw_tmp2, &sw_dpre, &sw_d64, &sw_mstart, &sw_guard, &sw_flag, &sw_in,
-                    &sw_out, &cg_args, &cg_s2};
+                    &sw_out, &cg_args};
   for (DevBuf *b : bufs) b->release();
   if (phase_exec) cudaGraphExecDestroy(phase_exec);
   phase_exec = nullptr;
@@ -452,7 +452,7 @@ void Context::count_cg_loop(std::chrono::steady_clock::time_point t_build,
 
 Context::CgLoop Context::cg_loop_kind() const {
   // Stored dense G runs the persistent loop's phase bodies: by default as a
-  // graph of three kernels per iteration (cg_phases.cu), each at its own
+  // graph of four kernels per iteration (cg_phases.cu), each at its own
   // occupancy; GRADA_CG_FUSED=1 takes the one-launch persistent loop (the
   // batched inversion's engine, bitwise the same solve).  The matrix-free and
   // wavelet products, and GRADA_CG_FUSED=0, take the graph of the generic
@@ -487,8 +487,6 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   a.p = dptr(cg_p);
   cg_p2.alloc(this, sizeof(double) * (size_t)n_cells);
   a.p2 = dptr(cg_p2);
-  cg_s2.alloc(this, sizeof(double) * (size_t)nrow);
-  a.s2 = dptr(cg_s2);
   a.pp = dptr(cg_pp);
   a.dx = dx;
   a.t = dptr(cg_t);
@@ -560,7 +558,7 @@ CgResult Context::solve_cg_fused(double tol, int maxit, const double *P, double 
   return res;
 }
 
-// The persistent loop's phases as a graph of three kernels per iteration
+// The persistent loop's phases as a graph of four kernels per iteration
 // (cg_phases.cu), replayed until the device raises ctl[CTL_DONE]; a holds the
 // state solve_cg_fused set up.  K iterations per graph, K even (or maxit), so
 // the p / p2 parity of a captured iteration is that of the solve's count.  The

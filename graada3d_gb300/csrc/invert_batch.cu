@@ -465,8 +465,6 @@ void Context::batch_problem(const grada_invert_params &prm, BatchProblem &bp) {
   a.p = dbuf(cg_p);
   cg_p2.alloc(this, sizeof(double) * (size_t)Nm);
   a.p2 = dbuf(cg_p2);
-  cg_s2.alloc(this, sizeof(double) * (size_t)nrow);
-  a.s2 = dbuf(cg_s2);
   a.pp = dbuf(cg_pp);
   a.dx = dbuf(iv_dx);
   a.t = dbuf(cg_t);

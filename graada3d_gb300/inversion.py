@@ -108,10 +108,9 @@ class GaussNewtonInversion(Fwd):
         return dx, err.value, it.value
 
     def cg_phase_times(self):
-        """Mean ns per CG iteration of the persistent loop's three phases (G p
-        with the forward regulariser rows; finish; step with G^T s and the
-        adjoint; a fourth entry 0) over the persistent solves since the last
-        invert, and their iteration count."""
+        """Mean ns per CG iteration of the persistent loop's four phases (G p,
+        finish and regulariser rows, step, G^T s and adjoint) over the persistent
+        solves since the last invert, and their iteration count."""
         out = np.zeros(4)
         n = ctypes.c_int64()
         self.ctx.check(self.ctx.lib.grada_cg_phase_times(self.ctx.handle, _ptr(out), ctypes.byref(n)))

@@ -359,12 +359,11 @@ int grada_set_inversion_model(grada_ctx *ctx, const double *m, const double *m_m
                               const double *m_max, const double *m0);
 /*
  * Trace of the persistent CG loop (no reference counterpart): the mean time per
- * CG iteration, in ns, of its three phases -- G p with the direction update and
- * the forward regulariser rows; the finish of G p with ||t||^2; the step with
- * G^T s, the adjoint and ||r||^2 -- each up to the end of its team barrier, as
- * CTA 0 saw them, in mean_ns[0..2] (mean_ns[3] = 0), over the persistent
- * solves since the last grada_invert (or since the context was made);
- * *iterations gets their iteration count.
+ * CG iteration, in ns, of its four phases -- G p with the direction update,
+ * the finish of G p with the regulariser rows and ||t||^2, the step, and G^T s
+ * with the adjoint and ||r||^2 -- each up to the end of its team barrier, as
+ * CTA 0 saw them, over the persistent solves since the last grada_invert (or
+ * since the context was made); *iterations gets their iteration count.
  */
 int grada_cg_phase_times(grada_ctx *ctx, double *mean_ns, int64_t *iterations);
 /*
