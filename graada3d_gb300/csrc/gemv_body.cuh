@@ -285,7 +285,10 @@ __device__ __forceinline__ void gty_rows(const void *__restrict__ G, int64_t ld,
                                          typename L::Acc (&acc)[kGtWarpCols]) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
-#pragma unroll 2
+  // two row steps per trip, one for 16-bit G (measured at 3,392 x 16,384:
+  // bf16 27.7 us with one, 28.6 with two; FP32 the same either way)
+  constexpr int kUnroll = VEC == 8 ? 1 : 2;
+#pragma unroll kUnroll
   for (int64_t row = row_begin; row < row_end; row += 32 * VEC) {
     Acc yv[VEC];
     y_at(row, yv);
