@@ -158,26 +158,21 @@ __device__ __forceinline__ double finish_rows(const double *partial, int n_split
 
 // G^T y for the 32 columns of block b (warp w takes columns 4w .. 4w + 3,
 // lanes striding the rows), then r_j for those columns (the adjoint of the
-// regulariser rows and P).  StageY: y through shared memory (gemv::gty_body,
-// for a kernel of its own at full occupancy), else read from L2 by each warp
-// (gemv::gty_body_l2, the persistent loop's); both sum each column in the same
-// order.  The regulariser terms of the warp's 4 columns run on one lane per
+// regulariser rows and P), y staged in shared memory (gemv::gty_body; read
+// from L2 by every warp instead, the same sums took 70 against 47 us for FP32
+// and 103 against 29 us for bf16 at 3,392 x 16,384).  The regulariser terms of the warp's 4 columns run on one lane per
 // (column, term), their dependent CSR loads in parallel; the lane holding a
 // column adds them to its G^T sum in term order (cgb::adjoint_column's
 // arithmetic).  Writes gtw and r; returns the block's sum of r_j^2 (valid in
 // every thread).
-template <class L, bool StageY = false>
+template <class L>
 __device__ __forceinline__ double gty_adjoint_block(const FusedCgArgs &a, const typename L::Acc *y,
                                                     int64_t b) {
   static_assert(gemv::kGtWarpCols * 8 <= 32, "one lane per (column, term)");
   __shared__ double wsum[cgb::VT / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int64_t j = -1;
-  double g;
-  if constexpr (StageY)
-    g = gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j);
-  else
-    g = gemv::gty_body_l2<L>(a.G, a.ld, a.nm, y, b, &j);
+  const double g = gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j);
   // lane 8c + q: term q of the warp's column c
   const int tc = lane >> 3, tq = lane & 7;
   const int64_t tj = b * gemv::kGtBlockCols + (int64_t)warp * gemv::kGtWarpCols + tc;

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(256) phase_d_kernel(const FusedCgArgs *__restr
   const RedLayout rl(a.nd, a.nm, a.FT.count);
   double *part_r = a.red + rl.nb_t;
   const double v =
-      fused::gty_adjoint_block<L, true>(a, reinterpret_cast<const Acc *>(a.scratch), blockIdx.x);
+      fused::gty_adjoint_block<L>(a, reinterpret_cast<const Acc *>(a.scratch), blockIdx.x);
   if (threadIdx.x == 0) part_r[blockIdx.x] = v;
   if (!last_block(a.red_count, (unsigned)rl.nb_r)) return;
   const double r2 = fused::sum_partials_all(part_r, rl.nb_r);

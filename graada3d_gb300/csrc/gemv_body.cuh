@@ -363,41 +363,5 @@ __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t l
   return mine;
 }
 
-// The same sums with y read straight from L2 by each warp (no shared-memory
-// staging): the persistent loop's variant, which runs with few CTAs per SM and
-// many problems at once, where the staging's block barriers cost more than the
-// repeated reads of y.
-template <class L>
-__device__ __forceinline__ double gty_body_l2(const void *__restrict__ G, int64_t ld, int64_t nm,
-                                              const typename L::Acc *y, int64_t b, int64_t *col) {
-  using Acc = typename L::Acc;
-  constexpr int VEC = L::VEC;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t c0 = b * kGtBlockCols + (int64_t)warp * kGtWarpCols;
-  const int64_t left = nm - c0;
-  const int ncol = left <= 0 ? 0 : (left < kGtWarpCols ? (int)left : kGtWarpCols);
-  Acc acc[kGtWarpCols];
-#pragma unroll
-  for (int c = 0; c < kGtWarpCols; c++) acc[c] = Acc(0);
-  auto y_at = [&](int64_t row, Acc (&yv)[VEC]) {
-#pragma unroll
-    for (int v = 0; v < VEC; v++) yv[v] = __ldcg(y + row + v);
-  };
-  if (ncol == kGtWarpCols)
-    gty_rows<L, true>(G, ld, c0, ncol, 0, (int64_t)lane * VEC, ld, y_at, acc);
-  else if (ncol > 0)
-    gty_rows<L, false>(G, ld, c0, ncol, 0, (int64_t)lane * VEC, ld, y_at, acc);
-  double mine = 0.0;
-#pragma unroll
-  for (int c = 0; c < kGtWarpCols; c++) {
-    double v = (double)acc[c];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == c) mine = v;
-  }
-  *col = (lane < ncol) ? c0 + lane : -1;
-  return mine;
-}
-
 }  // namespace gemv
 }  // namespace grada
