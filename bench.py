@@ -1298,6 +1298,63 @@ def run_wavelet_inversion_1m(rel: float = 5e-6):
     return out
 
 
+def run_cg_tall(storages=("fp64", "fp32", "bf16")):
+    """The CG loop on a tall G at the refined configs[2] height: gz, Tzz, Txz,
+    Tyz at 101 x 101 points 100 m above [0, 10 km]^2 (40,804 rows) over
+    40 x 40 x 20 = 32,000 cells to 5 km depth (G 2.6 GB in bf16, 5.2 GB in
+    FP32, 10.4 GB in FP64: small enough for ncu, the same row count as the
+    refined inversion).  Three solves of 100 CG iterations each (tolerance 0,
+    so every solve runs to its cap) on an L2 problem; the loop's host time per
+    iteration (grada_cg_loop_time) against two reads of G at the copy rate."""
+    import torch
+
+    from graada3d_gb300 import mesh
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.inversion import GaussNewtonInversion
+
+    n = (40, 40, 20)
+    prisms = mesh.regular_mesh((0.0, 10000.0), n[0], (0.0, 10000.0), n[1], (0.0, 5000.0), n[2])
+    obs = mesh.observation_grid(101, 0.0, 10000.0, 101, 0.0, 10000.0, -100.0)
+    rng = np.random.default_rng(11)
+    rho = mesh.set_boxes(prisms, [[2500, 3500, 1000, 9000, 500, 3500, 400.0],
+                                  [6000, 7000, 1000, 9000, 500, 3500, 400.0]])
+    inv = GaussNewtonInversion(prisms, obs, 0x072)
+    ops = reg.regular_mesh_operators(n, prisms, obs, 1.5)
+    peak = _peak_gbs()
+    out = {"case": "cg-tall", "rows": inv.Nd, "cells": inv.Nm, "solves": 3, "iterations_per_solve": 100}
+    d = None
+    for st in storages:
+        inv.compute_G(st)
+        if d is None:
+            d = inv.G_vec_mul(rho)
+            dobs = d + 0.02 * np.abs(d) * rng.standard_normal(d.size)
+            wd = reg.data_weights(dobs, [0.02] * 4, [1e-3, 1e-2, 1e-2, 1e-2], obs.shape[0])
+            inv.set_cross_gradient(False)
+            inv.set_operators(ops)
+            inv.set_dobs(dobs, wd)
+        nm = inv.Nm
+        mk, mref, P = np.zeros(nm), np.zeros(nm), np.ones(nm)
+        inv.solve_cg(0.0, 20, 1e-3, mk, mref, P)  # warm-up (graph built)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        base = inv.cg_loop_time()
+        for _ in range(3):
+            inv.solve_cg(0.0, 100, 1e-3, mk, mref, P)
+        wall = time.perf_counter() - t0
+        loop_s, _, iters = (a - b for a, b in zip(inv.cg_loop_time(), base))
+        bpe = {"fp64": 8, "fp32": 4, "bf16": 2, "fp16": 2}[st]
+        gbytes = 2.0 * inv.ld * nm * bpe
+        r = {"iterations": int(iters), "loop_ms_per_iteration": 1e3 * loop_s / max(1, iters),
+             "solve_ms_per_iteration": 1e3 * wall / max(1, iters),
+             "G_bytes_per_iteration": gbytes}
+        r["loop_TBps"] = gbytes / (loop_s / max(1, iters)) / 1e12
+        if peak:
+            r["loop_frac_of_hbm"] = r["loop_TBps"] * 1e3 / peak
+        out[st] = r
+    inv.ctx.close()
+    return out
+
+
 def run_profile_case(args):
     """The fixed small case profiles are taken on: 1,024 points (32 x 32 at
     50 m height over 20 km x 20 km) x 4,096 cells (16 x 16 x 16 over the
@@ -1328,7 +1385,7 @@ def main():
                                                          "matrix-free-1m",
                                                          "gemv", "batched-64", "block-gemm",
                                                          "lambda-sweep-16", "block-gemm-profile",
-                                                         "mf-profile", "assembly-refined",
+                                                         "mf-profile", "assembly-refined", "cg-tall",
                                                          "operators-refined", "wavelet",
                                                          "wavelet-1m", "wavelet-inversion-1m"])
     ap.add_argument("--gpus", type=int, default=1)
@@ -1350,6 +1407,9 @@ def main():
         run_profile_case(args)
     elif args.case == "block-gemm":
         print(json.dumps(run_block_gemm_case()))
+    elif args.case == "cg-tall":
+        st = tuple(args.storages.split(",")) if args.storages else ("fp64", "fp32", "bf16")
+        print(json.dumps(run_cg_tall(st)))
     elif args.case == "assembly-refined":
         print(json.dumps(run_assembly_refined()))
     elif args.case == "operators-refined":
