@@ -75,7 +75,7 @@ int fused_cg_grid(GKind kind, int sm_count) {
 
 void fused_gx_partition(const DevG &G, int sm_count, int &tiles, int &splits, int64_t &per) {
   const int vec = vec_of(G.kind);
-  const int64_t rows = 32 * (int64_t)vec;  // gemv::fold_tile_rows
+  const int64_t rows = gemv::fold_tile_rows_for_vec(vec);
   const int64_t esize = G.kind == GKind::FP64 ? 8 : (G.kind == GKind::FP32 ? 4 : 2);
   const int64_t t = ceil_div(G.ld, rows);
   const int64_t slots = (int64_t)cg_phase_a_blocks_per_sm(G.kind) * sm_count;

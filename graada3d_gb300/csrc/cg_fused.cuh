@@ -165,14 +165,14 @@ __device__ __forceinline__ double finish_rows(const double *partial, int n_split
 // column adds them to its G^T sum in term order (cgb::adjoint_column's
 // arithmetic).  Writes gtw and r; returns the block's sum of r_j^2 (valid in
 // every thread).
-template <class L>
+template <class L, int U = gemv::kGtUnroll>
 __device__ __forceinline__ double gty_adjoint_block(const FusedCgArgs &a, const typename L::Acc *y,
                                                     int64_t b) {
   static_assert(gemv::kGtWarpCols * 8 <= 32, "one lane per (column, term)");
   __shared__ double wsum[cgb::VT / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int64_t j = -1;
-  const double g = gemv::gty_body<L>(a.G, a.ld, a.nm, y, b, &j);
+  const double g = gemv::gty_body<L, U>(a.G, a.ld, a.nm, y, b, &j);
   // lane 8c + q: term q of the warp's column c
   const int tc = lane >> 3, tq = lane & 7;
   const int64_t tj = b * gemv::kGtBlockCols + (int64_t)warp * gemv::kGtWarpCols + tc;
@@ -235,8 +235,8 @@ struct RedLayout {
 // r (set up), p = dx = 0 and beta = 0.  Every CTA returns the same CgOut.
 // Four team barriers per iteration:
 //   A  p_new = -r + beta p_old and pp = P p_new folded into the partial row
-//      sums of G pp (row tiles of 32 VEC rows x column ranges, the block's 8
-//      warps splitting a range)
+//      sums of G pp (row tiles of 64 VEC rows x column ranges, the block's
+//      four warp pairs splitting a range)
 //   B  t_data = Wd (sum of the partials, 16 rows per block, the splits shared
 //      by 16 half-warps), the forward regulariser rows of t, per-block ||t||^2
 //   C  alpha = r2 / t2; s += alpha t, dx += alpha p_new, y = Wd s_data in G's

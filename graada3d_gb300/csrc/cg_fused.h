@@ -48,7 +48,7 @@ struct FusedCgArgs {
 // CTAs of a persistent CG launch for this storage (all co-resident).
 int fused_cg_grid(GKind kind, int sm_count);
 // G pp's partition in the persistent loop and its phase kernels: row tiles of
-// 32 * vec rows x column ranges, the split count chosen for whole rounds of
+// 64 * vec rows x column ranges, the split count chosen for whole rounds of
 // the phase-A kernel's resident blocks and few partial rows.  It depends on
 // G's shape, the SM count and that kernel's occupancy only, so the sums of a
 // solve do not depend on the launch.

@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(256)
 // D: G^T y and r for 32 columns per block, the per-block ||r||^2; the last
 // block: r2, beta = r2 / rlast2, err = r2 / ||A^T b||^2, the iteration count
 // and the stopping tests (:1674-1691).
-template <class L>
+template <class L, int U>
 __global__ void __launch_bounds__(256) phase_d_kernel(const FusedCgArgs *__restrict__ ap) {
   const FusedCgArgs &a = *ap;
   if (done(a)) return;
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(256) phase_d_kernel(const FusedCgArgs *__restr
   const RedLayout rl(a.nd, a.nm, a.FT.count);
   double *part_r = a.red + rl.nb_t;
   const double v =
-      fused::gty_adjoint_block<L>(a, reinterpret_cast<const Acc *>(a.scratch), blockIdx.x);
+      fused::gty_adjoint_block<L, U>(a, reinterpret_cast<const Acc *>(a.scratch), blockIdx.x);
   if (threadIdx.x == 0) part_r[blockIdx.x] = v;
   if (!last_block(a.red_count, (unsigned)rl.nb_r)) return;
   const double r2 = fused::sum_partials_all(part_r, rl.nb_r);
@@ -160,7 +160,14 @@ void launch_iteration(const FusedCgArgs &a, const FusedCgArgs *ap, int parity, c
   GRADA_LAUNCH_CHECK();
   phase_c_kernel<L><<<(unsigned)g[2], 256, 0, s>>>(ap, parity);
   GRADA_LAUNCH_CHECK();
-  phase_d_kernel<L><<<(unsigned)g[3], 256, 0, s>>>(ap);
+  if constexpr (L::VEC >= 4) {  // FP64 G stays FP64-pipe bound
+    if (a.ld >= gemv::kGtTallRows) {
+      phase_d_kernel<L, gemv::kGtUnrollTall><<<(unsigned)g[3], 256, 0, s>>>(ap);
+      GRADA_LAUNCH_CHECK();
+      return;
+    }
+  }
+  phase_d_kernel<L, gemv::kGtUnroll><<<(unsigned)g[3], 256, 0, s>>>(ap);
   GRADA_LAUNCH_CHECK();
 }
 

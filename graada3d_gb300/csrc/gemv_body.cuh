@@ -126,11 +126,16 @@ __device__ __forceinline__ void gx_partial_body(const void *__restrict__ G, int6
   }
 }
 
-// Rows of a fold-body tile: one warp's lanes x VEC rows (512 bytes of a
-// column per warp load for every storage).
+// Warps of a fold-body block that share a row tile (the block's 8 warps form
+// 8 / kFoldWarps groups that split the unit's columns), and the rows of a
+// tile: 1 KB of a column per pair of warp loads for every storage.  Measured
+// on 40,832 x 32,000 bf16 G: 417 us with two warps per tile against 495 us
+// with one; at 3,392 x 16,384 the same or better.
+constexpr int kFoldWarps = 2;
+__host__ __device__ constexpr int fold_tile_rows_for_vec(int vec) { return kFoldWarps * 32 * vec; }
 template <class L>
 __host__ __device__ constexpr int fold_tile_rows() {
-  return 32 * L::VEC;
+  return fold_tile_rows_for_vec(L::VEC);
 }
 
 // G pp's partial row sums for the CG with the direction update folded in:
@@ -138,11 +143,12 @@ __host__ __device__ constexpr int fold_tile_rows() {
 // also store p_new_j = -r_j + beta p_old_j and pp_j (GaussNewtonInversion.cpp:
 // 1562-1566), so no separate pass over p is needed before G pp.  Unit (tile,
 // split): the tile's fold_tile_rows rows over the split's columns.  Within a
-// staged chunk of columns warp w takes the w-th of 8 consecutive column
-// sub-ranges (eight columns' loads in flight, two accumulator chains per row);
-// the 8 warp sums of each row are added in warp order through shared memory
-// and stored to partial[split * ld + row].  Short, wide G thus gets many row
-// tiles and few column splits (few partial rows for the finish to add).
+// staged chunk of columns warp group g (kFoldWarps warps on the tile's rows)
+// takes the g-th of 8 / kFoldWarps consecutive column sub-ranges (eight
+// columns' loads in flight, two accumulator chains per row); the group sums
+// of each row are added in group order through shared memory and stored to
+// partial[split * ld + row].  Short, wide G thus gets many row tiles and few
+// column splits (few partial rows for the finish to add).
 template <class L>
 __device__ __forceinline__ void gx_partial_fold_body(
     const void *__restrict__ G, int64_t ld, int64_t nm, int64_t cols_per_split, const double *r,
@@ -150,12 +156,13 @@ __device__ __forceinline__ void gx_partial_fold_body(
     double *partial, int64_t tile, int64_t split) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
-  constexpr int kWarps = kThreads / 32;
+  constexpr int kGroups = (kThreads / 32) / kFoldWarps;
   constexpr int kRows = fold_tile_rows<L>();
   __shared__ Acc xs[kXChunk];
-  __shared__ double wsum[kWarps][kRows];
+  __shared__ double wsum[kGroups][kRows];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t row = tile * kRows + lane * VEC;
+  const int grp = warp / kFoldWarps, wig = warp % kFoldWarps;
+  const int64_t row = tile * kRows + (wig * 32 + lane) * VEC;
   const int64_t c_begin = split * cols_per_split;
   const int64_t c_end = min(nm, c_begin + cols_per_split);
   Acc acc[VEC], acc2[VEC];
@@ -175,7 +182,7 @@ __device__ __forceinline__ void gx_partial_fold_body(
       xs[t] = (Acc)q;
     }
     __syncthreads();
-    const int lo = (nc * warp) / kWarps, hi = (nc * (warp + 1)) / kWarps;
+    const int lo = (nc * grp) / kGroups, hi = (nc * (grp + 1)) / kGroups;
     if (row < ld) {
       const int64_t base = row + c0 * ld;
       int c = lo;
@@ -203,14 +210,15 @@ __device__ __forceinline__ void gx_partial_fold_body(
   }
   __syncthreads();  // wsum may still be read for the caller's previous unit
 #pragma unroll
-  for (int v = 0; v < VEC; v++) wsum[warp][lane * VEC + v] = (double)acc[v] + (double)acc2[v];
+  for (int v = 0; v < VEC; v++)
+    wsum[grp][(wig * 32 + lane) * VEC + v] = (double)acc[v] + (double)acc2[v];
   __syncthreads();
-  if (threadIdx.x < kRows) {
-    const int64_t rr = tile * kRows + threadIdx.x;
+  for (int t = threadIdx.x; t < kRows; t += kThreads) {
+    const int64_t rr = tile * kRows + t;
     if (rr < ld) {
       double sum = 0.0;
 #pragma unroll
-      for (int w = 0; w < kWarps; w++) sum += wsum[w][threadIdx.x];
+      for (int w = 0; w < kGroups; w++) sum += wsum[w][t];
       partial[split * ld + rr] = sum;
     }
   }
@@ -278,17 +286,14 @@ constexpr int kYChunkBytes = 32768;  // y staged 32 KB at a time: one chunk for 
 // y_at.  Full (ncol = kGtWarpCols, every warp but the last): no per-column
 // tests, so every column's loads of a row step issue before its FMAs.  Each
 // column adds its rows in the same order either way.
-template <class L, bool Full, class YAt>
+template <class L, int U, bool Full, class YAt>
 __device__ __forceinline__ void gty_rows(const void *__restrict__ G, int64_t ld, int64_t c0,
                                          int ncol, int64_t g_row0, int64_t row_begin,
                                          int64_t row_end, YAt y_at,
                                          typename L::Acc (&acc)[kGtWarpCols]) {
   using Acc = typename L::Acc;
   constexpr int VEC = L::VEC;
-  // two row steps per trip, one for 16-bit G (measured at 3,392 x 16,384:
-  // bf16 27.7 us with one, 28.6 with two; FP32 the same either way)
-  constexpr int kUnroll = VEC == 8 ? 1 : 2;
-#pragma unroll kUnroll
+#pragma unroll U
   for (int64_t row = row_begin; row < row_end; row += 32 * VEC) {
     Acc yv[VEC];
     y_at(row, yv);
@@ -314,7 +319,14 @@ __device__ __forceinline__ void gty_rows(const void *__restrict__ G, int64_t ld,
   }
 }
 
-template <class L>
+// Row steps per trip of G^T y (gty_body's U; the sums do not depend on it):
+// two in general, four on tall G (measured on 40,832 x 32,000: FP32 786
+// against 875 us, bf16 410 against 447 us), where short G loses with them
+// (bf16 at 3,392 x 16,384: 33.9 against 28 us).
+constexpr int kGtUnroll = 2, kGtUnrollTall = 4;
+constexpr int64_t kGtTallRows = 16384;
+
+template <class L, int U = kGtUnroll>
 __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t ld, int64_t nm,
                                            const typename L::Acc *y, int64_t b, int64_t *col) {
   using Acc = typename L::Acc;
@@ -347,9 +359,9 @@ __device__ __forceinline__ double gty_body(const void *__restrict__ G, int64_t l
     }
     __syncthreads();
     if (ncol == kGtWarpCols)
-      gty_rows<L, true>(G, ld, c0, ncol, r0, lane * VEC, n, y_at, acc);
+      gty_rows<L, U, true>(G, ld, c0, ncol, r0, lane * VEC, n, y_at, acc);
     else if (ncol > 0)
-      gty_rows<L, false>(G, ld, c0, ncol, r0, lane * VEC, n, y_at, acc);
+      gty_rows<L, U, false>(G, ld, c0, ncol, r0, lane * VEC, n, y_at, acc);
   }
   double mine = 0.0;
 #pragma unroll
