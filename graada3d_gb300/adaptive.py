@@ -85,13 +85,20 @@ def refine_mesh(inv, octree, m, fraction: float, min_size, beta: float,
 
 def invert_adaptive(inv, octree, prm: dict, m_ini, m_min, m_max, m0=None, *,
                     max_refinements: int, interval: int, fraction: float, min_size, beta: float,
-                    alphas=(1.0, 1.0, 1.0, 1.0), fp64_refinement: bool = False):
+                    alphas=(1.0, 1.0, 1.0, 1.0), fp64_refinement: bool = False,
+                    m0s=None, m0s_interpolator=None):
     """The adaptive inversion (invert_with_own_CG with its refinement branch,
     GaussNewtonInversion.cpp:1098-1294) through grada_invert_adaptive: the
     Gauss-Newton loop, lambda search and CG run in the library; at each
     refinement the library calls back here, and refine_mesh splits the marked
     cells of `octree` (on the host), expands G and rebuilds Ws/Wx/Wy/Wz (on the
     device), and the model, bounds and reference model follow the children.
+    With the cross-gradient constraint (m0s: the structure model on the
+    current cells, T_x, T_y, T_z set from it and the constraint enabled),
+    children take m0s_interpolator's value at their centre (refine_mesh(a,
+    interpolator, "crg"), AdaptiveInversion.cpp:206-386; children take their
+    parent's value without an interpolator) and T_x, T_y, T_z are rebuilt from
+    the new structure model (set_Tmatrix, GaussNewtonInversion.cpp:1266-1268).
     `inv` must hold G for octree.leaves() with its data and operators set.
     Returns (model on the final cells, report)."""
     import ctypes
@@ -103,16 +110,24 @@ def invert_adaptive(inv, octree, prm: dict, m_ini, m_min, m_max, m0=None, *,
     nm = inv.Nm
     state = {"mmin": np.asarray(m_min, dtype=np.float64).copy(),
              "mmax": np.asarray(m_max, dtype=np.float64).copy(),
-             "m0": np.zeros(nm) if m0 is None else np.asarray(m0, dtype=np.float64).copy()}
+             "m0": np.zeros(nm) if m0 is None else np.asarray(m0, dtype=np.float64).copy(),
+             "m0s": None if m0s is None else np.asarray(m0s, dtype=np.float64).copy()}
     errors = []
 
     def on_refine(user, ctx_handle, m_ptr, n):
         try:
             m = np.ctypeslib.as_array(m_ptr, shape=(n,)).copy()
-            new_m, mmin, mmax, m0v = refine_mesh(inv, octree, m, fraction, min_size, beta, alphas,
-                                                 extra=(state["mmin"], state["mmax"], state["m0"]))
+            extra = [state["mmin"], state["mmax"], state["m0"]]
+            if state["m0s"] is not None:
+                extra.append((state["m0s"], m0s_interpolator))
+            new_m, mmin, mmax, m0v, *rest = refine_mesh(inv, octree, m, fraction, min_size, beta,
+                                                        alphas, extra=tuple(extra))
             state.update(mmin=np.ascontiguousarray(mmin), mmax=np.ascontiguousarray(mmax),
                          m0=np.ascontiguousarray(m0v))
+            if state["m0s"] is not None and rest[0].shape[0] != state["m0s"].shape[0]:
+                state["m0s"] = np.ascontiguousarray(rest[0])
+                ops = reg.mesh_operators(inv.prisms, inv.obs, beta, *alphas)
+                inv.set_operators(reg.cross_gradient_operators(None, inv.prisms, state["m0s"], ops))
             new_m = np.ascontiguousarray(new_m)
             return lib.grada_set_inversion_model(inv.ctx.handle, _ptr(new_m), _ptr(state["mmin"]),
                                                  _ptr(state["mmax"]), _ptr(state["m0"]))

@@ -861,6 +861,20 @@ void Context::invert(const grada_invert_params &prm, const double *h_m_ini, cons
         if (!ops[t].set || ops[t].n != n_cells)
           throw Error(GRADA_ERR_STATE,
                       "the refine callback must rebuild Ws/Wx/Wy/Wz for the refined mesh");
+      if (crg_enabled) {
+        // the constrained refine_mesh(a, interpolator, "crg") re-interpolates the
+        // structure model and set_Tmatrix rebuilds T_x, T_y, T_z from it
+        // (AdaptiveInversion.cpp:206-386, GaussNewtonInversion.cpp:1266-1279)
+        for (int t = GRADA_OP_TX; t <= GRADA_OP_TZ; t++)
+          if (!ops[t].set || ops[t].n != n_cells)
+            throw Error(GRADA_ERR_STATE,
+                        "the refine callback must rebuild Tx/Ty/Tz for the refined mesh");
+        // init_matrices resets S_crg to the identity (InversionBase.cpp:113-130)
+        if (!s_crg.empty() && s_crg.size() != (size_t)n_cells) {
+          s_crg.clear();
+          for (auto &c : crg) c.set = false;
+        }
+      }
       Nm = n_cells;
       vb = sizeof(double) * Nm;
       DevBuf *vecs[] = {&iv_m, &iv_mt, &iv_mt_old, &iv_mopt, &iv_dx, &iv_P, &iv_mmin, &iv_mmax,

@@ -64,3 +64,75 @@ def test_adaptive_inversion_matches_reference(gpu_ctx, golden):
     assert abs(rep["final_misfit"] - float(f["ref_misfit"])) <= 1e-2 * float(f["ref_misfit"])
     assert np.linalg.norm(m - f["ref_m"]) <= 0.05 * np.linalg.norm(f["ref_m"])
     assert n_before[0] == nx * ny * nz
+
+
+def test_adaptive_crg_inversion_matches_reference(gpu_ctx, golden):
+    """The adaptive inversion with the cross-gradient constraint (refine_mesh(a,
+    interpolator, "crg"), AdaptiveInversion.cpp:206-386; set_Tmatrix after each
+    refinement, GaussNewtonInversion.cpp:1266-1268) against the reference's own
+    run (ref_adaptive_crg_inversion: the structure model of the l1_crg case on
+    8 x 8 x 4 cells, gridded at the cell centres as the reference reads it, two
+    refinements of 10 %).  The children take the structure model's
+    multilinear value at their centre, T_x, T_y, T_z are rebuilt from it, and
+    the run matches as the plain adaptive inversion does: the same cells split,
+    final leaves bitwise, the misfits of the first Gauss-Newton iterations to
+    1e-6, later ones to 1e-2."""
+    from graada3d_gb300 import adaptive, mesh
+    from graada3d_gb300 import regularization as reg
+    from graada3d_gb300.inversion import GaussNewtonInversion
+
+    f = golden("ref_adaptive_crg_inversion.npz")
+    nx, ny, nz = (int(v) for v in f["n"])
+    o = mesh.Octree.regular(tuple(f["xl"]), nx, tuple(f["yl"]), ny, tuple(f["zl"]), nz)
+    leaves = o.leaves()
+    assert np.array_equal(leaves, mesh.regular_mesh(tuple(f["xl"]), nx, tuple(f["yl"]), ny,
+                                                     tuple(f["zl"]), nz))
+    m0s = f["m0s"]
+    # the structure model gridded at the cell centres, x outermost
+    centres = mesh.cell_centres(leaves)
+    axes = [np.unique(centres[:, d]) for d in range(3)]
+    values = np.empty([a.size for a in axes])
+    idx = [np.searchsorted(axes[d], centres[:, d]) for d in range(3)]
+    values[idx[0], idx[1], idx[2]] = m0s
+    interp = mesh.Multilinear(*axes, values)
+    np.testing.assert_array_equal(interp(centres), m0s)
+
+    mask = int(f["mask"])
+    inv = GaussNewtonInversion(leaves, f["obs"], mask, ctx=gpu_ctx)
+    inv.compute_G("fp64")
+    beta = float(f["beta"])
+    alphas = tuple(float(v) for v in f["alphas"][:4])
+    inv.build_operators(reg.face_table(inv.prisms), beta, 0, alphas)
+    ops = reg.mesh_operators(inv.prisms, inv.obs, beta, *alphas)
+    inv.set_operators(reg.cross_gradient_operators(None, inv.prisms, m0s, ops))
+    inv.set_cross_gradient(True, float(f["alphas"][4]))
+    wd = reg.data_weights(f["dobs"], f["rel"], f["abs"], f["obs"].shape[0])
+    inv.set_dobs(f["dobs"], wd)
+    prm = {"max_lambda": float(f["max_lambda"]), "n_lambda": int(f["n_lambda"]),
+           "rate": float(f["rate"]), "target": float(f["target"]), "stag": float(f["stag"]),
+           "cg_tol": float(f["cg_tol"]), "cg_factor": float(f["cg_factor"]),
+           "gn_iter": int(f["gn_iter"]), "lp": [int(v) for v in f["lp"]], "eps2": float(f["eps2"])}
+    nm = inv.Nm
+    mmin, mmax, mini = f["bounds"]
+    m, rep = adaptive.invert_adaptive(
+        inv, o, prm, np.full(nm, mini), np.full(nm, mmin), np.full(nm, mmax),
+        max_refinements=int(f["max_refinements"]), interval=int(f["interval"]),
+        fraction=float(f["fraction"]), min_size=f["min_size"], beta=beta, alphas=alphas,
+        m0s=m0s, m0s_interpolator=interp)
+    assert rep["mesh_refinements"] == len(f["ref_splits"])
+    ref_leaves = f["ref_leaves"]
+    assert inv.prisms.shape == ref_leaves.shape
+    assert np.array_equal(inv.prisms.view(np.uint64), ref_leaves.view(np.uint64))
+    its = inv.iterations()
+    ref_its = f["ref_iterations"]
+    assert its.shape[0] == ref_its.shape[0]
+    np.testing.assert_allclose(its[:2, 2], ref_its[:2, 2], rtol=1e-6, atol=0)
+    np.testing.assert_allclose(its[:, 2], ref_its[:, 2], rtol=1e-2, atol=0)
+    trials = inv.trials()
+    n1 = int(its[0, 1])
+    np.testing.assert_allclose(trials[:n1, 1], f["ref_trials"][:n1, 0], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(trials[:n1, 2], f["ref_trials"][:n1, 1], rtol=1e-6, atol=0)
+    target = float(f["target"])
+    assert rep["final_misfit"] < target and float(f["ref_misfit"]) < target
+    assert abs(rep["final_misfit"] - float(f["ref_misfit"])) <= 1e-2 * float(f["ref_misfit"])
+    assert np.linalg.norm(m - f["ref_m"]) <= 0.05 * np.linalg.norm(f["ref_m"])
