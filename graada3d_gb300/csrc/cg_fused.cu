@@ -96,6 +96,10 @@ void fused_gx_partition(const DevG &G, int sm_count, int &tiles, int &splits, in
       best_s = sp;
     }
   }
+  if (const char *e = std::getenv("GRADA_GX_SPLITS")) {  // a fixed split count, for tuning
+    const long v = std::atol(e);
+    if (v >= 1) best_s = std::min<int64_t>(v, max_s);
+  }
   tiles = (int)t;
   splits = (int)best_s;
   per = ceil_div(G.nm, best_s);
