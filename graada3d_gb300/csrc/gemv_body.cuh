@@ -132,6 +132,12 @@ __device__ __forceinline__ void gx_partial_body(const void *__restrict__ G, int6
 // on 40,832 x 32,000 bf16 G: 417 us with two warps per tile against 495 us
 // with one; at 3,392 x 16,384 the same or better.
 constexpr int kFoldWarps = 2;
+// Two accumulator chains per row (even and odd columns of a batch) where a
+// thread has few rows (FP64, FP32): the FP64 pipe needs the independent FMAs.
+// 16-bit G has eight rows per thread, and there a second chain measured slower
+// (40,832 x 32,000 bf16: 542 against 417 us).
+template <int VEC>
+constexpr bool kFoldTwoChains = VEC < 8;
 __host__ __device__ constexpr int fold_tile_rows_for_vec(int vec) { return kFoldWarps * 32 * vec; }
 template <class L>
 __host__ __device__ constexpr int fold_tile_rows() {
@@ -145,7 +151,7 @@ __host__ __device__ constexpr int fold_tile_rows() {
 // split): the tile's fold_tile_rows rows over the split's columns.  Within a
 // staged chunk of columns warp group g (kFoldWarps warps on the tile's rows)
 // takes the g-th of 8 / kFoldWarps consecutive column sub-ranges (eight
-// columns' loads in flight, two accumulator chains per row); the group sums
+// columns' loads in flight, kFoldTwoChains accumulator chains); the group sums
 // of each row are added in group order through shared memory and stored to
 // partial[split * ld + row].  Short, wide G thus gets many row tiles and few
 // column splits (few partial rows for the finish to add).
@@ -190,13 +196,22 @@ __device__ __forceinline__ void gx_partial_fold_body(
         Acc g[8][VEC];
 #pragma unroll
         for (int q = 0; q < 8; q++) L::load(G, base + (int64_t)(c + q) * ld, g[q]);
+        if constexpr (kFoldTwoChains<VEC>) {
 #pragma unroll
-        for (int q = 0; q < 8; q += 2) {
-          const Acc xq = xs[c + q], xr = xs[c + q + 1];
+          for (int q = 0; q < 8; q += 2) {
+            const Acc xq = xs[c + q], xr = xs[c + q + 1];
 #pragma unroll
-          for (int v = 0; v < VEC; v++) {
-            acc[v] = fma(g[q][v], xq, acc[v]);
-            acc2[v] = fma(g[q + 1][v], xr, acc2[v]);
+            for (int v = 0; v < VEC; v++) {
+              acc[v] = fma(g[q][v], xq, acc[v]);
+              acc2[v] = fma(g[q + 1][v], xr, acc2[v]);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            const Acc xq = xs[c + q];
+#pragma unroll
+            for (int v = 0; v < VEC; v++) acc[v] = fma(g[q][v], xq, acc[v]);
           }
         }
       }
