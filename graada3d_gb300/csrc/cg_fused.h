@@ -51,7 +51,8 @@ int fused_cg_grid(GKind kind, int sm_count);
 // 64 * vec rows x column ranges, the split count chosen for whole rounds of
 // the phase-A kernel's resident blocks and few partial rows.  It depends on
 // G's shape, the SM count and that kernel's occupancy only, so the sums of a
-// solve do not depend on the launch.
+// solve do not depend on the launch.  GRADA_GX_SPLITS fixes the split count
+// (for tuning).
 void fused_gx_partition(const DevG &G, int sm_count, int &tiles, int &splits, int64_t &per);
 // Doubles and counters of a.red / a.red_count for a loop over Nm cells, Nd
 // rows and nterms regulariser terms.
