@@ -1299,8 +1299,8 @@ def run_wavelet_inversion_1m(rel: float = 5e-6):
 
 
 def run_cg_tall(storages=("fp64", "fp32", "bf16")):
-    """The CG loop on a tall G at the refined configs[2] height: gz, Tzz, Txz,
-    Tyz at 101 x 101 points 100 m above [0, 10 km]^2 (40,804 rows) over
+    """The CG loop on a tall G with the rows of the refined dyke inversion: gz,
+    Tzz, Txz, Tyz at 101 x 101 points 100 m above [0, 10 km]^2 (40,804 rows) over
     40 x 40 x 20 = 32,000 cells to 5 km depth (G 2.6 GB in bf16, 5.2 GB in
     FP32, 10.4 GB in FP64: small enough for ncu, the same row count as the
     refined inversion).  Three solves of 100 CG iterations each (tolerance 0,
