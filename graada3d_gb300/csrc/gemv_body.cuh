@@ -132,13 +132,13 @@ __device__ __forceinline__ void gx_partial_body(const void *__restrict__ G, int6
 // on 40,832 x 32,000 bf16 G: 417 us with two warps per tile against 495 us
 // with one; at 3,392 x 16,384 the same or better.
 constexpr int kFoldWarps = 2;
-// Two accumulator chains per row (even and odd columns of a batch) for FP64 G
-// only, whose pipe needs the independent FMAs.  With FP32 and 16-bit G (four
-// and eight rows per thread) a second chain measured slower: 40,832 x 32,000,
-// bf16 542 against 417 us, FP32 797 against 775 us; 3,392 x 16,384 FP32 45-53
-// against 44-47 us.
+// Two accumulator chains per row (even and odd columns of a batch) for FP64 and
+// FP32 G: the FP64 pipe needs the independent FMAs, and FP32's CG loop measured
+// a little faster with them (40,832 x 236,226: 10.5-10.8 against 10.9 ms per
+// iteration).  16-bit G has eight rows per thread, and there a second chain
+// measured slower (40,832 x 32,000 bf16 G x: 542 against 417 us).
 template <int VEC>
-constexpr bool kFoldTwoChains = VEC < 4;
+constexpr bool kFoldTwoChains = VEC < 8;
 __host__ __device__ constexpr int fold_tile_rows_for_vec(int vec) { return kFoldWarps * 32 * vec; }
 template <class L>
 __host__ __device__ constexpr int fold_tile_rows() {
