@@ -86,7 +86,7 @@ def refine_mesh(inv, octree, m, fraction: float, min_size, beta: float,
 def invert_adaptive(inv, octree, prm: dict, m_ini, m_min, m_max, m0=None, *,
                     max_refinements: int, interval: int, fraction: float, min_size, beta: float,
                     alphas=(1.0, 1.0, 1.0, 1.0), fp64_refinement: bool = False,
-                    m0s=None, m0s_interpolator=None):
+                    m0s=None, m0s_interpolator=None, m0_interpolator=None):
     """The adaptive inversion (invert_with_own_CG with its refinement branch,
     GaussNewtonInversion.cpp:1098-1294) through grada_invert_adaptive: the
     Gauss-Newton loop, lambda search and CG run in the library; at each
@@ -99,6 +99,9 @@ def invert_adaptive(inv, octree, prm: dict, m_ini, m_min, m_max, m0=None, *,
     interpolator, "crg"), AdaptiveInversion.cpp:206-386; children take their
     parent's value without an interpolator) and T_x, T_y, T_z are rebuilt from
     the new structure model (set_Tmatrix, GaussNewtonInversion.cpp:1266-1268).
+    With m0_interpolator the reference model's children likewise take its value
+    at their centre (refine_mesh(a, interpolator, "pet") and, with both models,
+    refine_mesh(a, interp_m0s, interp_m0), AdaptiveInversion.cpp:206-386, 388-534).
     `inv` must hold G for octree.leaves() with its data and operators set.
     Returns (model on the final cells, report)."""
     import ctypes
@@ -117,7 +120,8 @@ def invert_adaptive(inv, octree, prm: dict, m_ini, m_min, m_max, m0=None, *,
     def on_refine(user, ctx_handle, m_ptr, n):
         try:
             m = np.ctypeslib.as_array(m_ptr, shape=(n,)).copy()
-            extra = [state["mmin"], state["mmax"], state["m0"]]
+            extra = [state["mmin"], state["mmax"],
+                     state["m0"] if m0_interpolator is None else (state["m0"], m0_interpolator)]
             if state["m0s"] is not None:
                 extra.append((state["m0s"], m0s_interpolator))
             new_m, mmin, mmax, m0v, *rest = refine_mesh(inv, octree, m, fraction, min_size, beta,

@@ -240,19 +240,24 @@ def make_adaptive_case(seed: int = 21):
     return c, adaptive
 
 
-def make_adaptive_crg_case(seed: int = 23):
-    """The adaptive case with the cross-gradient constraint: the structure model
-    of the l1_crg case on the 8 x 8 x 4 cells (no reference model, so the
-    reference refines with refine_mesh(a, interpolator, "crg")), a_crg 1, L2
-    on every term."""
+def make_adaptive_crg_case(seed: int = 23, crg: bool = True, ref: bool = False):
+    """The adaptive case with gridded constraint models on the 8 x 8 x 4 cells:
+    the structure model of the l1_crg case (crg: the cross-gradient constraint,
+    a_crg 1) and / or its reference model (ref), each read by the reference from
+    a grid at the cell centres.  The reference then refines with refine_mesh(a,
+    interpolator, "crg"), (a, interpolator, "pet") or (a, interp_m0s, interp_m0).
+    L2 on every term."""
     from graada3d_gb300 import mesh as gm
 
     c, adaptive = make_adaptive_case(seed)
     prisms = gm.regular_mesh(c["xl"], c["n"][0], c["yl"], c["n"][1], c["zl"], c["n"][2])
     xc = 0.5 * (prisms[:, 0] + prisms[:, 1])
     zc = 0.5 * (prisms[:, 4] + prisms[:, 5])
-    c["m0s"] = np.sin(xc / 300.0) + 0.5 * np.cos(zc / 200.0)
-    c["alphas"] = (1.0, 1.0, 1.0, 1.0, 1.0)
+    if crg:
+        c["m0s"] = np.sin(xc / 300.0) + 0.5 * np.cos(zc / 200.0)
+        c["alphas"] = (1.0, 1.0, 1.0, 1.0, 1.0)
+    if ref:
+        c["m0"] = 50.0 * np.sin(xc / 400.0) * np.cos(zc / 250.0)
     return c, adaptive
 
 
@@ -294,8 +299,13 @@ def run_adaptive(c: dict, adaptive: dict, exe: Path = EXE):
                 "iterations": _parse_table(wd / "Iteration_misfit_GN")}
 
 
-def adaptive_fixture(crg: bool = False) -> None:
-    c, ad = make_adaptive_crg_case() if crg else make_adaptive_case()
+def adaptive_fixture(variant: str = "") -> None:
+    """variant "": the plain adaptive inversion; "crg", "pet", "crg_pet": with the
+    structure model, the reference model, or both."""
+    if variant:
+        c, ad = make_adaptive_crg_case(crg="crg" in variant, ref="pet" in variant)
+    else:
+        c, ad = make_adaptive_case()
     res = run_adaptive(c, ad)
     out = {"n": np.array(c["n"]), "xl": np.array(c["xl"]), "yl": np.array(c["yl"]),
            "zl": np.array(c["zl"]), "obs": c["obs"], "mask": np.array(c["mask"]),
@@ -308,11 +318,12 @@ def adaptive_fixture(crg: bool = False) -> None:
            "bounds": np.array([c["m_min"], c["m_max"], c["m_ini"]]),
            "max_refinements": np.array(ad["max_refinements"]), "interval": np.array(ad["interval"]),
            "fraction": np.array(ad["fraction"]), "min_size": np.array(ad["min_size"])}
-    if crg:
-        out["m0s"] = c["m0s"]
+    for k in ("m0s", "m0"):
+        if c.get(k) is not None:
+            out[k] = c[k]
     for k, v in res.items():
         out["ref_" + k] = np.asarray(v)
-    name = "ref_adaptive_crg_inversion" if crg else "ref_adaptive_inversion"
+    name = f"ref_adaptive_{variant}_inversion" if variant else "ref_adaptive_inversion"
     np.savez_compressed(HERE / f"{name}.npz", **out)
     print(f"{name}: leaves {res['leaves'].shape[0]} splits {res['splits']} "
           f"misfit {res['misfit']:.4f} trials {len(res['trials'])}")

@@ -66,36 +66,47 @@ def test_adaptive_inversion_matches_reference(gpu_ctx, golden):
     assert n_before[0] == nx * ny * nz
 
 
-def test_adaptive_crg_inversion_matches_reference(gpu_ctx, golden):
-    """The adaptive inversion with the cross-gradient constraint (refine_mesh(a,
-    interpolator, "crg"), AdaptiveInversion.cpp:206-386; set_Tmatrix after each
-    refinement, GaussNewtonInversion.cpp:1266-1268) against the reference's own
-    run (ref_adaptive_crg_inversion: the structure model of the l1_crg case on
-    8 x 8 x 4 cells, gridded at the cell centres as the reference reads it, two
-    refinements of 10 %).  The children take the structure model's
-    multilinear value at their centre, T_x, T_y, T_z are rebuilt from it, and
-    the run matches as the plain adaptive inversion does: the same cells split,
-    final leaves bitwise, the misfits of the first Gauss-Newton iterations to
-    1e-6, later ones to 1e-2."""
+def _gridded(leaves, values):
+    """The multilinear interpolator of per-cell values gridded at the centres of
+    a regular mesh's cells (x outermost), as the reference reads a model file."""
+    from graada3d_gb300 import mesh
+
+    centres = mesh.cell_centres(leaves)
+    axes = [np.unique(centres[:, d]) for d in range(3)]
+    grid = np.empty([a.size for a in axes])
+    idx = [np.searchsorted(axes[d], centres[:, d]) for d in range(3)]
+    grid[idx[0], idx[1], idx[2]] = values
+    interp = mesh.Multilinear(*axes, grid)
+    np.testing.assert_array_equal(interp(centres), values)
+    return interp
+
+
+@pytest.mark.parametrize("variant", ["crg", "pet", "crg_pet"])
+def test_adaptive_constrained_inversion_matches_reference(gpu_ctx, golden, variant):
+    """The adaptive inversion with gridded constraint models against the
+    reference's own runs (ref_adaptive_{variant}_inversion: on 8 x 8 x 4 cells
+    the l1_crg case's structure model with the cross-gradient constraint
+    ("crg": refine_mesh(a, interpolator, "crg"), T_x, T_y, T_z rebuilt after
+    each refinement by set_Tmatrix, GaussNewtonInversion.cpp:1266-1268), its
+    reference model ("pet": refine_mesh(a, interpolator, "pet")), or both
+    (refine_mesh(a, interp_m0s, interp_m0)); AdaptiveInversion.cpp:206-534; each
+    model gridded at the cell centres as the reference reads it; two
+    refinements of 10 %).  The children take each model's multilinear value at
+    their centre, and the run matches as the plain adaptive inversion does: the
+    same cells split, final leaves bitwise, the misfits of the first Gauss-Newton
+    iterations to 1e-6, later ones to 1e-2."""
     from graada3d_gb300 import adaptive, mesh
     from graada3d_gb300 import regularization as reg
     from graada3d_gb300.inversion import GaussNewtonInversion
 
-    f = golden("ref_adaptive_crg_inversion.npz")
+    f = golden(f"ref_adaptive_{variant}_inversion.npz")
     nx, ny, nz = (int(v) for v in f["n"])
     o = mesh.Octree.regular(tuple(f["xl"]), nx, tuple(f["yl"]), ny, tuple(f["zl"]), nz)
     leaves = o.leaves()
     assert np.array_equal(leaves, mesh.regular_mesh(tuple(f["xl"]), nx, tuple(f["yl"]), ny,
                                                      tuple(f["zl"]), nz))
-    m0s = f["m0s"]
-    # the structure model gridded at the cell centres, x outermost
-    centres = mesh.cell_centres(leaves)
-    axes = [np.unique(centres[:, d]) for d in range(3)]
-    values = np.empty([a.size for a in axes])
-    idx = [np.searchsorted(axes[d], centres[:, d]) for d in range(3)]
-    values[idx[0], idx[1], idx[2]] = m0s
-    interp = mesh.Multilinear(*axes, values)
-    np.testing.assert_array_equal(interp(centres), m0s)
+    m0s = f["m0s"] if "m0s" in f.files else None
+    m0 = f["m0"] if "m0" in f.files else None
 
     mask = int(f["mask"])
     inv = GaussNewtonInversion(leaves, f["obs"], mask, ctx=gpu_ctx)
@@ -103,9 +114,12 @@ def test_adaptive_crg_inversion_matches_reference(gpu_ctx, golden):
     beta = float(f["beta"])
     alphas = tuple(float(v) for v in f["alphas"][:4])
     inv.build_operators(reg.face_table(inv.prisms), beta, 0, alphas)
-    ops = reg.mesh_operators(inv.prisms, inv.obs, beta, *alphas)
-    inv.set_operators(reg.cross_gradient_operators(None, inv.prisms, m0s, ops))
-    inv.set_cross_gradient(True, float(f["alphas"][4]))
+    if m0s is not None:
+        ops = reg.mesh_operators(inv.prisms, inv.obs, beta, *alphas)
+        inv.set_operators(reg.cross_gradient_operators(None, inv.prisms, m0s, ops))
+        inv.set_cross_gradient(True, float(f["alphas"][4]))
+    else:
+        inv.set_cross_gradient(False)
     wd = reg.data_weights(f["dobs"], f["rel"], f["abs"], f["obs"].shape[0])
     inv.set_dobs(f["dobs"], wd)
     prm = {"max_lambda": float(f["max_lambda"]), "n_lambda": int(f["n_lambda"]),
@@ -115,10 +129,11 @@ def test_adaptive_crg_inversion_matches_reference(gpu_ctx, golden):
     nm = inv.Nm
     mmin, mmax, mini = f["bounds"]
     m, rep = adaptive.invert_adaptive(
-        inv, o, prm, np.full(nm, mini), np.full(nm, mmin), np.full(nm, mmax),
+        inv, o, prm, np.full(nm, mini), np.full(nm, mmin), np.full(nm, mmax), m0,
         max_refinements=int(f["max_refinements"]), interval=int(f["interval"]),
         fraction=float(f["fraction"]), min_size=f["min_size"], beta=beta, alphas=alphas,
-        m0s=m0s, m0s_interpolator=interp)
+        m0s=m0s, m0s_interpolator=None if m0s is None else _gridded(leaves, m0s),
+        m0_interpolator=None if m0 is None else _gridded(leaves, m0))
     assert rep["mesh_refinements"] == len(f["ref_splits"])
     ref_leaves = f["ref_leaves"]
     assert inv.prisms.shape == ref_leaves.shape
