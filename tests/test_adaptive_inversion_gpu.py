@@ -125,7 +125,10 @@ def test_adaptive_constrained_inversion_matches_reference(gpu_ctx, golden, varia
     prm = {"max_lambda": float(f["max_lambda"]), "n_lambda": int(f["n_lambda"]),
            "rate": float(f["rate"]), "target": float(f["target"]), "stag": float(f["stag"]),
            "cg_tol": float(f["cg_tol"]), "cg_factor": float(f["cg_factor"]),
-           "gn_iter": int(f["gn_iter"]), "lp": [int(v) for v in f["lp"]], "eps2": float(f["eps2"])}
+           "gn_iter": int(f["gn_iter"]), "lp": [int(v) for v in f["lp"]], "eps2": float(f["eps2"]),
+           # a reference model read from data makes the reference start from it
+           # (use_petrophysical_constraint, GaussNewtonInversion.cpp:752-765)
+           "start_from_reference": m0 is not None}
     nm = inv.Nm
     mmin, mmax, mini = f["bounds"]
     m, rep = adaptive.invert_adaptive(
