@@ -31,10 +31,10 @@ Fixtures written (all .npz):
   ref_adaptive_inversion.npz  the adaptive inversion (invert_with_own_CG with
                       two mesh refinements): final leaves, model, records and
                       the cells split per refinement (oracle/_ref/ref_inversion).
-  ref_adaptive_{crg,pet,crg_pet}_inversion.npz  the same with gridded constraint
-                      models: the structure model (cross-gradient, T rebuilt at
-                      each refinement), the reference model, or both,
-                      interpolated onto the children (oracle/_ref/ref_inversion).
+  ref_adaptive_{crg,pet}_inversion.npz  the same with a gridded constraint
+                      model: the structure model (cross-gradient, T rebuilt at
+                      each refinement) or the reference model, interpolated
+                      onto the children (oracle/_ref/ref_inversion).
 """
 from __future__ import annotations
 
@@ -624,7 +624,7 @@ def main() -> None:
         from inversion_cases import adaptive_fixture, inversion_fixtures  # noqa: E402
         jobs["ref_inversion"] = inversion_fixtures
         jobs["ref_adaptive_inversion"] = adaptive_fixture
-        for v in ("crg", "pet", "crg_pet"):
+        for v in ("crg", "pet"):
             jobs[f"ref_adaptive_{v}_inversion"] = (lambda v=v: adaptive_fixture(v))
     except ImportError:
         pass
